@@ -1,0 +1,324 @@
+"""Benchmark: incoherent closest-hit traversal, Mrays/s.
+
+Workload (one step): closest hit of 16,777,216 incoherent rays against a
+2^20-triangle soup of level-3 icospheres (centres uniform in [-50,50]^3, radii
+log-uniform in [0.5,3]; rays with origins uniform in the cube and directions
+uniform on the sphere), FP32, reference triangle test (bit-exact t and hit
+index against the reference). Synthetic, seeded inputs.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+``value``  : rays/s with rays resident in device memory (CUDA events on the
+             launching stream, max over ranks), in Mrays/s.
+``e2e``    : the same through dr_trace_closest_host with pinned host buffers:
+             the ray upload and the hit download are inside the timed region.
+``--impl reference`` times the reference's CPU traversal (the oracle's port of
+getIntersectionImpl over the reference's median-split BBH) on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+NUM_TRIS = 1 << 20
+NUM_RAYS = 1 << 24
+METRIC = "Mrays/s closest-hit"
+WORKLOAD = "incoherent closest-hit: 2^20-triangle icosphere soup, 16,777,216 rays"
+L2_BYTES = 129 * 1024 * 1024
+
+
+def _env_rank():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0")), int(os.environ.get("WORLD_SIZE", "1"))
+
+
+def _peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.file = None
+
+    def __enter__(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=self.file, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or self.file is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.file.flush()
+        rows = [r.split(",") for r in Path(self.file.name).read_text().strip().splitlines() if r.strip()]
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for k, name in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower().startswith("active"):
+                    reasons.add(name)
+        os.unlink(self.file.name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def build_workload(rank: int):
+    from devilray_gb300 import scenes
+    soup, _, _ = scenes.incoherent_soup(NUM_TRIS, seed=0)
+    rays = scenes.incoherent_rays(NUM_RAYS, seed=rank)
+    return soup, rays
+
+
+def cpu_baseline(soup, rays, sample: int, threads: int):
+    """The reference's traversal (oracle port) on a bounded sample; Mrays/s."""
+    from oracle import pyoracle as po
+    po.build(ref=False)
+    t0 = time.perf_counter()
+    bbh = po.BBH(soup)
+    build_s = time.perf_counter() - t0
+    from devilray_gb300.scenes import rays6
+    r6 = rays6(rays[:sample])
+    t0 = time.perf_counter()
+    t, prim, nb, nt = bbh.trace_reference(r6, threads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": sample / dt / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
+            "sample": f"{sample} of the {NUM_RAYS} rays, reference median-split BBH (built in {build_s:.1f} s, untimed), "
+                      f"reference triangle test, std::thread over ray chunks",
+            "seconds": dt, "box_tests_per_ray": float(nb.mean()), "tri_tests_per_ray": float(nt.mean())}, (t, prim)
+
+
+def run_reference(args):
+    rank, local, world = _env_rank()
+    if rank != 0:
+        return 0
+    soup, rays = build_workload(0)
+    threads = os.cpu_count() or 1
+    from oracle import pyoracle as po
+    po.build(ref=False)
+    bbh = po.BBH(soup)
+    from devilray_gb300.scenes import rays6
+    sample = args.ref_sample
+    r6 = rays6(rays[:sample])
+    for _ in range(args.warmup):
+        bbh.trace_reference(r6[: max(1, sample // 8)], threads=threads)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        bbh.trace_reference(r6, threads=threads)
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = sample * args.steps / total / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "num_triangles": NUM_TRIS, "num_rays": NUM_RAYS,
+                   "step_sample_rays": sample, "tri_mode": "reference"},
+        "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": threads, "kind": "port",
+                         "sample": f"{sample} rays per step of the {NUM_RAYS}-ray workload; the reference's "
+                                   "median-split BBH and getIntersectionImpl restated in C++ (oracle), "
+                                   "std::thread over ray chunks on all host cores"},
+        "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+    rank, local, world = _env_rank()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    from devilray_gb300 import native
+    soup, rays = build_workload(rank)
+    ctx = native.Context(local)
+    scene = native.Scene(ctx, soup)
+    info = scene.info()
+    stream = torch.cuda.Stream()
+    d_rays = torch.from_numpy(rays).to(f"cuda:{local}")
+    d_hits = torch.empty((NUM_RAYS, 2), dtype=torch.int32, device=f"cuda:{local}")
+    torch.cuda.synchronize()
+
+    # Counting pass (untimed): node and triangle visits per ray for the
+    # algorithmic-byte count of the roofline.
+    with torch.cuda.stream(stream):
+        cnt = scene.trace_closest(d_rays, NUM_RAYS, d_hits, native.DR_TRI_REFERENCE, counters=True, stream=stream)
+    stream.synchronize()
+    nodes_per_ray = cnt.node_visits / NUM_RAYS
+    tris_per_ray = cnt.tri_tests / NUM_RAYS
+    hit_frac = cnt.hits / NUM_RAYS
+
+    for _ in range(args.warmup):
+        scene.trace_closest(d_rays, NUM_RAYS, d_hits, native.DR_TRI_REFERENCE, stream=stream)
+    stream.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        for k in range(args.steps):
+            starts[k].record(stream)
+            scene.trace_closest(d_rays, NUM_RAYS, d_hits, native.DR_TRI_REFERENCE, stream=stream)
+            ends[k].record(stream)
+        stream.synchronize()
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = sum(step_ms)
+    ctx.check()
+
+    # End to end through the host-buffer entry point, pinned host memory.
+    h_rays = torch.from_numpy(rays).pin_memory()
+    h_hits = torch.empty((NUM_RAYS, 2), dtype=torch.int32).pin_memory()
+    e2e_steps = max(1, min(args.steps, 5))
+    for _ in range(1):
+        native.check(native.load().dr_trace_closest_host(scene.handle, h_rays.data_ptr(), NUM_RAYS,
+                                                         h_hits.data_ptr(), 0, stream.cuda_stream))
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        native.check(native.load().dr_trace_closest_host(scene.handle, h_rays.data_ptr(), NUM_RAYS,
+                                                         h_hits.data_ptr(), 0, stream.cuda_stream))
+    e2e_s = time.perf_counter() - t0
+    # the host copy of the hits equals the device-resident result
+    same = torch.equal(h_hits, d_hits.cpu())
+
+    if dist:
+        t = torch.tensor([total_ms, e2e_s], dtype=torch.float64, device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms, e2e_s = float(t[0]), float(t[1])
+    value = world * NUM_RAYS * args.steps / (total_ms / 1e3) / 1e6
+    e2e_value = world * NUM_RAYS * e2e_steps / e2e_s / 1e6
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return 0
+
+    hbm_peak, peak_kind = _peaks()
+    node_bytes, tri_bytes = 64, 48
+    bytes_per_ray = 32 + 8 + nodes_per_ray * node_bytes + tris_per_ray * tri_bytes
+    per_launch_ms = total_ms / args.steps
+    achieved = bytes_per_ray * NUM_RAYS / (per_launch_ms / 1e3) / 1e9
+    working_set = info.device_bytes
+    line = {
+        "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "num_triangles": NUM_TRIS, "num_rays": NUM_RAYS, "tri_mode": "reference",
+                   "layout": "binary two-box BVH, binned SAH", "bvh_nodes": info.num_nodes, "bvh_depth": info.depth,
+                   "scene_device_bytes": working_set, "bvh_build_s": round(info.build_seconds, 3),
+                   "l2": "rays 512 MiB per step > L2; scene arrays stay L2-resident across steps",
+                   "parallelism": f"replicas{world}" if world > 1 else "single"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "traffic": None,
+                     "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
+                     "kernel": "k_trace_closest<0,false>",
+                     "bytes_per_ray": bytes_per_ray, "node_visits_per_ray": nodes_per_ray,
+                     "tri_tests_per_ray": tris_per_ray, "hit_fraction": hit_frac,
+                     "per_launch_ms": per_launch_ms, "working_set_bytes": working_set,
+                     "working_set_fits_l2": working_set < L2_BYTES},
+        "clocks": clocks.summary(),
+        "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": NUM_RAYS * 32,
+                "d2h_bytes_per_step": NUM_RAYS * 8, "steps": e2e_steps, "api": "dr_trace_closest_host",
+                "matches_device_result": bool(same)},
+        "gpu_launches": args.steps,
+    }
+    if l2 := _l2_probe(local):
+        line["roofline"]["l2_read_gbs_measured"] = l2
+        line["roofline"]["frac_of_l2"] = achieved / l2
+    if world == 1 and not args.no_cpu_baseline:
+        cb, _ = cpu_baseline(soup, rays, args.cpu_sample, os.cpu_count() or 1)
+        line["cpu_baseline"] = cb
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def _l2_probe(device: int):
+    """Read bandwidth of a 48 MiB L2-resident buffer (torch reduction), GB/s."""
+    import torch
+    try:
+        x = torch.empty(12 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{device}").fill_(1.0)
+        for _ in range(3):
+            x.sum()
+        torch.cuda.synchronize()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        reps = 50
+        s.record()
+        for _ in range(reps):
+            x.sum()
+        e.record()
+        torch.cuda.synchronize()
+        return x.numel() * 4 * reps / (s.elapsed_time(e) / 1e3) / 1e9
+    except Exception:
+        return None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--cpu-sample", type=int, default=1 << 20)
+    ap.add_argument("--ref-sample", type=int, default=1 << 19)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

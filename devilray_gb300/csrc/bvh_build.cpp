@@ -1,0 +1,342 @@
+// bvh_build.cpp -- host binned-SAH BVH build for the GB300 traversal kernels.
+//
+// Replaces DevilRay's median-split generateSimpleBBH (src/models/BBH.cpp:38-115:
+// one triangle per leaf, split at the median of the max-vertex key along a
+// cycling axis) with a binned-SAH build and the two-box node layout that the
+// device traversal reads. Unlike the reference it never reorders the caller's
+// triangles: the leaf order is returned as a permutation.
+
+#include "dr_internal.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <memory>
+#include <thread>
+
+namespace dr {
+namespace {
+
+struct Box {
+    float lo[3], hi[3];
+    void reset()
+    {
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = std::numeric_limits<float>::infinity();
+            hi[a] = -std::numeric_limits<float>::infinity();
+        }
+    }
+    void grow(const Box &b)
+    {
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = std::min(lo[a], b.lo[a]);
+            hi[a] = std::max(hi[a], b.hi[a]);
+        }
+    }
+    void grow(const float p[3])
+    {
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = std::min(lo[a], p[a]);
+            hi[a] = std::max(hi[a], p[a]);
+        }
+    }
+    float area() const
+    {
+        const float dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
+        if (!(dx >= 0 && dy >= 0 && dz >= 0)) return 0.0f;
+        return 2.0f * (dx * dy + dy * dz + dz * dx);
+    }
+};
+
+struct Prim {
+    Box box;
+    float c[3];
+};
+
+struct TreeNode {
+    Box box;
+    std::unique_ptr<TreeNode> child[2];
+    uint32_t first = 0, count = 0;  // leaf range in the index array
+    int depth = 0;
+    bool leaf() const { return !child[0]; }
+};
+
+struct Builder {
+    const std::vector<Prim> &prims;
+    std::vector<uint32_t> &idx;
+    BuildParams params;
+    std::atomic<int> spare_threads;
+    std::atomic<int> max_depth{0};
+
+    Builder(const std::vector<Prim> &p, std::vector<uint32_t> &i, const BuildParams &bp, int threads)
+        : prims(p), idx(i), params(bp), spare_threads(threads - 1) {}
+
+    static constexpr float kTraversalCost = 1.0f;
+    static constexpr float kTriangleCost = 1.5f;
+
+    std::unique_ptr<TreeNode> build(uint32_t begin, uint32_t end, int depth)
+    {
+        auto node = std::make_unique<TreeNode>();
+        node->depth = depth;
+        int prev = max_depth.load();
+        while (depth > prev && !max_depth.compare_exchange_weak(prev, depth)) {}
+
+        Box bounds, cbounds;
+        bounds.reset();
+        cbounds.reset();
+        for (uint32_t i = begin; i < end; ++i) {
+            const Prim &p = prims[idx[i]];
+            bounds.grow(p.box);
+            cbounds.grow(p.c);
+        }
+        node->box = bounds;
+        const uint32_t n = end - begin;
+        if (n <= 1) {
+            node->first = begin;
+            node->count = n;
+            return node;
+        }
+
+        // Binned SAH over the three axes.
+        const uint32_t B = std::max<uint32_t>(4, std::min<uint32_t>(params.bins, 64));
+        float best_cost = std::numeric_limits<float>::infinity();
+        int best_axis = -1;
+        uint32_t best_split = 0;
+        const bool force_median = depth >= 32;  // bounds the depth: <= 32 + log2(n) levels
+        if (!force_median) {
+            for (int axis = 0; axis < 3; ++axis) {
+                const float cmin = cbounds.lo[axis], cmax = cbounds.hi[axis];
+                if (!(cmax > cmin)) continue;
+                const float scale = (float)B / (cmax - cmin);
+                Box bin_box[64];
+                uint32_t bin_count[64];
+                for (uint32_t b = 0; b < B; ++b) {
+                    bin_box[b].reset();
+                    bin_count[b] = 0;
+                }
+                for (uint32_t i = begin; i < end; ++i) {
+                    const Prim &p = prims[idx[i]];
+                    uint32_t b = (uint32_t)((p.c[axis] - cmin) * scale);
+                    if (b >= B) b = B - 1;
+                    bin_box[b].grow(p.box);
+                    ++bin_count[b];
+                }
+                float right_area[64];
+                uint32_t right_count[64];
+                Box acc;
+                acc.reset();
+                uint32_t cnt = 0;
+                for (uint32_t b = B - 1; b > 0; --b) {
+                    acc.grow(bin_box[b]);
+                    cnt += bin_count[b];
+                    right_area[b] = acc.area();
+                    right_count[b] = cnt;
+                }
+                acc.reset();
+                cnt = 0;
+                for (uint32_t b = 0; b + 1 < B; ++b) {
+                    acc.grow(bin_box[b]);
+                    cnt += bin_count[b];
+                    if (cnt == 0 || right_count[b + 1] == 0) continue;
+                    const float cost = acc.area() * cnt + right_area[b + 1] * right_count[b + 1];
+                    if (cost < best_cost) {
+                        best_cost = cost;
+                        best_axis = axis;
+                        best_split = b + 1;
+                    }
+                }
+            }
+        }
+        const float parent_area = bounds.area();
+        const float leaf_cost = kTriangleCost * n;
+        const float split_cost = best_axis >= 0 && parent_area > 0.0f
+                                     ? kTraversalCost + kTriangleCost * best_cost / parent_area
+                                     : std::numeric_limits<float>::infinity();
+        if (n <= params.max_leaf && (leaf_cost <= split_cost || best_axis < 0)) {
+            node->first = begin;
+            node->count = n;
+            return node;
+        }
+
+        uint32_t mid;
+        if (best_axis >= 0) {
+            const float cmin = cbounds.lo[best_axis], cmax = cbounds.hi[best_axis];
+            const float scale = (float)B / (cmax - cmin);
+            auto it = std::partition(idx.begin() + begin, idx.begin() + end, [&](uint32_t i) {
+                uint32_t b = (uint32_t)((prims[i].c[best_axis] - cmin) * scale);
+                if (b >= B) b = B - 1;
+                return b < best_split;
+            });
+            mid = (uint32_t)(it - idx.begin());
+            if (mid == begin || mid == end) mid = begin + n / 2;
+        } else {
+            // No useful SAH split (coincident centroids, or the depth cap):
+            // split at the median along the largest centroid extent.
+            int axis = 0;
+            float ext = -1.0f;
+            for (int a = 0; a < 3; ++a)
+                if (cbounds.hi[a] - cbounds.lo[a] > ext) {
+                    ext = cbounds.hi[a] - cbounds.lo[a];
+                    axis = a;
+                }
+            mid = begin + n / 2;
+            std::nth_element(idx.begin() + begin, idx.begin() + mid, idx.begin() + end,
+                             [&](uint32_t a, uint32_t b) {
+                                 if (prims[a].c[axis] != prims[b].c[axis]) return prims[a].c[axis] < prims[b].c[axis];
+                                 return a < b;
+                             });
+        }
+
+        if (n > 65536 && spare_threads.fetch_sub(1) > 0) {
+            std::unique_ptr<TreeNode> left;
+            std::thread th([&] { left = build(begin, mid, depth + 1); });
+            node->child[1] = build(mid, end, depth + 1);
+            th.join();
+            spare_threads.fetch_add(1);
+            node->child[0] = std::move(left);
+        } else {
+            if (n > 65536) spare_threads.fetch_add(1);
+            node->child[0] = build(begin, mid, depth + 1);
+            node->child[1] = build(mid, end, depth + 1);
+        }
+        return node;
+    }
+};
+
+// Rounds a widened bound outward so the stored float box contains the exact
+// widened box.
+inline float lower_bound_out(float v, float slack) { return std::nextafter(v - slack, -INFINITY); }
+inline float upper_bound_out(float v, float slack) { return std::nextafter(v + slack, INFINITY); }
+
+struct Flattener {
+    std::vector<Bvh2Node> &out;
+    float slack;
+
+    void set_child_box(Bvh2Node &n, int which, const Box &b)
+    {
+        const float lx = lower_bound_out(b.lo[0], slack), hx = upper_bound_out(b.hi[0], slack);
+        const float ly = lower_bound_out(b.lo[1], slack), hy = upper_bound_out(b.hi[1], slack);
+        const float lz = lower_bound_out(b.lo[2], slack), hz = upper_bound_out(b.hi[2], slack);
+        if (which == 0) {
+            n.c0xy = make_float4(lx, hx, ly, hy);
+            n.cz.x = lz;
+            n.cz.y = hz;
+        } else {
+            n.c1xy = make_float4(lx, hx, ly, hy);
+            n.cz.z = lz;
+            n.cz.w = hz;
+        }
+    }
+
+    // Emits `node` (an inner node) at the next index, depth-first with the
+    // left child right after its parent. Returns its index.
+    int32_t emit(const TreeNode *node)
+    {
+        const int32_t me = (int32_t)out.size();
+        out.push_back(Bvh2Node{});
+        for (int c = 0; c < 2; ++c) {
+            const TreeNode *ch = node->child[c].get();
+            int32_t link;
+            if (ch->leaf()) link = leaf_link(ch->first, ch->count);
+            else link = emit(ch);
+            Bvh2Node &n = out[me];
+            set_child_box(n, c, ch->box);
+            if (c == 0) n.link.x = link;
+            else n.link.y = link;
+        }
+        return me;
+    }
+};
+
+}  // namespace
+
+float scene_slack(float mag)
+{
+    // 2^-14 of the scene magnitude: two orders above the FP32 rounding of
+    // hit points, slab times and triangle-plane distances for rays whose
+    // origins lie within a few hundred scene radii.
+    const float m = std::max(mag, 1.0f / 1024.0f);
+    return std::ldexp(m, -14);
+}
+
+Bvh2 build_bvh2(const float *pos, uint32_t num_tris, const BuildParams &params, float slack)
+{
+    Bvh2 bvh;
+    bvh.slack = slack;
+    if (num_tris == 0) return bvh;
+    std::vector<Prim> prims(num_tris);
+    for (uint32_t i = 0; i < num_tris; ++i) {
+        Prim &p = prims[i];
+        p.box.reset();
+        for (int k = 0; k < 3; ++k) p.box.grow(pos + (size_t)i * 9 + k * 3);
+        for (int a = 0; a < 3; ++a) p.c[a] = 0.5f * (p.box.lo[a] + p.box.hi[a]);
+    }
+    std::vector<uint32_t> idx(num_tris);
+    for (uint32_t i = 0; i < num_tris; ++i) idx[i] = i;
+    int threads = (int)params.threads;
+    if (threads <= 0) threads = (int)std::max(1u, std::thread::hardware_concurrency());
+    BuildParams bp = params;
+    bp.max_leaf = std::max<uint32_t>(1, std::min(bp.max_leaf, kMaxLeafSize));
+    Builder builder(prims, idx, bp, threads);
+    std::unique_ptr<TreeNode> root = builder.build(0, num_tris, 0);
+
+    Flattener fl{bvh.nodes, slack};
+    bvh.nodes.reserve(2 * (size_t)num_tris / std::max<uint32_t>(1, bp.max_leaf) + 4);
+    if (root->leaf()) {
+        // A single leaf: the root record holds it as child 0 and an empty
+        // leaf (count 0) with the same box as child 1.
+        Bvh2Node n{};
+        fl.set_child_box(n, 0, root->box);
+        fl.set_child_box(n, 1, root->box);
+        n.link = make_int4(leaf_link(root->first, root->count), leaf_link(root->first, 0), 0, 0);
+        bvh.nodes.push_back(n);
+        bvh.depth = 1;
+    } else {
+        fl.emit(root.get());
+        bvh.depth = builder.max_depth.load() + 1;
+    }
+    bvh.order = std::move(idx);
+    return bvh;
+}
+
+void make_tri_records(const float *pos, const std::vector<uint32_t> &order,
+                      std::vector<float4> &ref, std::vector<float4> &wt)
+{
+    const size_t n = order.size();
+    ref.resize(n * 3);
+    wt.resize(n * 3);
+    for (size_t k = 0; k < n; ++k) {
+        const float *q = pos + (size_t)order[k] * 9;
+        const float Ax = q[0], Ay = q[1], Az = q[2];
+        const float Bx = q[3], By = q[4], Bz = q[5];
+        const float Cx = q[6], Cy = q[7], Cz = q[8];
+        // n_f = (A - B) x (A - C), sgn_area2 = n_f . n_f, n = n_f / |n_f|
+        // (IntersectionTestsImpl.hpp:261-266; Utils.hpp:88-109), compiled with
+        // -ffp-contract=off so it rounds like the reference.
+        const float ux = Ax - Bx, uy = Ay - By, uz = Az - Bz;
+        const float vx = Ax - Cx, vy = Ay - Cy, vz = Az - Cz;
+        const float nfx = uy * vz - uz * vy;
+        const float nfy = uz * vx - ux * vz;
+        const float nfz = ux * vy - uy * vx;
+        const float s = nfx * nfx + nfy * nfy + nfz * nfz;
+        float nx = 0.0f, ny = 0.0f, nz = 0.0f;
+        if (!(s < 1e-14f)) {
+            const float l = std::sqrt(nfx * nfx + nfy * nfy + nfz * nfz);
+            nx = nfx / l;
+            ny = nfy / l;
+            nz = nfz / l;
+        }
+        const float BAx = Bx - Ax, BAy = By - Ay, BAz = Bz - Az;
+        const float CAx = Cx - Ax, CAy = Cy - Ay, CAz = Cz - Az;
+        ref[k * 3 + 0] = make_float4(Ax, Ay, Az, nx);
+        ref[k * 3 + 1] = make_float4(ny, nz, BAx, BAy);
+        ref[k * 3 + 2] = make_float4(BAz, CAx, CAy, CAz);
+        wt[k * 3 + 0] = make_float4(Ax, Ay, Az, Bx);
+        wt[k * 3 + 1] = make_float4(By, Bz, Cx, Cy);
+        wt[k * 3 + 2] = make_float4(Cz, 0.0f, 0.0f, 0.0f);
+    }
+}
+
+}  // namespace dr

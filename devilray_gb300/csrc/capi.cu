@@ -1,0 +1,348 @@
+// capi.cu -- the C ABI entry points: context, scene and traversal.
+
+#include "dr_internal.h"
+#include "trace_kernels.cuh"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+namespace dr {
+
+namespace {
+thread_local char g_error[1024] = "";
+}
+
+void set_error(const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(g_error, sizeof(g_error), fmt, ap);
+    va_end(ap);
+}
+
+dr_status fail(dr_status code, const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(g_error, sizeof(g_error), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+dr_status cuda_fail(cudaError_t e, const char *what)
+{
+    set_error("%s: %s (%s)", what, cudaGetErrorString(e), cudaGetErrorName(e));
+    if (e == cudaErrorMemoryAllocation) return DR_ERR_OUT_OF_MEMORY;
+    if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return DR_ERR_NO_DEVICE;
+    return DR_ERR_CUDA;
+}
+
+namespace {
+
+template <typename T>
+cudaError_t upload(T **dst, const T *src, size_t count, uint64_t &bytes)
+{
+    *dst = nullptr;
+    if (count == 0) return cudaSuccess;
+    cudaError_t e = cudaMalloc(reinterpret_cast<void **>(dst), sizeof(T) * count);
+    if (e != cudaSuccess) return e;
+    bytes += sizeof(T) * count;
+    return cudaMemcpy(*dst, src, sizeof(T) * count, cudaMemcpyHostToDevice);
+}
+
+// Maps the context's device error word to a status and clears it.
+dr_status check_error_word(dr_context *ctx, cudaStream_t s)
+{
+    uint32_t word = 0;
+    DR_CUDA(cudaMemcpyAsync(&word, ctx->d_error, sizeof(word), cudaMemcpyDeviceToHost, s));
+    DR_CUDA(cudaStreamSynchronize(s));
+    if (word == 0) return DR_OK;
+    DR_CUDA(cudaMemsetAsync(ctx->d_error, 0, sizeof(uint32_t), s));
+    if (word & ERR_STACK_OVERFLOW) return fail(DR_ERR_STACK_OVERFLOW, "traversal stack overflow");
+    if (word & ERR_TIMEOUT) return fail(DR_ERR_TIMEOUT, "a bounded device loop gave up");
+    return fail(DR_ERR_CUDA, "device error word 0x%x", word);
+}
+
+TraceArgs trace_args(dr_scene *s)
+{
+    TraceArgs a{};
+    a.nodes = s->d_nodes;
+    a.tri_ref = s->d_tri_ref;
+    a.tri_wt = s->d_tri_wt;
+    a.prim = s->d_prim;
+    a.num_nodes = s->num_nodes;
+    a.counters = s->ctx->d_counters;
+    a.error = s->ctx->d_error;
+    return a;
+}
+
+}  // namespace
+}  // namespace dr
+
+using namespace dr;
+
+extern "C" {
+
+uint32_t dr_abi_version(void) { return DR_ABI_VERSION; }
+
+const char *dr_last_error_string(void) { return g_error; }
+
+dr_status dr_context_create(const dr_context_config *cfg, dr_context **out)
+{
+    DR_CHECK_ARG(out != nullptr, "dr_context_create: out is NULL");
+    *out = nullptr;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        return fail(DR_ERR_NO_DEVICE, "no CUDA device available (%s)", cudaGetErrorString(e));
+    }
+    const int dev = cfg ? cfg->device : 0;
+    DR_CHECK_ARG(dev >= 0 && dev < count, "dr_context_create: bad device ordinal");
+    DR_CUDA(cudaSetDevice(dev));
+    auto *ctx = new (std::nothrow) dr_context;
+    if (!ctx) return fail(DR_ERR_OUT_OF_MEMORY, "host allocation failed");
+    ctx->device = dev;
+    cudaDeviceProp prop;
+    if ((e = cudaGetDeviceProperties(&prop, dev)) != cudaSuccess) {
+        delete ctx;
+        return cuda_fail(e, "cudaGetDeviceProperties");
+    }
+    ctx->num_sms = prop.multiProcessorCount;
+    if ((e = cudaMalloc(&ctx->d_error, 256)) != cudaSuccess || (e = cudaMemset(ctx->d_error, 0, 256)) != cudaSuccess) {
+        delete ctx;
+        return cuda_fail(e, "cudaMalloc(error word)");
+    }
+    ctx->d_counters = reinterpret_cast<unsigned long long *>(reinterpret_cast<char *>(ctx->d_error) + 64);
+    ctx->d_work = reinterpret_cast<unsigned int *>(reinterpret_cast<char *>(ctx->d_error) + 192);
+    *out = ctx;
+    return DR_OK;
+}
+
+dr_status dr_context_destroy(dr_context *ctx)
+{
+    if (!ctx) return DR_OK;
+    cudaSetDevice(ctx->device);
+    cudaFree(ctx->d_error);
+    delete ctx;
+    return DR_OK;
+}
+
+dr_status dr_context_check(dr_context *ctx)
+{
+    DR_CHECK_ARG(ctx != nullptr, "dr_context_check: ctx is NULL");
+    DR_CUDA(cudaSetDevice(ctx->device));
+    return check_error_word(ctx, nullptr);
+}
+
+dr_status dr_scene_create(dr_context *ctx, const dr_scene_desc *desc, const dr_build_config *cfg, dr_scene **out)
+{
+    DR_CHECK_ARG(ctx && desc && out, "dr_scene_create: NULL argument");
+    *out = nullptr;
+    const uint32_t n = desc->num_triangles;
+    DR_CHECK_ARG(n == 0 || desc->positions_host, "dr_scene_create: positions_host is NULL");
+    if (n >= kMaxTriangles) return fail(DR_ERR_TOO_LARGE, "dr_scene_create: %u triangles (max %u)", n, kMaxTriangles - 1);
+    float mag = 0.0f;
+    for (size_t i = 0; i < (size_t)n * 9; ++i) {
+        const float v = desc->positions_host[i];
+        if (!std::isfinite(v)) return fail(DR_ERR_INVALID_ARGUMENT, "dr_scene_create: non-finite vertex coordinate");
+        mag = std::max(mag, std::fabs(v));
+    }
+    if (desc->objects_host) {
+        for (uint32_t o = 0; o < desc->num_objects; ++o) {
+            const dr_object &ob = desc->objects_host[o];
+            if ((uint64_t)ob.tri_begin + ob.tri_count > n)
+                return fail(DR_ERR_INVALID_ARGUMENT, "dr_scene_create: object %u range out of bounds", o);
+            if (ob.material < 0 || (uint32_t)ob.material >= std::max(1u, desc->num_materials))
+                return fail(DR_ERR_INVALID_ARGUMENT, "dr_scene_create: object %u material out of range", o);
+        }
+    }
+    DR_CUDA(cudaSetDevice(ctx->device));
+
+    const auto t_start = std::chrono::steady_clock::now();
+    BuildParams bp;
+    if (cfg) {
+        if (cfg->max_leaf_size) bp.max_leaf = cfg->max_leaf_size;
+        if (cfg->sah_bins) bp.bins = cfg->sah_bins;
+        bp.threads = cfg->threads;
+    }
+    const float slack = scene_slack(mag);
+    Bvh2 bvh = build_bvh2(desc->positions_host, n, bp, slack);
+    std::vector<float4> ref_rec, wt_rec;
+    make_tri_records(desc->positions_host, bvh.order, ref_rec, wt_rec);
+    std::vector<int32_t> prim(bvh.order.begin(), bvh.order.end());
+
+    auto *s = new (std::nothrow) dr_scene;
+    if (!s) return fail(DR_ERR_OUT_OF_MEMORY, "host allocation failed");
+    s->ctx = ctx;
+    s->num_tris = n;
+    s->num_nodes = (uint32_t)bvh.nodes.size();
+    s->depth = (uint32_t)bvh.depth;
+    s->slack = slack;
+    cudaError_t e = cudaSuccess;
+    if ((e = upload(&s->d_nodes, bvh.nodes.data(), bvh.nodes.size(), s->device_bytes)) != cudaSuccess ||
+        (e = upload(&s->d_tri_ref, ref_rec.data(), ref_rec.size(), s->device_bytes)) != cudaSuccess ||
+        (e = upload(&s->d_tri_wt, wt_rec.data(), wt_rec.size(), s->device_bytes)) != cudaSuccess ||
+        (e = upload(&s->d_prim, prim.data(), prim.size(), s->device_bytes)) != cudaSuccess) {
+        dr_scene_destroy(s);
+        return cuda_fail(e, "dr_scene_create upload");
+    }
+    if (desc->materials_host && desc->num_materials) {
+        if ((e = upload(&s->d_materials, desc->materials_host, desc->num_materials, s->device_bytes)) != cudaSuccess) {
+            dr_scene_destroy(s);
+            return cuda_fail(e, "dr_scene_create upload materials");
+        }
+        s->num_materials = desc->num_materials;
+    }
+    s->build_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+    *out = s;
+    return DR_OK;
+}
+
+dr_status dr_scene_destroy(dr_scene *s)
+{
+    if (!s) return DR_OK;
+    cudaSetDevice(s->ctx->device);
+    cudaFree(s->d_nodes);
+    cudaFree(s->d_tri_ref);
+    cudaFree(s->d_tri_wt);
+    cudaFree(s->d_prim);
+    cudaFree(s->d_materials);
+    cudaFree(s->d_stage_rays);
+    cudaFree(s->d_stage_hits);
+    delete s;
+    return DR_OK;
+}
+
+dr_status dr_scene_get_info(const dr_scene *s, dr_scene_info *info)
+{
+    DR_CHECK_ARG(s && info, "dr_scene_get_info: NULL argument");
+    info->num_triangles = s->num_tris;
+    info->num_nodes = s->num_nodes;
+    info->depth = s->depth;
+    info->layout = s->layout;
+    info->slack = s->slack;
+    info->total_radiant_power = s->total_radiant_power;
+    info->device_bytes = s->device_bytes;
+    info->build_seconds = s->build_seconds;
+    return DR_OK;
+}
+
+dr_status dr_trace_closest(dr_scene *s, const dr_ray *rays, uint64_t n, dr_hit *hits, int32_t tri_mode,
+                           dr_trace_counters *counters, void *stream)
+{
+    DR_CHECK_ARG(s != nullptr, "dr_trace_closest: scene is NULL");
+    DR_CHECK_ARG(n == 0 || (rays && hits), "dr_trace_closest: NULL buffer");
+    DR_CHECK_ARG(tri_mode == DR_TRI_REFERENCE || tri_mode == DR_TRI_WATERTIGHT, "dr_trace_closest: bad tri_mode");
+    DR_CHECK_ARG((reinterpret_cast<uintptr_t>(rays) & 15) == 0 && (reinterpret_cast<uintptr_t>(hits) & 7) == 0,
+                 "dr_trace_closest: rays must be 16-byte and hits 8-byte aligned");
+    DR_CUDA(cudaSetDevice(s->ctx->device));
+    auto st = static_cast<cudaStream_t>(stream);
+    TraceArgs a = trace_args(s);
+    a.rays = rays;
+    a.n = n;
+    a.hits = hits;
+    if (counters) DR_CUDA(cudaMemsetAsync(s->ctx->d_counters, 0, 8 * sizeof(unsigned long long), st));
+    DR_CUDA(launch_trace_closest(a, tri_mode, counters != nullptr, st));
+    if (counters) {
+        unsigned long long c[8];
+        DR_CUDA(cudaMemcpyAsync(c, s->ctx->d_counters, sizeof(c), cudaMemcpyDeviceToHost, st));
+        DR_CUDA(cudaStreamSynchronize(st));
+        counters->rays = n;
+        counters->node_visits = c[0];
+        counters->box_tests = c[1];
+        counters->tri_tests = c[2];
+        counters->hits = c[3];
+        return check_error_word(s->ctx, st);
+    }
+    return DR_OK;
+}
+
+dr_status dr_trace_any(dr_scene *s, const dr_ray *rays, uint64_t n, uint8_t *occluded, int32_t tri_mode, void *stream)
+{
+    DR_CHECK_ARG(s != nullptr, "dr_trace_any: scene is NULL");
+    DR_CHECK_ARG(n == 0 || (rays && occluded), "dr_trace_any: NULL buffer");
+    DR_CHECK_ARG(tri_mode == DR_TRI_REFERENCE || tri_mode == DR_TRI_WATERTIGHT, "dr_trace_any: bad tri_mode");
+    DR_CHECK_ARG((reinterpret_cast<uintptr_t>(rays) & 15) == 0, "dr_trace_any: rays must be 16-byte aligned");
+    DR_CUDA(cudaSetDevice(s->ctx->device));
+    TraceArgs a = trace_args(s);
+    a.rays = rays;
+    a.n = n;
+    a.occluded = occluded;
+    DR_CUDA(launch_trace_any(a, tri_mode, static_cast<cudaStream_t>(stream)));
+    return DR_OK;
+}
+
+dr_status dr_trace_closest_host(dr_scene *s, const dr_ray *rays_host, uint64_t n, dr_hit *hits_host,
+                                int32_t tri_mode, void *stream)
+{
+    DR_CHECK_ARG(s != nullptr, "dr_trace_closest_host: scene is NULL");
+    DR_CHECK_ARG(n == 0 || (rays_host && hits_host), "dr_trace_closest_host: NULL buffer");
+    DR_CHECK_ARG(tri_mode == DR_TRI_REFERENCE || tri_mode == DR_TRI_WATERTIGHT, "dr_trace_closest_host: bad tri_mode");
+    if (n == 0) return DR_OK;
+    DR_CUDA(cudaSetDevice(s->ctx->device));
+    auto st = static_cast<cudaStream_t>(stream);
+    if (s->stage_capacity < n) {
+        cudaFree(s->d_stage_rays);
+        cudaFree(s->d_stage_hits);
+        s->d_stage_rays = s->d_stage_hits = nullptr;
+        s->stage_capacity = 0;
+        DR_CUDA(cudaMalloc(&s->d_stage_rays, n * sizeof(dr_ray)));
+        DR_CUDA(cudaMalloc(&s->d_stage_hits, n * sizeof(dr_hit)));
+        s->stage_capacity = n;
+    }
+    // Pipeline in chunks: the copy-in of chunk k+1 and the copy-out of chunk
+    // k-1 overlap the traversal of chunk k (one stream per stage, ordered by
+    // events).
+    auto *d_rays = static_cast<dr_ray *>(s->d_stage_rays);
+    auto *d_hits = static_cast<dr_hit *>(s->d_stage_hits);
+    const uint64_t chunk = std::max<uint64_t>(1u << 18, (n + 7) / 8);
+    cudaStream_t copy_in, copy_out;
+    DR_CUDA(cudaStreamCreateWithFlags(&copy_in, cudaStreamNonBlocking));
+    DR_CUDA(cudaStreamCreateWithFlags(&copy_out, cudaStreamNonBlocking));
+    std::vector<cudaEvent_t> ev;
+    auto new_event = [&]() {
+        cudaEvent_t e;
+        cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+        ev.push_back(e);
+        return e;
+    };
+    cudaError_t err = cudaSuccess;
+    cudaEvent_t start = new_event();
+    err = cudaEventRecord(start, st);
+    if (err == cudaSuccess) err = cudaStreamWaitEvent(copy_in, start, 0);
+    TraceArgs a = trace_args(s);
+    for (uint64_t b = 0; b < n && err == cudaSuccess; b += chunk) {
+        const uint64_t m = std::min(chunk, n - b);
+        err = cudaMemcpyAsync(d_rays + b, rays_host + b, m * sizeof(dr_ray), cudaMemcpyHostToDevice, copy_in);
+        cudaEvent_t in_done = new_event();
+        if (err == cudaSuccess) err = cudaEventRecord(in_done, copy_in);
+        if (err == cudaSuccess) err = cudaStreamWaitEvent(st, in_done, 0);
+        a.rays = d_rays + b;
+        a.hits = d_hits + b;
+        a.n = m;
+        if (err == cudaSuccess) err = launch_trace_closest(a, tri_mode, false, st);
+        cudaEvent_t tr_done = new_event();
+        if (err == cudaSuccess) err = cudaEventRecord(tr_done, st);
+        if (err == cudaSuccess) err = cudaStreamWaitEvent(copy_out, tr_done, 0);
+        if (err == cudaSuccess)
+            err = cudaMemcpyAsync(hits_host + b, d_hits + b, m * sizeof(dr_hit), cudaMemcpyDeviceToHost, copy_out);
+    }
+    cudaEvent_t out_done = new_event();
+    if (err == cudaSuccess) err = cudaEventRecord(out_done, copy_out);
+    if (err == cudaSuccess) err = cudaStreamWaitEvent(st, out_done, 0);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(st);
+    for (auto e : ev) cudaEventDestroy(e);
+    cudaStreamDestroy(copy_in);
+    cudaStreamDestroy(copy_out);
+    if (err != cudaSuccess) return cuda_fail(err, "dr_trace_closest_host");
+    return DR_OK;
+}
+
+}  // extern "C"

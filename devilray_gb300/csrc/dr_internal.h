@@ -1,0 +1,129 @@
+// dr_internal.h -- internal types of the GB300 path-tracing core.
+#pragma once
+
+#include "devilray_gb300.h"
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace dr {
+
+// ---- errors ------------------------------------------------------------------
+
+void set_error(const char *fmt, ...);
+dr_status fail(dr_status code, const char *fmt, ...);
+dr_status cuda_fail(cudaError_t e, const char *what);
+
+#define DR_CUDA(call)                                                        \
+    do {                                                                     \
+        cudaError_t e_ = (call);                                             \
+        if (e_ != cudaSuccess) return ::dr::cuda_fail(e_, #call);            \
+    } while (0)
+
+#define DR_CHECK_ARG(cond, msg)                                              \
+    do {                                                                     \
+        if (!(cond)) return ::dr::fail(DR_ERR_INVALID_ARGUMENT, "%s", msg);   \
+    } while (0)
+
+// Device error word bits (dr_context::d_error), set by kernels instead of
+// trapping; the host maps them to dr_status.
+enum : uint32_t {
+    ERR_STACK_OVERFLOW = 1u << 0,
+    ERR_TIMEOUT = 1u << 1,
+    ERR_BAD_INDEX = 1u << 2,
+};
+
+// ---- BVH layouts ----------------------------------------------------------------
+
+// Binary node in the layout of Aila and Laine ("Understanding the Efficiency of
+// Ray Traversal on GPUs", HPG 2009): both child boxes in one 64-byte record so
+// one node fetch tests two boxes.
+//   c0xy = (c0.lo.x, c0.hi.x, c0.lo.y, c0.hi.y)
+//   c1xy = (c1.lo.x, c1.hi.x, c1.lo.y, c1.hi.y)
+//   cz   = (c0.lo.z, c0.hi.z, c1.lo.z, c1.hi.z)
+//   link = (c0, c1, -, -): >= 0 inner node index; < 0 leaf = ~((first << 4) | count)
+struct alignas(16) Bvh2Node {
+    float4 c0xy, c1xy, cz;
+    int4 link;
+};
+static_assert(sizeof(Bvh2Node) == 64, "Bvh2Node must be 64 bytes");
+
+constexpr int kLeafCountBits = 4;
+constexpr uint32_t kMaxLeafSize = (1u << kLeafCountBits) - 1;  // 15
+constexpr uint32_t kMaxTriangles = 1u << (31 - kLeafCountBits); // 2^27
+constexpr int kStackSize = 64;                                  // traversal stack entries
+constexpr int kMaxBuildDepth = 60;                              // < kStackSize
+
+inline int32_t leaf_link(uint32_t first, uint32_t count) { return ~int32_t((first << kLeafCountBits) | count); }
+
+struct Bvh2 {
+    std::vector<Bvh2Node> nodes;
+    std::vector<uint32_t> order;  // leaf-order position -> original triangle index
+    int depth = 0;
+    float slack = 0.0f;
+};
+
+struct BuildParams {
+    uint32_t max_leaf = 4;
+    uint32_t bins = 32;
+    uint32_t threads = 0;
+};
+
+// Binned-SAH build (Wald, "On fast Construction of SAH-based Bounding Volume
+// Hierarchies", RT 2007) over a triangle soup. Child boxes are widened by
+// `slack` world units (rounded outward) so box culling is conservative with
+// respect to the FP32 triangle tests.
+Bvh2 build_bvh2(const float *positions, uint32_t num_tris, const BuildParams &p, float slack);
+
+// Conservative world-space widening for a scene whose largest absolute
+// coordinate is `mag`.
+float scene_slack(float mag);
+
+// Triangle records in leaf order.
+//   reference-compat (3 x float4): (A.xyz, n.x) (n.y, n.z, BA.x, BA.y) (BA.z, CA.xyz)
+//     n = normalize((A-B) x (A-C)) evaluated like the reference, or 0 when
+//     |n_f|^2 < 1e-14 (the reference rejects such triangles).
+//   watertight (3 x float4): (A.xyz, B.x) (B.yz, C.xy) (C.z, 0, 0, 0)
+void make_tri_records(const float *positions, const std::vector<uint32_t> &order,
+                      std::vector<float4> &ref_records, std::vector<float4> &wt_records);
+
+}  // namespace dr
+
+// ---- opaque handles ----------------------------------------------------------------
+
+struct dr_context {
+    int device = 0;
+    int num_sms = 0;
+    uint32_t *d_error = nullptr;                // device error word
+    unsigned long long *d_counters = nullptr;   // 8 counters
+    unsigned int *d_work = nullptr;             // persistent-kernel work counters (8)
+};
+
+struct dr_scene {
+    dr_context *ctx = nullptr;
+    uint32_t num_tris = 0;
+    uint32_t num_nodes = 0;
+    uint32_t depth = 0;
+    uint32_t layout = 2;
+    float slack = 0.0f;
+    double build_seconds = 0.0;
+    uint64_t device_bytes = 0;
+
+    dr::Bvh2Node *d_nodes = nullptr;
+    float4 *d_tri_ref = nullptr;
+    float4 *d_tri_wt = nullptr;
+    int32_t *d_prim = nullptr;      // leaf-order position -> original triangle index
+
+    // scene data for shading
+    uint32_t num_objects = 0, num_materials = 0;
+    dr_material *d_materials = nullptr;
+    float total_radiant_power = 0.0f;
+
+    // staging for the host-buffer entry points
+    void *d_stage_rays = nullptr;
+    void *d_stage_hits = nullptr;
+    uint64_t stage_capacity = 0;
+};

@@ -1,0 +1,27 @@
+// trace_kernels.cuh -- launch interface of the traversal kernels.
+#pragma once
+
+#include "dr_internal.h"
+
+namespace dr {
+
+constexpr int kTraceBlock = 128;
+
+struct TraceArgs {
+    const Bvh2Node *nodes;
+    const float4 *tri_ref;
+    const float4 *tri_wt;
+    const int32_t *prim;
+    uint32_t num_nodes;
+    const dr_ray *rays;
+    uint64_t n;
+    dr_hit *hits;          // closest hit
+    uint8_t *occluded;     // any hit
+    unsigned long long *counters;
+    uint32_t *error;
+};
+
+cudaError_t launch_trace_closest(const TraceArgs &a, int mode, bool count, cudaStream_t s);
+cudaError_t launch_trace_any(const TraceArgs &a, int mode, cudaStream_t s);
+
+}  // namespace dr

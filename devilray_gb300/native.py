@@ -1,0 +1,246 @@
+"""ctypes binding of ``libdevilray_gb300.so`` (the C ABI of include/devilray_gb300.h).
+
+The library is built in-tree by :mod:`devilray_gb300.build`. Loading fails
+loudly when it is missing: there is no CPU fallback for any entry point.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from . import build as _build
+
+LIB_PATH = _build.LIB
+
+DR_OK = 0
+STATUS_NAMES = {
+    0: "DR_OK", 1: "DR_ERR_INVALID_ARGUMENT", 2: "DR_ERR_CUDA", 3: "DR_ERR_OUT_OF_MEMORY",
+    4: "DR_ERR_NO_DEVICE", 5: "DR_ERR_TIMEOUT", 6: "DR_ERR_STACK_OVERFLOW", 7: "DR_ERR_UNSUPPORTED",
+    8: "DR_ERR_TOO_LARGE",
+}
+
+DR_TRI_REFERENCE = 0
+DR_TRI_WATERTIGHT = 1
+DR_MAT_DIFFUSE = 0
+DR_MAT_DIELECTRIC = 1
+
+RAY_DTYPE = np.dtype([("ox", "<f4"), ("oy", "<f4"), ("oz", "<f4"), ("tmax", "<f4"),
+                      ("dx", "<f4"), ("dy", "<f4"), ("dz", "<f4"), ("pad", "<f4")])
+HIT_DTYPE = np.dtype([("t", "<f4"), ("prim", "<i4")])
+
+
+class DrError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+class ContextConfig(C.Structure):
+    _fields_ = [("device", C.c_int32), ("flags", C.c_uint32)]
+
+
+class Material(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("ior", C.c_float), ("pad0", C.c_float), ("pad1", C.c_float),
+                ("emission", C.c_float * 4), ("albedo", C.c_float * 4), ("debug_color", C.c_float * 4)]
+
+
+class Object(C.Structure):
+    _fields_ = [("tri_begin", C.c_uint32), ("tri_count", C.c_uint32), ("material", C.c_int32),
+                ("surface_area", C.c_float)]
+
+
+class SceneDesc(C.Structure):
+    _fields_ = [("positions_host", C.c_void_p), ("num_triangles", C.c_uint32),
+                ("objects_host", C.c_void_p), ("num_objects", C.c_uint32),
+                ("materials_host", C.c_void_p), ("num_materials", C.c_uint32),
+                ("tri_material_host", C.c_void_p), ("tri_weight_host", C.c_void_p)]
+
+
+class BuildConfig(C.Structure):
+    _fields_ = [("max_leaf_size", C.c_uint32), ("sah_bins", C.c_uint32), ("threads", C.c_uint32),
+                ("layout", C.c_uint32)]
+
+
+class SceneInfo(C.Structure):
+    _fields_ = [("num_triangles", C.c_uint32), ("num_nodes", C.c_uint32), ("depth", C.c_uint32),
+                ("layout", C.c_uint32), ("slack", C.c_float), ("total_radiant_power", C.c_float),
+                ("device_bytes", C.c_uint64), ("build_seconds", C.c_double)]
+
+
+class TraceCounters(C.Structure):
+    _fields_ = [("rays", C.c_uint64), ("node_visits", C.c_uint64), ("box_tests", C.c_uint64),
+                ("tri_tests", C.c_uint64), ("hits", C.c_uint64)]
+
+
+# Every symbol the public header declares, with its ctypes signature.
+SIGNATURES = {
+    "dr_abi_version": (C.c_uint32, []),
+    "dr_last_error_string": (C.c_char_p, []),
+    "dr_context_create": (C.c_int, [C.POINTER(ContextConfig), C.POINTER(C.c_void_p)]),
+    "dr_context_destroy": (C.c_int, [C.c_void_p]),
+    "dr_context_check": (C.c_int, [C.c_void_p]),
+    "dr_scene_create": (C.c_int, [C.c_void_p, C.POINTER(SceneDesc), C.POINTER(BuildConfig), C.POINTER(C.c_void_p)]),
+    "dr_scene_destroy": (C.c_int, [C.c_void_p]),
+    "dr_scene_get_info": (C.c_int, [C.c_void_p, C.POINTER(SceneInfo)]),
+    "dr_trace_closest": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_int32,
+                                   C.POINTER(TraceCounters), C.c_void_p]),
+    "dr_trace_any": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_int32, C.c_void_p]),
+    "dr_trace_closest_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_int32, C.c_void_p]),
+}
+
+_lib = None
+
+
+def load(path: Path | str | None = None):
+    """Loads the library (building it first if it is absent)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        _build.build()
+    if not p.exists():
+        raise FileNotFoundError(f"{p} is missing: build the CUDA library first")
+    L = C.CDLL(str(p))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def check(status: int) -> None:
+    if status != DR_OK:
+        msg = load().dr_last_error_string()
+        raise DrError(status, msg.decode() if msg else "")
+
+
+def _ptr(a) -> int:
+    """Device or host address of a torch tensor / numpy array / int."""
+    if a is None:
+        return 0
+    if isinstance(a, int):
+        return a
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr()
+    return a.ctypes.data
+
+
+def _stream_ptr(stream) -> int | None:
+    if stream is None:
+        return None
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream
+
+
+class Context:
+    def __init__(self, device: int = 0):
+        L = load()
+        self.handle = C.c_void_p()
+        cfg = ContextConfig(device, 0)
+        check(L.dr_context_create(C.byref(cfg), C.byref(self.handle)))
+        self.device = device
+
+    def close(self):
+        if self.handle:
+            load().dr_context_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def check(self):
+        check(load().dr_context_check(self.handle))
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Scene:
+    """A triangle soup uploaded with its BVH (dr_scene_create)."""
+
+    def __init__(self, ctx: Context, positions: np.ndarray, objects=None, materials=None,
+                 tri_material=None, tri_weight=None, max_leaf_size: int = 0, sah_bins: int = 0,
+                 threads: int = 0):
+        self.ctx = ctx
+        self.positions = np.ascontiguousarray(positions, np.float32).reshape(-1, 9)
+        desc = SceneDesc()
+        desc.positions_host = self.positions.ctypes.data
+        desc.num_triangles = self.positions.shape[0]
+        keep = [self.positions]
+        if objects is not None:
+            objs = (Object * len(objects))(*objects)
+            keep.append(objs)
+            desc.objects_host = C.addressof(objs)
+            desc.num_objects = len(objects)
+        if materials is not None:
+            mats = (Material * len(materials))(*materials)
+            keep.append(mats)
+            desc.materials_host = C.addressof(mats)
+            desc.num_materials = len(materials)
+        if tri_material is not None:
+            tm = np.ascontiguousarray(tri_material, np.int32)
+            keep.append(tm)
+            desc.tri_material_host = tm.ctypes.data
+        if tri_weight is not None:
+            tw = np.ascontiguousarray(tri_weight, np.float32)
+            keep.append(tw)
+            desc.tri_weight_host = tw.ctypes.data
+        cfg = BuildConfig(max_leaf_size, sah_bins, threads, 0)
+        self.handle = C.c_void_p()
+        check(load().dr_scene_create(ctx.handle, C.byref(desc), C.byref(cfg), C.byref(self.handle)))
+        self._keep = keep
+
+    def info(self) -> SceneInfo:
+        info = SceneInfo()
+        check(load().dr_scene_get_info(self.handle, C.byref(info)))
+        return info
+
+    def close(self):
+        if self.handle:
+            load().dr_scene_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- traversal on device buffers (torch tensors or raw addresses) --
+    def trace_closest(self, rays_dev, n: int, hits_dev, tri_mode: int = DR_TRI_REFERENCE,
+                      counters: bool = False, stream=None):
+        cnt = TraceCounters() if counters else None
+        check(load().dr_trace_closest(self.handle, _ptr(rays_dev), n, _ptr(hits_dev), tri_mode,
+                                      C.byref(cnt) if cnt is not None else None, _stream_ptr(stream)))
+        return cnt
+
+    def trace_any(self, rays_dev, n: int, occluded_dev, tri_mode: int = DR_TRI_REFERENCE, stream=None):
+        check(load().dr_trace_any(self.handle, _ptr(rays_dev), n, _ptr(occluded_dev), tri_mode,
+                                  _stream_ptr(stream)))
+
+    # -- traversal on host buffers --
+    def trace_closest_host(self, rays: np.ndarray, hits: np.ndarray | None = None,
+                           tri_mode: int = DR_TRI_REFERENCE, stream=None) -> np.ndarray:
+        rays = np.ascontiguousarray(rays)
+        assert rays.dtype == RAY_DTYPE or (rays.dtype == np.float32 and rays.shape[-1] == 8)
+        n = rays.shape[0]
+        if hits is None:
+            hits = np.empty(n, HIT_DTYPE)
+        check(load().dr_trace_closest_host(self.handle, _ptr(rays), n, _ptr(hits), tri_mode,
+                                           _stream_ptr(stream)))
+        return hits
+
+
+def make_rays(origins: np.ndarray, dirs: np.ndarray, tmax=np.inf) -> np.ndarray:
+    """Packs origins/directions into the 32-byte dr_ray layout (float32 [n, 8])."""
+    n = origins.shape[0]
+    r = np.zeros((n, 8), np.float32)
+    r[:, 0:3] = origins
+    r[:, 3] = tmax
+    r[:, 4:7] = dirs
+    return r

@@ -1,0 +1,189 @@
+/*
+ * devilray_gb300.h -- C ABI of the GB300 path-tracing core.
+ *
+ * The drop-in boundary for DevilRay's hot path. DevilRay itself has no FFI: its
+ * plugin surface is the C++ classes Renderer / Scene / GpuTris and the
+ * DistributionSamplers functions. Each entry point below names the reference
+ * interface it replaces (file:line in the DevilRay tree). The C++ classes of
+ * include/devilray/ rebuild that class surface on top of these functions.
+ *
+ * Conventions
+ *   - Every call returns a dr_status; nothing throws across the ABI and nothing
+ *     calls exit() (DevilRay's CUDA_ERROR_CHECK exits: src/device/DevUtils.cu:12-22).
+ *     dr_last_error_string() describes the last failure of the calling thread.
+ *   - Pointers named *_dev are device pointers; *_host are host pointers.
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default stream).
+ *     Calls that take a stream are asynchronous unless stated otherwise.
+ *   - No CPU fallback: without a usable GPU, calls fail with DR_ERR_NO_DEVICE.
+ */
+#ifndef DEVILRAY_GB300_H
+#define DEVILRAY_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DR_ABI_VERSION 1
+
+typedef enum dr_status {
+    DR_OK = 0,
+    DR_ERR_INVALID_ARGUMENT = 1,
+    DR_ERR_CUDA = 2,
+    DR_ERR_OUT_OF_MEMORY = 3,
+    DR_ERR_NO_DEVICE = 4,
+    DR_ERR_TIMEOUT = 5,        /* a bounded device loop gave up (error word set) */
+    DR_ERR_STACK_OVERFLOW = 6, /* a traversal stack would have overflowed */
+    DR_ERR_UNSUPPORTED = 7,
+    DR_ERR_TOO_LARGE = 8
+} dr_status;
+
+/* Triangle test used by traversal. */
+typedef enum dr_tri_mode {
+    /* FP32 operation sequence of testTriangleIntersection
+     * (include/tracing/IntersectionTestsImpl.hpp:253-297): bit-identical t. */
+    DR_TRI_REFERENCE = 0,
+    /* Watertight test (Woop, Benthin, Wald, JCGT 2013), two-sided. */
+    DR_TRI_WATERTIGHT = 1
+} dr_tri_mode;
+
+/* Ray record, 32 bytes. A hit counts when its t <= tmax (use INFINITY for an
+ * unbounded ray, which is the reference's only kind: Ray, include/Utils.hpp:191). */
+typedef struct dr_ray {
+    float ox, oy, oz, tmax;
+    float dx, dy, dz, pad;
+} dr_ray;
+
+/* Closest-hit record, 8 bytes: prim is the triangle's index in the soup given
+ * to dr_scene_create (-1 and t = +INFINITY on a miss). Replaces the optional
+ * Intersection of getIntersection/cast (IntersectionTestsImpl.hpp:222-251),
+ * which carries no triangle index. Ties in t go to the smaller prim. */
+typedef struct dr_hit {
+    float t;
+    int32_t prim;
+} dr_hit;
+
+/* Per-call traversal counters (benchmark::HitTests, include/tracing/Benchmark.hpp:3-14). */
+typedef struct dr_trace_counters {
+    uint64_t rays;
+    uint64_t node_visits;    /* BVH nodes fetched */
+    uint64_t box_tests;      /* child boxes tested */
+    uint64_t tri_tests;      /* triangle tests */
+    uint64_t hits;
+} dr_trace_counters;
+
+/* ---- context ----------------------------------------------------------------- */
+
+typedef struct dr_context dr_context;
+
+typedef struct dr_context_config {
+    int32_t device;          /* CUDA ordinal */
+    uint32_t flags;          /* reserved, 0 */
+} dr_context_config;
+
+/* Binds a device and creates the per-context scratch (work counters, error word). */
+dr_status dr_context_create(const dr_context_config *cfg, dr_context **out);
+dr_status dr_context_destroy(dr_context *ctx);
+/* Reads and clears the device error word of the context (see dr_status). */
+dr_status dr_context_check(dr_context *ctx);
+
+/* ---- materials and scene --------------------------------------------------------- */
+
+/* Flat POD material, replacing the std::variant<TransparentMaterial, DiffuseMaterial>
+ * of include/tracing/Material.hpp:9-32. 64 bytes. */
+typedef enum dr_material_kind { DR_MAT_DIFFUSE = 0, DR_MAT_DIELECTRIC = 1 } dr_material_kind;
+typedef struct dr_material {
+    int32_t kind;            /* dr_material_kind */
+    float ior;               /* TransparentMaterial::inside_medium.ior (Medium.hpp:3-10) */
+    float pad0, pad1;
+    float emission[4];       /* DiffuseMaterial::emission */
+    float albedo[4];         /* DiffuseMaterial::diffuse_reflectance */
+    float debug_color[4];    /* BaseMaterial::debug_color */
+} dr_material;
+
+/* An object: a contiguous triangle range of the soup with one material, the
+ * flattened form of one TriangleMesh view (include/tracing/TriangleMesh.hpp:9-27).
+ * surface_area is TriangleMesh::surface_area (the light-power weight area). */
+typedef struct dr_object {
+    uint32_t tri_begin;
+    uint32_t tri_count;
+    int32_t material;
+    float surface_area;
+} dr_object;
+
+/* Scene description. positions: 9 floats per triangle (A, B, C) in world space
+ * (object transforms already applied). When objects is NULL the whole soup is
+ * one object using material 0. tri_material (optional) overrides the object's
+ * material per triangle. tri_weight (optional) is the per-triangle weight of
+ * the second-level light table (reference: triangle area, src/GpuTris.cpp:7-21). */
+typedef struct dr_scene_desc {
+    const float *positions_host;
+    uint32_t num_triangles;
+    const dr_object *objects_host;
+    uint32_t num_objects;
+    const dr_material *materials_host;
+    uint32_t num_materials;
+    const int32_t *tri_material_host;
+    const float *tri_weight_host;
+} dr_scene_desc;
+
+typedef struct dr_build_config {
+    uint32_t max_leaf_size;  /* 0 = default (tuned) */
+    uint32_t sah_bins;       /* 0 = default */
+    uint32_t threads;        /* host build threads, 0 = all cores */
+    uint32_t layout;         /* 0 = default, 2 = binary, 8 = compressed 8-wide */
+} dr_build_config;
+
+typedef struct dr_scene dr_scene;
+
+/* Builds the acceleration structure (binned-SAH, conservative boxes) on the
+ * host and uploads scene, BVH and light tables to the device. Replaces
+ * convertMeshToTris + generateSimpleBBH + viewGpuTris + Renderer::setScene /
+ * calculateLightWeights (src/GpuTris.cpp:5-85, src/models/BBH.cpp:101-115,
+ * src/Renderer.cpp:113-152). Synchronous. */
+dr_status dr_scene_create(dr_context *ctx, const dr_scene_desc *desc,
+                          const dr_build_config *cfg, dr_scene **out);
+dr_status dr_scene_destroy(dr_scene *scene);
+
+typedef struct dr_scene_info {
+    uint32_t num_triangles;
+    uint32_t num_nodes;
+    uint32_t depth;
+    uint32_t layout;
+    float slack;             /* world-space box widening used for conservative culling */
+    float total_radiant_power; /* ObjectsInfo::total_radiant_power (Scene.hpp:10-13) */
+    uint64_t device_bytes;
+    double build_seconds;
+} dr_scene_info;
+dr_status dr_scene_get_info(const dr_scene *scene, dr_scene_info *info);
+
+/* ---- traversal ------------------------------------------------------------------- */
+
+/* Closest hit for n rays (device buffers). Replaces cast / getIntersection
+ * (IntersectionTestsImpl.hpp:222-251) and the runRaycasts kernel
+ * (benchmark/src/benchmark.cu:16-55). counters_host may be NULL (no counting). */
+dr_status dr_trace_closest(dr_scene *scene, const dr_ray *rays_dev, uint64_t n, dr_hit *hits_dev,
+                           int32_t tri_mode, dr_trace_counters *counters_host, void *stream);
+
+/* Any hit with t <= tmax: occluded_dev[i] = 1 or 0. Replaces visible()
+ * (include/tracing/PathGeneration.hpp:213-224), which runs a full closest hit. */
+dr_status dr_trace_any(dr_scene *scene, const dr_ray *rays_dev, uint64_t n, uint8_t *occluded_dev,
+                       int32_t tri_mode, void *stream);
+
+/* Same as dr_trace_closest over HOST buffers: copies rays in and hits out through
+ * pinned staging on `stream`; returns after the hits are in hits_host. */
+dr_status dr_trace_closest_host(dr_scene *scene, const dr_ray *rays_host, uint64_t n, dr_hit *hits_host,
+                                int32_t tri_mode, void *stream);
+
+/* ---- version ----------------------------------------------------------------------- */
+
+uint32_t dr_abi_version(void);
+const char *dr_last_error_string(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DEVILRAY_GB300_H */

@@ -1,0 +1,109 @@
+/*
+ * oracle.h -- CPU restatement of DevilRay's tracing path (TEST INFRASTRUCTURE).
+ *
+ * This library is the checker for the GB300 kernels. Only the test suite,
+ * the smoke check and the CPU-baseline leg of the benchmark load it; the
+ * product library never links or calls it.
+ *
+ * Every function restates one reference function (file:line cited beside it,
+ * paths relative to the DevilRay source tree) in plain C++ compiled with
+ * -ffp-contract=off, so that FP32 results are bit-identical to the reference
+ * compiled the same way. The restatement is pinned against the reference
+ * itself (oracle/_ref harness, tests/golden fixtures).
+ */
+#ifndef DEVILRAY_ORACLE_H
+#define DEVILRAY_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- triangle / box tests ------------------------------------------------ */
+
+/* include/tracing/IntersectionTestsImpl.hpp:253-297 (testTriangleIntersection).
+ * ray = {px,py,pz,vx,vy,vz}, tri = {A,B,C}. Returns 1 on hit with
+ * out = {t, wA, wB, wC}. */
+int or_tri_test_ref(const float ray[6], const float tri[9], float out[4]);
+
+/* Watertight ray/triangle test (Woop, Benthin, Wald, JCGT 2013), two-sided,
+ * FP32 with the FP64 edge-function fallback of the paper. out = {t, wA, wB, wC}. */
+int or_tri_test_watertight(const float ray[6], const float tri[9], float out[4]);
+
+/* include/tracing/IntersectionTestsImpl.hpp:91-105 (testBoxIntersection). */
+int or_box_test_ref(const float box[6], const float ray[6], float *t_out);
+
+/* ---- median-split BBH (src/models/BBH.cpp:38-115) ------------------------ */
+
+typedef struct or_bbh or_bbh;
+
+/* Builds the reference BBH over a triangle soup (9 floats per triangle, triangle
+ * k owning vertices 3k..3k+2). `order` receives, for each sorted position, the
+ * original triangle index. */
+or_bbh *or_bbh_create(const float *positions, int32_t num_triangles);
+void or_bbh_destroy(or_bbh *h);
+int32_t or_bbh_num_nodes(const or_bbh *h);
+int32_t or_bbh_depth(const or_bbh *h);
+/* boxes: 6 floats per node; links: 5 ints per node {left,right,parent,begin,end};
+ * order: num_triangles ints. Any pointer may be NULL. */
+void or_bbh_export(const or_bbh *h, float *boxes, int32_t *links, int32_t *order);
+
+/* Closest hit, reference-exact: restates getIntersectionImpl
+ * (IntersectionTestsImpl.hpp:141-220) including its traversal order, its
+ * culling and its first-found tie rule. rays: 6 floats each. Outputs per ray:
+ * t (+inf on miss), prim (original triangle index, -1 on miss), optional
+ * counters (box tests, triangle tests; benchmark::HitTests, Benchmark.hpp:3-14).
+ * tri_mode: 0 = reference triangle test, 1 = watertight. */
+void or_bbh_trace_reference(const or_bbh *h, const float *rays, int64_t num_rays,
+                            float *t_out, int32_t *prim_out,
+                            int64_t *box_tests, int64_t *tri_tests,
+                            int32_t tri_mode, int32_t threads);
+
+/* Closest hit, canonical semantics shared with the GPU kernels: the minimum t
+ * over all triangles (reference triangle test or watertight test), ties broken
+ * by the smaller original triangle index; a hit counts when t <= tmax.
+ * Implemented as a conservative traversal of the BBH (boxes widened by
+ * `slack` world units) so it equals a brute-force scan. rays: 8 floats each
+ * {ox,oy,oz,tmax,dx,dy,dz,pad} (the dr_ray layout). */
+void or_bbh_trace_canonical(const or_bbh *h, const float *rays8, int64_t num_rays,
+                            float slack, float *t_out, int32_t *prim_out,
+                            int32_t tri_mode, int32_t threads);
+
+/* Any hit with t <= tmax (same test semantics): occluded[i] = 1 or 0. */
+void or_bbh_trace_any(const or_bbh *h, const float *rays8, int64_t num_rays,
+                      float slack, uint8_t *occluded, int32_t tri_mode, int32_t threads);
+
+/* Brute force over a soup, canonical semantics. */
+void or_trace_brute(const float *positions, int32_t num_triangles,
+                    const float *rays8, int64_t num_rays,
+                    float *t_out, int32_t *prim_out, int32_t tri_mode, int32_t threads);
+
+/* ---- alias tables (src/DistributionSamplers.cpp:39-149) ------------------ */
+
+/* AliasEntry layout of include/tracing/DistributionSamplers.hpp:44-51. */
+typedef struct or_alias_entry { float p_A, pdf_A, pdf_B; int32_t A, B; } or_alias_entry;
+
+/* generateAliasTable restated with the same std::priority_queue pairing. */
+void or_alias_build_ref(const float *weights, int32_t n, or_alias_entry *out);
+
+/* Sweep-pairing build restated on the CPU; the device's parallel build must
+ * match it bit for bit (see the product's alias kernels). */
+void or_alias_build_sweep(const float *weights, int32_t n, or_alias_entry *out);
+
+/* sample(), DistributionSamplers.hpp:64-88, given the two uniforms. */
+void or_alias_sample(const or_alias_entry *table, int32_t n, float u0, float u1,
+                     int32_t *index, float *pdf);
+
+/* The StressTest input of test/src/test_alias.cpp:193-229:
+ * std::mt19937(seed) + std::lognormal_distribution<float>(0,1). */
+void or_lognormal_input(int32_t n, uint32_t seed, float *out);
+
+/* ---- Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) ------------------- */
+void or_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,283 @@
+"""ctypes bindings of the CPU oracle and of the reference harness.
+
+TEST INFRASTRUCTURE. Only the tests, ``__graft_entry__.smoke()`` and the
+CPU-baseline leg of ``bench.py`` import this module; the product package never
+does. ``liboracle.so`` is the CPU restatement of DevilRay's tracing path;
+``libref_harness.so`` (built only where the DevilRay sources exist) calls the
+reference's own host code and pins the restatement.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ORACLE_SO = HERE / "lib" / "liboracle.so"
+REF_SO = HERE / "_ref" / "libref_harness.so"
+REF_ROOT = Path(os.environ.get("DEVILRAY_REF_ROOT", "/root/reference"))
+
+_f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+_i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+_i64p = np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")
+_u8p = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
+_u32p = np.ctypeslib.ndpointer(np.uint32, flags="C_CONTIGUOUS")
+
+ALIAS_DTYPE = np.dtype([("p_A", "<f4"), ("pdf_A", "<f4"), ("pdf_B", "<f4"), ("A", "<i4"), ("B", "<i4")])
+
+
+def build(ref: bool | None = None, quiet: bool = True) -> None:
+    """Compiles liboracle.so (and the reference harness when the sources exist)."""
+    targets = ["all"]
+    if ref is None:
+        ref = (REF_ROOT / "include" / "Utils.hpp").exists()
+    if ref:
+        targets.append("ref")
+    out = subprocess.run(["make", "-C", str(HERE), f"REF_ROOT={REF_ROOT}", "-j4", *targets],
+                         capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError(f"oracle build failed:\n{out.stdout}\n{out.stderr}")
+
+
+_lib = None
+_ref = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not ORACLE_SO.exists():
+            build(ref=False)
+        L = C.CDLL(str(ORACLE_SO))
+        L.or_tri_test_ref.argtypes = [_f32p, _f32p, _f32p]
+        L.or_tri_test_watertight.argtypes = [_f32p, _f32p, _f32p]
+        L.or_box_test_ref.argtypes = [_f32p, _f32p, _f32p]
+        L.or_bbh_create.argtypes = [_f32p, C.c_int32]
+        L.or_bbh_create.restype = C.c_void_p
+        L.or_bbh_destroy.argtypes = [C.c_void_p]
+        L.or_bbh_num_nodes.argtypes = [C.c_void_p]
+        L.or_bbh_depth.argtypes = [C.c_void_p]
+        L.or_bbh_export.argtypes = [C.c_void_p, _f32p, _i32p, _i32p]
+        L.or_bbh_trace_reference.argtypes = [C.c_void_p, _f32p, C.c_int64, _f32p, _i32p, _i64p, _i64p,
+                                             C.c_int32, C.c_int32]
+        L.or_bbh_trace_canonical.argtypes = [C.c_void_p, _f32p, C.c_int64, C.c_float, _f32p, _i32p,
+                                             C.c_int32, C.c_int32]
+        L.or_bbh_trace_any.argtypes = [C.c_void_p, _f32p, C.c_int64, C.c_float, _u8p, C.c_int32, C.c_int32]
+        L.or_trace_brute.argtypes = [_f32p, C.c_int32, _f32p, C.c_int64, _f32p, _i32p, C.c_int32, C.c_int32]
+        L.or_alias_build_ref.argtypes = [_f32p, C.c_int32, C.c_void_p]
+        L.or_alias_build_sweep.argtypes = [_f32p, C.c_int32, C.c_void_p]
+        L.or_alias_sample.argtypes = [C.c_void_p, C.c_int32, C.c_float, C.c_float,
+                                      C.POINTER(C.c_int32), C.POINTER(C.c_float)]
+        L.or_lognormal_input.argtypes = [C.c_int32, C.c_uint32, _f32p]
+        L.or_philox4x32_10.argtypes = [_u32p, _u32p, _u32p]
+        _lib = L
+    return _lib
+
+
+def ref_available() -> bool:
+    return REF_SO.exists()
+
+
+def ref():
+    """The harness over the reference's own code (only where it was built)."""
+    global _ref
+    if _ref is None:
+        if not REF_SO.exists():
+            raise FileNotFoundError("reference harness not built (needs the DevilRay sources)")
+        L = C.CDLL(str(REF_SO))
+        L.refh_tri_test.argtypes = [_f32p, _f32p, _f32p]
+        L.refh_box_test.argtypes = [_f32p, _f32p, _f32p]
+        L.refh_bbh_create.argtypes = [_f32p, C.c_int]
+        L.refh_bbh_create.restype = C.c_void_p
+        L.refh_bbh_destroy.argtypes = [C.c_void_p]
+        L.refh_bbh_num_nodes.argtypes = [C.c_void_p]
+        L.refh_bbh_depth.argtypes = [C.c_void_p]
+        L.refh_bbh_export.argtypes = [C.c_void_p, _f32p, _i32p, _i32p]
+        L.refh_bbh_trace.argtypes = [C.c_void_p, _f32p, C.c_int, _f32p, _i32p, C.c_void_p, C.c_void_p,
+                                     _i64p, _i64p]
+        L.refh_alias_build.argtypes = [_f32p, C.c_int, _f32p, _f32p, _f32p, _i32p, _i32p]
+        L.refh_alias_sample.argtypes = [_f32p, _f32p, _f32p, _i32p, _i32p, C.c_int, _f32p, C.c_int, _i32p, _f32p]
+        L.refh_lognormal.argtypes = [C.c_int, C.c_uint, _f32p]
+        L.refh_sphere_sample.argtypes = [_f32p, C.c_int, _f32p]
+        L.refh_cosine_sample.argtypes = [_f32p, _f32p, C.c_int, _f32p]
+        L.refh_camera_ray.argtypes = [_f32p, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float,
+                                      C.c_float, C.c_float, C.c_int, _f32p, _f32p]
+        _ref = L
+    return _ref
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+# ---- oracle wrappers ---------------------------------------------------------
+
+def tri_test(ray6, tri9, mode: int = 0):
+    out = np.zeros(4, np.float32)
+    fn = lib().or_tri_test_watertight if mode == 1 else lib().or_tri_test_ref
+    hit = fn(_f32(ray6), _f32(tri9), out)
+    return (bool(hit), out)
+
+
+def box_test(box6, ray6):
+    out = np.zeros(1, np.float32)
+    hit = lib().or_box_test_ref(_f32(box6), _f32(ray6), out)
+    return bool(hit), float(out[0])
+
+
+class BBH:
+    """The reference's median-split BBH (src/models/BBH.cpp) over a soup."""
+
+    def __init__(self, positions: np.ndarray):
+        self.positions = _f32(positions).reshape(-1, 9)
+        self.ntri = self.positions.shape[0]
+        self.h = lib().or_bbh_create(self.positions.reshape(-1), self.ntri)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().or_bbh_destroy(self.h)
+            self.h = None
+
+    @property
+    def num_nodes(self) -> int:
+        return lib().or_bbh_num_nodes(self.h)
+
+    @property
+    def depth(self) -> int:
+        return lib().or_bbh_depth(self.h)
+
+    def export(self):
+        n = self.num_nodes
+        boxes = np.zeros((n, 6), np.float32)
+        links = np.zeros((n, 5), np.int32)
+        order = np.zeros(self.ntri, np.int32)
+        lib().or_bbh_export(self.h, boxes.reshape(-1), links.reshape(-1), order)
+        return boxes, links, order
+
+    def trace_reference(self, rays6: np.ndarray, tri_mode: int = 0, threads: int = 0):
+        rays6 = _f32(rays6).reshape(-1, 6)
+        n = rays6.shape[0]
+        t = np.zeros(n, np.float32)
+        prim = np.zeros(n, np.int32)
+        nb = np.zeros(n, np.int64)
+        nt = np.zeros(n, np.int64)
+        lib().or_bbh_trace_reference(self.h, rays6.reshape(-1), n, t, prim, nb, nt, tri_mode, threads)
+        return t, prim, nb, nt
+
+    def trace_canonical(self, rays8: np.ndarray, slack: float, tri_mode: int = 0, threads: int = 0):
+        rays8 = _f32(rays8).reshape(-1, 8)
+        n = rays8.shape[0]
+        t = np.zeros(n, np.float32)
+        prim = np.zeros(n, np.int32)
+        lib().or_bbh_trace_canonical(self.h, rays8.reshape(-1), n, slack, t, prim, tri_mode, threads)
+        return t, prim
+
+    def trace_any(self, rays8: np.ndarray, slack: float, tri_mode: int = 0, threads: int = 0):
+        rays8 = _f32(rays8).reshape(-1, 8)
+        n = rays8.shape[0]
+        occ = np.zeros(n, np.uint8)
+        lib().or_bbh_trace_any(self.h, rays8.reshape(-1), n, slack, occ, tri_mode, threads)
+        return occ
+
+
+def trace_brute(positions, rays8, tri_mode: int = 0, threads: int = 0):
+    positions = _f32(positions).reshape(-1)
+    rays8 = _f32(rays8).reshape(-1, 8)
+    n = rays8.shape[0]
+    t = np.zeros(n, np.float32)
+    prim = np.zeros(n, np.int32)
+    lib().or_trace_brute(positions, positions.size // 9, rays8.reshape(-1), n, t, prim, tri_mode, threads)
+    return t, prim
+
+
+def alias_build_ref(weights) -> np.ndarray:
+    w = _f32(weights)
+    out = np.zeros(w.size, ALIAS_DTYPE)
+    lib().or_alias_build_ref(w, w.size, out.ctypes.data)
+    return out
+
+
+def alias_build_sweep(weights) -> np.ndarray:
+    w = _f32(weights)
+    out = np.zeros(w.size, ALIAS_DTYPE)
+    lib().or_alias_build_sweep(w, w.size, out.ctypes.data)
+    return out
+
+
+def alias_sample(table: np.ndarray, u0: float, u1: float):
+    idx = C.c_int32()
+    pdf = C.c_float()
+    lib().or_alias_sample(table.ctypes.data, table.size, u0, u1, C.byref(idx), C.byref(pdf))
+    return idx.value, pdf.value
+
+
+def lognormal_input(n: int, seed: int = 42) -> np.ndarray:
+    out = np.zeros(n, np.float32)
+    lib().or_lognormal_input(n, seed, out)
+    return out
+
+
+def philox(ctr, key) -> np.ndarray:
+    out = np.zeros(4, np.uint32)
+    lib().or_philox4x32_10(np.ascontiguousarray(ctr, np.uint32), np.ascontiguousarray(key, np.uint32), out)
+    return out
+
+
+# ---- reference harness wrappers ------------------------------------------------
+
+def ref_tri_test(ray6, tri9):
+    out = np.zeros(4, np.float32)
+    hit = ref().refh_tri_test(_f32(ray6), _f32(tri9), out)
+    return bool(hit), out
+
+
+def ref_box_test(box6, ray6):
+    out = np.zeros(1, np.float32)
+    hit = ref().refh_box_test(_f32(box6), _f32(ray6), out)
+    return bool(hit), float(out[0])
+
+
+def ref_bbh_trace(positions, rays6):
+    positions = _f32(positions).reshape(-1)
+    ntri = positions.size // 9
+    h = ref().refh_bbh_create(positions, ntri)
+    try:
+        rays6 = _f32(rays6).reshape(-1, 6)
+        n = rays6.shape[0]
+        t = np.zeros(n, np.float32)
+        prim = np.zeros(n, np.int32)
+        nrm = np.zeros((n, 3), np.float32)
+        area = np.zeros(n, np.float32)
+        nb = np.zeros(n, np.int64)
+        nt = np.zeros(n, np.int64)
+        ref().refh_bbh_trace(h, rays6.reshape(-1), n, t, prim, nrm.ctypes.data, area.ctypes.data, nb, nt)
+        nn = ref().refh_bbh_num_nodes(h)
+        boxes = np.zeros((nn, 6), np.float32)
+        links = np.zeros((nn, 5), np.int32)
+        order = np.zeros(ntri, np.int32)
+        ref().refh_bbh_export(h, boxes.reshape(-1), links.reshape(-1), order)
+        depth = ref().refh_bbh_depth(h)
+    finally:
+        ref().refh_bbh_destroy(h)
+    return dict(t=t, prim=prim, normal=nrm, area=area, box_tests=nb, tri_tests=nt,
+                boxes=boxes, links=links, order=order, depth=depth)
+
+
+def ref_alias_build(weights) -> np.ndarray:
+    w = _f32(weights)
+    n = w.size
+    pA, pdfA, pdfB = (np.zeros(n, np.float32) for _ in range(3))
+    A, B = np.zeros(n, np.int32), np.zeros(n, np.int32)
+    ref().refh_alias_build(w, n, pA, pdfA, pdfB, A, B)
+    out = np.zeros(n, ALIAS_DTYPE)
+    out["p_A"], out["pdf_A"], out["pdf_B"], out["A"], out["B"] = pA, pdfA, pdfB, A, B
+    return out
+
+
+def ref_lognormal(n: int, seed: int = 42) -> np.ndarray:
+    out = np.zeros(n, np.float32)
+    ref().refh_lognormal(n, seed, out)
+    return out

@@ -1,0 +1,238 @@
+// ref_harness.cpp -- thin C entry points over DevilRay's OWN host code
+// (TEST INFRASTRUCTURE). Compiled by oracle/Makefile directly against the
+// reference headers and sources where they lie; its output library goes to
+// oracle/_ref/ and is used only to pin the oracle restatement and to write the
+// golden fixtures under tests/golden/. Nothing here re-implements the
+// reference: every result comes from calling the reference function named.
+
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <numbers>
+#include <random>
+#include <vector>
+
+#include "tracing/Camera.hpp"  // must precede PathGeneration.hpp (src/device/implementation.cu:6-8)
+#include "tracing/PathGeneration.hpp"
+#include "tracing/IntersectionTestsImpl.hpp"
+#include "tracing/LightSampling.hpp"
+#include "tracing/DistributionSamplers.hpp"
+#include "models/BBH.hpp"
+
+// Replays caller-provided uniforms through the `.rnd()` interface the
+// reference samplers are templated on (test/src/TracingTestHelpers.hpp:45-57).
+struct ReplayRng {
+    const float *values;
+    size_t count;
+    size_t cursor = 0;
+    float rnd()
+    {
+        const float v = values[cursor < count ? cursor : count - 1];
+        ++cursor;
+        return v;
+    }
+};
+
+namespace {
+struct RefBBH {
+    Mesh mesh;
+    BBH bbh;
+    int ntri;
+};
+
+TriangleMesh hostView(RefBBH &h)
+{
+    // test/src/TracingTestHelpers.hpp:69-83
+    TriangleMesh object{};
+    object.points = h.mesh.points.data();
+    object.normals = h.mesh.normals.data();
+    object.triangles = h.mesh.triangles.data();
+    object.triangle_count = static_cast<int>(h.mesh.triangles.size());
+    object.model_to_world = Transform{};
+    object.material = 0;
+    object.triangle_sampler = nullptr;
+    object.surface_area = 0;
+    object.base_surface_area = 0;
+    object.bbh = BBHGpuView{std::span<const BBHNode>{h.bbh.nodes.hostPtr(), h.bbh.nodes.size()}};
+    return object;
+}
+}  // namespace
+
+extern "C" {
+
+int refh_tri_test(const float ray[6], const float tri[9], float out[4])
+{
+    const Ray r{.p = {ray[0], ray[1], ray[2]}, .v = {ray[3], ray[4], ray[5]}};
+    const TriangleVertices t{{tri[0], tri[1], tri[2]}, {tri[3], tri[4], tri[5]}, {tri[6], tri[7], tri[8]}};
+    const auto hit = testTriangleIntersection(r, t);
+    if (!hit.has_value()) return 0;
+    out[0] = hit->t;
+    out[1] = hit->bari.x;
+    out[2] = hit->bari.y;
+    out[3] = hit->bari.z;
+    return 1;
+}
+
+int refh_box_test(const float box[6], const float ray[6], float *t)
+{
+    const AABB b{.min = {box[0], box[1], box[2]}, .max = {box[3], box[4], box[5]}};
+    const Ray r{.p = {ray[0], ray[1], ray[2]}, .v = {ray[3], ray[4], ray[5]}};
+    const auto hit = testBoxIntersection(b, r);
+    if (!hit.has_value()) return 0;
+    *t = *hit;
+    return 1;
+}
+
+// Soup -> Mesh with triangle k owning points 3k..3k+2 and normal index k (the
+// traversal never reads normal indices, so ni carries the original id through
+// generateSimpleBBH's in-place sort).
+void *refh_bbh_create(const float *pos, int ntri)
+{
+    auto *h = new RefBBH{Mesh{}, BBH{0, DeviceVector<BBHNode>{{}}}, ntri};
+    h->mesh.name = "soup";
+    for (int k = 0; k < ntri; ++k) {
+        for (int j = 0; j < 3; ++j)
+            h->mesh.points.push_back(Vec3{pos[k * 9 + j * 3], pos[k * 9 + j * 3 + 1], pos[k * 9 + j * 3 + 2]});
+        h->mesh.normals.push_back(Vec3{0, 0, 1});
+        const uint32_t b = 3u * k;
+        h->mesh.triangles.push_back(Triangle{.a = {b, (uint32_t)k}, .b = {b + 1, (uint32_t)k}, .c = {b + 2, (uint32_t)k}});
+    }
+    h->bbh = generateSimpleBBH(h->mesh);
+    return h;
+}
+
+void refh_bbh_destroy(void *p) { delete static_cast<RefBBH *>(p); }
+
+int refh_bbh_num_nodes(void *p) { return (int)static_cast<RefBBH *>(p)->bbh.nodes.size(); }
+int refh_bbh_depth(void *p) { return static_cast<RefBBH *>(p)->bbh.depth; }
+
+void refh_bbh_export(void *p, float *boxes, int *links, int *order)
+{
+    auto *h = static_cast<RefBBH *>(p);
+    const BBHNode *nodes = h->bbh.nodes.hostPtr();
+    for (size_t i = 0; i < h->bbh.nodes.size(); ++i) {
+        const auto &n = nodes[i];
+        const float b[6] = {n.box.min.x, n.box.min.y, n.box.min.z, n.box.max.x, n.box.max.y, n.box.max.z};
+        std::memcpy(boxes + i * 6, b, sizeof(b));
+        links[i * 5 + 0] = n.left_child;
+        links[i * 5 + 1] = n.right_child;
+        links[i * 5 + 2] = n.parent_index;
+        links[i * 5 + 3] = n.tris_begin;
+        links[i * 5 + 4] = n.tris_end;
+    }
+    for (int i = 0; i < h->ntri; ++i) order[i] = (int)h->mesh.triangles[i].a.ni;
+}
+
+// getIntersectionBenchmark on every ray. The original triangle index of a hit
+// is recovered as the unique triangle whose reference test reproduces the hit's
+// t and barycentrics bit for bit; -2 marks an ambiguous (tied) recovery.
+void refh_bbh_trace(void *p, const float *rays, int nray, float *t_out, int *id_out,
+                    float *n_out, float *area_out, int64_t *box_tests, int64_t *tri_tests)
+{
+    auto *h = static_cast<RefBBH *>(p);
+    const TriangleMesh view = hostView(*h);
+    for (int r = 0; r < nray; ++r) {
+        const Ray ray{.p = {rays[r * 6], rays[r * 6 + 1], rays[r * 6 + 2]},
+                      .v = {rays[r * 6 + 3], rays[r * 6 + 4], rays[r * 6 + 5]}};
+        benchmark::HitTests counts;
+        const auto hit = getIntersectionBenchmark(ray, view, counts);
+        box_tests[r] = counts.bbox_tests;
+        tri_tests[r] = counts.triangle_tests;
+        if (!hit.has_value()) {
+            t_out[r] = std::numeric_limits<float>::infinity();
+            id_out[r] = -1;
+            continue;
+        }
+        t_out[r] = hit->t;
+        if (n_out) {
+            n_out[r * 3] = hit->n.x;
+            n_out[r * 3 + 1] = hit->n.y;
+            n_out[r * 3 + 2] = hit->n.z;
+        }
+        if (area_out) area_out[r] = hit->triangle.area;
+        int found = -1;
+        for (int i = 0; i < h->ntri; ++i) {
+            const auto &tri = h->mesh.triangles[i];
+            const TriangleVertices tv{h->mesh.points[tri.a.pi], h->mesh.points[tri.b.pi], h->mesh.points[tri.c.pi]};
+            const auto c = testTriangleIntersection(ray, tv);
+            if (!c.has_value()) continue;
+            if (std::memcmp(&c->t, &hit->t, 4) == 0 && std::memcmp(&c->bari, &hit->triangle.bari, 12) == 0) {
+                found = found == -1 ? (int)tri.a.ni : -2;
+            }
+        }
+        id_out[r] = found;
+    }
+}
+
+// generateAliasTable on the given weights.
+void refh_alias_build(const float *w, int n, float *pA, float *pdfA, float *pdfB, int *A, int *B)
+{
+    const AliasTable table = generateAliasTable(std::span<const float>{w, static_cast<size_t>(n)});
+    const AliasEntry *e = table.entries.hostPtr();
+    for (int i = 0; i < n; ++i) {
+        pA[i] = e[i].p_A;
+        pdfA[i] = e[i].pdf_A;
+        pdfB[i] = e[i].pdf_B;
+        A[i] = e[i].A;
+        B[i] = e[i].B;
+    }
+}
+
+// sample() over a table given as struct-of-arrays, with replayed uniforms.
+void refh_alias_sample(const float *pA, const float *pdfA, const float *pdfB, const int *A, const int *B,
+                       int n, const float *uniforms, int ndraw, int *idx_out, float *pdf_out)
+{
+    std::vector<AliasEntry> t(n);
+    for (int i = 0; i < n; ++i) t[i] = AliasEntry{pA[i], pdfA[i], pdfB[i], A[i], B[i]};
+    ReplayRng rng{uniforms, (size_t)ndraw * 2};
+    for (int d = 0; d < ndraw; ++d) {
+        const auto s = sample(std::span<const AliasEntry>{t}, rng);
+        idx_out[d] = s.index;
+        pdf_out[d] = s.pdf;
+    }
+}
+
+// The 200,000-weight lognormal input of test/src/test_alias.cpp:193-229.
+void refh_lognormal(int n, unsigned seed, float *out)
+{
+    std::mt19937 rng(seed);
+    std::lognormal_distribution<float> dist(0.0f, 1.0f);
+    for (int i = 0; i < n; ++i) out[i] = dist(rng);
+}
+
+// uniformSphereSample / cosineWeightedHemisphereSample / uniformTriangleSample
+// (DistributionSamplers.hpp:8-42, 92-104) with replayed uniforms.
+void refh_sphere_sample(const float *u, int n, float *out)
+{
+    ReplayRng rng{u, (size_t)n * 2};
+    for (int i = 0; i < n; ++i) {
+        const Vec3 v = uniformSphereSample(rng);
+        out[i * 3] = v.x; out[i * 3 + 1] = v.y; out[i * 3 + 2] = v.z;
+    }
+}
+
+void refh_cosine_sample(const float *normal, const float *u, int n, float *out)
+{
+    ReplayRng rng{u, (size_t)n * 2};
+    const Vec3 nn{normal[0], normal[1], normal[2]};
+    for (int i = 0; i < n; ++i) {
+        const Vec3 v = cosineWeightedHemisphereSample(nn, rng);
+        out[i * 3] = v.x; out[i * 3 + 1] = v.y; out[i * 3 + 2] = v.z;
+    }
+}
+
+// cameraRay (include/tracing/CameraRay.hpp:6-34) for a row-major 4x4 transform.
+void refh_camera_ray(const float *m16, float focal, float cx, float cy, float psx, float psy,
+                     float px, float py, int sampling, const float *u, float *ray_out)
+{
+    Camera cam{};
+    std::memcpy(cam.transform.values, m16, sizeof(float) * 16);
+    cam.intrinsics = Intrinsics{.focal_length = focal, .center = Vec2f{cx, cy}};
+    cam.physical_pixel_size = Size2f{psx, psy};
+    ReplayRng rng{u, 2};
+    const Ray r = cameraRay(cam, Vec2f{px, py}, static_cast<PixelSampling>(sampling), 0, rng);
+    ray_out[0] = r.p.x; ray_out[1] = r.p.y; ray_out[2] = r.p.z;
+    ray_out[3] = r.v.x; ray_out[4] = r.v.y; ray_out[5] = r.v.z;
+}
+
+}  // extern "C"

@@ -1,0 +1,168 @@
+"""GPU traversal parity through the C ABI.
+
+Closest hit: the GPU's (t, prim) must equal the oracle's canonical closest hit
+bit for bit (smallest t of the reference triangle test over the soup, ties to
+the smaller triangle index), and the reference's own traversal on the golden
+fixture. Any hit: the occlusion flag must equal the oracle's.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from devilray_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def _bits(a):
+    return np.ascontiguousarray(a, np.float32).view(np.uint32)
+
+
+def gpu_closest(native, scene, rays8, mode=0, counters=False):
+    r = torch.from_numpy(np.ascontiguousarray(rays8, np.float32)).cuda()
+    hits = torch.empty((len(rays8), 2), dtype=torch.int32, device="cuda")
+    cnt = scene.trace_closest(r, len(rays8), hits, mode, counters=counters)
+    torch.cuda.synchronize()
+    h = hits.cpu().numpy()
+    return h[:, 0].copy().view(np.float32), h[:, 1].copy(), cnt
+
+
+def gpu_any(native, scene, rays8, mode=0):
+    r = torch.from_numpy(np.ascontiguousarray(rays8, np.float32)).cuda()
+    occ = torch.empty(len(rays8), dtype=torch.uint8, device="cuda")
+    scene.trace_any(r, len(rays8), occ, mode)
+    torch.cuda.synchronize()
+    return occ.cpu().numpy()
+
+
+def rays8_from6(r6, tmax=np.inf):
+    r8 = np.zeros((len(r6), 8), np.float32)
+    r8[:, 0:3], r8[:, 3], r8[:, 4:7] = r6[:, 0:3], tmax, r6[:, 3:6]
+    return r8
+
+
+def test_closest_hit_matches_reference_fixture(native, ctx, oracle, golden):
+    g = golden("bbh_trace.npz")
+    scene = native.Scene(ctx, g["soup"])
+    r8 = rays8_from6(g["rays6"])
+    t, prim, _ = gpu_closest(native, scene, r8)
+    assert np.array_equal(_bits(t), _bits(g["t"])), "t differs from the reference's getIntersection"
+    ok = g["prim"] != -2
+    assert np.array_equal(prim[ok], g["prim"][ok])
+    b = oracle.BBH(g["soup"])
+    tc, pc = b.trace_canonical(r8, slack=scene.info().slack)
+    assert np.array_equal(_bits(t), _bits(tc)) and np.array_equal(prim, pc)
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+@pytest.mark.parametrize("ntri,nray,leaf", [(1, 4096, 0), (37, 20000, 1), (5000, 100000, 0), (65536, 262144, 0),
+                                            (65536, 262144, 8)])
+def test_closest_hit_bit_exact_vs_oracle(native, ctx, oracle, mode, ntri, nray, leaf):
+    half = max(1.0, scenes.density_half(ntri))
+    soup, _, _ = scenes.incoherent_soup(ntri, seed=ntri, half=half)
+    rays = scenes.incoherent_rays(nray, seed=nray, half=half)
+    scene = native.Scene(ctx, soup, max_leaf_size=leaf)
+    t, prim, _ = gpu_closest(native, scene, rays, mode)
+    b = oracle.BBH(soup)
+    tc, pc = b.trace_canonical(rays, slack=scene.info().slack, tri_mode=mode)
+    assert (pc >= 0).sum() > 0 or ntri == 1
+    mism = np.flatnonzero((_bits(t) != _bits(tc)) | (prim != pc))
+    assert mism.size == 0, f"{mism.size} mismatches, first {mism[:5]}: gpu {t[mism[:5]]},{prim[mism[:5]]} oracle {tc[mism[:5]]},{pc[mism[:5]]}"
+
+
+def test_closest_hit_brute_force_small(native, ctx, oracle):
+    half = scenes.density_half(2000)
+    soup, _, _ = scenes.incoherent_soup(2000, seed=5, half=half)
+    rays = scenes.incoherent_rays(20000, seed=6, half=half)
+    scene = native.Scene(ctx, soup)
+    t, prim, _ = gpu_closest(native, scene, rays)
+    tb, pb = oracle.trace_brute(soup, rays)
+    assert np.array_equal(_bits(t), _bits(tb)) and np.array_equal(prim, pb)
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_any_hit_matches_oracle(native, ctx, oracle, mode):
+    half = scenes.density_half(30000)
+    soup, _, _ = scenes.incoherent_soup(30000, seed=9, half=half)
+    rays = scenes.incoherent_rays(200000, seed=10, half=half)
+    rng = np.random.default_rng(1)
+    rays[:, 3] = rng.uniform(0, 40, len(rays)).astype(np.float32)
+    scene = native.Scene(ctx, soup)
+    occ = gpu_any(native, scene, rays, mode)
+    b = oracle.BBH(soup)
+    occ_o = b.trace_any(rays, slack=scene.info().slack, tri_mode=mode)
+    assert np.array_equal(occ, occ_o)
+    t, prim, _ = gpu_closest(native, scene, rays, mode)
+    assert np.array_equal(occ.astype(bool), prim >= 0)  # closest hit honours tmax too
+    assert 0.05 < occ.mean() < 0.95
+
+
+def test_edge_cases(native, ctx, oracle):
+    unit = np.array([[0, 0, 0, 1, 0, 0, 0, 1, 0]], np.float32)
+    degenerate = np.array([[0, 0, 0, 0, 0, 0, 0, 0, 0], [0, 0, 0, 1, 0, 0, 2, 0, 0]], np.float32)
+    dup = np.concatenate([unit, unit, unit + np.float32([0, 0, -1] * 3)])
+    quad = np.array([[-1, -1, 0, 1, -1, 0, 1, 1, 0], [-1, -1, 0, 1, 1, 0, -1, 1, 0]], np.float32)
+    soup = np.concatenate([degenerate, dup, quad + np.float32([5, 0, 0] * 3)])
+    r6 = np.array([
+        [0.2, 0.2, 5, 0, 0, -1],       # hits the duplicated unit triangle -> smaller index wins
+        [0.2, 0.2, -5, 0, 0, 1],       # from below: the lower copy first
+        [0, 0, 10, 0, 0, -1],          # on a vertex
+        [5.0, 0.0, 3, 0, 0, -1],       # on the shared diagonal of the quad
+        [5.5, -0.5, 3, 0, 0, -1],
+        [0.2, 0.2, 5, 0, 0, 0],        # zero direction
+        [0, 0, 0, np.nan, np.nan, np.nan],
+        [np.inf, 0, 0, 0, 0, -1],
+        [-1, 0.2, 1, 1, 0, 0],         # parallel
+        [0.2, 0.2, 0, 0, 0, -1],       # starts on the surface (t = 0)
+    ], np.float32)
+    r8 = rays8_from6(r6)
+    scene = native.Scene(ctx, soup)
+    t, prim, _ = gpu_closest(native, scene, r8)
+    tb, pb = oracle.trace_brute(soup, r8)
+    assert np.array_equal(_bits(t), _bits(tb)) and np.array_equal(prim, pb)
+    assert prim[0] == 2 and prim[1] == 4 and prim[5] == -1 and prim[6] == -1 and prim[7] == -1
+    assert np.isinf(t[5]) and prim[8] == -1
+    # tmax: a hit at exactly t == tmax counts; below it does not
+    r8b = r8[:1].copy()
+    r8b[0, 3] = np.float32(5.0)
+    assert gpu_closest(native, scene, r8b)[1][0] == 2
+    r8b[0, 3] = np.nextafter(np.float32(5.0), np.float32(0))
+    assert gpu_closest(native, scene, r8b)[1][0] == -1
+
+
+def test_empty_and_single_triangle_scenes(native, ctx):
+    rays = scenes.incoherent_rays(1000, seed=3)
+    empty = native.Scene(ctx, np.zeros((0, 9), np.float32))
+    t, prim, _ = gpu_closest(native, empty, rays)
+    assert (prim == -1).all() and np.isinf(t).all()
+    assert gpu_any(native, empty, rays).sum() == 0
+    one = native.Scene(ctx, np.array([[-60, -60, 0, 60, -60, 0, 0, 60, 0]], np.float32))
+    t, prim, _ = gpu_closest(native, one, rays)
+    assert set(np.unique(prim)) <= {-1, 0} and (prim == 0).sum() > 300
+
+
+def test_counters_and_host_path(native, ctx, oracle):
+    half = scenes.density_half(20000)
+    soup, _, _ = scenes.incoherent_soup(20000, seed=2, half=half)
+    rays = scenes.incoherent_rays(50000, seed=4, half=half)
+    scene = native.Scene(ctx, soup)
+    t, prim, cnt = gpu_closest(native, scene, rays, counters=True)
+    assert cnt.rays == len(rays) and cnt.hits == (prim >= 0).sum()
+    assert cnt.node_visits > len(rays) and cnt.tri_tests > 0 and cnt.box_tests == 2 * cnt.node_visits
+    hits = scene.trace_closest_host(rays)
+    assert np.array_equal(hits["prim"], prim) and np.array_equal(_bits(hits["t"]), _bits(t))
+    info = scene.info()
+    assert info.depth < 64 and info.num_nodes > 0 and info.slack > 0
+
+
+def test_invalid_arguments_return_status(native, ctx):
+    scene = native.Scene(ctx, np.array([[0, 0, 0, 1, 0, 0, 0, 1, 0]], np.float32))
+    with pytest.raises(native.DrError) as e:
+        scene.trace_closest(0, 10, 0)
+    assert e.value.status == 1
+    bad = np.array([[0, 0, np.nan, 1, 0, 0, 0, 1, 0]], np.float32)
+    with pytest.raises(native.DrError):
+        native.Scene(ctx, bad)
