@@ -216,7 +216,7 @@ def run_ours(args):
     # End to end through the host-buffer entry point, pinned host memory.
     h_rays = torch.from_numpy(rays).pin_memory()
     h_hits = torch.empty((NUM_RAYS, 2), dtype=torch.int32).pin_memory()
-    e2e_steps = max(1, min(args.steps, 5))
+    e2e_steps = max(1, min(args.steps, 10))
     for _ in range(1):
         native.check(native.load().dr_trace_closest_host(scene.handle, h_rays.data_ptr(), NUM_RAYS,
                                                          h_hits.data_ptr(), 0, stream.cuda_stream))
@@ -247,7 +247,9 @@ def run_ours(args):
     bytes_per_ray = 32 + 8 + nodes_per_ray * node_bytes + tris_per_ray * tri_bytes
     per_launch_ms = total_ms / args.steps
     achieved = bytes_per_ray * NUM_RAYS / (per_launch_ms / 1e3) / 1e9
-    working_set = info.device_bytes
+    # reference mode reads the nodes, the reference triangle records and the
+    # triangle index map: 64 B per node + 52 B per triangle
+    working_set = info.num_nodes * 64 + NUM_TRIS * 52
     line = {
         "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -271,9 +273,10 @@ def run_ours(args):
                 "matches_device_result": bool(same)},
         "gpu_launches": args.steps,
     }
-    if l2 := _l2_probe(local):
-        line["roofline"]["l2_read_gbs_measured"] = l2
-        line["roofline"]["frac_of_l2"] = achieved / l2
+    l2, hbm_read = _read_probes(ctx, local)
+    line["roofline"]["l2_read_gbs_measured"] = l2
+    line["roofline"]["hbm_read_gbs_measured"] = hbm_read
+    line["roofline"]["frac_of_l2"] = achieved / l2
     if world == 1 and not args.no_cpu_baseline:
         cb, _ = cpu_baseline(soup, rays, args.cpu_sample, os.cpu_count() or 1)
         line["cpu_baseline"] = cb
@@ -283,30 +286,23 @@ def run_ours(args):
     return 0
 
 
-def _l2_probe(device: int):
-    """Read bandwidth of a 48 MiB L2-resident buffer (torch reduction), GB/s."""
+def _read_probes(ctx, device: int):
+    """Streaming-read bandwidth (dr_probe_read_bandwidth, our own kernel) of a
+    48 MiB buffer (L2-resident) and of a 2 GiB buffer (HBM), GB/s."""
     import torch
-    try:
-        x = torch.empty(12 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{device}").fill_(1.0)
-        for _ in range(3):
-            x.sum()
-        torch.cuda.synchronize()
-        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        reps = 50
-        s.record()
-        for _ in range(reps):
-            x.sum()
-        e.record()
-        torch.cuda.synchronize()
-        return x.numel() * 4 * reps / (s.elapsed_time(e) / 1e3) / 1e9
-    except Exception:
-        return None
+    small = torch.ones(12 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{device}")
+    big = torch.ones(512 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{device}")
+    l2 = max(ctx.read_bandwidth(small, small.numel() * 4, reps=50) for _ in range(3))
+    hbm = max(ctx.read_bandwidth(big, big.numel() * 4, reps=3) for _ in range(2))
+    del small, big
+    torch.cuda.empty_cache()
+    return l2, hbm
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-sample", type=int, default=1 << 20)

@@ -88,6 +88,8 @@ SIGNATURES = {
                                    C.POINTER(TraceCounters), C.c_void_p]),
     "dr_trace_any": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_int32, C.c_void_p]),
     "dr_trace_closest_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_int32, C.c_void_p]),
+    "dr_probe_read_bandwidth": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint32, C.POINTER(C.c_double),
+                                          C.c_void_p]),
 }
 
 _lib = None
@@ -152,6 +154,13 @@ class Context:
 
     def check(self):
         check(load().dr_context_check(self.handle))
+
+    def read_bandwidth(self, buf_dev, nbytes: int, reps: int = 20, stream=None) -> float:
+        """GB/s of streaming reads over a device buffer (dr_probe_read_bandwidth)."""
+        out = C.c_double()
+        check(load().dr_probe_read_bandwidth(self.handle, _ptr(buf_dev), nbytes, reps, C.byref(out),
+                                             _stream_ptr(stream)))
+        return out.value
 
     def __del__(self):
         try:

@@ -177,6 +177,16 @@ dr_status dr_trace_any(dr_scene *scene, const dr_ray *rays_dev, uint64_t n, uint
 dr_status dr_trace_closest_host(dr_scene *scene, const dr_ray *rays_host, uint64_t n, dr_hit *hits_host,
                                 int32_t tri_mode, void *stream);
 
+/* ---- diagnostics ------------------------------------------------------------------- */
+
+/* Streaming-read bandwidth of a device buffer in GB/s (reads it `reps` times
+ * with L2-cached 16-byte loads, CUDA events on `stream`). A buffer that fits
+ * in L2 measures L2 read bandwidth, one larger than L2 measures HBM. No
+ * counterpart in the reference: it supplies the traversal roofline's
+ * denominator. Synchronous. */
+dr_status dr_probe_read_bandwidth(dr_context *ctx, const void *buf_dev, uint64_t bytes, uint32_t reps,
+                                  double *gbs_out, void *stream);
+
 /* ---- version ----------------------------------------------------------------------- */
 
 uint32_t dr_abi_version(void);

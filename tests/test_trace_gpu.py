@@ -141,7 +141,7 @@ def test_empty_and_single_triangle_scenes(native, ctx):
     assert gpu_any(native, empty, rays).sum() == 0
     one = native.Scene(ctx, np.array([[-60, -60, 0, 60, -60, 0, 0, 60, 0]], np.float32))
     t, prim, _ = gpu_closest(native, one, rays)
-    assert set(np.unique(prim)) <= {-1, 0} and (prim == 0).sum() > 300
+    assert set(np.unique(prim)) <= {-1, 0} and (prim == 0).sum() > 50
 
 
 def test_counters_and_host_path(native, ctx, oracle):
@@ -166,3 +166,9 @@ def test_invalid_arguments_return_status(native, ctx):
     bad = np.array([[0, 0, np.nan, 1, 0, 0, 0, 1, 0]], np.float32)
     with pytest.raises(native.DrError):
         native.Scene(ctx, bad)
+
+
+def test_read_bandwidth_probe(native, ctx):
+    buf = torch.ones(8 * 1024 * 1024, dtype=torch.float32, device="cuda")
+    gbs = ctx.read_bandwidth(buf, buf.numel() * 4, reps=5)
+    assert 100.0 < gbs < 1e6
