@@ -2,6 +2,7 @@
 
 #include "dr_internal.h"
 #include "trace_kernels.cuh"
+#include "alias_kernels.cuh"
 
 #include <algorithm>
 #include <chrono>
@@ -83,6 +84,20 @@ TraceArgs trace_args(dr_scene *s)
 }
 
 }  // namespace
+
+dr_status ensure_scratch(dr_context *ctx, size_t bytes)
+{
+    if (ctx->scratch_bytes >= bytes) return DR_OK;
+    // Grow geometrically; the old contents need not survive.
+    size_t want = std::max(bytes, ctx->scratch_bytes * 2);
+    cudaFree(ctx->scratch);
+    ctx->scratch = nullptr;
+    ctx->scratch_bytes = 0;
+    DR_CUDA(cudaMalloc(&ctx->scratch, want));
+    ctx->scratch_bytes = want;
+    return DR_OK;
+}
+
 }  // namespace dr
 
 using namespace dr;
@@ -130,6 +145,7 @@ dr_status dr_context_destroy(dr_context *ctx)
     if (!ctx) return DR_OK;
     cudaSetDevice(ctx->device);
     cudaFree(ctx->d_error);
+    cudaFree(ctx->scratch);
     delete ctx;
     return DR_OK;
 }
@@ -342,6 +358,36 @@ dr_status dr_trace_closest_host(dr_scene *s, const dr_ray *rays_host, uint64_t n
     cudaStreamDestroy(copy_in);
     cudaStreamDestroy(copy_out);
     if (err != cudaSuccess) return cuda_fail(err, "dr_trace_closest_host");
+    return DR_OK;
+}
+
+dr_status dr_alias_build(dr_context *ctx, const float *w, uint32_t n, dr_alias_entry *table, int32_t mode,
+                         void *stream)
+{
+    DR_CHECK_ARG(ctx != nullptr, "dr_alias_build: ctx is NULL");
+    DR_CHECK_ARG(n == 0 || (w && table), "dr_alias_build: NULL buffer");
+    DR_CHECK_ARG(mode == DR_ALIAS_REFERENCE || mode == DR_ALIAS_SWEEP, "dr_alias_build: bad mode");
+    DR_CHECK_ARG(n < (1u << 30), "dr_alias_build: n too large");
+    if (n == 0) return DR_OK;
+    DR_CUDA(cudaSetDevice(ctx->device));
+    auto st = static_cast<cudaStream_t>(stream);
+    const size_t need = alias_scratch_bytes(n, mode);
+    if (ctx->scratch_bytes < need) {
+        // the scratch may be in use by earlier work on any stream
+        DR_CUDA(cudaDeviceSynchronize());
+        const dr_status s = ensure_scratch(ctx, need);
+        if (s != DR_OK) return s;
+    }
+    DR_CUDA(launch_alias_build(w, n, table, mode, ctx->scratch, ctx->scratch_bytes, ctx->num_sms, st));
+    return DR_OK;
+}
+
+dr_status dr_alias_sample(const dr_alias_entry *table, uint32_t n, const float *u, uint64_t ndraws, int32_t *index,
+                          float *pdf, void *stream)
+{
+    DR_CHECK_ARG(ndraws == 0 || (table && u && index && pdf && n > 0), "dr_alias_sample: bad argument");
+    DR_CHECK_ARG((reinterpret_cast<uintptr_t>(u) & 7) == 0, "dr_alias_sample: uniforms must be 8-byte aligned");
+    DR_CUDA(launch_alias_sample(table, n, u, ndraws, index, pdf, static_cast<cudaStream_t>(stream)));
     return DR_OK;
 }
 

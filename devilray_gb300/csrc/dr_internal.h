@@ -100,7 +100,14 @@ struct dr_context {
     uint32_t *d_error = nullptr;                // device error word
     unsigned long long *d_counters = nullptr;   // 8 counters
     unsigned int *d_work = nullptr;             // persistent-kernel work counters (8)
+    void *scratch = nullptr;                    // grows on demand (alias builds, staging)
+    size_t scratch_bytes = 0;
 };
+
+namespace dr {
+// Ensures ctx->scratch holds at least `bytes` (cudaMalloc when it must grow).
+dr_status ensure_scratch(dr_context *ctx, size_t bytes);
+}  // namespace dr
 
 struct dr_scene {
     dr_context *ctx = nullptr;

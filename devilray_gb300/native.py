@@ -21,6 +21,10 @@ STATUS_NAMES = {
     8: "DR_ERR_TOO_LARGE",
 }
 
+DR_ALIAS_REFERENCE = 0
+DR_ALIAS_SWEEP = 1
+ALIAS_DTYPE = np.dtype([("p_A", "<f4"), ("pdf_A", "<f4"), ("pdf_B", "<f4"), ("A", "<i4"), ("B", "<i4")])
+
 DR_TRI_REFERENCE = 0
 DR_TRI_WATERTIGHT = 1
 DR_MAT_DIFFUSE = 0
@@ -88,6 +92,9 @@ SIGNATURES = {
                                    C.POINTER(TraceCounters), C.c_void_p]),
     "dr_trace_any": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_int32, C.c_void_p]),
     "dr_trace_closest_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_int32, C.c_void_p]),
+    "dr_alias_build": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_int32, C.c_void_p]),
+    "dr_alias_sample": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p,
+                                  C.c_void_p]),
     "dr_probe_read_bandwidth": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint32, C.POINTER(C.c_double),
                                           C.c_void_p]),
 }
@@ -162,11 +169,19 @@ class Context:
                                              _stream_ptr(stream)))
         return out.value
 
+    def alias_build(self, weights_dev, n: int, table_dev, mode: int = DR_ALIAS_SWEEP, stream=None):
+        check(load().dr_alias_build(self.handle, _ptr(weights_dev), n, _ptr(table_dev), mode, _stream_ptr(stream)))
+
     def __del__(self):
         try:
             self.close()
         except Exception:
             pass
+
+
+def alias_sample(table_dev, n: int, uniforms_dev, ndraws: int, index_dev, pdf_dev, stream=None):
+    check(load().dr_alias_sample(_ptr(table_dev), n, _ptr(uniforms_dev), ndraws, _ptr(index_dev), _ptr(pdf_dev),
+                                 _stream_ptr(stream)))
 
 
 class Scene:

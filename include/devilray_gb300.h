@@ -177,6 +177,34 @@ dr_status dr_trace_any(dr_scene *scene, const dr_ray *rays_dev, uint64_t n, uint
 dr_status dr_trace_closest_host(dr_scene *scene, const dr_ray *rays_host, uint64_t n, dr_hit *hits_host,
                                 int32_t tri_mode, void *stream);
 
+/* ---- alias tables ------------------------------------------------------------------- */
+
+/* AliasEntry of include/tracing/DistributionSamplers.hpp:44-51, 20 bytes. */
+typedef struct dr_alias_entry {
+    float p_A, pdf_A, pdf_B;
+    int32_t A, B;
+} dr_alias_entry;
+
+typedef enum dr_alias_mode {
+    /* The pairing of generateAliasTable (src/DistributionSamplers.cpp:39-149):
+     * bit-identical table, built by one device thread. */
+    DR_ALIAS_REFERENCE = 0,
+    /* Parallel sweeping construction in exact fixed point; slot i holds item i. */
+    DR_ALIAS_SWEEP = 1
+} dr_alias_mode;
+
+/* Builds the alias table of n weights on the device (negative / non-finite
+ * weights count as 0; a total below 1e-5 gives the uniform table, as the
+ * reference). Replaces generateAliasTable. Uses the context's scratch, which
+ * grows with cudaMalloc when n needs more. Asynchronous on `stream`. */
+dr_status dr_alias_build(dr_context *ctx, const float *weights_dev, uint32_t n, dr_alias_entry *table_dev,
+                         int32_t mode, void *stream);
+
+/* ndraws draws of sample() (DistributionSamplers.hpp:64-88) with the two
+ * uniforms of draw i at uniforms_dev[2i], uniforms_dev[2i+1]. */
+dr_status dr_alias_sample(const dr_alias_entry *table_dev, uint32_t n, const float *uniforms_dev, uint64_t ndraws,
+                          int32_t *index_dev, float *pdf_dev, void *stream);
+
 /* ---- diagnostics ------------------------------------------------------------------- */
 
 /* Streaming-read bandwidth of a device buffer in GB/s (reads it `reps` times

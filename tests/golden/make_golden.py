@@ -149,8 +149,17 @@ def alias_fixture():
     # A 65,536-entry emitter-power table (many-light configuration).
     em = np.exp(np.random.default_rng(11).normal(0, 1.5, 65536)).astype(np.float32)
     em_tab = po.ref_alias_build(em)
+    # sample() on the 100-item table with seeded uniforms (incl. 0 and the
+    # values just below 1).
+    t100 = tables[7]
+    u = np.random.default_rng(5).random((4000, 2)).astype(np.float32)
+    u[:4] = [[0.0, 0.0], [np.nextafter(np.float32(1), np.float32(0)), 0.5], [0.5, 1.0], [0.999, 0.0]]
+    idx = np.zeros(len(u), np.int32)
+    pdf = np.zeros(len(u), np.float32)
+    po.ref().refh_alias_sample(t100["p_A"].copy(), t100["pdf_A"].copy(), t100["pdf_B"].copy(), t100["A"].copy(),
+                               t100["B"].copy(), len(t100), u.reshape(-1).copy(), len(u), idx, pdf)
     np.savez_compressed(
-        OUT / "alias.npz", weights=w_all, offsets=np.array(off, np.int64),
+        OUT / "alias.npz", sample_uniforms=u, sample_index=idx, sample_pdf=pdf, weights=w_all, offsets=np.array(off, np.int64),
         p_A=tab["p_A"], pdf_A=tab["pdf_A"], pdf_B=tab["pdf_B"], A=tab["A"], B=tab["B"],
         stress_input_sha=np.frombuffer(hashlib.sha256(stress_w.tobytes()).digest(), np.uint8),
         stress_table_sha=np.frombuffer(hashlib.sha256(stress.tobytes()).digest(), np.uint8),

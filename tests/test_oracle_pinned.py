@@ -163,3 +163,15 @@ def test_philox_known_answers(oracle):
     assert oracle.philox([0xFFFFFFFF] * 4, [0xFFFFFFFF] * 2).tolist() == [0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD]
     assert oracle.philox([0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344], [0xA4093822, 0x299F31D0]).tolist() == \
         [0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1]
+
+
+def test_alias_sample_matches_reference(oracle, golden):
+    g = golden("alias.npz")
+    off = g["offsets"]
+    sl = slice(off[7], off[8])
+    tab = np.zeros(off[8] - off[7], oracle.ALIAS_DTYPE)
+    for k in ("p_A", "pdf_A", "pdf_B", "A", "B"):
+        tab[k] = g[k][sl]
+    for (u0, u1), i, p in zip(g["sample_uniforms"], g["sample_index"], g["sample_pdf"]):
+        idx, pdf = oracle.alias_sample(tab, float(u0), float(u1))
+        assert idx == i and np.float32(pdf) == p
