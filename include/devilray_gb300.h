@@ -205,6 +205,18 @@ dr_status dr_alias_build(dr_context *ctx, const float *weights_dev, uint32_t n, 
 dr_status dr_alias_sample(const dr_alias_entry *table_dev, uint32_t n, const float *uniforms_dev, uint64_t ndraws,
                           int32_t *index_dev, float *pdf_dev, void *stream);
 
+/* Sweep-mode alias build (same table as dr_alias_build with DR_ALIAS_SWEEP)
+ * that allocates no device memory. No counterpart in the reference. For
+ * callers that may not call cudaMalloc: a host application that owns every
+ * device allocation and passes in only pre-allocated buffers, or a frame loop
+ * that must not stall on cudaMalloc's implicit synchronisation. Its scratch is
+ * a fixed array inside the library (about 2.6 MB on every GPU that loads it),
+ * so n is limited to 65,536 weights (DR_ERR_TOO_LARGE above that). Needs no
+ * context: it runs on the current device. The first call on a device sets up
+ * the array's device address; make it before any stream capture. All calls
+ * share the array: calls whose work overlaps on the GPU race. */
+dr_status dr_alias_build_noalloc(const float *weights_dev, uint32_t n, dr_alias_entry *table_dev, void *stream);
+
 /* ---- diagnostics ------------------------------------------------------------------- */
 
 /* Streaming-read bandwidth of a device buffer in GB/s (reads it `reps` times
