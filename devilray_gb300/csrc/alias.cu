@@ -87,18 +87,20 @@ __host__ __device__ __forceinline__ void ensure_pa_larger(dr_alias_entry &e)
     }
 }
 
-// Single thread: filter, sequential total, heap pairing, entries in order.
-__global__ void k_alias_ref_pair(const float *__restrict__ w, uint32_t n, dr_alias_entry *__restrict__ out,
-                                 HeapItem *under, HeapItem *over, float *filtered, float *total_out)
+// One table, one thread: filter, sequential total, heap pairing, entries in
+// processing order, then the pdf fill (src/DistributionSamplers.cpp:39-149).
+__device__ void alias_ref_build_one(const float *__restrict__ w, uint32_t n, dr_alias_entry *__restrict__ out,
+                                    HeapItem *under, HeapItem *over, float *filtered, bool fill_pdfs,
+                                    float *total_out)
 {
-    if (blockIdx.x != 0 || threadIdx.x != 0) return;
     float total = 0.f;
     for (uint32_t i = 0; i < n; ++i) {
         const float fi = (0.f < w[i]) ? w[i] : 0.f;  // std::max(0.f, w[i])
         filtered[i] = fi;
         total = total + fi;
     }
-    *total_out = total;
+    if (total_out) *total_out = total;
+    if (n == 0) return;
     if (total < 1e-5f) {
         const float u = 1.0f / (float)n;
         for (uint32_t i = 0; i < n; ++i) out[i] = dr_alias_entry{1.0f, u, 0.0f, (int32_t)i, -1};
@@ -141,9 +143,23 @@ __global__ void k_alias_ref_pair(const float *__restrict__ w, uint32_t n, dr_ali
         heap_pop(over, no);
         out[ptr++] = dr_alias_entry{1.0f, 0.f, 0.f, e.a, -1};
     }
+    if (fill_pdfs) {
+        for (uint32_t i = 0; i < n; ++i) {
+            dr_alias_entry &e = out[i];
+            e.pdf_A = filtered[e.A] / total;
+            e.pdf_B = (e.B >= 0 && (uint32_t)e.B < n) ? filtered[e.B] / total : 0.0f;
+        }
+    }
 }
 
-// pdf fill (src/DistributionSamplers.cpp:135-146), parallel.
+__global__ void k_alias_ref_pair(const float *__restrict__ w, uint32_t n, dr_alias_entry *__restrict__ out,
+                                 HeapItem *under, HeapItem *over, float *filtered, float *total_out)
+{
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    alias_ref_build_one(w, n, out, under, over, filtered, false, total_out);
+}
+
+// pdf fill (src/DistributionSamplers.cpp:135-146) of the single-table build, parallel.
 __global__ void k_alias_ref_pdfs(uint32_t n, dr_alias_entry *__restrict__ out, const float *__restrict__ filtered,
                                  const float *__restrict__ total_in)
 {
@@ -155,6 +171,19 @@ __global__ void k_alias_ref_pdfs(uint32_t n, dr_alias_entry *__restrict__ out, c
         e.pdf_B = (e.B >= 0 && (uint32_t)e.B < n) ? filtered[e.B] / total : 0.0f;
         out[i] = e;
     }
+}
+
+// Many independent tables, one thread each: table s covers entries
+// [begin[s], begin[s] + count[s]) of w and out (object-local indices).
+__global__ void k_alias_ref_segments(const float *__restrict__ w, const uint32_t *__restrict__ begin,
+                                     const uint32_t *__restrict__ count, uint32_t nseg,
+                                     dr_alias_entry *__restrict__ out, HeapItem *heaps, float *filtered)
+{
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nseg) return;
+    const uint32_t b = begin[s], n = count[s];
+    alias_ref_build_one(w + b, n, out + b, heaps + 2 * (size_t)b, heaps + 2 * (size_t)b + n, filtered + b, true,
+                        nullptr);
 }
 
 // ---- sweep build -----------------------------------------------------------------------
@@ -525,6 +554,19 @@ cudaError_t launch_alias_build(const float *w, uint32_t n, dr_alias_entry *out, 
     k_sweep_scan_tiles<<<1, kSweepBlock, 0, st>>>(tile_agg, tiles, sc, n);
     k_sweep_scatter<<<tiles, kSweepBlock, 0, st>>>(w, n, sc, tile_agg, lights, Dexcl, heavies, Sincl);
     k_sweep_assign<<<(n + 255) / 256, 256, 0, st>>>(w, n, sc, lights, Dexcl, heavies, Sincl, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_alias_ref_segments(const float *w, uint32_t total_n, const uint32_t *begin, const uint32_t *count,
+                                     uint32_t nseg, dr_alias_entry *out, void *scratch, size_t scratch_bytes,
+                                     cudaStream_t st)
+{
+    if (nseg == 0) return cudaSuccess;
+    if (scratch_bytes < (size_t)total_n * (2 * sizeof(HeapItem) + sizeof(float)) + 512) return cudaErrorInvalidValue;
+    char *p = align256(static_cast<char *>(scratch));
+    HeapItem *heaps = reinterpret_cast<HeapItem *>(p);
+    float *filtered = reinterpret_cast<float *>(heaps + 2 * (size_t)total_n);
+    k_alias_ref_segments<<<(nseg + 63) / 64, 64, 0, st>>>(w, begin, count, nseg, out, heaps, filtered);
     return cudaGetLastError();
 }
 

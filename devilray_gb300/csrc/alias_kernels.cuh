@@ -30,6 +30,10 @@ __device__ __forceinline__ void alias_sample(const dr_alias_entry *__restrict__ 
 size_t alias_scratch_bytes(uint32_t n, int mode);
 cudaError_t launch_alias_build(const float *w, uint32_t n, dr_alias_entry *out, int mode, void *scratch,
                                size_t scratch_bytes, int num_sms, cudaStream_t st);
+// Reference-mode builds of many small tables (one device thread per table).
+cudaError_t launch_alias_ref_segments(const float *w, uint32_t total_n, const uint32_t *begin, const uint32_t *count,
+                                     uint32_t nseg, dr_alias_entry *out, void *scratch, size_t scratch_bytes,
+                                     cudaStream_t st);
 cudaError_t launch_alias_sample(const dr_alias_entry *table, uint32_t n, const float *u, uint64_t draws,
                                 int32_t *index, float *pdf, cudaStream_t st);
 

@@ -216,6 +216,11 @@ dr_status dr_scene_create(dr_context *ctx, const dr_scene_desc *desc, const dr_b
         }
         s->num_materials = desc->num_materials;
     }
+    const dr_status rs = build_render_data(s, desc);
+    if (rs != DR_OK) {
+        dr_scene_destroy(s);
+        return rs;
+    }
     s->build_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
     *out = s;
     return DR_OK;
@@ -230,6 +235,11 @@ dr_status dr_scene_destroy(dr_scene *s)
     cudaFree(s->d_tri_wt);
     cudaFree(s->d_prim);
     cudaFree(s->d_materials);
+    cudaFree(s->d_objects);
+    cudaFree(s->d_shade);
+    cudaFree(s->d_light_table);
+    cudaFree(s->d_tri_tables);
+    cudaFree(s->d_wave);
     cudaFree(s->d_stage_rays);
     cudaFree(s->d_stage_hits);
     delete s;

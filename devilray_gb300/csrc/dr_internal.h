@@ -109,6 +109,13 @@ namespace dr {
 dr_status ensure_scratch(dr_context *ctx, size_t bytes);
 }  // namespace dr
 
+struct dr_scene;
+namespace dr {
+// Uploads the shading records, objects, materials and light tables of a scene
+// (part of dr_scene_create).
+dr_status build_render_data(dr_scene *s, const dr_scene_desc *d);
+}  // namespace dr
+
 struct dr_scene {
     dr_context *ctx = nullptr;
     uint32_t num_tris = 0;
@@ -124,10 +131,19 @@ struct dr_scene {
     float4 *d_tri_wt = nullptr;
     int32_t *d_prim = nullptr;      // leaf-order position -> original triangle index
 
-    // scene data for shading
+    // scene data for shading (original triangle order)
     uint32_t num_objects = 0, num_materials = 0;
     dr_material *d_materials = nullptr;
+    dr_object *d_objects = nullptr;
+    float4 *d_shade = nullptr;            // 3 per triangle: (A, B.x) (B.yz, C.xy) (C.z, object, material, -)
+    dr_alias_entry *d_light_table = nullptr;  // over objects, by emitted power
+    dr_alias_entry *d_tri_tables = nullptr;   // per object, over its triangles (object-local indices)
     float total_radiant_power = 0.0f;
+    bool lights = false;                  // some object emits
+
+    // wavefront buffers of dr_render, grown on demand
+    void *d_wave = nullptr;
+    size_t wave_bytes = 0;
 
     // staging for the host-buffer entry points
     void *d_stage_rays = nullptr;

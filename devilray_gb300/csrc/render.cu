@@ -1,0 +1,522 @@
+// render.cu -- wavefront path tracer on sm_103a.
+//
+// Replaces cuda_render + sampleColor (DevilRay src/device/RendererImpl.hpp:
+// 22-102, include/tracing/PathGeneration.hpp:363-515): one thread per pixel
+// that builds a whole path, then shades it, becomes a wave of kernels over a
+// batch of path slots:
+//   camera -> for each bounce: closest hit -> shade (emission with MIS, a light
+//   sample, the BSDF sample; compaction of surviving paths and of shadow rays by
+//   warp ballot) -> shadow any hit (+ next-event contribution) -> accumulate.
+// The shading restates the reference's arithmetic in a forward order that adds
+// the same terms in the same sequence (emission of vertex k, then its light
+// sample, then vertex k+1), so each sample's colour is bit-identical to the
+// reference evaluated on the same random numbers, with the portable sin/cos/acos
+// of ptmath.cuh. Uniforms: Philox4x32-10 with counter (pixel, sample, group,
+// tag) and key = seed; camera dims 0,1; bounce b: 4 + 12 b + {0,1 sphere,
+// 2 Fresnel, 3..8 light sample}.
+
+#include "dr_internal.h"
+#include "alias_kernels.cuh"
+#include "ptmath.cuh"
+#include "trace_device.cuh"
+
+#include <algorithm>
+
+namespace dr {
+namespace {
+
+constexpr float kPi = 3.14159274f;
+constexpr uint32_t kStreamTag = 0x44526E67u;
+constexpr int kMaxDepth = 63;
+constexpr int kRenderBlock = 128;
+
+struct RenderParams {
+    TraceArgs trace;
+    const float4 *shade;
+    const dr_object *objects;
+    const dr_material *materials;
+    const dr_alias_entry *light_table;
+    const dr_alias_entry *tri_tables;
+    uint32_t num_objects;
+    float total_power;
+    int lights;
+    // camera
+    float m[12];
+    float focal, cx, cy, psx, psy;
+    int width, height, pixel_sampling;
+    // wave
+    uint32_t npix, wave, sample_base, spp_wave, max_depth;
+    uint32_t seed_lo, seed_hi;
+    // per-slot buffers
+    float4 *rays;      // dr_ray, 2 x float4
+    float2 *hits;
+    float4 *thr, *color, *prev_p, *prev_n, *pending, *shadow_rays;
+    int4 *stack;
+    uint32_t *casts;
+    uint32_t *list[2];
+    uint32_t *shadow_list;
+    uint32_t *counts;  // [0, 64): active paths per bounce, [64, 128): shadow rays per bounce
+    float4 *accum;
+    uint32_t *pix_casts;
+};
+
+struct F3 {
+    float x, y, z;
+};
+__device__ __forceinline__ F3 f3(float x, float y, float z) { return F3{x, y, z}; }
+__device__ __forceinline__ F3 sub(F3 a, F3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ F3 add(F3 a, F3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ F3 mul(F3 a, float f) { return f3(a.x * f, a.y * f, a.z * f); }
+__device__ __forceinline__ float dot(F3 a, F3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ F3 cross(F3 a, F3 v)
+{
+    return f3(a.y * v.z - a.z * v.y, a.z * v.x - a.x * v.z, a.x * v.y - a.y * v.x);
+}
+__device__ __forceinline__ float length(F3 a) { return __fsqrt_rn(a.x * a.x + a.y * a.y + a.z * a.z); }
+__device__ __forceinline__ F3 normalized(F3 a)
+{
+    const float l = length(a);
+    return f3(a.x / l, a.y / l, a.z / l);
+}
+__device__ __forceinline__ F3 divs(F3 a, float f) { return mul(a, 1.0f / f); }  // Vec3::operator/ multiplies by 1/f
+__device__ __forceinline__ float4 mul4(float4 a, float4 b) { return make_float4(a.x * b.x, a.y * b.y, a.z * b.z, a.w * b.w); }
+__device__ __forceinline__ float4 mul4s(float4 a, float f) { return make_float4(a.x * f, a.y * f, a.z * f, a.w * f); }
+__device__ __forceinline__ float4 add4(float4 a, float4 b) { return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
+__device__ __forceinline__ float luminance(float4 c) { return 0.2126f * c.x + 0.7152f * c.y + 0.0722f * c.z; }
+__device__ __forceinline__ float power_heuristic(float a, float b) { return a * a / (a * a + b * b); }
+
+// areaToSolidAngle (include/Utils.hpp:236-247)
+__device__ __forceinline__ float area_to_solid_angle(F3 from, F3 to, F3 to_n)
+{
+    const F3 diff = sub(to, from);
+    const float d2 = dot(diff, diff);
+    const F3 dir = normalized(diff);
+    const float c = fabsf(dot(dir, to_n));
+    if (c < 1e-6f) return 0.0f;
+    return d2 / c;
+}
+
+// cosineWeightedHemispherePdf (include/Utils.hpp:249-254)
+__device__ __forceinline__ float cosine_pdf(F3 cur, F3 next, F3 n)
+{
+    const F3 dir = normalized(sub(next, cur));
+    const float c = dot(dir, n);
+    return c > 0 ? c / kPi : 0.0f;
+}
+
+__device__ __forceinline__ void uniforms4(const RenderParams &p, uint32_t pixel, uint32_t sample, uint32_t group,
+                                          float u[4])
+{
+    uint32_t o[4];
+    pt::philox4x32_10(pixel, sample, group, kStreamTag, p.seed_lo, p.seed_hi, o);
+    u[0] = pt::u01(o[0]);
+    u[1] = pt::u01(o[1]);
+    u[2] = pt::u01(o[2]);
+    u[3] = pt::u01(o[3]);
+}
+
+__device__ __forceinline__ void slot_pixel(const RenderParams &p, uint32_t slot, uint32_t &pixel, uint32_t &sample)
+{
+    pixel = slot % p.npix;
+    sample = p.sample_base + slot / p.npix;
+}
+
+// Appends `slot` to a list with one atomic per warp. Every lane of the warp
+// must call it (with keep = false where it has nothing to add).
+__device__ __forceinline__ void warp_append(bool keep, uint32_t slot, uint32_t *list, uint32_t *count)
+{
+    const unsigned mask = __ballot_sync(0xffffffffu, keep);
+    if (mask == 0) return;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(mask) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(count, (uint32_t)__popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (keep) list[base + __popc(mask & ((1u << lane) - 1u))] = slot;
+}
+
+__global__ void __launch_bounds__(kRenderBlock) k_camera(RenderParams p)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) p.counts[0] = p.wave;
+    if (i >= p.wave) return;
+    uint32_t pixel, sample;
+    slot_pixel(p, i, pixel, sample);
+    const int px = (int)(pixel % (uint32_t)p.width), py = (int)(pixel / (uint32_t)p.width);
+    // cameraRay (include/tracing/CameraRay.hpp:6-34)
+    float subx = 0.5f, suby = 0.5f;
+    if (p.pixel_sampling == DR_PIXEL_UNIFORM_RANDOM) {
+        float u[4];
+        uniforms4(p, pixel, sample, 0, u);
+        subx = u[0];
+        suby = u[1];
+    }
+    const float pcx = (float)px + subx, pcy = (float)py + suby;
+    const float physx = pcx * p.psx - p.cx, physy = pcy * p.psy - p.cy;
+    const float dx = physx / p.focal, dy = physy / p.focal;
+    const F3 v = normalized(f3(dx, dy, 1.0f));
+    const float ox = p.m[3], oy = p.m[7], oz = p.m[11];
+    const float vx = p.m[0] * v.x + p.m[1] * v.y + p.m[2] * v.z;
+    const float vy = p.m[4] * v.x + p.m[5] * v.y + p.m[6] * v.z;
+    const float vz = p.m[8] * v.x + p.m[9] * v.y + p.m[10] * v.z;
+    p.rays[2 * i] = make_float4(ox, oy, oz, __int_as_float(0x7f800000));
+    p.rays[2 * i + 1] = make_float4(vx, vy, vz, 0.0f);
+    p.thr[i] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+    p.color[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    p.prev_p[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);  // w = 0: no diffuse vertex before
+    p.stack[i] = make_int4(0, 0, 0, 0);                 // w = size
+    p.casts[i] = 0;
+    p.list[0][i] = i;
+}
+
+// Closest hit of the surviving paths of bounce b.
+template <int MODE>
+__global__ void __launch_bounds__(kTraceBlock) k_wave_closest(RenderParams p, int b)
+{
+    const uint32_t count = p.counts[b];
+    const uint32_t *list = p.list[b & 1];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const uint32_t slot = list[i];
+        DevRay r;
+        const bool valid = load_ray(reinterpret_cast<const dr_ray *>(p.rays), slot, r);
+        float t = r.tmax;
+        int32_t prim = INT_MAX;
+        TraceStats st;
+        if (valid) closest_hit<MODE, false>(p.trace, r, t, prim, st);
+        p.hits[slot] = prim != INT_MAX ? make_float2(t, __int_as_float(prim))
+                                       : make_float2(__int_as_float(0x7f800000), __int_as_float(-1));
+    }
+}
+
+__device__ __forceinline__ float object_ior(const RenderParams &p, int obj)
+{
+    const dr_material &m = p.materials[p.objects[obj].material];
+    return m.kind == DR_MAT_DIELECTRIC ? m.ior : 1.0f;
+}
+
+__global__ void __launch_bounds__(kRenderBlock) k_shade(RenderParams p, int b)
+{
+    const uint32_t count = p.counts[b];
+    const uint32_t *list = p.list[b & 1];
+    uint32_t *next_list = p.list[(b + 1) & 1];
+    const bool last = b + 1 >= (int)p.max_depth;
+    // warp-uniform loop so that every lane reaches the ballots
+    const uint32_t warp_first = (blockIdx.x * blockDim.x + (threadIdx.x & ~31u));
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = warp_first; base < count; base += stride) {
+        const uint32_t i = base + (threadIdx.x & 31);
+        bool keep = false, shadow = false;
+        uint32_t slot = 0;
+        if (i < count) {
+            slot = list[i];
+            p.casts[slot] += 1;
+            const float2 h = p.hits[slot];
+            const int prim = __float_as_int(h.y);
+            if (prim >= 0) {
+                const float t = h.x;
+                const float4 r0 = p.rays[2 * slot], r1 = p.rays[2 * slot + 1];
+                const F3 ro = f3(r0.x, r0.y, r0.z), rv = f3(r1.x, r1.y, r1.z);
+                const float4 s0 = __ldg(p.shade + 3 * prim), s1 = __ldg(p.shade + 3 * prim + 1),
+                             s2 = __ldg(p.shade + 3 * prim + 2);
+                const F3 A = f3(s0.x, s0.y, s0.z), B = f3(s0.w, s1.x, s1.y), C = f3(s1.z, s1.w, s2.x);
+                const int obj = __float_as_int(s2.y), mat_id = __float_as_int(s2.z);
+                // getIntersectionTris (IntersectionTestsImpl.hpp:36-67), identity transform
+                F3 n = normalized(cross(sub(A, B), sub(A, C)));
+                if (dot(n, rv) > 0) n = mul(n, -1.0f);
+                n = normalized(f3(n.x * 1.0f, n.y * 1.0f, n.z * 1.0f));
+                F3 hp = add(ro, mul(rv, t));
+                hp = f3(hp.x * 1.0f + 0.0f, hp.y * 1.0f + 0.0f, hp.z * 1.0f + 0.0f);
+                const dr_material &M = p.materials[mat_id];
+                float4 thr = p.thr[slot];
+                float4 col = p.color[slot];
+                const float4 pp4 = p.prev_p[slot];
+                uint32_t pixel, sample;
+                slot_pixel(p, slot, pixel, sample);
+                float u[12];
+                const uint32_t g = 1u + 3u * (uint32_t)b;
+                uniforms4(p, pixel, sample, g, u);
+                F3 normal = n;
+                F3 new_o, new_v;
+                if (M.kind == DR_MAT_DIFFUSE) {
+                    const float4 E = make_float4(M.emission[0], M.emission[1], M.emission[2], M.emission[3]);
+                    const float4 alb = make_float4(M.albedo[0], M.albedo[1], M.albedo[2], M.albedo[3]);
+                    // misWeightedEmission (PathGeneration.hpp:306-318) with the
+                    // pdfs of computeNextBounceMisPdfs (:320-334) for (prev, this)
+                    if (pp4.w == 0.0f) {
+                        col = add4(col, mul4(E, thr));
+                    } else {
+                        const float4 pn4 = p.prev_n[slot];
+                        const F3 pp = f3(pp4.x, pp4.y, pp4.z), pn = f3(pn4.x, pn4.y, pn4.z);
+                        const float pdf_bsdf = cosine_pdf(pp, hp, pn);
+                        const float L = luminance(mul4s(E, kPi));
+                        const float pdf_area = L / p.total_power;
+                        const float pdf_nee = pdf_area * area_to_solid_angle(pp, hp, n);
+                        if (pdf_bsdf + pdf_nee > 0)
+                            col = add4(col, mul4s(mul4(E, thr), power_heuristic(pdf_bsdf, pdf_nee)));
+                    }
+                    // next-event estimation: samplePointOnLights (:234-272) and
+                    // evaluateDirectLighting (:336-361); visibility is the shadow ray
+                    if (p.lights) {
+                        uniforms4(p, pixel, sample, g + 1, u + 4);
+                        uniforms4(p, pixel, sample, g + 2, u + 8);
+                        int32_t oi, ti;
+                        float opdf, tpdf;
+                        alias_sample(p.light_table, p.num_objects, u[3], u[4], oi, opdf);
+                        const dr_object ob = p.objects[oi];
+                        alias_sample(p.tri_tables + ob.tri_begin, ob.tri_count, u[5], u[6], ti, tpdf);
+                        const int lt = (int)ob.tri_begin + ti;
+                        const float4 l0 = __ldg(p.shade + 3 * lt), l1 = __ldg(p.shade + 3 * lt + 1),
+                                     l2 = __ldg(p.shade + 3 * lt + 2);
+                        const F3 LA = f3(l0.x, l0.y, l0.z), LB = f3(l0.w, l1.x, l1.y), LC = f3(l1.z, l1.w, l2.x);
+                        float uu = u[7], vv = u[8];
+                        if (uu + vv > 1) {
+                            uu = 1 - uu;
+                            vv = 1 - vv;
+                        }
+                        F3 lp = add(add(LA, mul(sub(LB, LA), uu)), mul(sub(LC, LA), vv));
+                        const F3 Aw = f3(LA.x * 1.0f, LA.y * 1.0f, LA.z * 1.0f);
+                        const F3 Bw = f3(LB.x * 1.0f, LB.y * 1.0f, LB.z * 1.0f);
+                        const F3 Cw = f3(LC.x * 1.0f, LC.y * 1.0f, LC.z * 1.0f);
+                        const F3 perp = cross(sub(Aw, Bw), sub(Aw, Cw));
+                        const float plen = length(perp);
+                        const F3 ln = divs(perp, plen);
+                        const float area = plen / 2.0f;
+                        const float lpdf = opdf * tpdf / area;
+                        lp = f3(lp.x * 1.0f + 0.0f, lp.y * 1.0f + 0.0f, lp.z * 1.0f + 0.0f);
+                        const dr_material &LM = p.materials[ob.material];
+                        const float nee_pdf_bsdf = cosine_pdf(hp, lp, n);
+                        const float nee_pdf_nee = lpdf * area_to_solid_angle(hp, lp, ln);
+                        const float dist = length(sub(lp, hp));
+                        const F3 wl = divs(sub(lp, hp), dist);
+                        const float cos_s = dot(wl, n);
+                        const float cos_l = dot(wl, ln);
+                        if (cos_s > 0 && nee_pdf_nee + nee_pdf_bsdf > 0) {
+                            const float4 brdf = mul4s(alb, 1.0f / kPi);
+                            const float G = cos_s * fabsf(cos_l) / (dist * dist);
+                            const float4 LE = make_float4(LM.emission[0], LM.emission[1], LM.emission[2],
+                                                          LM.emission[3]);
+                            const float4 Ld = mul4s(mul4s(mul4(LE, brdf), G), 1.0f / lpdf);
+                            p.pending[slot] = mul4s(mul4(Ld, thr), power_heuristic(nee_pdf_nee, nee_pdf_bsdf));
+                            // visible(): ray from p0 + v 1e-5, occluded when a hit has
+                            // t <= distance - 2e-5 (evaluated in double)
+                            const F3 so = add(hp, mul(wl, 1e-5f));
+                            const float tmax = __double2float_rd((double)dist - 1e-5 * 2);
+                            p.shadow_rays[2 * slot] = make_float4(so.x, so.y, so.z, tmax);
+                            p.shadow_rays[2 * slot + 1] = make_float4(wl.x, wl.y, wl.z, 0.0f);
+                            shadow = true;
+                        }
+                    }
+                    // cosineWeightedHemisphereSample (DistributionSamplers.hpp:33-42)
+                    const float theta0 = 2 * kPi * u[0];
+                    const float theta1 = pt::acos(1 - 2 * u[1]);
+                    float sn0, cs0, sn1, cs1;
+                    pt::sincos(theta0, sn0, cs0);
+                    pt::sincos(theta1, sn1, cs1);
+                    const F3 sph = f3(sn1 * sn0, sn1 * cs0, cs1);
+                    new_v = normalized(add(sph, normal));
+                    thr = mul4(thr, alb);
+                    new_o = hp;
+                    p.prev_p[slot] = make_float4(hp.x, hp.y, hp.z, 1.0f);
+                    p.prev_n[slot] = make_float4(n.x, n.y, n.z, 0.0f);
+                } else {
+                    // transparent branch of generateNewRay (PathGeneration.hpp:138-208),
+                    // including Stack::top() popping (:64-67); capacity 3
+                    int4 st = p.stack[slot];
+                    int stk[3] = {st.x, st.y, st.z};
+                    int ss = st.w;
+                    float n1, n2;
+                    if (ss > 0 && stk[ss - 1] == obj) {
+                        n1 = M.ior;
+                        --ss;
+                        if (ss == 0) n2 = 1;
+                        else n2 = object_ior(p, stk[--ss]);
+                        if (ss < 3) stk[ss++] = obj;
+                    } else {
+                        n2 = M.ior;
+                        if (ss == 0) n1 = 1;
+                        else n1 = object_ior(p, stk[--ss]);
+                    }
+                    const float eta = n1 / n2;
+                    const float d = dot(rv, normal);
+                    const float k = 1 - eta * eta * (1 - d * d);
+                    if (n1 > n2 && k < 0) {
+                        new_v = sub(rv, mul(mul(normal, 2.0f), d));
+                    } else {
+                        const float rr = (n1 - n2) / (n1 + n2);
+                        const float R0 = rr * rr;
+                        const float cosT1 = 1 - (-d);
+                        const float c2 = cosT1 * cosT1;
+                        const float c4 = c2 * c2;
+                        const float c5 = c4 * cosT1;
+                        const float F = (float)((double)R0 + (1.0 - (double)R0) * (double)c5);
+                        if (u[2] < F) {
+                            new_v = sub(rv, mul(mul(normal, 2.0f), d));
+                        } else {
+                            if (ss > 0 && stk[ss - 1] == obj) --ss;
+                            else if (ss < 3) stk[ss++] = obj;
+                            normal = mul(normal, -1.0f);
+                            const float dotp = -d;
+                            new_v = add(mul(normal, __fsqrt_rn(k) - dotp * eta), mul(rv, eta));
+                        }
+                    }
+                    new_o = hp;
+                    p.stack[slot] = make_int4(stk[0], stk[1], stk[2], ss);
+                    p.prev_p[slot] = make_float4(hp.x, hp.y, hp.z, 0.0f);
+                }
+                new_o = add(new_o, mul(normal, 1e-5f));
+                p.rays[2 * slot] = make_float4(new_o.x, new_o.y, new_o.z, __int_as_float(0x7f800000));
+                p.rays[2 * slot + 1] = make_float4(new_v.x, new_v.y, new_v.z, 0.0f);
+                p.thr[slot] = thr;
+                p.color[slot] = col;
+                keep = !last;
+            }
+        }
+        warp_append(keep, slot, next_list, p.counts + b + 1);
+        warp_append(shadow, slot, p.shadow_list, p.counts + 64 + b);
+    }
+}
+
+// Shadow rays of bounce b: the next-event contribution counts when unoccluded.
+template <int MODE>
+__global__ void __launch_bounds__(kTraceBlock) k_wave_shadow(RenderParams p, int b)
+{
+    const uint32_t count = p.counts[64 + b];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const uint32_t slot = p.shadow_list[i];
+        DevRay r;
+        const bool valid = load_ray(reinterpret_cast<const dr_ray *>(p.shadow_rays), slot, r);
+        const bool occluded = valid && any_hit<MODE>(p.trace, r);
+        if (!occluded) p.color[slot] = add4(p.color[slot], p.pending[slot]);
+    }
+}
+
+// Buffers::color update of the reference (pixel.w++; pixel = pixel + color),
+// samples of a pixel in sample order.
+__global__ void __launch_bounds__(256) k_accumulate(RenderParams p)
+{
+    const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pix >= p.npix) return;
+    float4 acc = p.accum[pix];
+    uint32_t casts = 0;
+    for (uint32_t s = 0; s < p.spp_wave; ++s) {
+        const uint32_t slot = s * p.npix + pix;
+        acc.w = acc.w + 1.0f;
+        acc = add4(acc, p.color[slot]);
+        casts += p.casts[slot];
+    }
+    p.accum[pix] = acc;
+    if (p.pix_casts) p.pix_casts[pix] += casts;
+}
+
+template <typename T>
+T *carve(char *&ptr, size_t count)
+{
+    T *out = reinterpret_cast<T *>(ptr);
+    ptr += (count * sizeof(T) + 255) & ~size_t(255);
+    return out;
+}
+
+size_t wave_bytes(uint32_t W)
+{
+    return (size_t)W * 200 + 128 * sizeof(uint32_t) + 16 * 256;
+}
+
+}  // namespace
+}  // namespace dr
+
+using namespace dr;
+
+extern "C" dr_status dr_render(dr_scene *s, const dr_camera *cam, const dr_render_config *cfg, float *accum_dev,
+                               uint32_t *casts_dev, void *stream)
+{
+    DR_CHECK_ARG(s && cam && cfg && accum_dev, "dr_render: NULL argument");
+    DR_CHECK_ARG(cam->width > 0 && cam->height > 0, "dr_render: empty image");
+    DR_CHECK_ARG(cfg->max_depth >= 1 && cfg->max_depth <= (uint32_t)kMaxDepth, "dr_render: max_depth must be in [1, 63]");
+    DR_CHECK_ARG(cfg->tri_mode == DR_TRI_REFERENCE || cfg->tri_mode == DR_TRI_WATERTIGHT, "dr_render: bad tri_mode");
+    DR_CHECK_ARG((reinterpret_cast<uintptr_t>(accum_dev) & 15) == 0, "dr_render: accum must be 16-byte aligned");
+    if (cfg->spp == 0) return DR_OK;
+    DR_CUDA(cudaSetDevice(s->ctx->device));
+    auto st = static_cast<cudaStream_t>(stream);
+    const uint64_t npix64 = (uint64_t)cam->width * (uint64_t)cam->height;
+    DR_CHECK_ARG(npix64 < (1ull << 31), "dr_render: image too large");
+    const uint32_t npix = (uint32_t)npix64;
+    const uint32_t target = cfg->wave_paths ? cfg->wave_paths : (1u << 21);
+    const uint32_t spp_wave = std::max<uint32_t>(1, std::min<uint32_t>(cfg->spp, target / npix));
+    const uint32_t W = npix * spp_wave;
+    const size_t need = wave_bytes(W);
+    if (s->wave_bytes < need) {
+        DR_CUDA(cudaStreamSynchronize(st));
+        cudaFree(s->d_wave);
+        s->d_wave = nullptr;
+        s->wave_bytes = 0;
+        DR_CUDA(cudaMalloc(&s->d_wave, need));
+        s->wave_bytes = need;
+    }
+    RenderParams p{};
+    p.trace.nodes = s->d_nodes;
+    p.trace.tri_ref = s->d_tri_ref;
+    p.trace.tri_wt = s->d_tri_wt;
+    p.trace.prim = s->d_prim;
+    p.trace.num_nodes = s->num_nodes;
+    p.trace.error = s->ctx->d_error;
+    p.shade = s->d_shade;
+    p.objects = s->d_objects;
+    p.materials = s->d_materials;
+    p.light_table = s->d_light_table;
+    p.tri_tables = s->d_tri_tables;
+    p.num_objects = s->num_objects;
+    p.total_power = s->total_radiant_power;
+    p.lights = s->lights ? 1 : 0;
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 4; ++c) p.m[r * 4 + c] = cam->transform[r * 4 + c];
+    p.focal = cam->focal_length;
+    p.cx = cam->center[0];
+    p.cy = cam->center[1];
+    p.psx = cam->pixel_size[0];
+    p.psy = cam->pixel_size[1];
+    p.width = cam->width;
+    p.height = cam->height;
+    p.pixel_sampling = cfg->pixel_sampling;
+    p.npix = npix;
+    p.max_depth = cfg->max_depth;
+    p.seed_lo = (uint32_t)cfg->seed;
+    p.seed_hi = (uint32_t)(cfg->seed >> 32);
+    char *ptr = static_cast<char *>(s->d_wave);
+    p.rays = carve<float4>(ptr, (size_t)W * 2);
+    p.hits = carve<float2>(ptr, W);
+    p.thr = carve<float4>(ptr, W);
+    p.color = carve<float4>(ptr, W);
+    p.prev_p = carve<float4>(ptr, W);
+    p.prev_n = carve<float4>(ptr, W);
+    p.pending = carve<float4>(ptr, W);
+    p.shadow_rays = carve<float4>(ptr, (size_t)W * 2);
+    p.stack = carve<int4>(ptr, W);
+    p.casts = carve<uint32_t>(ptr, W);
+    p.list[0] = carve<uint32_t>(ptr, W);
+    p.list[1] = carve<uint32_t>(ptr, W);
+    p.shadow_list = carve<uint32_t>(ptr, W);
+    p.counts = carve<uint32_t>(ptr, 128);
+    p.accum = reinterpret_cast<float4 *>(accum_dev);
+    p.pix_casts = casts_dev;
+
+    const int sms = s->ctx->num_sms;
+    const unsigned trace_grid = (unsigned)std::min<uint64_t>((W + kTraceBlock - 1) / kTraceBlock, (uint64_t)sms * 16);
+    const unsigned shade_grid = (unsigned)std::min<uint64_t>((W + kRenderBlock - 1) / kRenderBlock, (uint64_t)sms * 16);
+    for (uint32_t done = 0; done < cfg->spp; done += spp_wave) {
+        p.spp_wave = std::min(spp_wave, cfg->spp - done);
+        p.wave = npix * p.spp_wave;
+        p.sample_base = cfg->sample_offset + done;
+        DR_CUDA(cudaMemsetAsync(p.counts, 0, 128 * sizeof(uint32_t), st));
+        k_camera<<<(p.wave + kRenderBlock - 1) / kRenderBlock, kRenderBlock, 0, st>>>(p);
+        for (int b = 0; b < (int)cfg->max_depth; ++b) {
+            if (cfg->tri_mode == DR_TRI_WATERTIGHT) k_wave_closest<1><<<trace_grid, kTraceBlock, 0, st>>>(p, b);
+            else k_wave_closest<0><<<trace_grid, kTraceBlock, 0, st>>>(p, b);
+            k_shade<<<shade_grid, kRenderBlock, 0, st>>>(p, b);
+            if (cfg->tri_mode == DR_TRI_WATERTIGHT) k_wave_shadow<1><<<trace_grid, kTraceBlock, 0, st>>>(p, b);
+            else k_wave_shadow<0><<<trace_grid, kTraceBlock, 0, st>>>(p, b);
+        }
+        k_accumulate<<<(npix + 255) / 256, 256, 0, st>>>(p);
+        DR_CUDA(cudaGetLastError());
+    }
+    return DR_OK;
+}

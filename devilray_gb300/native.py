@@ -73,6 +73,29 @@ class SceneInfo(C.Structure):
                 ("device_bytes", C.c_uint64), ("build_seconds", C.c_double)]
 
 
+class Camera(C.Structure):
+    _fields_ = [("transform", C.c_float * 16), ("focal_length", C.c_float), ("center", C.c_float * 2),
+                ("width", C.c_int32), ("height", C.c_int32), ("pixel_size", C.c_float * 2)]
+
+
+class RenderConfig(C.Structure):
+    _fields_ = [("max_depth", C.c_uint32), ("spp", C.c_uint32), ("sample_offset", C.c_uint32),
+                ("pixel_sampling", C.c_int32), ("seed", C.c_uint64), ("tri_mode", C.c_int32),
+                ("wave_paths", C.c_uint32), ("flags", C.c_uint32), ("pad", C.c_uint32)]
+
+
+def make_camera(cam: dict) -> Camera:
+    """dr_camera from the dict of devilray_gb300.scenes.camera()."""
+    c = Camera()
+    for i in range(16):
+        c.transform[i] = float(cam["m"][i])
+    c.focal_length = float(cam["focal"])
+    c.center[0], c.center[1] = float(cam["cx"]), float(cam["cy"])
+    c.width, c.height = int(cam["width"]), int(cam["height"])
+    c.pixel_size[0], c.pixel_size[1] = float(cam["psx"]), float(cam["psy"])
+    return c
+
+
 class TraceCounters(C.Structure):
     _fields_ = [("rays", C.c_uint64), ("node_visits", C.c_uint64), ("box_tests", C.c_uint64),
                 ("tri_tests", C.c_uint64), ("hits", C.c_uint64)]
@@ -92,6 +115,8 @@ SIGNATURES = {
                                    C.POINTER(TraceCounters), C.c_void_p]),
     "dr_trace_any": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_int32, C.c_void_p]),
     "dr_trace_closest_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_int32, C.c_void_p]),
+    "dr_render": (C.c_int, [C.c_void_p, C.POINTER(Camera), C.POINTER(RenderConfig), C.c_void_p, C.c_void_p,
+                            C.c_void_p]),
     "dr_alias_build": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_int32, C.c_void_p]),
     "dr_alias_build_noalloc": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
     "dr_alias_sample": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p,
@@ -188,6 +213,19 @@ def alias_sample(table_dev, n: int, uniforms_dev, ndraws: int, index_dev, pdf_de
 class Scene:
     """A triangle soup uploaded with its BVH (dr_scene_create)."""
 
+    @classmethod
+    def from_spec(cls, ctx: "Context", spec, **kw) -> "Scene":
+        """Scene from a devilray_gb300.scenes.SceneSpec (objects + materials)."""
+        objs = [Object(int(b), int(c), int(m), float(a)) for (b, c, m, a) in spec.objects]
+        mats = []
+        for m in spec.materials:
+            mm = Material()
+            mm.kind, mm.ior = m["kind"], m["ior"]
+            for i in range(4):
+                mm.emission[i], mm.albedo[i], mm.debug_color[i] = m["emission"][i], m["albedo"][i], m["debug"][i]
+            mats.append(mm)
+        return cls(ctx, spec.positions, objects=objs, materials=mats, **kw)
+
     def __init__(self, ctx: Context, positions: np.ndarray, objects=None, materials=None,
                  tri_material=None, tri_weight=None, max_leaf_size: int = 0, sah_bins: int = 0,
                  threads: int = 0):
@@ -247,6 +285,15 @@ class Scene:
     def trace_any(self, rays_dev, n: int, occluded_dev, tri_mode: int = DR_TRI_REFERENCE, stream=None):
         check(load().dr_trace_any(self.handle, _ptr(rays_dev), n, _ptr(occluded_dev), tri_mode,
                                   _stream_ptr(stream)))
+
+    # -- rendering --
+    def render(self, cam: dict, accum_dev, casts_dev=None, spp: int = 1, max_depth: int = 10,
+               sample_offset: int = 0, pixel_sampling: int = 1, seed: int = 0, tri_mode: int = DR_TRI_REFERENCE,
+               wave_paths: int = 0, stream=None):
+        c = make_camera(cam)
+        cfg = RenderConfig(max_depth, spp, sample_offset, pixel_sampling, seed, tri_mode, wave_paths, 0, 0)
+        check(load().dr_render(self.handle, C.byref(c), C.byref(cfg), _ptr(accum_dev), _ptr(casts_dev),
+                               _stream_ptr(stream)))
 
     # -- traversal on host buffers --
     def trace_closest_host(self, rays: np.ndarray, hits: np.ndarray | None = None,

@@ -102,3 +102,122 @@ def incoherent_rays(n: int, seed: int = 0, tmax: float = np.inf, chunk: int = 1 
 def rays6(rays8: np.ndarray) -> np.ndarray:
     """dr_ray [n, 8] -> reference Ray {p, v} [n, 6]."""
     return np.ascontiguousarray(np.concatenate([rays8[:, 0:3], rays8[:, 4:7]], axis=1), np.float32)
+
+
+# ---- scenes with materials (flattened: objects are contiguous triangle ranges) ----
+
+def _f32(x):
+    return np.asarray(x, np.float32)
+
+
+def _cross32(a, b):
+    return np.stack([a[..., 1] * b[..., 2] - a[..., 2] * b[..., 1],
+                     a[..., 2] * b[..., 0] - a[..., 0] * b[..., 2],
+                     a[..., 0] * b[..., 1] - a[..., 1] * b[..., 0]], axis=-1).astype(np.float32)
+
+
+def tri_area_f32(soup: np.ndarray) -> np.ndarray:
+    """triangleArea (include/Utils.hpp:218-224) in FP32, one rounding per op."""
+    s = _f32(soup).reshape(-1, 3, 3)
+    A, B, C = s[:, 0], s[:, 1], s[:, 2]
+    c = _cross32((A - B).astype(np.float32), (A - C).astype(np.float32))
+    l2 = ((c[:, 0] * c[:, 0]).astype(np.float32) + (c[:, 1] * c[:, 1]).astype(np.float32)).astype(np.float32)
+    l2 = (l2 + (c[:, 2] * c[:, 2]).astype(np.float32)).astype(np.float32)
+    return (np.sqrt(l2).astype(np.float32) / np.float32(2)).astype(np.float32)
+
+
+def surface_area(soup: np.ndarray) -> float:
+    """totalSurfaceArea (src/GpuTris.cpp:40-58): FP32 triangle areas summed in
+    order in double, then rounded to FP32."""
+    a = tri_area_f32(soup).astype(np.float64)
+    return float(np.float32(np.cumsum(a)[-1] if a.size else 0.0))
+
+
+def quad(center, normal, right, size) -> np.ndarray:
+    """createQuadMesh (src/GpuTris.cpp:87-107) in FP32: two triangles (0,2,1), (0,3,2)."""
+    c, n, r = _f32(center), _f32(normal), _f32(right)
+    up = _cross32(r, n)
+    h = np.float32(size) / np.float32(2)
+    pts = [((c + r * -h).astype(np.float32) + up * -h).astype(np.float32),
+           ((c + r * h).astype(np.float32) + up * -h).astype(np.float32),
+           ((c + r * h).astype(np.float32) + up * h).astype(np.float32),
+           ((c + r * -h).astype(np.float32) + up * h).astype(np.float32)]
+    return np.array([np.concatenate([pts[0], pts[2], pts[1]]), np.concatenate([pts[0], pts[3], pts[2]])], np.float32)
+
+
+def material(kind=0, emission=(0, 0, 0), albedo=(0, 0, 0), ior=1.0, debug=(0.5, 0.5, 0.5)):
+    return {"kind": int(kind), "ior": float(ior), "emission": tuple(emission) + (0.0,) * (4 - len(emission)),
+            "albedo": tuple(albedo) + (0.0,) * (4 - len(albedo)), "debug": tuple(debug) + (0.0,) * (4 - len(debug))}
+
+
+class SceneSpec:
+    """A flattened scene: soup [N, 9] float32, objects (tri_begin, tri_count,
+    material, surface_area) and materials."""
+
+    def __init__(self):
+        self.parts: list[np.ndarray] = []
+        self.objects: list[tuple[int, int, int, float]] = []
+        self.materials: list[dict] = []
+        self.count = 0
+
+    def add_material(self, m: dict) -> int:
+        self.materials.append(m)
+        return len(self.materials) - 1
+
+    def add_object(self, soup: np.ndarray, mat: int, area: float | None = None) -> int:
+        soup = _f32(soup).reshape(-1, 9)
+        self.parts.append(soup)
+        self.objects.append((self.count, soup.shape[0], mat, surface_area(soup) if area is None else area))
+        self.count += soup.shape[0]
+        return len(self.objects) - 1
+
+    @property
+    def positions(self) -> np.ndarray:
+        return np.concatenate(self.parts).astype(np.float32) if self.parts else np.zeros((0, 9), np.float32)
+
+    def materials_array(self) -> np.ndarray:
+        """dr_material layout: [kind, ior, 0, 0, emission4, albedo4, debug4] as float32
+        (kind stored as its int32 bit pattern)."""
+        out = np.zeros((len(self.materials), 16), np.float32)
+        for i, m in enumerate(self.materials):
+            out[i, 0] = np.array([m["kind"]], np.int32).view(np.float32)[0]
+            out[i, 1] = m["ior"]
+            out[i, 4:8] = m["emission"]
+            out[i, 8:12] = m["albedo"]
+            out[i, 12:16] = m["debug"]
+        return out
+
+    def objects_array(self) -> np.ndarray:
+        dt = np.dtype([("tri_begin", "<u4"), ("tri_count", "<u4"), ("material", "<i4"), ("surface_area", "<f4")])
+        return np.array(self.objects, dt)
+
+
+def camera(width: int, height: int, focal: float = 1.0, fov_half_width: float = 0.375, transform=None) -> dict:
+    """Pinhole camera (include/tracing/Camera.hpp) with the principal point at
+    the image centre; `fov_half_width` = half the sensor width / focal length."""
+    ps = np.float32(2.0 * fov_half_width * focal / width)
+    m = np.eye(4, dtype=np.float32) if transform is None else _f32(transform)
+    return {"m": m.reshape(16), "focal": np.float32(focal), "cx": np.float32(width / 2.0) * ps,
+            "cy": np.float32(height / 2.0) * ps, "width": int(width), "height": int(height), "psx": ps, "psy": ps}
+
+
+def box_room(sphere_level: int = 3) -> SceneSpec:
+    """The box room of the plain-method configuration: five axis-aligned
+    quads (albedo 0.75, red/green side walls 0.6), a ceiling light quad
+    (radiance 15) and a dielectric icosphere (IOR 1.5) in the middle; laid out
+    like the reference's interactive scene (renderer/src/SceneSetup.cpp:120-131)."""
+    s = SceneSpec()
+    white = s.add_material(material(0, albedo=(0.75, 0.75, 0.75)))
+    red = s.add_material(material(0, albedo=(0.6, 0.1, 0.1)))
+    green = s.add_material(material(0, albedo=(0.1, 0.6, 0.1)))
+    light = s.add_material(material(0, emission=(15.0, 15.0, 15.0)))
+    glass = s.add_material(material(1, ior=1.5))
+    s.add_object(quad((0, 0, 2.5), (0, 0, -1), (1, 0, 0), 1.0), white)
+    s.add_object(quad((0.5, 0, 2), (-1, 0, 0), (0, 1, 0), 1.0), red)
+    s.add_object(quad((-0.5, 0, 2), (1, 0, 0), (0, 1, 0), 1.0), green)
+    s.add_object(quad((0, 0.5, 2), (0, -1, 0), (0, 0, 1), 1.0), white)
+    s.add_object(quad((0, -0.5, 2), (0, 1, 0), (0, 0, 1), 1.0), white)
+    s.add_object(quad((0, 0.4999, 2), (0, -1, 0), (0, 0, 1), 0.4), light)
+    sph = (np.array([0.0, -0.2, 2.0]) + 0.25 * icosphere_soup(sphere_level).reshape(-1, 3, 3)).reshape(-1, 9)
+    s.add_object(sph.astype(np.float32), glass)
+    return s

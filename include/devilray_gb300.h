@@ -177,6 +177,46 @@ dr_status dr_trace_any(dr_scene *scene, const dr_ray *rays_dev, uint64_t n, uint
 dr_status dr_trace_closest_host(dr_scene *scene, const dr_ray *rays_host, uint64_t n, dr_hit *hits_host,
                                 int32_t tri_mode, void *stream);
 
+/* ---- rendering ----------------------------------------------------------------------- */
+
+/* Pinhole camera (include/tracing/Camera.hpp:6-19): row-major 4x4
+ * camera-to-world transform (Matrix4x4f::values), focal length, principal
+ * point and physical pixel size in sensor units, resolution in pixels. */
+typedef struct dr_camera {
+    float transform[16];
+    float focal_length;
+    float center[2];
+    int32_t width, height;
+    float pixel_size[2];
+} dr_camera;
+
+typedef enum dr_pixel_sampling { DR_PIXEL_CENTER = 0, DR_PIXEL_UNIFORM_RANDOM = 1 } dr_pixel_sampling;
+
+typedef struct dr_render_config {
+    uint32_t max_depth;      /* path vertices per sample (reference: 10, PathGeneration.hpp:380) */
+    uint32_t spp;            /* samples per pixel added by this call */
+    uint32_t sample_offset;  /* index of the first sample (progressive rendering) */
+    int32_t pixel_sampling;  /* dr_pixel_sampling */
+    uint64_t seed;           /* Philox key */
+    int32_t tri_mode;        /* dr_tri_mode */
+    uint32_t wave_paths;     /* paths in flight per wave, 0 = automatic */
+    uint32_t flags;          /* reserved, 0 */
+    uint32_t pad;
+} dr_render_config;
+
+/* Adds cfg->spp path samples per pixel to accum_dev (float4 per pixel, row
+ * major: rgb sums and the sample count in w, as Buffers::color of
+ * include/Buffers.hpp:9-22) and the path-ray casts to casts_dev (uint32 per
+ * pixel, may be NULL). Replaces Renderer::render / cuda_render / sampleColor
+ * (src/Renderer.cpp:198-233, src/device/RendererImpl.hpp:22-102,
+ * include/tracing/PathGeneration.hpp:363-515) with a wavefront of kernels:
+ * camera rays, closest hit, shading with next-event estimation and MIS, shadow
+ * any hit, accumulation. Uniforms come from Philox4x32-10 indexed by (pixel,
+ * sample, dimension); samples are added to a pixel in sample order.
+ * Asynchronous on `stream`. */
+dr_status dr_render(dr_scene *scene, const dr_camera *camera, const dr_render_config *cfg, float *accum_dev,
+                    uint32_t *casts_dev, void *stream);
+
 /* ---- alias tables ------------------------------------------------------------------- */
 
 /* AliasEntry of include/tracing/DistributionSamplers.hpp:44-51, 20 bytes. */

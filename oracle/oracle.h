@@ -99,6 +99,43 @@ void or_alias_sample(const or_alias_entry *table, int32_t n, float u0, float u1,
  * std::mt19937(seed) + std::lognormal_distribution<float>(0,1). */
 void or_lognormal_input(int32_t n, uint32_t seed, float *out);
 
+/* ---- integrator (include/tracing/PathGeneration.hpp:363-515) ------------- */
+
+typedef struct or_object { uint32_t tri_begin, tri_count; int32_t material; float surface_area; } or_object;
+typedef struct or_material {
+    int32_t kind; float ior; float pad0, pad1;
+    float emission[4]; float albedo[4]; float debug_color[4];
+} or_material;                                           /* the dr_material layout */
+typedef struct or_camera {
+    float m[16];                                         /* row-major camera-to-world */
+    float focal, cx, cy;
+    int32_t width, height;
+    float psx, psy;
+} or_camera;
+typedef struct or_render_cfg {
+    int32_t max_depth, spp, sample_offset, pixel_sampling;   /* 0 centre, 1 uniform random */
+    uint64_t seed;
+    int32_t rng_mode;        /* 0: Philox indexed by (pixel, sample, dim); 1: replayed stream */
+    int32_t trig_mode;       /* 0: portable polynomials; 1: std::sin/cos/acos */
+    int32_t cast_mode;       /* 0: canonical closest hit; 1: the reference's per-object cast */
+    int32_t tri_table_order; /* 0: soup order; 1: per-object BBH-sorted order */
+    int32_t threads;
+    int32_t replay_stride;   /* uniforms per (pixel, sample) in `replay` */
+    const float *replay;     /* [pixel][sample][replay_stride] */
+} or_render_cfg;
+
+typedef struct or_scene or_scene;
+or_scene *or_scene_create(const float *positions, int32_t num_tris, const or_object *objects, int32_t num_objects,
+                          const or_material *materials, int32_t num_materials, const int32_t *tri_material);
+void or_scene_destroy(or_scene *s);
+float or_scene_total_power(const or_scene *s);
+void or_scene_light_table(const or_scene *s, or_alias_entry *out);
+/* sample_rgb: [spp][height*width][3] per-sample colour, accum: [height*width][4]
+ * (sum and sample count as Buffers::color), casts: [height*width] path rays.
+ * Any output may be NULL. */
+void or_render(const or_scene *s, const or_camera *cam, const or_render_cfg *cfg, float *sample_rgb, float *accum,
+               uint32_t *casts);
+
 /* ---- Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) ------------------- */
 void or_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 

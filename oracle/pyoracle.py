@@ -281,3 +281,109 @@ def ref_lognormal(n: int, seed: int = 42) -> np.ndarray:
     out = np.zeros(n, np.float32)
     ref().refh_lognormal(n, seed, out)
     return out
+
+
+# ---- integrator ------------------------------------------------------------------
+
+class RenderCfg(C.Structure):
+    _fields_ = [("max_depth", C.c_int32), ("spp", C.c_int32), ("sample_offset", C.c_int32),
+                ("pixel_sampling", C.c_int32), ("seed", C.c_uint64), ("rng_mode", C.c_int32),
+                ("trig_mode", C.c_int32), ("cast_mode", C.c_int32), ("tri_table_order", C.c_int32),
+                ("threads", C.c_int32), ("replay_stride", C.c_int32), ("replay", C.c_void_p)]
+
+
+class Camera(C.Structure):
+    _fields_ = [("m", C.c_float * 16), ("focal", C.c_float), ("cx", C.c_float), ("cy", C.c_float),
+                ("width", C.c_int32), ("height", C.c_int32), ("psx", C.c_float), ("psy", C.c_float)]
+
+
+def make_camera(cam: dict) -> Camera:
+    c = Camera()
+    for i in range(16):
+        c.m[i] = float(cam["m"][i])
+    c.focal, c.cx, c.cy = float(cam["focal"]), float(cam["cx"]), float(cam["cy"])
+    c.width, c.height = int(cam["width"]), int(cam["height"])
+    c.psx, c.psy = float(cam["psx"]), float(cam["psy"])
+    return c
+
+
+def _render_lib():
+    L = lib()
+    if not getattr(L, "_render_bound", False):
+        L.or_scene_create.argtypes = [_f32p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p]
+        L.or_scene_create.restype = C.c_void_p
+        L.or_scene_destroy.argtypes = [C.c_void_p]
+        L.or_scene_total_power.argtypes = [C.c_void_p]
+        L.or_scene_total_power.restype = C.c_float
+        L.or_scene_light_table.argtypes = [C.c_void_p, C.c_void_p]
+        L.or_render.argtypes = [C.c_void_p, C.POINTER(Camera), C.POINTER(RenderCfg), C.c_void_p, C.c_void_p,
+                                C.c_void_p]
+        L._render_bound = True
+    return L
+
+
+class RenderScene:
+    """Oracle scene for the integrator restatement."""
+
+    def __init__(self, spec):
+        L = _render_lib()
+        self.pos = _f32(spec.positions).reshape(-1)
+        self.objs = spec.objects_array()
+        self.mats = spec.materials_array()
+        self.h = L.or_scene_create(self.pos, self.pos.size // 9, self.objs.ctypes.data, len(self.objs),
+                                   self.mats.ctypes.data, len(self.mats), None)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            _render_lib().or_scene_destroy(self.h)
+            self.h = None
+
+    @property
+    def total_power(self) -> float:
+        return _render_lib().or_scene_total_power(self.h)
+
+    def light_table(self) -> np.ndarray:
+        out = np.zeros(len(self.objs), ALIAS_DTYPE)
+        _render_lib().or_scene_light_table(self.h, out.ctypes.data)
+        return out
+
+    def render(self, cam: dict, spp: int, max_depth: int = 10, seed: int = 0, sample_offset: int = 0,
+               pixel_sampling: int = 1, rng_mode: int = 0, trig_mode: int = 0, cast_mode: int = 0,
+               tri_table_order: int = 0, replay: np.ndarray | None = None, threads: int = 0,
+               per_sample: bool = False):
+        cfg = RenderCfg(max_depth, spp, sample_offset, pixel_sampling, seed, rng_mode, trig_mode, cast_mode,
+                        tri_table_order, threads, 0, None)
+        if replay is not None:
+            replay = _f32(replay)
+            cfg.replay_stride = replay.shape[-1]
+            cfg.replay = replay.ctypes.data
+        w, h = cam["width"], cam["height"]
+        accum = np.zeros((h * w, 4), np.float32)
+        casts = np.zeros(h * w, np.uint32)
+        rgb = np.zeros((spp, h * w, 3), np.float32) if per_sample else None
+        c = make_camera(cam)
+        _render_lib().or_render(self.h, C.byref(c), C.byref(cfg), rgb.ctypes.data if rgb is not None else None,
+                                accum.ctypes.data, casts.ctypes.data)
+        return accum, casts, rgb
+
+
+def ref_render_samples(spec, cam: dict, spp: int, replay: np.ndarray, sampling: int = 1):
+    """The reference's own sampleColor (depth 10) on every pixel sample."""
+    L = ref()
+    if not getattr(L, "_render_bound", False):
+        L.refh_render_samples.argtypes = [_f32p, _i32p, _i32p, _i32p, _f32p, C.c_int, _f32p, C.c_int, _f32p,
+                                          C.c_float, C.c_float, C.c_float, C.c_int, C.c_int, C.c_float, C.c_float,
+                                          C.c_int, C.c_int, _f32p, C.c_int, _f32p, _u32p]
+        L._render_bound = True
+    objs = spec.objects_array()
+    w, h = cam["width"], cam["height"]
+    rgb = np.zeros((spp, h * w, 3), np.float32)
+    casts = np.zeros(h * w, np.uint32)
+    replay = _f32(replay)
+    L.refh_render_samples(_f32(spec.positions).reshape(-1), objs["tri_begin"].astype(np.int32),
+                          objs["tri_count"].astype(np.int32), objs["material"].astype(np.int32),
+                          objs["surface_area"].astype(np.float32), len(objs), spec.materials_array().reshape(-1),
+                          len(spec.materials), _f32(cam["m"]), float(cam["focal"]), float(cam["cx"]),
+                          float(cam["cy"]), w, h, float(cam["psx"]), float(cam["psy"]), sampling, spp,
+                          replay.reshape(-1), replay.shape[-1], rgb.reshape(-1), casts)
+    return rgb, casts

@@ -7,6 +7,7 @@
 
 #include <cstdint>
 #include <cstring>
+#include <memory>
 #include <limits>
 #include <numbers>
 #include <random>
@@ -233,6 +234,112 @@ void refh_camera_ray(const float *m16, float focal, float cx, float cy, float ps
     const Ray r = cameraRay(cam, Vec2f{px, py}, static_cast<PixelSampling>(sampling), 0, rng);
     ray_out[0] = r.p.x; ray_out[1] = r.p.y; ray_out[2] = r.p.z;
     ray_out[3] = r.v.x; ray_out[4] = r.v.y; ray_out[5] = r.v.z;
+}
+
+// sampleColor (include/tracing/PathGeneration.hpp:363-515, max_depth 10) on a
+// flattened scene: each object becomes a Mesh of its triangles (triangle k
+// owning points 3k..3k+2) with an identity transform, its BBH from
+// generateSimpleBBH and its triangle sampler built after the sort
+// (test/src/TracingTestHelpers.hpp:97-112); the light table follows
+// Renderer::calculateLightWeights (src/Renderer.cpp:113-152) with the
+// reference's radiantExitance and luminance. Uniforms are replayed from
+// `replay` ([pixel][sample][stride]); out_rgb receives each sample's colour.
+void refh_render_samples(const float *pos, const int *obj_begin, const int *obj_count, const int *obj_mat,
+                         const float *obj_area, int nobj, const float *mats, int nmat, const float *m16, float focal,
+                         float cx, float cy, int width, int height, float psx, float psy, int sampling, int spp,
+                         const float *replay, int stride, float *out_rgb, unsigned *casts_out)
+{
+    std::vector<Material> materials;
+    for (int i = 0; i < nmat; ++i) {
+        const float *m = mats + i * 16;
+        int32_t kind;  // dr_material::kind is an int32 in the first word
+        std::memcpy(&kind, m, sizeof(kind));
+        if (kind == 1) {
+            TransparentMaterial t{};
+            t.debug_color = Vec4{m[12], m[13], m[14], m[15]};
+            t.inside_medium = Medium{.ior = m[1]};
+            materials.push_back(t);
+        } else {
+            DiffuseMaterial d{};
+            d.debug_color = Vec4{m[12], m[13], m[14], m[15]};
+            d.emission = Vec4{m[4], m[5], m[6], m[7]};
+            d.diffuse_reflectance = Vec4{m[8], m[9], m[10], m[11]};
+            materials.push_back(d);
+        }
+    }
+    struct Obj {
+        Mesh mesh;
+        BBH bbh{0, DeviceVector<BBHNode>{{}}};
+        AliasTable sampler;
+    };
+    std::vector<std::unique_ptr<Obj>> store;
+    std::vector<TriangleMesh> objects;
+    for (int o = 0; o < nobj; ++o) {
+        auto ob = std::make_unique<Obj>();
+        ob->mesh.name = "object";
+        for (int k = 0; k < obj_count[o]; ++k) {
+            const float *q = pos + (size_t)(obj_begin[o] + k) * 9;
+            for (int j = 0; j < 3; ++j) ob->mesh.points.push_back(Vec3{q[j * 3], q[j * 3 + 1], q[j * 3 + 2]});
+            ob->mesh.normals.push_back(Vec3{0, 0, 1});
+            const uint32_t b = 3u * k;
+            ob->mesh.triangles.push_back(Triangle{.a = {b, (uint32_t)k}, .b = {b + 1, (uint32_t)k}, .c = {b + 2, (uint32_t)k}});
+        }
+        ob->bbh = generateSimpleBBH(ob->mesh);
+        std::vector<float> areas;
+        for (const auto &t : ob->mesh.triangles)
+            areas.push_back(triangleArea(ob->mesh.points[t.a.pi], ob->mesh.points[t.b.pi], ob->mesh.points[t.c.pi]));
+        ob->sampler = generateAliasTable(areas);
+        TriangleMesh view{};
+        view.points = ob->mesh.points.data();
+        view.normals = ob->mesh.normals.data();
+        view.triangles = ob->mesh.triangles.data();
+        view.triangle_count = (int)ob->mesh.triangles.size();
+        view.model_to_world = Transform{};
+        view.material = obj_mat[o];
+        view.triangle_sampler = ob->sampler.entries.hostPtr();
+        view.surface_area = obj_area[o];
+        view.base_surface_area = obj_area[o];
+        view.bbh = BBHGpuView{std::span<const BBHNode>{ob->bbh.nodes.hostPtr(), ob->bbh.nodes.size()}};
+        objects.push_back(view);
+        store.push_back(std::move(ob));
+    }
+    std::vector<float> weights(objects.size(), 0.0f);
+    float total = 0.0f;
+    for (size_t i = 0; i < objects.size(); ++i) {
+        const auto A = objects[i].surface_area;
+        const auto M = radiantExitance(materials[objects[i].material]);
+        weights[i] = A * luminance(M);
+        total += weights[i];
+    }
+    for (size_t i = 0; i < objects.size(); ++i) weights[i] /= total;
+    const AliasTable light = generateAliasTable(weights);
+    const ObjectsInfo info{.total_radiant_power = total};
+    Camera cam{};
+    std::memcpy(cam.transform.values, m16, sizeof(float) * 16);
+    cam.intrinsics = Intrinsics{.focal_length = focal, .center = Vec2f{cx, cy}};
+    cam.resolution = Size2i{width, height};
+    cam.physical_pixel_size = Size2f{psx, psy};
+    const size_t npix = (size_t)width * height;
+    for (int y = 0; y < height; ++y)
+        for (int x = 0; x < width; ++x) {
+            const size_t pix = (size_t)y * width + x;
+            unsigned casts = 0;
+            for (int s2 = 0; s2 < spp; ++s2) {
+                Vec4 pixel{0, 0, 0, 0};
+                SampleStats stats{.ray_casts = 0};
+                ReplayRng rng{replay + (pix * spp + s2) * stride, (size_t)stride};
+                sampleColor(Vec2f{(float)x, (float)y}, pixel, stats, cam, static_cast<PixelSampling>(sampling),
+                            std::span<const TriangleMesh>{objects}, info, std::span<const Material>{materials},
+                            std::span<const AliasEntry>{light.entries.hostPtr(), light.entries.size()},
+                            DebugOptions::Off, rng);
+                float *o = out_rgb + ((size_t)s2 * npix + pix) * 3;
+                o[0] = pixel.x;
+                o[1] = pixel.y;
+                o[2] = pixel.z;
+                casts += stats.ray_casts;
+            }
+            casts_out[pix] = casts;
+        }
 }
 
 }  // extern "C"

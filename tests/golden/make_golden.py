@@ -167,8 +167,27 @@ def alias_fixture():
         emitter_weights=em, emitter_table_sha=np.frombuffer(hashlib.sha256(em_tab.tobytes()).digest(), np.uint8))
 
 
+def render_fixture():
+    # sampleColor (include/tracing/PathGeneration.hpp:363-515) of the
+    # reference on the box room with a level-1 glass icosphere, every pixel
+    # sample fed a replayed stream of uniforms.
+    spec = scenes.box_room(sphere_level=1)
+    w, h, spp, stride = 12, 9, 6, 96
+    cam = scenes.camera(w, h)
+    replay = np.random.default_rng(7).random((w * h, spp, stride)).astype(np.float32)
+    out = {}
+    for sampling in (0, 1):
+        rgb, casts = po.ref_render_samples(spec, cam, spp, replay, sampling)
+        out[f"rgb_{sampling}"] = rgb
+        out[f"casts_{sampling}"] = casts
+    np.savez_compressed(OUT / "render_pin.npz", positions=spec.positions, objects=spec.objects_array(),
+                        materials=spec.materials_array(), replay=replay, width=np.int32(w), height=np.int32(h),
+                        spp=np.int32(spp), **out)
+
+
 def main():
     po.build(ref=True)
+    render_fixture()
     tri_fixture()
     box_fixture()
     bbh_fixture()
