@@ -176,7 +176,7 @@ def run_ours(args):
     from devilray_gb300 import native
     soup, rays = build_workload(rank)
     ctx = native.Context(local)
-    scene = native.Scene(ctx, soup)
+    scene = native.Scene(ctx, soup, layout=args.layout)
     info = scene.info()
     stream = torch.cuda.Stream()
     d_rays = torch.from_numpy(rays).to(f"cuda:{local}")
@@ -243,26 +243,27 @@ def run_ours(args):
         return 0
 
     hbm_peak, peak_kind = _peaks()
-    node_bytes, tri_bytes = 64, 48
+    node_bytes, tri_bytes = (80 if info.layout == 8 else 64), 48
     bytes_per_ray = 32 + 8 + nodes_per_ray * node_bytes + tris_per_ray * tri_bytes
     per_launch_ms = total_ms / args.steps
     achieved = bytes_per_ray * NUM_RAYS / (per_launch_ms / 1e3) / 1e9
     # reference mode reads the nodes, the reference triangle records and the
-    # triangle index map: 64 B per node + 52 B per triangle
-    working_set = info.num_nodes * 64 + NUM_TRIS * 52
+    # triangle index map: 64 or 80 B per node + 52 B per triangle
+    working_set = info.num_nodes * node_bytes + NUM_TRIS * 52
     line = {
         "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "num_triangles": NUM_TRIS, "num_rays": NUM_RAYS, "tri_mode": "reference",
-                   "layout": "binary two-box BVH, binned SAH", "bvh_nodes": info.num_nodes, "bvh_depth": info.depth,
+                   "layout": ("compressed 8-wide BVH (80-byte nodes), binned SAH" if info.layout == 8
+                              else "binary two-box BVH, binned SAH"), "bvh_nodes": info.num_nodes, "bvh_depth": info.depth,
                    "scene_device_bytes": working_set, "bvh_build_s": round(info.build_seconds, 3),
                    "l2": "rays 512 MiB per step > L2; scene arrays stay L2-resident across steps",
                    "parallelism": f"replicas{world}" if world > 1 else "single"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": None,
                      "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
-                     "kernel": "k_trace_closest<0,false>",
+                     "kernel": f"k_trace_closest<0,false,{info.layout}>",
                      "bytes_per_ray": bytes_per_ray, "node_visits_per_ray": nodes_per_ray,
                      "tri_tests_per_ray": tris_per_ray, "hit_fraction": hit_frac,
                      "per_launch_ms": per_launch_ms, "working_set_bytes": working_set,
@@ -280,10 +281,84 @@ def run_ours(args):
     if world == 1 and not args.no_cpu_baseline:
         cb, _ = cpu_baseline(soup, rays, args.cpu_sample, os.cpu_count() or 1)
         line["cpu_baseline"] = cb
+    if not args.no_render:
+        del d_rays, d_hits, h_rays, h_hits
+        torch.cuda.empty_cache()
+        line["render"] = render_section(ctx, native, local, stream, cpu=(world == 1 and not args.no_cpu_baseline),
+                                        threads=os.cpu_count() or 1, layout=args.render_layout)
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
     return 0
+
+
+def render_section(ctx, native, device: int, stream, cpu: bool, threads: int, layout: int = 0):
+    """1080p samples/s on the many-light configuration (1920x1080, 64 spp,
+    depth 16, 65,536 emitters) and the box room (256x256, 16 spp, depth 8);
+    each with the reference's CPU integrator (oracle port: per-object cast,
+    reference random-number order) timed on a pixel subset."""
+    import torch
+    from devilray_gb300 import scenes
+    out = {}
+    cases = [
+        ("box_room", scenes.box_room(3), scenes.camera(256, 256), 16, 8, 3),
+        ("many_light_1080p", scenes.many_light(), scenes.outside_camera(1920, 1080), 64, 16, 1),
+    ]
+    for name, spec, cam, spp, depth, reps in cases:
+        t0 = time.perf_counter()
+        scene = native.Scene.from_spec(ctx, spec, layout=layout)
+        build_s = time.perf_counter() - t0
+        npix = cam["width"] * cam["height"]
+        accum = torch.zeros((npix, 4), dtype=torch.float32, device=f"cuda:{device}")
+        casts = torch.zeros(npix, dtype=torch.int32, device=f"cuda:{device}")
+        scene.render(cam, accum, casts, spp=1, max_depth=depth, stream=stream)  # warm-up
+        stream.synchronize()
+        times = []
+        for r in range(reps):
+            accum.zero_()
+            casts.zero_()
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            scene.render(cam, accum, casts, spp=spp, max_depth=depth, stream=stream)
+            b.record(stream)
+            stream.synchronize()
+            times.append(a.elapsed_time(b) / 1e3)
+        t = min(times)
+        path_rays = int(casts.sum().item())
+        entry = {"width": cam["width"], "height": cam["height"], "spp": spp, "max_depth": depth,
+                 "layout": scene.info().layout,
+                 "triangles": int(spec.positions.shape[0]), "objects": len(spec.objects),
+                 "scene_build_s": round(build_s, 3), "seconds": t,
+                 "samples_per_s": npix * spp / t, "path_mrays_per_s": path_rays / t / 1e6,
+                 "path_rays_per_sample": path_rays / (npix * spp)}
+        if cpu:
+            entry["cpu_baseline"] = render_cpu_baseline(spec, cam, depth, threads,
+                                                        pixels=65536 if name == "box_room" else 1024)
+        out[name] = entry
+        del scene, accum, casts
+    torch.cuda.empty_cache()
+    return out
+
+
+def render_cpu_baseline(spec, cam, depth: int, threads: int, pixels: int):
+    """The reference's integrator on the CPU (oracle port of sampleColor with the
+    reference's per-object cast), `pixels` pixels x 1 sample; samples/s."""
+    from oracle import pyoracle as po
+    po.build(ref=False)
+    sub = dict(cam)
+    # a centred window of the image with the same camera geometry
+    wsub = int(np.sqrt(pixels))
+    sub["width"] = sub["height"] = wsub
+    sub["cx"] = np.float32(cam["cx"] - np.float32((cam["width"] - wsub) // 2) * cam["psx"])
+    sub["cy"] = np.float32(cam["cy"] - np.float32((cam["height"] - wsub) // 2) * cam["psy"])
+    sc = po.RenderScene(spec)
+    t0 = time.perf_counter()
+    sc.render(sub, 1, max_depth=depth, cast_mode=1, tri_table_order=1, threads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": wsub * wsub / dt, "unit": "samples/s", "cores": threads, "kind": "port",
+            "sample": f"{wsub}x{wsub} pixels x 1 sample, reference integrator and per-object cast (oracle)",
+            "seconds": dt}
 
 
 def _read_probes(ctx, device: int):
@@ -308,6 +383,9 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=1 << 20)
     ap.add_argument("--ref-sample", type=int, default=1 << 19)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-render", action="store_true")
+    ap.add_argument("--layout", type=int, default=0, help="BVH layout of the trace workload: 0 default, 2, 8")
+    ap.add_argument("--render-layout", type=int, default=0, help="BVH layout of the render workloads")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

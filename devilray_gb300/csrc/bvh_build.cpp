@@ -261,6 +261,193 @@ float scene_slack(float mag)
     return std::ldexp(m, -14);
 }
 
+namespace {
+
+// The binned-SAH binary tree over the soup; idx receives the leaf order.
+std::unique_ptr<TreeNode> build_tree(const float *pos, uint32_t num_tris, const BuildParams &params,
+                                     std::vector<uint32_t> &idx, int &depth)
+{
+    std::vector<Prim> prims(num_tris);
+    for (uint32_t i = 0; i < num_tris; ++i) {
+        Prim &p = prims[i];
+        p.box.reset();
+        for (int k = 0; k < 3; ++k) p.box.grow(pos + (size_t)i * 9 + k * 3);
+        for (int a = 0; a < 3; ++a) p.c[a] = 0.5f * (p.box.lo[a] + p.box.hi[a]);
+    }
+    idx.resize(num_tris);
+    for (uint32_t i = 0; i < num_tris; ++i) idx[i] = i;
+    int threads = (int)params.threads;
+    if (threads <= 0) threads = (int)std::max(1u, std::thread::hardware_concurrency());
+    Builder builder(prims, idx, params, threads);
+    std::unique_ptr<TreeNode> root = builder.build(0, num_tris, 0);
+    depth = builder.max_depth.load() + 1;
+    return root;
+}
+
+struct WideBuilder {
+    Bvh8 &out;
+    const std::vector<uint32_t> &idx;  // binary-tree leaf order
+    float slack;
+    std::vector<uint32_t> order;       // wide leaf order
+    int max_depth = 0;
+
+    static float area(const Box &b) { return b.area(); }
+
+    // Up to 8 children: repeatedly open the internal child of largest area.
+    static void collect(const TreeNode *n, std::vector<const TreeNode *> &ch)
+    {
+        ch.clear();
+        ch.push_back(n->child[0].get());
+        ch.push_back(n->child[1].get());
+        while (ch.size() < 8) {
+            int best = -1;
+            float best_area = -1.0f;
+            for (int i = 0; i < (int)ch.size(); ++i)
+                if (!ch[i]->leaf() && ch[i]->box.area() > best_area) {
+                    best_area = ch[i]->box.area();
+                    best = i;
+                }
+            if (best < 0) break;
+            const TreeNode *c = ch[best];
+            ch[best] = c->child[0].get();
+            ch.push_back(c->child[1].get());
+        }
+    }
+
+    // Writes the node for binary subtree `n` at out.nodes[index].
+    void emit(const TreeNode *n, uint32_t index, int depth)
+    {
+        max_depth = std::max(max_depth, depth);
+        std::vector<const TreeNode *> ch;
+        if (n->leaf()) ch.push_back(n);  // only the root can be a leaf
+        else collect(n, ch);
+        // widened child boxes and their union
+        Box cb[8];
+        Box u;
+        u.reset();
+        for (size_t i = 0; i < ch.size(); ++i) {
+            for (int a = 0; a < 3; ++a) {
+                cb[i].lo[a] = std::nextafter(ch[i]->box.lo[a] - slack, -INFINITY);
+                cb[i].hi[a] = std::nextafter(ch[i]->box.hi[a] + slack, INFINITY);
+            }
+            u.grow(cb[i]);
+        }
+        // octant slots: greedy assignment of the child whose centroid lies
+        // furthest towards the slot's corner
+        int slot_of[8], child_in[8];
+        for (int s = 0; s < 8; ++s) child_in[s] = -1;
+        {
+            float pc[3];
+            for (int a = 0; a < 3; ++a) pc[a] = 0.5f * (u.lo[a] + u.hi[a]);
+            struct Cand {
+                float v;
+                int c, s;
+            };
+            std::vector<Cand> cand;
+            for (int c = 0; c < (int)ch.size(); ++c)
+                for (int s = 0; s < 8; ++s) {
+                    float v = 0.0f;
+                    for (int a = 0; a < 3; ++a) {
+                        const float d = ((s >> a) & 1) ? 1.0f : -1.0f;
+                        v += d * (0.5f * (cb[c].lo[a] + cb[c].hi[a]) - pc[a]);
+                    }
+                    cand.push_back(Cand{v, c, s});
+                }
+            std::stable_sort(cand.begin(), cand.end(), [](const Cand &x, const Cand &y) { return x.v > y.v; });
+            for (int c = 0; c < 8; ++c) slot_of[c] = -1;
+            for (const Cand &k : cand)
+                if (slot_of[k.c] < 0 && child_in[k.s] < 0) {
+                    slot_of[k.c] = k.s;
+                    child_in[k.s] = k.c;
+                }
+        }
+        // quantisation grid
+        uint32_t ebias[3];
+        float scale[3];
+        for (int a = 0; a < 3; ++a) {
+            const double ext = (double)u.hi[a] - (double)u.lo[a];
+            int e = -100;
+            if (ext > 0.0) e = (int)std::ceil(std::log2(ext / 255.0));
+            while (std::ldexp(255.0, e) < ext) ++e;
+            e = std::max(-126, std::min(127, e));
+            ebias[a] = (uint32_t)(e + 127);
+            scale[a] = std::ldexp(1.0f, e);
+        }
+        uint8_t qlo[3][8], qhi[3][8], meta[8];
+        uint32_t imask = 0;
+        for (int s = 0; s < 8; ++s) {
+            meta[s] = 0;
+            for (int a = 0; a < 3; ++a) {
+                qlo[a][s] = 255;
+                qhi[a][s] = 0;
+            }
+        }
+        // internal children first (contiguous, slot order), then triangles
+        const uint32_t child_base = (uint32_t)out.nodes.size();
+        std::vector<std::pair<const TreeNode *, uint32_t>> todo;
+        uint32_t n_internal = 0;
+        for (int s = 0; s < 8; ++s) {
+            const int c = child_in[s];
+            if (c >= 0 && !ch[c]->leaf()) ++n_internal;
+        }
+        out.nodes.resize(out.nodes.size() + n_internal);
+        const uint32_t tri_base = (uint32_t)order.size();
+        uint32_t next_child = child_base, tri_off = 0;
+        for (int s = 0; s < 8; ++s) {
+            const int c = child_in[s];
+            if (c < 0) continue;
+            for (int a = 0; a < 3; ++a) {
+                const double lo = std::floor(((double)cb[c].lo[a] - (double)u.lo[a]) / scale[a]);
+                const double hi = std::ceil(((double)cb[c].hi[a] - (double)u.lo[a]) / scale[a]);
+                qlo[a][s] = (uint8_t)std::max(0.0, std::min(255.0, lo));
+                qhi[a][s] = (uint8_t)std::max(0.0, std::min(255.0, hi));
+            }
+            const TreeNode *t = ch[c];
+            if (!t->leaf()) {
+                imask |= 1u << s;
+                meta[s] = (uint8_t)(0x20 | s);
+                todo.push_back({t, next_child++});
+            } else if (t->count > 0) {
+                meta[s] = (uint8_t)((((1u << t->count) - 1u) << 5) | tri_off);
+                for (uint32_t k = 0; k < t->count; ++k) order.push_back(idx[t->first + k]);
+                tri_off += t->count;
+            }
+        }
+        Bvh8Node &nd = out.nodes[index];
+        nd.w[0] = make_uint4(__builtin_bit_cast(uint32_t, u.lo[0]), __builtin_bit_cast(uint32_t, u.lo[1]),
+                             __builtin_bit_cast(uint32_t, u.lo[2]),
+                             ebias[0] | (ebias[1] << 8) | (ebias[2] << 16) | (imask << 24));
+        auto pack = [](const uint8_t *b) {
+            return (uint32_t)b[0] | ((uint32_t)b[1] << 8) | ((uint32_t)b[2] << 16) | ((uint32_t)b[3] << 24);
+        };
+        nd.w[1] = make_uint4(child_base, tri_base, pack(meta), pack(meta + 4));
+        for (int a = 0; a < 3; ++a)
+            nd.w[2 + a] = make_uint4(pack(qlo[a]), pack(qlo[a] + 4), pack(qhi[a]), pack(qhi[a] + 4));
+        for (auto &[t, i] : todo) emit(t, i, depth + 1);
+    }
+};
+
+}  // namespace
+
+Bvh8 build_bvh8(const float *pos, uint32_t num_tris, const BuildParams &params, float slack)
+{
+    Bvh8 bvh;
+    bvh.slack = slack;
+    if (num_tris == 0) return bvh;
+    BuildParams bp = params;
+    bp.max_leaf = std::max<uint32_t>(1, std::min<uint32_t>(bp.max_leaf, 3));
+    std::vector<uint32_t> idx;
+    int depth2 = 0;
+    std::unique_ptr<TreeNode> root = build_tree(pos, num_tris, bp, idx, depth2);
+    WideBuilder wb{bvh, idx, slack, {}, 0};
+    wb.order.reserve(num_tris);
+    bvh.nodes.resize(1);
+    wb.emit(root.get(), 0, 1);
+    bvh.order = std::move(wb.order);
+    bvh.depth = wb.max_depth;
+    return bvh;
+}
+
 Bvh2 build_bvh2(const float *pos, uint32_t num_tris, const BuildParams &params, float slack)
 {
     Bvh2 bvh;

@@ -74,12 +74,16 @@ TraceArgs trace_args(dr_scene *s)
 {
     TraceArgs a{};
     a.nodes = s->d_nodes;
+    a.nodes8 = s->d_nodes8;
+    a.layout = (int)s->layout;
     a.tri_ref = s->d_tri_ref;
     a.tri_wt = s->d_tri_wt;
     a.prim = s->d_prim;
     a.num_nodes = s->num_nodes;
     a.counters = s->ctx->d_counters;
     a.error = s->ctx->d_error;
+    a.work = reinterpret_cast<unsigned long long *>(s->ctx->d_work);
+    a.num_sms = s->ctx->num_sms;
     return a;
 }
 
@@ -189,20 +193,34 @@ dr_status dr_scene_create(dr_context *ctx, const dr_scene_desc *desc, const dr_b
         bp.threads = cfg->threads;
     }
     const float slack = scene_slack(mag);
-    Bvh2 bvh = build_bvh2(desc->positions_host, n, bp, slack);
+    const uint32_t layout = (cfg && cfg->layout == 2) ? 2u : 8u;
+    if (cfg && cfg->layout != 0 && cfg->layout != 2 && cfg->layout != 8)
+        return fail(DR_ERR_INVALID_ARGUMENT, "dr_scene_create: layout must be 0, 2 or 8");
+    Bvh2 bvh2;
+    Bvh8 bvh8;
+    const std::vector<uint32_t> *order;
+    if (layout == 8) {
+        bvh8 = build_bvh8(desc->positions_host, n, bp, slack);
+        order = &bvh8.order;
+    } else {
+        bvh2 = build_bvh2(desc->positions_host, n, bp, slack);
+        order = &bvh2.order;
+    }
     std::vector<float4> ref_rec, wt_rec;
-    make_tri_records(desc->positions_host, bvh.order, ref_rec, wt_rec);
-    std::vector<int32_t> prim(bvh.order.begin(), bvh.order.end());
+    make_tri_records(desc->positions_host, *order, ref_rec, wt_rec);
+    std::vector<int32_t> prim(order->begin(), order->end());
 
     auto *s = new (std::nothrow) dr_scene;
     if (!s) return fail(DR_ERR_OUT_OF_MEMORY, "host allocation failed");
     s->ctx = ctx;
     s->num_tris = n;
-    s->num_nodes = (uint32_t)bvh.nodes.size();
-    s->depth = (uint32_t)bvh.depth;
+    s->layout = layout;
+    s->num_nodes = (uint32_t)(layout == 8 ? bvh8.nodes.size() : bvh2.nodes.size());
+    s->depth = (uint32_t)(layout == 8 ? bvh8.depth : bvh2.depth);
     s->slack = slack;
     cudaError_t e = cudaSuccess;
-    if ((e = upload(&s->d_nodes, bvh.nodes.data(), bvh.nodes.size(), s->device_bytes)) != cudaSuccess ||
+    if ((e = (layout == 8 ? upload(&s->d_nodes8, bvh8.nodes.data(), bvh8.nodes.size(), s->device_bytes)
+                          : upload(&s->d_nodes, bvh2.nodes.data(), bvh2.nodes.size(), s->device_bytes))) != cudaSuccess ||
         (e = upload(&s->d_tri_ref, ref_rec.data(), ref_rec.size(), s->device_bytes)) != cudaSuccess ||
         (e = upload(&s->d_tri_wt, wt_rec.data(), wt_rec.size(), s->device_bytes)) != cudaSuccess ||
         (e = upload(&s->d_prim, prim.data(), prim.size(), s->device_bytes)) != cudaSuccess) {
@@ -231,6 +249,7 @@ dr_status dr_scene_destroy(dr_scene *s)
     if (!s) return DR_OK;
     cudaSetDevice(s->ctx->device);
     cudaFree(s->d_nodes);
+    cudaFree(s->d_nodes8);
     cudaFree(s->d_tri_ref);
     cudaFree(s->d_tri_wt);
     cudaFree(s->d_prim);
@@ -239,7 +258,13 @@ dr_status dr_scene_destroy(dr_scene *s)
     cudaFree(s->d_shade);
     cudaFree(s->d_light_table);
     cudaFree(s->d_tri_tables);
-    cudaFree(s->d_wave);
+    for (int k = 0; k < dr_scene::kWaveStreams; ++k) {
+        cudaFree(s->d_wave[k]);
+        if (s->wave_stream[k]) cudaStreamDestroy(s->wave_stream[k]);
+    }
+    for (int k = 0; k <= dr_scene::kWaveStreams; ++k)
+        if (s->wave_event[k]) cudaEventDestroy(s->wave_event[k]);
+    cudaFree(s->d_samples);
     cudaFree(s->d_stage_rays);
     cudaFree(s->d_stage_hits);
     delete s;

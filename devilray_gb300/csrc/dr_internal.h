@@ -66,6 +66,32 @@ struct Bvh2 {
     float slack = 0.0f;
 };
 
+// Compressed 8-wide node after Ylitie, Karras and Laine ("Efficient Incoherent
+// Ray Traversal on GPUs Through Compressed Wide BVHs", HPG 2017), 80 bytes:
+//   w[0] = (p.x, p.y, p.z bits, ex | ey << 8 | ez << 16 | imask << 24)
+//          p = quantisation origin, e* = biased FP32 exponents of the per-axis
+//          scale 2^e, imask bit s = slot s holds an internal child
+//   w[1] = (child_base, tri_base, meta[0..3], meta[4..7])
+//          internal children are stored from child_base in slot order, the
+//          leaf children's triangles from tri_base; meta[s] of a leaf slot =
+//          (unary triangle count << 5) | triangle offset (0..23), 0 = empty
+//   w[2] = (qlo.x[0..3], qlo.x[4..7], qhi.x[0..3], qhi.x[4..7]) 8-bit child
+//          bounds, rounded outward; w[3], w[4]: y and z
+// Child slots are ordered by octant: slot s sits towards the corner
+// (s&1 ? +x : -x, s&2 ? +y : -y, s&4 ? +z : -z), so a ray whose direction
+// signs are o (bit set = negative) visits slots in the order k ^ o.
+struct alignas(16) Bvh8Node {
+    uint4 w[5];
+};
+static_assert(sizeof(Bvh8Node) == 80, "Bvh8Node must be 80 bytes");
+
+struct Bvh8 {
+    std::vector<Bvh8Node> nodes;
+    std::vector<uint32_t> order;  // wide leaf-order position -> original triangle index
+    int depth = 0;
+    float slack = 0.0f;
+};
+
 struct BuildParams {
     uint32_t max_leaf = 4;
     uint32_t bins = 32;
@@ -77,6 +103,10 @@ struct BuildParams {
 // `slack` world units (rounded outward) so box culling is conservative with
 // respect to the FP32 triangle tests.
 Bvh2 build_bvh2(const float *positions, uint32_t num_tris, const BuildParams &p, float slack);
+
+// Binned-SAH binary tree (leaves of at most 3 triangles) collapsed into
+// compressed 8-wide nodes.
+Bvh8 build_bvh8(const float *positions, uint32_t num_tris, const BuildParams &p, float slack);
 
 // Conservative world-space widening for a scene whose largest absolute
 // coordinate is `mag`.
@@ -126,7 +156,8 @@ struct dr_scene {
     double build_seconds = 0.0;
     uint64_t device_bytes = 0;
 
-    dr::Bvh2Node *d_nodes = nullptr;
+    dr::Bvh2Node *d_nodes = nullptr;     // layout 2
+    dr::Bvh8Node *d_nodes8 = nullptr;    // layout 8
     float4 *d_tri_ref = nullptr;
     float4 *d_tri_wt = nullptr;
     int32_t *d_prim = nullptr;      // leaf-order position -> original triangle index
@@ -141,9 +172,15 @@ struct dr_scene {
     float total_radiant_power = 0.0f;
     bool lights = false;                  // some object emits
 
-    // wavefront buffers of dr_render, grown on demand
-    void *d_wave = nullptr;
-    size_t wave_bytes = 0;
+    // wavefront buffers of dr_render (one set per concurrent wave stream) and
+    // the per-sample colours of a call, grown on demand
+    static constexpr int kWaveStreams = 3;
+    void *d_wave[kWaveStreams] = {};
+    size_t wave_bytes[kWaveStreams] = {};
+    cudaStream_t wave_stream[kWaveStreams] = {};
+    cudaEvent_t wave_event[kWaveStreams + 1] = {};
+    void *d_samples = nullptr;
+    size_t samples_bytes = 0;
 
     // staging for the host-buffer entry points
     void *d_stage_rays = nullptr;

@@ -1,0 +1,120 @@
+// persistent.cuh -- persistent-warp traversal over the compressed 8-wide BVH.
+//
+// A warp keeps all 32 lanes busy: whenever lanes have finished their ray they
+// take the next ray indices from a chunk the warp reserved with one atomic add
+// (128 indices per chunk), so a slow ray no longer idles the other 31 lanes of
+// its warp (Aila and Laine, "Understanding the Efficiency of Ray Traversal on
+// GPUs", HPG 2009, persistent threads with dynamic fetch). Each loop iteration
+// advances every active lane by one node (its 8 boxes and its leaf triangles).
+// The traversal of a single ray is unchanged, so results stay bit-identical.
+#pragma once
+
+#include "trace_kernels.cuh"
+#include "trace_wide.cuh"
+
+namespace dr {
+
+constexpr uint32_t kPersistentChunk = 128;
+
+// Indices a warp reserves at once: 128 when there is plenty of work, down to
+// one per lane when few rays are left, so a small launch still spreads over
+// many warps (warp-uniform).
+__device__ __forceinline__ uint32_t persistent_chunk(uint64_t n)
+{
+    const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x / 32);
+    const uint64_t per = n / (warps ? warps : 1);
+    uint32_t c = per >= kPersistentChunk ? kPersistentChunk : (uint32_t)((per + 31) & ~31ull);
+    return c < 32 ? 32 : c;
+}
+
+// Ray source of the public entry points: ray i of a contiguous array.
+struct DirectSource {
+    const dr_ray *rays;
+    dr_hit *hits;
+    uint8_t *occluded;
+    __device__ __forceinline__ bool load(uint64_t i, DevRay &r) const { return load_ray(rays, i, r); }
+    __device__ __forceinline__ void closest(uint64_t i, float t, int32_t prim) const
+    {
+        reinterpret_cast<float2 *>(hits)[i] =
+            prim != INT_MAX ? make_float2(t, __int_as_float(prim))
+                            : make_float2(__int_as_float(0x7f800000), __int_as_float(-1));
+    }
+    __device__ __forceinline__ void any(uint64_t i, bool hit) const { occluded[i] = hit ? 1 : 0; }
+};
+
+template <int MODE, bool ANY, bool COUNT, class Source>
+__device__ __forceinline__ void persistent_wide(const Wide8Args &a, const Source &src, uint64_t n,
+                                                unsigned long long *counter, unsigned long long &nn,
+                                                unsigned long long &nb, unsigned long long &nt,
+                                                unsigned long long &nhits)
+{
+    constexpr unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const unsigned lower = (1u << lane) - 1u;
+    WideState s;
+    uint2 stack[kWideStack];
+    uint64_t idx = 0;
+    bool active = false, exhausted = false;
+    uint64_t chunk_next = 0, chunk_end = 0;  // warp-uniform
+    const uint32_t chunk = persistent_chunk(n);
+    unsigned long long cn = 0, cb = 0, ct = 0, ch = 0;
+    while (true) {
+        unsigned want = __ballot_sync(FULL, !active);
+        while (want != 0 && !exhausted) {
+            if (chunk_next == chunk_end) {
+                unsigned long long b = 0;
+                if (lane == 0) b = atomicAdd(counter, (unsigned long long)chunk);
+                b = __shfl_sync(FULL, b, 0);
+                if (b >= n) {
+                    exhausted = true;
+                    break;
+                }
+                chunk_next = b;
+                chunk_end = b + chunk < n ? b + chunk : n;
+            }
+            const uint32_t avail = (uint32_t)(chunk_end - chunk_next);
+            const bool take = ((want >> lane) & 1u) && (uint32_t)__popc(want & lower) < avail;
+            const unsigned took = __ballot_sync(FULL, take);
+            if (take) {
+                idx = chunk_next + (uint64_t)__popc(want & lower);
+                DevRay r;
+                // an empty scene (no nodes) has nothing to traverse: every ray misses
+                if (src.load(idx, r) && a.num_nodes != 0) {
+                    wide_init<MODE>(s, r);
+                    active = true;
+                } else if (ANY) {
+                    src.any(idx, false);
+                } else {
+                    src.closest(idx, 0.0f, INT_MAX);
+                }
+            }
+            chunk_next += (uint64_t)__popc(took);
+            want &= ~took;
+        }
+        const unsigned busy = __ballot_sync(FULL, active);
+        if (busy == 0) {
+            if (exhausted) break;
+            continue;
+        }
+        if (active) {
+            bool found = false;
+            if (wide_step<MODE, ANY>(a, s, stack, found, cn, cb, ct)) {
+                if (ANY) {
+                    src.any(idx, found);
+                } else {
+                    src.closest(idx, s.best_t, s.best_prim);
+                    if (s.best_prim != INT_MAX) ++ch;
+                }
+                active = false;
+            }
+        }
+    }
+    if (COUNT) {
+        nn += cn;
+        nb += cb;
+        nt += ct;
+        nhits += ch;
+    }
+}
+
+}  // namespace dr

@@ -19,6 +19,7 @@
 #include "alias_kernels.cuh"
 #include "ptmath.cuh"
 #include "trace_device.cuh"
+#include "persistent.cuh"
 
 #include <algorithm>
 
@@ -56,6 +57,7 @@ struct RenderParams {
     uint32_t *list[2];
     uint32_t *shadow_list;
     uint32_t *counts;  // [0, 64): active paths per bounce, [64, 128): shadow rays per bounce
+    unsigned long long *work;  // persistent-kernel counters: [b] closest hit, [64 + b] shadow rays
     float4 *accum;
     uint32_t *pix_casts;
 };
@@ -169,8 +171,63 @@ __global__ void __launch_bounds__(kRenderBlock) k_camera(RenderParams p)
     p.list[0][i] = i;
 }
 
-// Closest hit of the surviving paths of bounce b.
+// Ray sources of the persistent wide kernels: list entry i names a path slot.
+struct PathSource {
+    const uint32_t *list;
+    const float4 *rays;
+    float2 *hits;
+    __device__ __forceinline__ bool load(uint64_t i, DevRay &r) const
+    {
+        return load_ray(reinterpret_cast<const dr_ray *>(rays), list[i], r);
+    }
+    __device__ __forceinline__ void closest(uint64_t i, float t, int32_t prim) const
+    {
+        hits[list[i]] = prim != INT_MAX ? make_float2(t, __int_as_float(prim))
+                                        : make_float2(__int_as_float(0x7f800000), __int_as_float(-1));
+    }
+    __device__ __forceinline__ void any(uint64_t, bool) const {}
+};
+
+struct ShadowSource {
+    const uint32_t *list;
+    const float4 *rays;
+    float4 *color;
+    const float4 *pending;
+    __device__ __forceinline__ bool load(uint64_t i, DevRay &r) const
+    {
+        return load_ray(reinterpret_cast<const dr_ray *>(rays), list[i], r);
+    }
+    __device__ __forceinline__ void closest(uint64_t, float, int32_t) const {}
+    __device__ __forceinline__ void any(uint64_t i, bool occluded) const
+    {
+        if (!occluded) {
+            const uint32_t slot = list[i];
+            const float4 c = color[slot], q = pending[slot];
+            color[slot] = make_float4(c.x + q.x, c.y + q.y, c.z + q.z, c.w + q.w);
+        }
+    }
+};
+
 template <int MODE>
+__global__ void __launch_bounds__(kTraceBlock) k_wave_closest_p8(RenderParams p, int b)
+{
+    const Wide8Args w{p.trace.nodes8, p.trace.tri_ref, p.trace.tri_wt, p.trace.prim, p.trace.num_nodes, p.trace.error};
+    const PathSource src{p.list[b & 1], p.rays, p.hits};
+    unsigned long long nn = 0, nb = 0, nt = 0, nh = 0;
+    persistent_wide<MODE, false, false>(w, src, p.counts[b], p.work + b, nn, nb, nt, nh);
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kTraceBlock) k_wave_shadow_p8(RenderParams p, int b)
+{
+    const Wide8Args w{p.trace.nodes8, p.trace.tri_ref, p.trace.tri_wt, p.trace.prim, p.trace.num_nodes, p.trace.error};
+    const ShadowSource src{p.shadow_list, p.shadow_rays, p.color, p.pending};
+    unsigned long long nn = 0, nb = 0, nt = 0, nh = 0;
+    persistent_wide<MODE, true, false>(w, src, p.counts[64 + b], p.work + 64 + b, nn, nb, nt, nh);
+}
+
+// Closest hit of the surviving paths of bounce b.
+template <int MODE, int LAYOUT>
 __global__ void __launch_bounds__(kTraceBlock) k_wave_closest(RenderParams p, int b)
 {
     const uint32_t count = p.counts[b];
@@ -182,7 +239,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_wave_closest(RenderParams p, in
         float t = r.tmax;
         int32_t prim = INT_MAX;
         TraceStats st;
-        if (valid) closest_hit<MODE, false>(p.trace, r, t, prim, st);
+        if (valid) scene_closest<MODE, false, LAYOUT>(p.trace, r, t, prim, st);
         p.hits[slot] = prim != INT_MAX ? make_float2(t, __int_as_float(prim))
                                        : make_float2(__int_as_float(0x7f800000), __int_as_float(-1));
     }
@@ -377,7 +434,7 @@ __global__ void __launch_bounds__(kRenderBlock) k_shade(RenderParams p, int b)
 }
 
 // Shadow rays of bounce b: the next-event contribution counts when unoccluded.
-template <int MODE>
+template <int MODE, int LAYOUT>
 __global__ void __launch_bounds__(kTraceBlock) k_wave_shadow(RenderParams p, int b)
 {
     const uint32_t count = p.counts[64 + b];
@@ -385,27 +442,43 @@ __global__ void __launch_bounds__(kTraceBlock) k_wave_shadow(RenderParams p, int
         const uint32_t slot = p.shadow_list[i];
         DevRay r;
         const bool valid = load_ray(reinterpret_cast<const dr_ray *>(p.shadow_rays), slot, r);
-        const bool occluded = valid && any_hit<MODE>(p.trace, r);
+        const bool occluded = valid && scene_any<MODE, LAYOUT>(p.trace, r);
         if (!occluded) p.color[slot] = add4(p.color[slot], p.pending[slot]);
     }
 }
 
+// Copies the finished wave into the per-sample buffers of the call:
+// sample_color[sample - first][pixel], sample_casts[...].
+__global__ void __launch_bounds__(256) k_store_wave(RenderParams p, float4 *sample_color, uint32_t *sample_casts,
+                                                    uint32_t first_sample)
+{
+    const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= p.wave) return;
+    uint32_t pixel, sample;
+    slot_pixel(p, slot, pixel, sample);
+    const size_t o = (size_t)(sample - first_sample) * p.npix + pixel;
+    sample_color[o] = p.color[slot];
+    sample_casts[o] = p.casts[slot];
+}
+
 // Buffers::color update of the reference (pixel.w++; pixel = pixel + color),
-// samples of a pixel in sample order.
-__global__ void __launch_bounds__(256) k_accumulate(RenderParams p)
+// the samples of a pixel added in sample order.
+__global__ void __launch_bounds__(256) k_accumulate_samples(float4 *accum, uint32_t *pix_casts,
+                                                            const float4 *sample_color, const uint32_t *sample_casts,
+                                                            uint32_t npix, uint32_t nsamples)
 {
     const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
-    if (pix >= p.npix) return;
-    float4 acc = p.accum[pix];
+    if (pix >= npix) return;
+    float4 acc = accum[pix];
     uint32_t casts = 0;
-    for (uint32_t s = 0; s < p.spp_wave; ++s) {
-        const uint32_t slot = s * p.npix + pix;
+    for (uint32_t s = 0; s < nsamples; ++s) {
+        const size_t o = (size_t)s * npix + pix;
         acc.w = acc.w + 1.0f;
-        acc = add4(acc, p.color[slot]);
-        casts += p.casts[slot];
+        acc = add4(acc, sample_color[o]);
+        casts += sample_casts[o];
     }
-    p.accum[pix] = acc;
-    if (p.pix_casts) p.pix_casts[pix] += casts;
+    accum[pix] = acc;
+    if (pix_casts) pix_casts[pix] += casts;
 }
 
 template <typename T>
@@ -418,7 +491,7 @@ T *carve(char *&ptr, size_t count)
 
 size_t wave_bytes(uint32_t W)
 {
-    return (size_t)W * 200 + 128 * sizeof(uint32_t) + 16 * 256;
+    return (size_t)W * 200 + 128 * sizeof(uint32_t) + 128 * sizeof(unsigned long long) + 18 * 256;
 }
 
 }  // namespace
@@ -443,17 +516,42 @@ extern "C" dr_status dr_render(dr_scene *s, const dr_camera *cam, const dr_rende
     const uint32_t target = cfg->wave_paths ? cfg->wave_paths : (1u << 21);
     const uint32_t spp_wave = std::max<uint32_t>(1, std::min<uint32_t>(cfg->spp, target / npix));
     const uint32_t W = npix * spp_wave;
+    const uint32_t nwaves_total = (cfg->spp + spp_wave - 1) / spp_wave;
+    const int K = (int)std::min<uint32_t>(dr_scene::kWaveStreams, nwaves_total);
     const size_t need = wave_bytes(W);
-    if (s->wave_bytes < need) {
-        DR_CUDA(cudaStreamSynchronize(st));
-        cudaFree(s->d_wave);
-        s->d_wave = nullptr;
-        s->wave_bytes = 0;
-        DR_CUDA(cudaMalloc(&s->d_wave, need));
-        s->wave_bytes = need;
+    // samples held at once: whole waves, at most ~2 GiB of per-sample colours
+    const uint64_t per_sample = (uint64_t)npix * (sizeof(float4) + sizeof(uint32_t));
+    uint32_t chunk_spp = (uint32_t)std::max<uint64_t>(spp_wave, std::min<uint64_t>(cfg->spp, (2ull << 30) / per_sample));
+    chunk_spp = std::max<uint32_t>(spp_wave, chunk_spp / spp_wave * spp_wave);
+    const size_t samples_need = (size_t)std::min(chunk_spp, cfg->spp) * per_sample + 512;
+    bool grow = s->samples_bytes < samples_need;
+    for (int k = 0; k < K; ++k) grow = grow || s->wave_bytes[k] < need;
+    if (grow) {
+        DR_CUDA(cudaDeviceSynchronize());
+        for (int k = 0; k < K; ++k)
+            if (s->wave_bytes[k] < need) {
+                cudaFree(s->d_wave[k]);
+                s->d_wave[k] = nullptr;
+                s->wave_bytes[k] = 0;
+                DR_CUDA(cudaMalloc(&s->d_wave[k], need));
+                s->wave_bytes[k] = need;
+            }
+        if (s->samples_bytes < samples_need) {
+            cudaFree(s->d_samples);
+            s->d_samples = nullptr;
+            s->samples_bytes = 0;
+            DR_CUDA(cudaMalloc(&s->d_samples, samples_need));
+            s->samples_bytes = samples_need;
+        }
     }
+    for (int k = 0; k < K; ++k)
+        if (!s->wave_stream[k]) DR_CUDA(cudaStreamCreateWithFlags(&s->wave_stream[k], cudaStreamNonBlocking));
+    for (int k = 0; k <= K; ++k)
+        if (!s->wave_event[k]) DR_CUDA(cudaEventCreateWithFlags(&s->wave_event[k], cudaEventDisableTiming));
     RenderParams p{};
     p.trace.nodes = s->d_nodes;
+    p.trace.nodes8 = s->d_nodes8;
+    p.trace.layout = (int)s->layout;
     p.trace.tri_ref = s->d_tri_ref;
     p.trace.tri_wt = s->d_tri_wt;
     p.trace.prim = s->d_prim;
@@ -481,41 +579,90 @@ extern "C" dr_status dr_render(dr_scene *s, const dr_camera *cam, const dr_rende
     p.max_depth = cfg->max_depth;
     p.seed_lo = (uint32_t)cfg->seed;
     p.seed_hi = (uint32_t)(cfg->seed >> 32);
-    char *ptr = static_cast<char *>(s->d_wave);
-    p.rays = carve<float4>(ptr, (size_t)W * 2);
-    p.hits = carve<float2>(ptr, W);
-    p.thr = carve<float4>(ptr, W);
-    p.color = carve<float4>(ptr, W);
-    p.prev_p = carve<float4>(ptr, W);
-    p.prev_n = carve<float4>(ptr, W);
-    p.pending = carve<float4>(ptr, W);
-    p.shadow_rays = carve<float4>(ptr, (size_t)W * 2);
-    p.stack = carve<int4>(ptr, W);
-    p.casts = carve<uint32_t>(ptr, W);
-    p.list[0] = carve<uint32_t>(ptr, W);
-    p.list[1] = carve<uint32_t>(ptr, W);
-    p.shadow_list = carve<uint32_t>(ptr, W);
-    p.counts = carve<uint32_t>(ptr, 128);
     p.accum = reinterpret_cast<float4 *>(accum_dev);
     p.pix_casts = casts_dev;
+    RenderParams ps[dr_scene::kWaveStreams];
+    for (int k = 0; k < K; ++k) {
+        ps[k] = p;
+        char *ptr = static_cast<char *>(s->d_wave[k]);
+        ps[k].rays = carve<float4>(ptr, (size_t)W * 2);
+        ps[k].hits = carve<float2>(ptr, W);
+        ps[k].thr = carve<float4>(ptr, W);
+        ps[k].color = carve<float4>(ptr, W);
+        ps[k].prev_p = carve<float4>(ptr, W);
+        ps[k].prev_n = carve<float4>(ptr, W);
+        ps[k].pending = carve<float4>(ptr, W);
+        ps[k].shadow_rays = carve<float4>(ptr, (size_t)W * 2);
+        ps[k].stack = carve<int4>(ptr, W);
+        ps[k].casts = carve<uint32_t>(ptr, W);
+        ps[k].list[0] = carve<uint32_t>(ptr, W);
+        ps[k].list[1] = carve<uint32_t>(ptr, W);
+        ps[k].shadow_list = carve<uint32_t>(ptr, W);
+        ps[k].counts = carve<uint32_t>(ptr, 128);
+        ps[k].work = carve<unsigned long long>(ptr, 128);
+    }
+    char *sp = static_cast<char *>(s->d_samples);
+    float4 *sample_color = carve<float4>(sp, (size_t)std::min(chunk_spp, cfg->spp) * npix);
+    uint32_t *sample_casts = carve<uint32_t>(sp, (size_t)std::min(chunk_spp, cfg->spp) * npix);
 
     const int sms = s->ctx->num_sms;
     const unsigned trace_grid = (unsigned)std::min<uint64_t>((W + kTraceBlock - 1) / kTraceBlock, (uint64_t)sms * 16);
     const unsigned shade_grid = (unsigned)std::min<uint64_t>((W + kRenderBlock - 1) / kRenderBlock, (uint64_t)sms * 16);
-    for (uint32_t done = 0; done < cfg->spp; done += spp_wave) {
-        p.spp_wave = std::min(spp_wave, cfg->spp - done);
-        p.wave = npix * p.spp_wave;
-        p.sample_base = cfg->sample_offset + done;
-        DR_CUDA(cudaMemsetAsync(p.counts, 0, 128 * sizeof(uint32_t), st));
-        k_camera<<<(p.wave + kRenderBlock - 1) / kRenderBlock, kRenderBlock, 0, st>>>(p);
-        for (int b = 0; b < (int)cfg->max_depth; ++b) {
-            if (cfg->tri_mode == DR_TRI_WATERTIGHT) k_wave_closest<1><<<trace_grid, kTraceBlock, 0, st>>>(p, b);
-            else k_wave_closest<0><<<trace_grid, kTraceBlock, 0, st>>>(p, b);
-            k_shade<<<shade_grid, kRenderBlock, 0, st>>>(p, b);
-            if (cfg->tri_mode == DR_TRI_WATERTIGHT) k_wave_shadow<1><<<trace_grid, kTraceBlock, 0, st>>>(p, b);
-            else k_wave_shadow<0><<<trace_grid, kTraceBlock, 0, st>>>(p, b);
+    // persistent wide kernels: one resident set of blocks
+    static int p8_per_sm = 0;
+    if (p8_per_sm == 0) {
+        int b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_wave_closest_p8<0>, kTraceBlock, 0) != cudaSuccess || b <= 0)
+            b = 4;
+        p8_per_sm = b;
+    }
+    const unsigned pgrid = (unsigned)std::min<uint64_t>((W + kTraceBlock - 1) / kTraceBlock, (uint64_t)sms * p8_per_sm);
+    // Waves run on K streams so that the short, latency-bound late bounces of
+    // one wave overlap the full early bounces of the next; each wave writes its
+    // samples' colours, and one ordered pass per chunk adds them to the image.
+    const bool wt = cfg->tri_mode == DR_TRI_WATERTIGHT, wide = s->layout == 8;
+    for (uint32_t chunk0 = 0; chunk0 < cfg->spp; chunk0 += chunk_spp) {
+        const uint32_t chunk_n = std::min(chunk_spp, cfg->spp - chunk0);
+        DR_CUDA(cudaEventRecord(s->wave_event[K], st));
+        for (int k = 0; k < K; ++k) DR_CUDA(cudaStreamWaitEvent(s->wave_stream[k], s->wave_event[K], 0));
+        int wave_index = 0;
+        for (uint32_t done = 0; done < chunk_n; done += spp_wave, ++wave_index) {
+            const int k = wave_index % K;
+            cudaStream_t ws = s->wave_stream[k];
+            RenderParams &q = ps[k];
+            q.spp_wave = std::min(spp_wave, chunk_n - done);
+            q.wave = npix * q.spp_wave;
+            q.sample_base = cfg->sample_offset + chunk0 + done;
+            DR_CUDA(cudaMemsetAsync(q.counts, 0, 128 * sizeof(uint32_t), ws));
+            DR_CUDA(cudaMemsetAsync(q.work, 0, 128 * sizeof(unsigned long long), ws));
+            k_camera<<<(q.wave + kRenderBlock - 1) / kRenderBlock, kRenderBlock, 0, ws>>>(q);
+            for (int b = 0; b < (int)cfg->max_depth; ++b) {
+                if (wide) {
+                    if (wt) k_wave_closest_p8<1><<<pgrid, kTraceBlock, 0, ws>>>(q, b);
+                    else k_wave_closest_p8<0><<<pgrid, kTraceBlock, 0, ws>>>(q, b);
+                } else {
+                    if (wt) k_wave_closest<1, 2><<<trace_grid, kTraceBlock, 0, ws>>>(q, b);
+                    else k_wave_closest<0, 2><<<trace_grid, kTraceBlock, 0, ws>>>(q, b);
+                }
+                k_shade<<<shade_grid, kRenderBlock, 0, ws>>>(q, b);
+                if (wide) {
+                    if (wt) k_wave_shadow_p8<1><<<pgrid, kTraceBlock, 0, ws>>>(q, b);
+                    else k_wave_shadow_p8<0><<<pgrid, kTraceBlock, 0, ws>>>(q, b);
+                } else {
+                    if (wt) k_wave_shadow<1, 2><<<trace_grid, kTraceBlock, 0, ws>>>(q, b);
+                    else k_wave_shadow<0, 2><<<trace_grid, kTraceBlock, 0, ws>>>(q, b);
+                }
+            }
+            k_store_wave<<<(q.wave + 255) / 256, 256, 0, ws>>>(q, sample_color, sample_casts,
+                                                             cfg->sample_offset + chunk0);
+            DR_CUDA(cudaGetLastError());
         }
-        k_accumulate<<<(npix + 255) / 256, 256, 0, st>>>(p);
+        for (int k = 0; k < K; ++k) {
+            DR_CUDA(cudaEventRecord(s->wave_event[k], s->wave_stream[k]));
+            DR_CUDA(cudaStreamWaitEvent(st, s->wave_event[k], 0));
+        }
+        k_accumulate_samples<<<(npix + 255) / 256, 256, 0, st>>>(p.accum, p.pix_casts, sample_color, sample_casts, npix,
+                                                                 chunk_n);
         DR_CUDA(cudaGetLastError());
     }
     return DR_OK;

@@ -8,6 +8,9 @@
 
 #include "dr_internal.h"
 #include "trace_device.cuh"
+#include "persistent.cuh"
+
+#include <algorithm>
 
 namespace dr {
 
@@ -30,7 +33,7 @@ __device__ __forceinline__ void add_counters(unsigned long long *c, unsigned lon
     }
 }
 
-template <int MODE, bool COUNT>
+template <int MODE, bool COUNT, int LAYOUT>
 __global__ void __launch_bounds__(kTraceBlock)
 k_trace_closest(TraceArgs a)
 {
@@ -42,7 +45,7 @@ k_trace_closest(TraceArgs a)
         const bool valid = load_ray(a.rays, i, r);
         float best_t = r.tmax;
         int32_t best_prim = INT_MAX;
-        if (valid) closest_hit<MODE, COUNT>(a, r, best_t, best_prim, st);
+        if (valid) scene_closest<MODE, COUNT, LAYOUT>(a, r, best_t, best_prim, st);
         float2 out;
         if (best_prim != INT_MAX) {
             out = make_float2(best_t, __int_as_float(best_prim));
@@ -55,7 +58,7 @@ k_trace_closest(TraceArgs a)
     if (COUNT) add_counters(a.counters, st.nodes, st.boxes, st.tris, n_hits);
 }
 
-template <int MODE>
+template <int MODE, int LAYOUT>
 __global__ void __launch_bounds__(kTraceBlock)
 k_trace_any(TraceArgs a)
 {
@@ -63,7 +66,40 @@ k_trace_any(TraceArgs a)
     if (i >= a.n) return;
     DevRay r;
     const bool valid = load_ray(a.rays, i, r);
-    a.occluded[i] = (valid && any_hit<MODE>(a, r)) ? 1 : 0;
+    a.occluded[i] = (valid && scene_any<MODE, LAYOUT>(a, r)) ? 1 : 0;
+}
+
+// Persistent kernels for the compressed 8-wide layout.
+template <int MODE, bool COUNT>
+__global__ void __launch_bounds__(kTraceBlock) k_trace_closest_p8(TraceArgs a)
+{
+    const Wide8Args w{a.nodes8, a.tri_ref, a.tri_wt, a.prim, a.num_nodes, a.error};
+    const DirectSource src{a.rays, a.hits, nullptr};
+    unsigned long long nn = 0, nb = 0, nt = 0, nh = 0;
+    persistent_wide<MODE, false, COUNT>(w, src, a.n, a.work, nn, nb, nt, nh);
+    if (COUNT) add_counters(a.counters, nn, nb, nt, nh);
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kTraceBlock) k_trace_any_p8(TraceArgs a)
+{
+    const Wide8Args w{a.nodes8, a.tri_ref, a.tri_wt, a.prim, a.num_nodes, a.error};
+    const DirectSource src{a.rays, nullptr, a.occluded};
+    unsigned long long nn = 0, nb = 0, nt = 0, nh = 0;
+    persistent_wide<MODE, true, false>(w, src, a.n, a.work, nn, nb, nt, nh);
+}
+
+template <typename K>
+unsigned persistent_grid(K kernel, int num_sms, uint64_t n)
+{
+    static int per_sm = 0;  // resident blocks per SM of this kernel
+    if (per_sm == 0) {
+        int b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, kTraceBlock, 0) != cudaSuccess || b <= 0) b = 4;
+        per_sm = b;
+    }
+    const uint64_t need = (n + kTraceBlock - 1) / kTraceBlock;
+    return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(need, (uint64_t)num_sms * per_sm));
 }
 
 cudaError_t launch_trace_closest(const TraceArgs &a, int mode, bool count, cudaStream_t s)
@@ -72,12 +108,24 @@ cudaError_t launch_trace_closest(const TraceArgs &a, int mode, bool count, cudaS
     const uint64_t blocks = (a.n + kTraceBlock - 1) / kTraceBlock;
     if (blocks > 0x7fffffffull) return cudaErrorInvalidValue;
     const dim3 grid((unsigned)blocks), block(kTraceBlock);
-    if (mode == 1) {
-        if (count) k_trace_closest<1, true><<<grid, block, 0, s>>>(a);
-        else k_trace_closest<1, false><<<grid, block, 0, s>>>(a);
+    if (a.layout == 8) {
+        cudaError_t e = cudaMemsetAsync(a.work, 0, sizeof(unsigned long long), s);
+        if (e != cudaSuccess) return e;
+        if (mode == 1) {
+            if (count) k_trace_closest_p8<1, true><<<persistent_grid(k_trace_closest_p8<1, true>, a.num_sms, a.n), block, 0, s>>>(a);
+            else k_trace_closest_p8<1, false><<<persistent_grid(k_trace_closest_p8<1, false>, a.num_sms, a.n), block, 0, s>>>(a);
+        } else {
+            if (count) k_trace_closest_p8<0, true><<<persistent_grid(k_trace_closest_p8<0, true>, a.num_sms, a.n), block, 0, s>>>(a);
+            else k_trace_closest_p8<0, false><<<persistent_grid(k_trace_closest_p8<0, false>, a.num_sms, a.n), block, 0, s>>>(a);
+        }
     } else {
-        if (count) k_trace_closest<0, true><<<grid, block, 0, s>>>(a);
-        else k_trace_closest<0, false><<<grid, block, 0, s>>>(a);
+        if (mode == 1) {
+            if (count) k_trace_closest<1, true, 2><<<grid, block, 0, s>>>(a);
+            else k_trace_closest<1, false, 2><<<grid, block, 0, s>>>(a);
+        } else {
+            if (count) k_trace_closest<0, true, 2><<<grid, block, 0, s>>>(a);
+            else k_trace_closest<0, false, 2><<<grid, block, 0, s>>>(a);
+        }
     }
     return cudaGetLastError();
 }
@@ -88,8 +136,15 @@ cudaError_t launch_trace_any(const TraceArgs &a, int mode, cudaStream_t s)
     const uint64_t blocks = (a.n + kTraceBlock - 1) / kTraceBlock;
     if (blocks > 0x7fffffffull) return cudaErrorInvalidValue;
     const dim3 grid((unsigned)blocks), block(kTraceBlock);
-    if (mode == 1) k_trace_any<1><<<grid, block, 0, s>>>(a);
-    else k_trace_any<0><<<grid, block, 0, s>>>(a);
+    if (a.layout == 8) {
+        cudaError_t e = cudaMemsetAsync(a.work, 0, sizeof(unsigned long long), s);
+        if (e != cudaSuccess) return e;
+        if (mode == 1) k_trace_any_p8<1><<<persistent_grid(k_trace_any_p8<1>, a.num_sms, a.n), block, 0, s>>>(a);
+        else k_trace_any_p8<0><<<persistent_grid(k_trace_any_p8<0>, a.num_sms, a.n), block, 0, s>>>(a);
+    } else {
+        if (mode == 1) k_trace_any<1, 2><<<grid, block, 0, s>>>(a);
+        else k_trace_any<0, 2><<<grid, block, 0, s>>>(a);
+    }
     return cudaGetLastError();
 }
 

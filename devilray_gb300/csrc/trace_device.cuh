@@ -9,6 +9,7 @@
 
 #include "trace_kernels.cuh"
 #include "tri_device.cuh"
+#include "trace_wide.cuh"
 
 #include <climits>
 
@@ -128,6 +129,32 @@ __device__ __forceinline__ bool any_hit(const TraceArgs &a, const DevRay &r)
             cur = stack[--sp];
         }
     }
+}
+
+// Closest / any hit in the scene's layout.
+template <int MODE, bool COUNT, int LAYOUT>
+__device__ __forceinline__ void scene_closest(const TraceArgs &a, const DevRay &r, float &best_t, int32_t &best_prim,
+                                              TraceStats &st)
+{
+    if (LAYOUT == 8) {
+        const Wide8Args w{a.nodes8, a.tri_ref, a.tri_wt, a.prim, a.num_nodes, a.error};
+        if (COUNT) wide_traverse<MODE, false>(w, r, best_t, best_prim, &st.nodes, &st.boxes, &st.tris);
+        else wide_traverse<MODE, false>(w, r, best_t, best_prim, nullptr, nullptr, nullptr);
+    } else {
+        closest_hit<MODE, COUNT>(a, r, best_t, best_prim, st);
+    }
+}
+
+template <int MODE, int LAYOUT>
+__device__ __forceinline__ bool scene_any(const TraceArgs &a, const DevRay &r)
+{
+    if (LAYOUT == 8) {
+        const Wide8Args w{a.nodes8, a.tri_ref, a.tri_wt, a.prim, a.num_nodes, a.error};
+        float t;
+        int32_t prim;
+        return wide_traverse<MODE, true>(w, r, t, prim, nullptr, nullptr, nullptr);
+    }
+    return any_hit<MODE>(a, r);
 }
 
 }  // namespace dr

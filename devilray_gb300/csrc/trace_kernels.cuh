@@ -9,6 +9,8 @@ constexpr int kTraceBlock = 128;
 
 struct TraceArgs {
     const Bvh2Node *nodes;
+    const Bvh8Node *nodes8;   // compressed 8-wide layout (used when layout == 8)
+    int layout;
     const float4 *tri_ref;
     const float4 *tri_wt;
     const int32_t *prim;
@@ -19,8 +21,11 @@ struct TraceArgs {
     uint8_t *occluded;     // any hit
     unsigned long long *counters;
     uint32_t *error;
+    unsigned long long *work;  // persistent-kernel ray counter (zeroed before each launch)
+    int num_sms;
 };
 
+// Launch helpers dispatch on a.layout (2 or 8) and the triangle mode.
 cudaError_t launch_trace_closest(const TraceArgs &a, int mode, bool count, cudaStream_t s);
 cudaError_t launch_trace_any(const TraceArgs &a, int mode, cudaStream_t s);
 

@@ -1,0 +1,308 @@
+// trace_wide.cuh -- closest-hit and any-hit traversal of the compressed
+// 8-wide BVH (node layout in dr_internal.h).
+//
+// After Ylitie, Karras and Laine (HPG 2017): a ray keeps the current "node
+// group" (the internal children of one node still to visit, as a bit mask in
+// the ray's octant order) and the "triangle group" (the hit leaf triangles of
+// the last node, as a 24-bit mask). One node fetch tests 8 child boxes, which
+// the lanes of a warp do in lockstep. Culling and the candidate rule are the
+// same as the binary traversal (enter <= best, smaller t or equal t with a
+// smaller triangle index), so the result equals a brute-force scan.
+#pragma once
+
+#include "dr_internal.h"
+#include "tri_device.cuh"
+
+#include <climits>
+
+#if defined(__CUDA_ARCH__)
+#define DR_LD(p) __ldg(p)
+#else
+#define DR_LD(p) (*(p))
+#endif
+
+namespace dr {
+
+struct Wide8Args {
+    const Bvh8Node *nodes;
+    const float4 *tri_ref;
+    const float4 *tri_wt;
+    const int32_t *prim;
+    uint32_t num_nodes;
+    uint32_t *error;
+};
+
+constexpr int kWideStack = 64;
+
+// Byte j of w as a float. On the device: a byte permute builds the FP32 bit
+// pattern of 2^23 + byte, and one exact subtraction removes 2^23 (avoids the
+// integer-to-float conversion pipe).
+__host__ __device__ __forceinline__ float byte_f(uint32_t w, int j)
+{
+#if defined(__CUDA_ARCH__)
+    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | (uint32_t)j)) - 8388608.0f;
+#else
+    return (float)((w >> (8 * j)) & 0xffu);
+#endif
+}
+
+__host__ __device__ __forceinline__ float exp2_bits(uint32_t biased)
+{
+    const uint32_t bits = biased << 23;
+    float f;
+    memcpy(&f, &bits, 4);
+    return f;
+}
+
+__host__ __device__ __forceinline__ float bits_f(uint32_t u)
+{
+    float f;
+    memcpy(&f, &u, 4);
+    return f;
+}
+
+// Tests the 8 child boxes of `node` against [0, tmax]; returns the internal
+// hit mask in traversal order (bit k = slot k ^ oct) and the triangle mask.
+__host__ __device__ __forceinline__ void wide_node_test(const Bvh8Node *node, const DevRay &r, uint32_t oct, float tmax,
+                                                        uint32_t &child_base, uint32_t &imask, uint32_t &hit_internal,
+                                                        uint32_t &tri_base, uint32_t &tri_mask, uint32_t &nboxes)
+{
+    const uint4 w0 = DR_LD(&node->w[0]);
+    const uint4 w1 = DR_LD(&node->w[1]);
+    const uint4 wx = DR_LD(&node->w[2]);
+    const uint4 wy = DR_LD(&node->w[3]);
+    const uint4 wz = DR_LD(&node->w[4]);
+    const float px = bits_f(w0.x), py = bits_f(w0.y), pz = bits_f(w0.z);
+    const float sx = exp2_bits(w0.w & 0xffu), sy = exp2_bits((w0.w >> 8) & 0xffu), sz = exp2_bits((w0.w >> 16) & 0xffu);
+    imask = w0.w >> 24;
+    child_base = w1.x;
+    tri_base = w1.y;
+    // slab time of grid coordinate q on each axis: t = q * a + b
+    const float ax = sx * r.inv.x, ay = sy * r.inv.y, az = sz * r.inv.z;
+    const float bx = (px - r.o.x) * r.inv.x, by = (py - r.o.y) * r.inv.y, bz = (pz - r.o.z) * r.inv.z;
+    // near/far words by direction sign
+    const bool fx = r.inv.x < 0.0f, fy = r.inv.y < 0.0f, fz = r.inv.z < 0.0f;
+    const uint32_t nx0 = fx ? wx.z : wx.x, nx1 = fx ? wx.w : wx.y, fx0 = fx ? wx.x : wx.z, fx1 = fx ? wx.y : wx.w;
+    const uint32_t ny0 = fy ? wy.z : wy.x, ny1 = fy ? wy.w : wy.y, fy0 = fy ? wy.x : wy.z, fy1 = fy ? wy.y : wy.w;
+    const uint32_t nz0 = fz ? wz.z : wz.x, nz1 = fz ? wz.w : wz.y, fz0 = fz ? wz.x : wz.z, fz1 = fz ? wz.y : wz.w;
+    hit_internal = 0;
+    tri_mask = 0;
+    uint32_t boxes = 0;
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+        const int j = s & 3;
+        const uint32_t wnx = s < 4 ? nx0 : nx1, wfx = s < 4 ? fx0 : fx1;
+        const uint32_t wny = s < 4 ? ny0 : ny1, wfy = s < 4 ? fy0 : fy1;
+        const uint32_t wnz = s < 4 ? nz0 : nz1, wfz = s < 4 ? fz0 : fz1;
+        const float tnx = fmaf(byte_f(wnx, j), ax, bx), tfx = fmaf(byte_f(wfx, j), ax, bx);
+        const float tny = fmaf(byte_f(wny, j), ay, by), tfy = fmaf(byte_f(wfy, j), ay, by);
+        const float tnz = fmaf(byte_f(wnz, j), az, bz), tfz = fmaf(byte_f(wfz, j), az, bz);
+        const float tmin = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, 0.0f));
+        const float tmx = fminf(fminf(tfx, tfy), fminf(tfz, tmax));
+        const uint32_t meta = ((s < 4 ? w1.z : w1.w) >> (8 * j)) & 0xffu;
+        if (meta != 0) ++boxes;
+        if (tmin <= tmx && meta != 0) {
+            if ((imask >> s) & 1u) hit_internal |= 1u << (s ^ oct);
+            else tri_mask |= (meta >> 5) << (meta & 31u);
+        }
+    }
+    nboxes = boxes;
+}
+
+__host__ __device__ __forceinline__ uint32_t ray_octant(const DevRay &r)
+{
+    return (r.v.x < 0.0f ? 1u : 0u) | (r.v.y < 0.0f ? 2u : 0u) | (r.v.z < 0.0f ? 4u : 0u);
+}
+
+__host__ __device__ __forceinline__ int lowest_bit(uint32_t m)
+{
+#if defined(__CUDA_ARCH__)
+    return __ffs(m) - 1;
+#else
+    return __builtin_ctz(m);
+#endif
+}
+
+__host__ __device__ __forceinline__ int popcount(uint32_t m)
+{
+#if defined(__CUDA_ARCH__)
+    return __popc(m);
+#else
+    return __builtin_popcount(m);
+#endif
+}
+
+// Resumable traversal state of one ray (for the persistent kernels).
+struct WideState {
+    DevRay r;
+    WtSetup w;
+    uint32_t oct, node;
+    float best_t;
+    int32_t best_prim;
+    uint2 group;
+    int sp;
+    bool have_node;
+};
+
+template <int MODE>
+__host__ __device__ __forceinline__ void wide_init(WideState &s, const DevRay &r)
+{
+    s.r = r;
+    if (MODE == 1) s.w = wt_setup(r.v);
+    s.oct = ray_octant(r);
+    s.best_t = r.tmax;
+    s.best_prim = INT_MAX;
+    s.node = 0;
+    s.group = make_uint2(0, 0);
+    s.sp = 0;
+    s.have_node = true;
+}
+
+// One node (its 8 boxes and its leaf triangles) of the ray's traversal.
+// Returns true when the ray is finished (no node left, or a hit for ANY).
+template <int MODE, bool ANY>
+__host__ __device__ __forceinline__ bool wide_step(const Wide8Args &a, WideState &s, uint2 *stack, bool &found,
+                                                   unsigned long long &nn, unsigned long long &nb,
+                                                   unsigned long long &nt)
+{
+    uint32_t tri_base = 0, tri_mask = 0;
+    if (s.have_node) {
+        uint32_t child_base, imask, hit_int, nbx;
+        wide_node_test(a.nodes + s.node, s.r, s.oct, s.best_t, child_base, imask, hit_int, tri_base, tri_mask, nbx);
+        ++nn;
+        nb += nbx;
+        s.group = make_uint2(child_base, (hit_int << 8) | imask);
+        s.have_node = false;
+    }
+    while (tri_mask) {
+        const int b = lowest_bit(tri_mask);
+        tri_mask &= tri_mask - 1u;
+        const uint32_t k = tri_base + (uint32_t)b;
+        ++nt;
+        float t;
+        const bool ok = MODE == 1 ? tri_test_wt(a.tri_wt, k, s.r, s.w, ANY ? s.r.tmax : s.best_t, t)
+                                  : tri_test_ref(a.tri_ref, k, s.r, ANY ? s.r.tmax : s.best_t, t);
+        if (ok) {
+            if (ANY) {
+                found = true;
+                return true;
+            }
+            const int32_t prim = DR_LD(a.prim + k);
+            if (t < s.best_t || prim < s.best_prim) {
+                s.best_t = t;
+                s.best_prim = prim;
+            }
+        }
+    }
+    if ((s.group.y >> 8) == 0) {
+        if (s.sp == 0) return true;
+        s.group = stack[--s.sp];
+    }
+    const uint32_t hits = s.group.y >> 8;
+    const int k = lowest_bit(hits);
+    const uint32_t rest = hits & (hits - 1u);
+    const uint32_t slot = (uint32_t)k ^ s.oct;
+    const uint32_t imask = s.group.y & 0xffu;
+    s.node = s.group.x + (uint32_t)popcount(imask & ((1u << slot) - 1u));
+    s.have_node = true;
+    s.group.y = (rest << 8) | imask;
+    if (rest) {
+        if (s.sp >= kWideStack) {
+#if defined(__CUDA_ARCH__)
+            atomicOr(a.error, ERR_STACK_OVERFLOW);
+#endif
+            return true;
+        }
+        stack[s.sp++] = s.group;
+        s.group.y = imask;
+    }
+    return false;
+}
+
+// Node group on the stack: x = child_base, y = (internal hit mask << 8) | imask.
+template <int MODE, bool ANY>
+__host__ __device__ __forceinline__ bool wide_traverse(const Wide8Args &a, const DevRay &r, float &best_t,
+                                                       int32_t &best_prim, unsigned long long *nodes_out,
+                                                       unsigned long long *boxes_out, unsigned long long *tris_out)
+{
+    best_t = r.tmax;
+    best_prim = INT_MAX;
+    if (a.num_nodes == 0) return false;
+    WtSetup w;
+    if (MODE == 1) w = wt_setup(r.v);
+    const uint32_t oct = ray_octant(r);
+    uint2 stack[kWideStack];
+    int sp = 0;
+    // the root is visited directly
+    uint32_t node = 0;
+    bool have_node = true;
+    uint2 group = make_uint2(0, 0);
+    unsigned long long nn = 0, nb = 0, nt = 0;
+    while (true) {
+        uint32_t tri_base = 0, tri_mask = 0;
+        if (have_node) {
+            uint32_t child_base, imask, hit_int, nbx;
+            wide_node_test(a.nodes + node, r, oct, best_t, child_base, imask, hit_int, tri_base, tri_mask, nbx);
+            ++nn;
+            nb += nbx;
+            group = make_uint2(child_base, (hit_int << 8) | imask);
+            have_node = false;
+        }
+        // triangles of the last node
+        while (tri_mask) {
+            const int b = lowest_bit(tri_mask);
+            tri_mask &= tri_mask - 1u;
+            const uint32_t k = tri_base + (uint32_t)b;
+            ++nt;
+            float t;
+            const bool ok = MODE == 1 ? tri_test_wt(a.tri_wt, k, r, w, ANY ? r.tmax : best_t, t)
+                                      : tri_test_ref(a.tri_ref, k, r, ANY ? r.tmax : best_t, t);
+            if (ok) {
+                if (ANY) {
+                    if (nodes_out) {
+                        *nodes_out += nn;
+                        *boxes_out += nb;
+                        *tris_out += nt;
+                    }
+                    return true;
+                }
+                const int32_t prim = DR_LD(a.prim + k);
+                if (t < best_t || prim < best_prim) {
+                    best_t = t;
+                    best_prim = prim;
+                }
+            }
+        }
+        // next internal child: from the current group, else from the stack
+        if ((group.y >> 8) == 0) {
+            if (sp == 0) break;
+            group = stack[--sp];
+        }
+        const uint32_t hits = group.y >> 8;
+        const int k = lowest_bit(hits);
+        const uint32_t rest = hits & (hits - 1u);
+        const uint32_t slot = (uint32_t)k ^ oct;
+        const uint32_t imask = group.y & 0xffu;
+        node = group.x + (uint32_t)popcount(imask & ((1u << slot) - 1u));
+        have_node = true;
+        group.y = (rest << 8) | imask;
+        if (rest) {
+            if (sp >= kWideStack) {
+#if defined(__CUDA_ARCH__)
+                atomicOr(a.error, ERR_STACK_OVERFLOW);
+#endif
+                break;
+            }
+            stack[sp++] = group;
+            group.y = imask;  // the current group is now empty
+        }
+    }
+    if (nodes_out) {
+        *nodes_out += nn;
+        *boxes_out += nb;
+        *tris_out += nt;
+    }
+    return false;
+}
+
+}  // namespace dr

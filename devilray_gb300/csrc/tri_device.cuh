@@ -7,7 +7,14 @@
 
 #include "dr_internal.h"
 
+#include <cmath>
 #include <cstdint>
+
+#if defined(__CUDA_ARCH__)
+#define DR_LDG(p) __ldg(p)
+#else
+#define DR_LDG(p) (*(p))
+#endif
 
 namespace dr {
 
@@ -18,20 +25,21 @@ struct DevRay {
 
 // Reciprocal that maps a zero (or denormal) direction component to +-1e30 so
 // slab times stay finite and ordered.
-__device__ __forceinline__ float safe_rcp(float x)
+__host__ __device__ __forceinline__ float safe_rcp(float x)
 {
     return 1.0f / (fabsf(x) >= 1e-30f ? x : copysignf(1e-30f, x));
 }
 
-__device__ __forceinline__ bool load_ray(const dr_ray *rays, uint64_t i, DevRay &r)
+__host__ __device__ __forceinline__ bool load_ray(const dr_ray *rays, uint64_t i, DevRay &r)
 {
     const float4 *p = reinterpret_cast<const float4 *>(rays) + 2 * i;
-    const float4 a = __ldg(p), b = __ldg(p + 1);
+    const float4 a = DR_LDG(p), b = DR_LDG(p + 1);
     r.o = make_float3(a.x, a.y, a.z);
     r.tmax = a.w;
     r.v = make_float3(b.x, b.y, b.z);
     r.inv = make_float3(safe_rcp(b.x), safe_rcp(b.y), safe_rcp(b.z));
     r.ooi = make_float3(r.o.x * r.inv.x, r.o.y * r.inv.y, r.o.z * r.inv.z);
+    using std::isfinite;
     const bool finite = isfinite(a.x) && isfinite(a.y) && isfinite(a.z) && isfinite(b.x) &&
                         isfinite(b.y) && isfinite(b.z);
     const bool nonzero = !(b.x == 0.0f && b.y == 0.0f && b.z == 0.0f);
@@ -40,7 +48,7 @@ __device__ __forceinline__ bool load_ray(const dr_ray *rays, uint64_t i, DevRay 
 
 // Slab test of both children of a two-box node against [0, tmax]. Boxes are
 // stored widened (conservative), so the FMA form of the slab times is safe.
-__device__ __forceinline__ void intersect_children(const float4 c0xy, const float4 c1xy, const float4 cz,
+__host__ __device__ __forceinline__ void intersect_children(const float4 c0xy, const float4 c1xy, const float4 cz,
                                                    const DevRay &r, float tmax,
                                                    float &t0, float &t1, bool &h0, bool &h1)
 {
@@ -65,11 +73,11 @@ __device__ __forceinline__ void intersect_children(const float4 c0xy, const floa
 // hit/miss decision are bit-identical to the reference; the test stops after t
 // when t cannot beat (best_t, best_prim) under the smaller-t-then-smaller-index
 // rule. Returns true when the triangle beats the current best.
-__device__ __forceinline__ bool tri_test_ref(const float4 *__restrict__ rec, uint32_t k, const DevRay &r,
+__host__ __device__ __forceinline__ bool tri_test_ref(const float4 *__restrict__ rec, uint32_t k, const DevRay &r,
                                              float best_t, float &t_out)
 {
-    const float4 r0 = __ldg(rec + 3 * k);
-    const float4 r1 = __ldg(rec + 3 * k + 1);
+    const float4 r0 = DR_LDG(rec + 3 * k);
+    const float4 r1 = DR_LDG(rec + 3 * k + 1);
     float nx = r0.w, ny = r1.x, nz = r1.y;
     const float px = r.o.x - r0.x, py = r.o.y - r0.y, pz = r.o.z - r0.z;
     float dp = px * nx + py * ny + pz * nz;
@@ -83,7 +91,7 @@ __device__ __forceinline__ bool tri_test_ref(const float4 *__restrict__ rec, uin
     if (d < 1e-7f) return false;
     const float t = dp / d;
     if (!(t <= best_t)) return false;
-    const float4 r2 = __ldg(rec + 3 * k + 2);
+    const float4 r2 = DR_LDG(rec + 3 * k + 2);
     const float BAx = r1.z, BAy = r1.w, BAz = r2.x;
     const float CAx = r2.y, CAy = r2.z, CAz = r2.w;
     const float hx = r.o.x + r.v.x * t, hy = r.o.y + r.v.y * t, hz = r.o.z + r.v.z * t;
@@ -107,9 +115,9 @@ struct WtSetup {
     float Sx, Sy, Sz;
 };
 
-__device__ __forceinline__ float comp(const float3 &a, int k) { return k == 0 ? a.x : (k == 1 ? a.y : a.z); }
+__host__ __device__ __forceinline__ float comp(const float3 &a, int k) { return k == 0 ? a.x : (k == 1 ? a.y : a.z); }
 
-__device__ __forceinline__ WtSetup wt_setup(const float3 &d)
+__host__ __device__ __forceinline__ WtSetup wt_setup(const float3 &d)
 {
     const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
     int kz = 0;
@@ -136,12 +144,12 @@ __device__ __forceinline__ WtSetup wt_setup(const float3 &d)
 }
 
 // Watertight two-sided test on a record {A, B, C}.
-__device__ __forceinline__ bool tri_test_wt(const float4 *__restrict__ rec, uint32_t k, const DevRay &r,
+__host__ __device__ __forceinline__ bool tri_test_wt(const float4 *__restrict__ rec, uint32_t k, const DevRay &r,
                                             const WtSetup &w, float best_t, float &t_out)
 {
-    const float4 r0 = __ldg(rec + 3 * k);
-    const float4 r1 = __ldg(rec + 3 * k + 1);
-    const float4 r2 = __ldg(rec + 3 * k + 2);
+    const float4 r0 = DR_LDG(rec + 3 * k);
+    const float4 r1 = DR_LDG(rec + 3 * k + 1);
+    const float4 r2 = DR_LDG(rec + 3 * k + 2);
     const float3 a = make_float3(r0.x - r.o.x, r0.y - r.o.y, r0.z - r.o.z);
     const float3 b = make_float3(r0.w - r.o.x, r1.x - r.o.y, r1.y - r.o.z);
     const float3 c = make_float3(r1.z - r.o.x, r1.w - r.o.y, r2.x - r.o.z);

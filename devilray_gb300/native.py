@@ -228,7 +228,7 @@ class Scene:
 
     def __init__(self, ctx: Context, positions: np.ndarray, objects=None, materials=None,
                  tri_material=None, tri_weight=None, max_leaf_size: int = 0, sah_bins: int = 0,
-                 threads: int = 0):
+                 threads: int = 0, layout: int = 0):
         self.ctx = ctx
         self.positions = np.ascontiguousarray(positions, np.float32).reshape(-1, 9)
         desc = SceneDesc()
@@ -253,7 +253,7 @@ class Scene:
             tw = np.ascontiguousarray(tri_weight, np.float32)
             keep.append(tw)
             desc.tri_weight_host = tw.ctypes.data
-        cfg = BuildConfig(max_leaf_size, sah_bins, threads, 0)
+        cfg = BuildConfig(max_leaf_size, sah_bins, threads, layout)
         self.handle = C.c_void_p()
         check(load().dr_scene_create(ctx.handle, C.byref(desc), C.byref(cfg), C.byref(self.handle)))
         self._keep = keep

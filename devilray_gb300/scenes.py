@@ -221,3 +221,45 @@ def box_room(sphere_level: int = 3) -> SceneSpec:
     sph = (np.array([0.0, -0.2, 2.0]) + 0.25 * icosphere_soup(sphere_level).reshape(-1, 3, 3)).reshape(-1, 9)
     s.add_object(sph.astype(np.float32), glass)
     return s
+
+
+def many_light(num_triangles: int = 1 << 20, num_emitters: int = 65536, seed: int = 0,
+               half: float = CUBE_HALF) -> SceneSpec:
+    """The many-light configuration: the incoherent soup's spheres; a seeded
+    choice of `num_emitters` triangles emit grey radiance exp(N(0, 1.5^2)); of
+    the remaining spheres half are diffuse (albedo uniform in [0.2, 0.8]) and
+    half dielectric (IOR uniform in [1.3, 1.7]). Materials are per object as in
+    the reference's data model: each sphere's non-emitting triangles form one
+    object, each emitting triangle is an object of its own."""
+    soup, centres, radii = incoherent_soup(num_triangles, seed=seed, half=half)
+    per = 1280
+    rng = np.random.default_rng(seed + 17)
+    n = soup.shape[0]
+    num_emitters = min(num_emitters, n)
+    emit_idx = rng.permutation(n)[:num_emitters]
+    emissive = np.zeros(n, bool)
+    emissive[emit_idx] = True
+    radiance = np.exp(rng.normal(0.0, 1.5, n)).astype(np.float32)
+    nsph = (n + per - 1) // per
+    kind = rng.random(nsph) < 0.5
+    albedo = rng.uniform(0.2, 0.8, nsph)
+    ior = rng.uniform(1.3, 1.7, nsph)
+    s = SceneSpec()
+    for k in range(nsph):
+        tris = np.arange(k * per, min(n, (k + 1) * per))
+        body = tris[~emissive[tris]]
+        if body.size:
+            m = s.add_material(material(0, albedo=(albedo[k],) * 3) if kind[k] else material(1, ior=ior[k]))
+            s.add_object(soup[body], m)
+        for t in tris[emissive[tris]]:
+            L = float(radiance[t])
+            m = s.add_material(material(0, emission=(L, L, L)))
+            s.add_object(soup[t:t + 1], m)
+    return s
+
+
+def outside_camera(width: int, height: int, distance: float = 150.0, half: float = CUBE_HALF) -> dict:
+    """Camera on the -z axis outside the cube, looking at its centre."""
+    m = np.eye(4, dtype=np.float32)
+    m[2, 3] = -distance
+    return camera(width, height, focal=1.0, fov_half_width=0.62 * half / distance * 1.6, transform=m)

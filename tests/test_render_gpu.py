@@ -90,3 +90,20 @@ def test_scene_without_lights_renders_emission_only(native, ctx):
     acc, casts, scene = gpu_render(native, ctx, spec, cam, 4)
     assert scene.info().total_radiant_power == 0.0
     assert (acc[:, :3] == 0).all() and (acc[:, 3] == 4).all() and (casts > 0).all()
+
+
+@pytest.mark.parametrize("mode", ["small", "wave"])
+def test_many_light_render_bit_exact_vs_oracle(native, ctx, oracle, mode):
+    """Reduced many-light configuration: 16,384 triangles, 1,024 emitters with
+    log-normal radiance, diffuse and dielectric spheres; depth 16."""
+    half = 0.35 * scenes.density_half(16384)
+    spec = scenes.many_light(16384, 1024, seed=5, half=half)
+    cam = scenes.outside_camera(40, 30, distance=3 * half, half=half)
+    kw = dict(max_depth=16, seed=9)
+    acc, casts, scene = gpu_render(native, ctx, spec, cam, 4, wave_paths=(1200 if mode == "wave" else 0), **kw)
+    oacc, ocasts, osc = oracle_render(oracle, spec, cam, 4, **kw)
+    assert scene.info().total_radiant_power == np.float32(osc.total_power)
+    mism = np.flatnonzero((acc.view(np.uint32) != oacc.view(np.uint32)).any(1))
+    assert mism.size == 0, f"{mism.size} pixels differ, e.g. {mism[:3]}: {acc[mism[:3]]} vs {oacc[mism[:3]]}"
+    assert np.array_equal(casts, ocasts)
+    assert (acc[:, :3] > 0).mean() > 0.08

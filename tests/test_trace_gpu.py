@@ -57,14 +57,16 @@ def test_closest_hit_matches_reference_fixture(native, ctx, oracle, golden):
     assert np.array_equal(_bits(t), _bits(tc)) and np.array_equal(prim, pc)
 
 
+@pytest.mark.parametrize("layout", [2, 8])
 @pytest.mark.parametrize("mode", [0, 1])
 @pytest.mark.parametrize("ntri,nray,leaf", [(1, 4096, 0), (37, 20000, 1), (5000, 100000, 0), (65536, 262144, 0),
                                             (65536, 262144, 8)])
-def test_closest_hit_bit_exact_vs_oracle(native, ctx, oracle, mode, ntri, nray, leaf):
+def test_closest_hit_bit_exact_vs_oracle(native, ctx, oracle, mode, ntri, nray, leaf, layout):
     half = max(1.0, scenes.density_half(ntri))
     soup, _, _ = scenes.incoherent_soup(ntri, seed=ntri, half=half)
     rays = scenes.incoherent_rays(nray, seed=nray, half=half)
-    scene = native.Scene(ctx, soup, max_leaf_size=leaf)
+    scene = native.Scene(ctx, soup, max_leaf_size=leaf, layout=layout)
+    assert scene.info().layout == layout
     t, prim, _ = gpu_closest(native, scene, rays, mode)
     b = oracle.BBH(soup)
     tc, pc = b.trace_canonical(rays, slack=scene.info().slack, tri_mode=mode)
@@ -83,14 +85,15 @@ def test_closest_hit_brute_force_small(native, ctx, oracle):
     assert np.array_equal(_bits(t), _bits(tb)) and np.array_equal(prim, pb)
 
 
+@pytest.mark.parametrize("layout", [2, 8])
 @pytest.mark.parametrize("mode", [0, 1])
-def test_any_hit_matches_oracle(native, ctx, oracle, mode):
+def test_any_hit_matches_oracle(native, ctx, oracle, mode, layout):
     half = scenes.density_half(30000)
     soup, _, _ = scenes.incoherent_soup(30000, seed=9, half=half)
     rays = scenes.incoherent_rays(200000, seed=10, half=half)
     rng = np.random.default_rng(1)
     rays[:, 3] = rng.uniform(0, 40, len(rays)).astype(np.float32)
-    scene = native.Scene(ctx, soup)
+    scene = native.Scene(ctx, soup, layout=layout)
     occ = gpu_any(native, scene, rays, mode)
     b = oracle.BBH(soup)
     occ_o = b.trace_any(rays, slack=scene.info().slack, tri_mode=mode)
@@ -100,7 +103,8 @@ def test_any_hit_matches_oracle(native, ctx, oracle, mode):
     assert 0.05 < occ.mean() < 0.95
 
 
-def test_edge_cases(native, ctx, oracle):
+@pytest.mark.parametrize("layout", [2, 8])
+def test_edge_cases(native, ctx, oracle, layout):
     unit = np.array([[0, 0, 0, 1, 0, 0, 0, 1, 0]], np.float32)
     degenerate = np.array([[0, 0, 0, 0, 0, 0, 0, 0, 0], [0, 0, 0, 1, 0, 0, 2, 0, 0]], np.float32)
     dup = np.concatenate([unit, unit, unit + np.float32([0, 0, -1] * 3)])
@@ -119,7 +123,7 @@ def test_edge_cases(native, ctx, oracle):
         [0.2, 0.2, 0, 0, 0, -1],       # starts on the surface (t = 0)
     ], np.float32)
     r8 = rays8_from6(r6)
-    scene = native.Scene(ctx, soup)
+    scene = native.Scene(ctx, soup, layout=layout)
     t, prim, _ = gpu_closest(native, scene, r8)
     tb, pb = oracle.trace_brute(soup, r8)
     assert np.array_equal(_bits(t), _bits(tb)) and np.array_equal(prim, pb)
@@ -133,25 +137,31 @@ def test_edge_cases(native, ctx, oracle):
     assert gpu_closest(native, scene, r8b)[1][0] == -1
 
 
-def test_empty_and_single_triangle_scenes(native, ctx):
+@pytest.mark.parametrize("layout", [2, 8])
+def test_empty_and_single_triangle_scenes(native, ctx, layout):
     rays = scenes.incoherent_rays(1000, seed=3)
-    empty = native.Scene(ctx, np.zeros((0, 9), np.float32))
+    empty = native.Scene(ctx, np.zeros((0, 9), np.float32), layout=layout)
     t, prim, _ = gpu_closest(native, empty, rays)
     assert (prim == -1).all() and np.isinf(t).all()
     assert gpu_any(native, empty, rays).sum() == 0
-    one = native.Scene(ctx, np.array([[-60, -60, 0, 60, -60, 0, 0, 60, 0]], np.float32))
+    one = native.Scene(ctx, np.array([[-60, -60, 0, 60, -60, 0, 0, 60, 0]], np.float32), layout=layout)
     t, prim, _ = gpu_closest(native, one, rays)
     assert set(np.unique(prim)) <= {-1, 0} and (prim == 0).sum() > 50
 
 
-def test_counters_and_host_path(native, ctx, oracle):
+@pytest.mark.parametrize("layout", [2, 8])
+def test_counters_and_host_path(native, ctx, oracle, layout):
     half = scenes.density_half(20000)
     soup, _, _ = scenes.incoherent_soup(20000, seed=2, half=half)
     rays = scenes.incoherent_rays(50000, seed=4, half=half)
-    scene = native.Scene(ctx, soup)
+    scene = native.Scene(ctx, soup, layout=layout)
     t, prim, cnt = gpu_closest(native, scene, rays, counters=True)
     assert cnt.rays == len(rays) and cnt.hits == (prim >= 0).sum()
-    assert cnt.node_visits > len(rays) and cnt.tri_tests > 0 and cnt.box_tests == 2 * cnt.node_visits
+    assert cnt.node_visits >= len(rays) and cnt.tri_tests > 0
+    if layout == 2:
+        assert cnt.box_tests == 2 * cnt.node_visits
+    else:
+        assert cnt.node_visits <= cnt.box_tests <= 8 * cnt.node_visits
     hits = scene.trace_closest_host(rays)
     assert np.array_equal(hits["prim"], prim) and np.array_equal(_bits(hits["t"]), _bits(t))
     info = scene.info()
