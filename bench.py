@@ -34,6 +34,11 @@ sys.path.insert(0, str(ROOT))
 
 NUM_TRIS = 1 << 20
 NUM_RAYS = 1 << 24
+# DRAM bytes of one full 16.8 M-ray launch of the dominant kernel, from one
+# `ncu --set full` capture of this workload (the profiles named beside them).
+NCU_TRAFFIC = {8: 1_171_826_000 + 140_918_528, 2: 1_652_000_000 + 152_000_000}
+NCU_PROFILE = {8: "trace_closest_p8_incoherent_1M_tris_16M_rays.md",
+               2: "trace_closest_bvh2_incoherent_1M_tris_16M_rays.md"}
 METRIC = "Mrays/s closest-hit"
 WORKLOAD = "incoherent closest-hit: 2^20-triangle icosphere soup, 16,777,216 rays"
 L2_BYTES = 129 * 1024 * 1024
@@ -261,9 +266,11 @@ def run_ours(args):
                    "l2": "rays 512 MiB per step > L2; scene arrays stay L2-resident across steps",
                    "parallelism": f"replicas{world}" if world > 1 else "single"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "traffic": None,
+                     "frac": achieved / hbm_peak, "traffic": NCU_TRAFFIC.get(info.layout),
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one full launch "
+                                       "(profiles/" + NCU_PROFILE.get(info.layout, "") + ")",
                      "peak_kind": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
-                     "kernel": f"k_trace_closest<0,false,{info.layout}>",
+                     "kernel": ("k_trace_closest_p8<0,false>" if info.layout == 8 else "k_trace_closest<0,false,2>"),
                      "bytes_per_ray": bytes_per_ray, "node_visits_per_ray": nodes_per_ray,
                      "tri_tests_per_ray": tris_per_ray, "hit_fraction": hit_frac,
                      "per_launch_ms": per_launch_ms, "working_set_bytes": working_set,

@@ -137,15 +137,10 @@ __device__ __forceinline__ void warp_append(bool keep, uint32_t slot, uint32_t *
     if (keep) list[base + __popc(mask & ((1u << lane) - 1u))] = slot;
 }
 
-__global__ void __launch_bounds__(kRenderBlock) k_camera(RenderParams p)
+// cameraRay (include/tracing/CameraRay.hpp:6-34) for sample `sample` of `pixel`.
+__device__ __forceinline__ void camera_ray(const RenderParams &p, uint32_t pixel, uint32_t sample, float3 &o, float3 &d)
 {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i == 0) p.counts[0] = p.wave;
-    if (i >= p.wave) return;
-    uint32_t pixel, sample;
-    slot_pixel(p, i, pixel, sample);
     const int px = (int)(pixel % (uint32_t)p.width), py = (int)(pixel / (uint32_t)p.width);
-    // cameraRay (include/tracing/CameraRay.hpp:6-34)
     float subx = 0.5f, suby = 0.5f;
     if (p.pixel_sampling == DR_PIXEL_UNIFORM_RANDOM) {
         float u[4];
@@ -157,18 +152,90 @@ __global__ void __launch_bounds__(kRenderBlock) k_camera(RenderParams p)
     const float physx = pcx * p.psx - p.cx, physy = pcy * p.psy - p.cy;
     const float dx = physx / p.focal, dy = physy / p.focal;
     const F3 v = normalized(f3(dx, dy, 1.0f));
-    const float ox = p.m[3], oy = p.m[7], oz = p.m[11];
-    const float vx = p.m[0] * v.x + p.m[1] * v.y + p.m[2] * v.z;
-    const float vy = p.m[4] * v.x + p.m[5] * v.y + p.m[6] * v.z;
-    const float vz = p.m[8] * v.x + p.m[9] * v.y + p.m[10] * v.z;
-    p.rays[2 * i] = make_float4(ox, oy, oz, __int_as_float(0x7f800000));
-    p.rays[2 * i + 1] = make_float4(vx, vy, vz, 0.0f);
+    o = make_float3(p.m[3], p.m[7], p.m[11]);
+    d = make_float3(p.m[0] * v.x + p.m[1] * v.y + p.m[2] * v.z, p.m[4] * v.x + p.m[5] * v.y + p.m[6] * v.z,
+                    p.m[8] * v.x + p.m[9] * v.y + p.m[10] * v.z);
+}
+
+__global__ void __launch_bounds__(kRenderBlock) k_camera(RenderParams p)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) p.counts[0] = p.wave;
+    if (i >= p.wave) return;
+    uint32_t pixel, sample;
+    slot_pixel(p, i, pixel, sample);
+    float3 o, d;
+    camera_ray(p, pixel, sample, o, d);
+    p.rays[2 * i] = make_float4(o.x, o.y, o.z, __int_as_float(0x7f800000));
+    p.rays[2 * i + 1] = make_float4(d.x, d.y, d.z, 0.0f);
     p.thr[i] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
     p.color[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     p.prev_p[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);  // w = 0: no diffuse vertex before
     p.stack[i] = make_int4(0, 0, 0, 0);                 // w = size
     p.casts[i] = 0;
     p.list[0][i] = i;
+}
+
+// First-hit debug views: sampleColorDebug (UV checker) and the debug branch of
+// sampleColor (barycentrics, winding order), include/tracing/PathGeneration.hpp:
+// 274-299, 393-429. One thread per pixel adds its samples in order. The
+// reference's hit uv is always (0, 0) (IntersectionTestsImpl.hpp:58), so the
+// checker pattern is its dark colour 0.5 everywhere; the UV view adds a sample
+// (w + 1) only where the camera ray hits.
+template <int MODE, int LAYOUT>
+__global__ void __launch_bounds__(kRenderBlock) k_debug(RenderParams p, int view, uint32_t spp)
+{
+    const uint32_t pixel = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pixel >= p.npix) return;
+    float4 acc = p.accum[pixel];
+    uint32_t casts = 0;
+    for (uint32_t k = 0; k < spp; ++k) {
+        float3 o, d;
+        camera_ray(p, pixel, p.sample_base + k, o, d);
+        const float4 ray[2] = {make_float4(o.x, o.y, o.z, __int_as_float(0x7f800000)), make_float4(d.x, d.y, d.z, 0.0f)};
+        DevRay r;
+        const bool valid = load_ray(reinterpret_cast<const dr_ray *>(ray), 0, r);
+        float t = r.tmax;
+        int32_t prim = INT_MAX;
+        TraceStats st;
+        if (valid) scene_closest<MODE, false, LAYOUT>(p.trace, r, t, prim, st);
+        ++casts;
+        float4 color = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        bool counted = true;
+        if (prim != INT_MAX) {
+            const float4 s0 = p.shade[3 * prim], s1 = p.shade[3 * prim + 1], s2 = p.shade[3 * prim + 2];
+            const dr_material &m = p.materials[__float_as_int(s2.z)];
+            if (view == DR_DEBUG_UV_CHECKER) {
+                color = mul4(make_float4(0.5f, 0.5f, 0.5f, 0.0f),
+                             make_float4(m.debug_color[0], m.debug_color[1], m.debug_color[2], m.debug_color[3]));
+            } else {
+                // testTriangleIntersection's barycentrics and the ccw flag of
+                // getIntersectionTris, in the reference's expression order
+                const F3 A = f3(s0.x, s0.y, s0.z), B = f3(s0.w, s1.x, s1.y), C = f3(s1.z, s1.w, s2.x);
+                const F3 v = f3(d.x, d.y, d.z);
+                const F3 nf = cross(sub(A, B), sub(A, C));
+                if (view == DR_DEBUG_BARI_COORDS) {
+                    const float s2a = dot(nf, nf);
+                    const F3 hp = add(f3(o.x, o.y, o.z), mul(v, t));
+                    const F3 n1 = cross(sub(hp, A), sub(C, A));
+                    const F3 n2 = cross(sub(B, A), sub(hp, A));
+                    const float wB = dot(nf, n1) / s2a, wC = dot(nf, n2) / s2a;
+                    const float wA = 1 - wB - wC;
+                    color = make_float4(wA, wB, wC, 0.0f);
+                } else {
+                    color = dot(nf, v) > 0 ? make_float4(1.0f, 0.73f, 0.47f, 0.0f) : make_float4(0.53f, 0.82f, 1.0f, 0.0f);
+                }
+            }
+        } else if (view == DR_DEBUG_UV_CHECKER) {
+            counted = false;
+        }
+        if (counted) {
+            acc.w = acc.w + 1.0f;
+            acc = add4(acc, color);
+        }
+    }
+    p.accum[pixel] = acc;
+    if (p.pix_casts) p.pix_casts[pixel] += casts;
 }
 
 // Ray sources of the persistent wide kernels: list entry i names a path slot.
@@ -494,6 +561,46 @@ size_t wave_bytes(uint32_t W)
     return (size_t)W * 200 + 128 * sizeof(uint32_t) + 128 * sizeof(unsigned long long) + 18 * 256;
 }
 
+// Scene, camera and output fields of the render parameters.
+RenderParams base_params(const dr_scene *s, const dr_camera *cam, const dr_render_config *cfg, float *accum_dev,
+                         uint32_t *casts_dev, uint32_t npix)
+{
+    RenderParams p{};
+    p.trace.nodes = s->d_nodes;
+    p.trace.nodes8 = s->d_nodes8;
+    p.trace.layout = (int)s->layout;
+    p.trace.tri_ref = s->d_tri_ref;
+    p.trace.tri_wt = s->d_tri_wt;
+    p.trace.prim = s->d_prim;
+    p.trace.num_nodes = s->num_nodes;
+    p.trace.error = s->ctx->d_error;
+    p.shade = s->d_shade;
+    p.objects = s->d_objects;
+    p.materials = s->d_materials;
+    p.light_table = s->d_light_table;
+    p.tri_tables = s->d_tri_tables;
+    p.num_objects = s->num_objects;
+    p.total_power = s->total_radiant_power;
+    p.lights = s->lights ? 1 : 0;
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 4; ++c) p.m[r * 4 + c] = cam->transform[r * 4 + c];
+    p.focal = cam->focal_length;
+    p.cx = cam->center[0];
+    p.cy = cam->center[1];
+    p.psx = cam->pixel_size[0];
+    p.psy = cam->pixel_size[1];
+    p.width = cam->width;
+    p.height = cam->height;
+    p.pixel_sampling = cfg->pixel_sampling;
+    p.npix = npix;
+    p.max_depth = cfg->max_depth;
+    p.seed_lo = (uint32_t)cfg->seed;
+    p.seed_hi = (uint32_t)(cfg->seed >> 32);
+    p.accum = reinterpret_cast<float4 *>(accum_dev);
+    p.pix_casts = casts_dev;
+    return p;
+}
+
 }  // namespace
 }  // namespace dr
 
@@ -507,12 +614,28 @@ extern "C" dr_status dr_render(dr_scene *s, const dr_camera *cam, const dr_rende
     DR_CHECK_ARG(cfg->max_depth >= 1 && cfg->max_depth <= (uint32_t)kMaxDepth, "dr_render: max_depth must be in [1, 63]");
     DR_CHECK_ARG(cfg->tri_mode == DR_TRI_REFERENCE || cfg->tri_mode == DR_TRI_WATERTIGHT, "dr_render: bad tri_mode");
     DR_CHECK_ARG((reinterpret_cast<uintptr_t>(accum_dev) & 15) == 0, "dr_render: accum must be 16-byte aligned");
+    DR_CHECK_ARG(cfg->debug >= DR_DEBUG_OFF && cfg->debug <= DR_DEBUG_WINDING_ORDER, "dr_render: bad debug view");
     if (cfg->spp == 0) return DR_OK;
     DR_CUDA(cudaSetDevice(s->ctx->device));
     auto st = static_cast<cudaStream_t>(stream);
     const uint64_t npix64 = (uint64_t)cam->width * (uint64_t)cam->height;
     DR_CHECK_ARG(npix64 < (1ull << 31), "dr_render: image too large");
     const uint32_t npix = (uint32_t)npix64;
+    if (cfg->debug != DR_DEBUG_OFF) {
+        RenderParams p = base_params(s, cam, cfg, accum_dev, casts_dev, npix);
+        p.sample_base = cfg->sample_offset;
+        const unsigned grid = (npix + kRenderBlock - 1) / kRenderBlock;
+        const bool wt = cfg->tri_mode == DR_TRI_WATERTIGHT;
+        if (s->layout == 8) {
+            if (wt) k_debug<1, 8><<<grid, kRenderBlock, 0, st>>>(p, cfg->debug, cfg->spp);
+            else k_debug<0, 8><<<grid, kRenderBlock, 0, st>>>(p, cfg->debug, cfg->spp);
+        } else {
+            if (wt) k_debug<1, 2><<<grid, kRenderBlock, 0, st>>>(p, cfg->debug, cfg->spp);
+            else k_debug<0, 2><<<grid, kRenderBlock, 0, st>>>(p, cfg->debug, cfg->spp);
+        }
+        DR_CUDA(cudaGetLastError());
+        return DR_OK;
+    }
     const uint32_t target = cfg->wave_paths ? cfg->wave_paths : (1u << 21);
     const uint32_t spp_wave = std::max<uint32_t>(1, std::min<uint32_t>(cfg->spp, target / npix));
     const uint32_t W = npix * spp_wave;
@@ -548,39 +671,7 @@ extern "C" dr_status dr_render(dr_scene *s, const dr_camera *cam, const dr_rende
         if (!s->wave_stream[k]) DR_CUDA(cudaStreamCreateWithFlags(&s->wave_stream[k], cudaStreamNonBlocking));
     for (int k = 0; k <= K; ++k)
         if (!s->wave_event[k]) DR_CUDA(cudaEventCreateWithFlags(&s->wave_event[k], cudaEventDisableTiming));
-    RenderParams p{};
-    p.trace.nodes = s->d_nodes;
-    p.trace.nodes8 = s->d_nodes8;
-    p.trace.layout = (int)s->layout;
-    p.trace.tri_ref = s->d_tri_ref;
-    p.trace.tri_wt = s->d_tri_wt;
-    p.trace.prim = s->d_prim;
-    p.trace.num_nodes = s->num_nodes;
-    p.trace.error = s->ctx->d_error;
-    p.shade = s->d_shade;
-    p.objects = s->d_objects;
-    p.materials = s->d_materials;
-    p.light_table = s->d_light_table;
-    p.tri_tables = s->d_tri_tables;
-    p.num_objects = s->num_objects;
-    p.total_power = s->total_radiant_power;
-    p.lights = s->lights ? 1 : 0;
-    for (int r = 0; r < 3; ++r)
-        for (int c = 0; c < 4; ++c) p.m[r * 4 + c] = cam->transform[r * 4 + c];
-    p.focal = cam->focal_length;
-    p.cx = cam->center[0];
-    p.cy = cam->center[1];
-    p.psx = cam->pixel_size[0];
-    p.psy = cam->pixel_size[1];
-    p.width = cam->width;
-    p.height = cam->height;
-    p.pixel_sampling = cfg->pixel_sampling;
-    p.npix = npix;
-    p.max_depth = cfg->max_depth;
-    p.seed_lo = (uint32_t)cfg->seed;
-    p.seed_hi = (uint32_t)(cfg->seed >> 32);
-    p.accum = reinterpret_cast<float4 *>(accum_dev);
-    p.pix_casts = casts_dev;
+    const RenderParams p = base_params(s, cam, cfg, accum_dev, casts_dev, npix);
     RenderParams ps[dr_scene::kWaveStreams];
     for (int k = 0; k < K; ++k) {
         ps[k] = p;

@@ -81,7 +81,7 @@ class Camera(C.Structure):
 class RenderConfig(C.Structure):
     _fields_ = [("max_depth", C.c_uint32), ("spp", C.c_uint32), ("sample_offset", C.c_uint32),
                 ("pixel_sampling", C.c_int32), ("seed", C.c_uint64), ("tri_mode", C.c_int32),
-                ("wave_paths", C.c_uint32), ("flags", C.c_uint32), ("pad", C.c_uint32)]
+                ("wave_paths", C.c_uint32), ("flags", C.c_uint32), ("debug", C.c_int32)]
 
 
 def make_camera(cam: dict) -> Camera:
@@ -117,6 +117,14 @@ SIGNATURES = {
     "dr_trace_closest_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_int32, C.c_void_p]),
     "dr_render": (C.c_int, [C.c_void_p, C.POINTER(Camera), C.POINTER(RenderConfig), C.c_void_p, C.c_void_p,
                             C.c_void_p]),
+    "dr_framebuffer_create": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
+    "dr_framebuffer_destroy": (C.c_int, [C.c_void_p]),
+    "dr_framebuffer_clear": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "dr_framebuffer_device_buffers": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
+    "dr_framebuffer_read": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_uint64)]),
+    "dr_framebuffer_tonemap": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+    "dr_tonemap": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
+    "dr_alias_build_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_int32]),
     "dr_alias_build": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_int32, C.c_void_p]),
     "dr_alias_build_noalloc": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
     "dr_alias_sample": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p,
@@ -289,9 +297,9 @@ class Scene:
     # -- rendering --
     def render(self, cam: dict, accum_dev, casts_dev=None, spp: int = 1, max_depth: int = 10,
                sample_offset: int = 0, pixel_sampling: int = 1, seed: int = 0, tri_mode: int = DR_TRI_REFERENCE,
-               wave_paths: int = 0, stream=None):
+               wave_paths: int = 0, debug: int = 0, stream=None):
         c = make_camera(cam)
-        cfg = RenderConfig(max_depth, spp, sample_offset, pixel_sampling, seed, tri_mode, wave_paths, 0, 0)
+        cfg = RenderConfig(max_depth, spp, sample_offset, pixel_sampling, seed, tri_mode, wave_paths, 0, debug)
         check(load().dr_render(self.handle, C.byref(c), C.byref(cfg), _ptr(accum_dev), _ptr(casts_dev),
                                _stream_ptr(stream)))
 
@@ -306,6 +314,54 @@ class Scene:
         check(load().dr_trace_closest_host(self.handle, _ptr(rays), n, _ptr(hits), tri_mode,
                                            _stream_ptr(stream)))
         return hits
+
+
+class Framebuffer:
+    """Accumulation buffers of a progressive render (Buffers of the reference)."""
+
+    def __init__(self, ctx: "Context", width: int, height: int):
+        self.ctx = ctx
+        self.width, self.height = int(width), int(height)
+        h = C.c_void_p()
+        check(load().dr_framebuffer_create(ctx.handle, self.width, self.height, C.byref(h)))
+        self.handle = h.value
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            load().dr_framebuffer_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def clear(self, stream=None) -> None:
+        check(load().dr_framebuffer_clear(self.handle, _stream_ptr(stream)))
+
+    def device_buffers(self) -> tuple[int, int]:
+        a, c = C.c_void_p(), C.c_void_p()
+        check(load().dr_framebuffer_device_buffers(self.handle, C.byref(a), C.byref(c)))
+        return a.value, c.value
+
+    def read(self):
+        n = self.width * self.height
+        acc = np.zeros((n, 4), np.float32)
+        casts = np.zeros(n, np.uint32)
+        total = C.c_uint64()
+        check(load().dr_framebuffer_read(self.handle, _ptr(acc), _ptr(casts), C.byref(total)))
+        return acc, casts, total.value
+
+    def tonemap(self, gamma: bool = True) -> np.ndarray:
+        out = np.zeros(self.width * self.height, np.uint32)
+        check(load().dr_framebuffer_tonemap(self.handle, 1 if gamma else 0, _ptr(out)))
+        return out
+
+
+def tonemap(accum_dev, width: int, height: int, rgba_dev, gamma: bool = True, stream=None) -> None:
+    check(load().dr_tonemap(_ptr(accum_dev), width, height, 1 if gamma else 0, _ptr(rgba_dev),
+                            _stream_ptr(stream)))
 
 
 def make_rays(origins: np.ndarray, dirs: np.ndarray, tmax=np.inf) -> np.ndarray:

@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define DR_ABI_VERSION 1
+#define DR_ABI_VERSION 2
 
 typedef enum dr_status {
     DR_OK = 0,
@@ -192,6 +192,16 @@ typedef struct dr_camera {
 
 typedef enum dr_pixel_sampling { DR_PIXEL_CENTER = 0, DR_PIXEL_UNIFORM_RANDOM = 1 } dr_pixel_sampling;
 
+/* First-hit debug views (DebugOptions, include/DebugOptions.hpp): the camera ray's
+ * closest hit coloured by material debug colour x 0.5 (UV checker; only hits add
+ * a sample), by its barycentrics, or by its winding order. */
+typedef enum dr_debug_view {
+    DR_DEBUG_OFF = 0,
+    DR_DEBUG_UV_CHECKER = 1,
+    DR_DEBUG_BARI_COORDS = 2,
+    DR_DEBUG_WINDING_ORDER = 3
+} dr_debug_view;
+
 typedef struct dr_render_config {
     uint32_t max_depth;      /* path vertices per sample (reference: 10, PathGeneration.hpp:380) */
     uint32_t spp;            /* samples per pixel added by this call */
@@ -201,7 +211,7 @@ typedef struct dr_render_config {
     int32_t tri_mode;        /* dr_tri_mode */
     uint32_t wave_paths;     /* paths in flight per wave, 0 = automatic */
     uint32_t flags;          /* reserved, 0 */
-    uint32_t pad;
+    int32_t debug;           /* dr_debug_view */
 } dr_render_config;
 
 /* Adds cfg->spp path samples per pixel to accum_dev (float4 per pixel, row
@@ -216,6 +226,30 @@ typedef struct dr_render_config {
  * Asynchronous on `stream`. */
 dr_status dr_render(dr_scene *scene, const dr_camera *camera, const dr_render_config *cfg, float *accum_dev,
                     uint32_t *casts_dev, void *stream);
+
+/* Accumulation buffers of a progressive render (Buffers, include/Buffers.hpp:9-22):
+ * float4 colour sums with the sample count in w, and uint32 path-ray casts. */
+typedef struct dr_framebuffer dr_framebuffer;
+
+dr_status dr_framebuffer_create(dr_context *ctx, int32_t width, int32_t height, dr_framebuffer **out);
+dr_status dr_framebuffer_destroy(dr_framebuffer *fb);
+/* Zeroes colour and casts (Buffers::reset, src/Renderer.cpp:17-21). Asynchronous. */
+dr_status dr_framebuffer_clear(dr_framebuffer *fb, void *stream);
+/* Device pointers to pass to dr_render. */
+dr_status dr_framebuffer_device_buffers(dr_framebuffer *fb, float **accum_dev, uint32_t **casts_dev);
+/* Copies the buffers to the host (either pointer may be NULL) and the total of
+ * the casts (Buffers::totalCasts, src/Renderer.cpp:29-35). Synchronous. */
+dr_status dr_framebuffer_read(dr_framebuffer *fb, float *accum_host, uint32_t *casts_host, uint64_t *total_casts);
+/* Renderer::createPixels (src/Renderer.cpp:51-90) on the device: average of the
+ * samples, optional sRGB encoding, 8-bit RGBA with alpha 255, rows flipped so
+ * the first row written is the top of the image. rgba_host: width * height
+ * uint32 values. Synchronous. */
+dr_status dr_framebuffer_tonemap(dr_framebuffer *fb, int32_t gamma_corrected, uint32_t *rgba_host);
+/* The same conversion on any device accumulation buffer (float4 per pixel,
+ * 16-byte aligned) into a device RGBA8 buffer. Asynchronous on `stream`.
+ * height <= 65535. */
+dr_status dr_tonemap(const float *accum_dev, int32_t width, int32_t height, int32_t gamma_corrected,
+                     uint32_t *rgba_dev, void *stream);
 
 /* ---- alias tables ------------------------------------------------------------------- */
 
@@ -244,6 +278,10 @@ dr_status dr_alias_build(dr_context *ctx, const float *weights_dev, uint32_t n, 
  * uniforms of draw i at uniforms_dev[2i], uniforms_dev[2i+1]. */
 dr_status dr_alias_sample(const dr_alias_entry *table_dev, uint32_t n, const float *uniforms_dev, uint64_t ndraws,
                           int32_t *index_dev, float *pdf_dev, void *stream);
+
+/* dr_alias_build over host buffers (copies in and out). Synchronous. */
+dr_status dr_alias_build_host(dr_context *ctx, const float *weights_host, uint32_t n, dr_alias_entry *table_host,
+                              int32_t mode);
 
 /* Sweep-mode alias build (same table as dr_alias_build with DR_ALIAS_SWEEP)
  * that allocates no device memory. No counterpart in the reference. For

@@ -122,6 +122,7 @@ typedef struct or_render_cfg {
     int32_t threads;
     int32_t replay_stride;   /* uniforms per (pixel, sample) in `replay` */
     const float *replay;     /* [pixel][sample][replay_stride] */
+    int32_t debug;           /* 0 off, 1 UV checker, 2 barycentrics, 3 winding order */
 } or_render_cfg;
 
 typedef struct or_scene or_scene;
@@ -135,6 +136,11 @@ void or_scene_light_table(const or_scene *s, or_alias_entry *out);
  * Any output may be NULL. */
 void or_render(const or_scene *s, const or_camera *cam, const or_render_cfg *cfg, float *sample_rgb, float *accum,
                uint32_t *casts);
+
+/* Renderer::createPixels (src/Renderer.cpp:51-90): accum [height*width][4]
+ * (colour sums, sample count in w) to RGBA8 rows, first row = top of the image.
+ * gamma != 0: OutputLinearity::GammaCorrected (sRGB); 0: Linear. */
+void or_create_pixels(const float *accum, int32_t width, int32_t height, int32_t gamma, uint32_t *out);
 
 /* ---- Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) ------------------- */
 void or_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);

@@ -70,7 +70,7 @@ inline float cosineHemispherePdf(const V3 &cur, const V3 &next, const V3 &n)
 struct Mat {
     int kind;
     float ior;
-    V4 emission, albedo;
+    V4 emission, albedo, debug;
 };
 
 inline V4 radiantExitance(const Mat &m)  // include/tracing/LightSampling.hpp:7-13
@@ -214,9 +214,10 @@ or_scene *or_scene_create(const float *positions, int32_t num_tris, const or_obj
     for (int i = 0; i < num_materials; ++i) {
         const or_material &m = materials[i];
         s->mats.push_back(Mat{m.kind, m.ior, V4{m.emission[0], m.emission[1], m.emission[2], m.emission[3]},
-                              V4{m.albedo[0], m.albedo[1], m.albedo[2], m.albedo[3]}});
+                              V4{m.albedo[0], m.albedo[1], m.albedo[2], m.albedo[3]},
+                              V4{m.debug_color[0], m.debug_color[1], m.debug_color[2], m.debug_color[3]}});
     }
-    if (s->mats.empty()) s->mats.push_back(Mat{0, 1.0f, V4{0, 0, 0, 0}, V4{0.5f, 0.5f, 0.5f, 0}});
+    if (s->mats.empty()) s->mats.push_back(Mat{0, 1.0f, V4{0, 0, 0, 0}, V4{0.5f, 0.5f, 0.5f, 0}, V4{0, 0, 0, 0}});
     s->tri_object.assign((size_t)num_tris, 0);
     s->tri_material.assign((size_t)num_tris, 0);
     for (size_t o = 0; o < s->objects.size(); ++o)
@@ -320,6 +321,51 @@ void or_render(const or_scene *s, const or_camera *cam, const or_render_cfg *cfg
                 V3 rp{m[3], m[7], m[11]};
                 V3 rv{m[0] * cv.x + m[1] * cv.y + m[2] * cv.z, m[4] * cv.x + m[5] * cv.y + m[6] * cv.z,
                       m[8] * cv.x + m[9] * cv.y + m[10] * cv.z};
+
+                if (cfg->debug != 0) {
+                    // first-hit debug views (PathGeneration.hpp:274-299, 393-429);
+                    // the reference's hit uv is (0, 0), so the checker is its dark colour
+                    const Hit hit = castRay(*s, cfg->cast_mode, rp, rv);
+                    pixel_casts += 1;
+                    V4 color{0, 0, 0, 0};
+                    bool counted = true;
+                    if (hit.prim >= 0) {
+                        const Mat &mat = s->mats[s->tri_material[hit.prim]];
+                        if (cfg->debug == 1) {
+                            color = mul4(V4{0.5f, 0.5f, 0.5f, 0.0f}, mat.debug);
+                        } else {
+                            const V3 A = vtx(*s, hit.prim, 0), B = vtx(*s, hit.prim, 1), C = vtx(*s, hit.prim, 2);
+                            if (cfg->debug == 2) {
+                                // testTriangleIntersection's barycentrics at the hit's t
+                                const V3 n_f = cross(sub(A, B), sub(A, C));
+                                const float sgn_area2 = dot(n_f, n_f);
+                                const V3 hp = add(rp, mul(rv, hit.t));
+                                const V3 n_1 = cross(sub(hp, A), sub(C, A));
+                                const V3 n_2 = cross(sub(B, A), sub(hp, A));
+                                const float w_B = dot(n_f, n_1) / sgn_area2;
+                                const float w_C = dot(n_f, n_2) / sgn_area2;
+                                const float w_A = 1 - w_B - w_C;
+                                color = V4{w_A, w_B, w_C, 0.0f};
+                            } else {
+                                const bool ccw = dot(cross(sub(A, B), sub(A, C)), rv) > 0;
+                                color = ccw ? V4{1.0f, 0.73f, 0.47f, 0.0f} : V4{0.53f, 0.82f, 1.0f, 0.0f};
+                            }
+                        }
+                    } else if (cfg->debug == 1) {
+                        counted = false;
+                    }
+                    if (sample_rgb) {
+                        float *o = sample_rgb + ((size_t)si * npix + pix) * 3;
+                        o[0] = color.x;
+                        o[1] = color.y;
+                        o[2] = color.z;
+                    }
+                    if (counted) {
+                        pixel.w += 1;
+                        pixel = add4(pixel, color);
+                    }
+                    continue;
+                }
 
                 // path construction (:431-447)
                 V4 thr{1, 1, 1, 0};
@@ -519,6 +565,32 @@ void or_render(const or_scene *s, const or_camera *cam, const or_render_cfg *cfg
         pool.emplace_back(work, b, e);
     }
     for (auto &th : pool) th.join();
+}
+
+void or_create_pixels(const float *accum, int32_t width, int32_t height, int32_t gamma, uint32_t *out)
+{
+    // toSRGB, to_u32, packPixel and setPixel of src/Renderer.cpp:53-79, in the
+    // same mixed float/double arithmetic.
+    auto to_srgb = [gamma](float linear) -> float {
+        if (!gamma) return linear;
+        const float r = std::clamp(linear, 0.f, 1.f);
+        if (r < 0.0031308) return r * 12.92;
+        return std::pow(r, 1 / 2.4f) * 1.055 - 0.055f;
+    };
+    auto to_u32 = [](float f) -> uint32_t { return static_cast<uint32_t>(std::round(f)); };
+    auto pack = [&](float r, float g, float b, float a) -> uint32_t {
+        return (to_u32(to_srgb(r) * 255) << 0) | (to_u32(to_srgb(g) * 255) << 8) |
+               (to_u32(to_srgb(b) * 255) << 16) | (to_u32(std::clamp(a, 0.0f, 1.0f) * 255) << 24);
+    };
+    for (int32_t y = 0; y < height; ++y)
+        for (int32_t x = 0; x < width; ++x) {
+            const float *p = accum + 4 * ((size_t)x + (size_t)y * width);
+            const size_t dst = (size_t)x + (size_t)(height - y - 1) * width;
+            if (p[3] == 0)
+                out[dst] = pack(0, 0, 0, 1.0f);
+            else
+                out[dst] = pack(p[0] / p[3], p[1] / p[3], p[2] / p[3], 1.0f);
+        }
 }
 
 }  // extern "C"

@@ -73,8 +73,18 @@ def lib():
                                       C.POINTER(C.c_int32), C.POINTER(C.c_float)]
         L.or_lognormal_input.argtypes = [C.c_int32, C.c_uint32, _f32p]
         L.or_philox4x32_10.argtypes = [_u32p, _u32p, _u32p]
+        L.or_create_pixels.argtypes = [_f32p, C.c_int32, C.c_int32, C.c_int32, _u32p]
         _lib = L
     return _lib
+
+
+def create_pixels(accum, width: int, height: int, gamma: bool = True) -> np.ndarray:
+    """Renderer::createPixels restated: RGBA8 pixels, rows top first."""
+    a = _f32(accum).reshape(-1)
+    assert a.size == 4 * width * height
+    out = np.zeros(width * height, np.uint32)
+    lib().or_create_pixels(a, width, height, 1 if gamma else 0, out)
+    return out
 
 
 def ref_available() -> bool:
@@ -289,7 +299,8 @@ class RenderCfg(C.Structure):
     _fields_ = [("max_depth", C.c_int32), ("spp", C.c_int32), ("sample_offset", C.c_int32),
                 ("pixel_sampling", C.c_int32), ("seed", C.c_uint64), ("rng_mode", C.c_int32),
                 ("trig_mode", C.c_int32), ("cast_mode", C.c_int32), ("tri_table_order", C.c_int32),
-                ("threads", C.c_int32), ("replay_stride", C.c_int32), ("replay", C.c_void_p)]
+                ("threads", C.c_int32), ("replay_stride", C.c_int32), ("replay", C.c_void_p),
+                ("debug", C.c_int32)]
 
 
 class Camera(C.Structure):
@@ -350,9 +361,9 @@ class RenderScene:
     def render(self, cam: dict, spp: int, max_depth: int = 10, seed: int = 0, sample_offset: int = 0,
                pixel_sampling: int = 1, rng_mode: int = 0, trig_mode: int = 0, cast_mode: int = 0,
                tri_table_order: int = 0, replay: np.ndarray | None = None, threads: int = 0,
-               per_sample: bool = False):
+               per_sample: bool = False, debug: int = 0):
         cfg = RenderCfg(max_depth, spp, sample_offset, pixel_sampling, seed, rng_mode, trig_mode, cast_mode,
-                        tri_table_order, threads, 0, None)
+                        tri_table_order, threads, 0, None, debug)
         if replay is not None:
             replay = _f32(replay)
             cfg.replay_stride = replay.shape[-1]
@@ -367,17 +378,19 @@ class RenderScene:
         return accum, casts, rgb
 
 
-def ref_render_samples(spec, cam: dict, spp: int, replay: np.ndarray, sampling: int = 1):
-    """The reference's own sampleColor (depth 10) on every pixel sample."""
+def ref_render_samples(spec, cam: dict, spp: int, replay: np.ndarray, sampling: int = 1, debug: int = 0):
+    """The reference's own sampleColor (depth 10) on every pixel sample:
+    per-sample colours, per-pixel path-ray counts and per-sample counts (w)."""
     L = ref()
     if not getattr(L, "_render_bound", False):
         L.refh_render_samples.argtypes = [_f32p, _i32p, _i32p, _i32p, _f32p, C.c_int, _f32p, C.c_int, _f32p,
                                           C.c_float, C.c_float, C.c_float, C.c_int, C.c_int, C.c_float, C.c_float,
-                                          C.c_int, C.c_int, _f32p, C.c_int, _f32p, _u32p]
+                                          C.c_int, C.c_int, _f32p, C.c_int, _f32p, _u32p, C.c_int, _f32p]
         L._render_bound = True
     objs = spec.objects_array()
     w, h = cam["width"], cam["height"]
     rgb = np.zeros((spp, h * w, 3), np.float32)
+    sw = np.zeros((spp, h * w), np.float32)
     casts = np.zeros(h * w, np.uint32)
     replay = _f32(replay)
     L.refh_render_samples(_f32(spec.positions).reshape(-1), objs["tri_begin"].astype(np.int32),
@@ -385,5 +398,5 @@ def ref_render_samples(spec, cam: dict, spp: int, replay: np.ndarray, sampling: 
                           objs["surface_area"].astype(np.float32), len(objs), spec.materials_array().reshape(-1),
                           len(spec.materials), _f32(cam["m"]), float(cam["focal"]), float(cam["cx"]),
                           float(cam["cy"]), w, h, float(cam["psx"]), float(cam["psy"]), sampling, spp,
-                          replay.reshape(-1), replay.shape[-1], rgb.reshape(-1), casts)
-    return rgb, casts
+                          replay.reshape(-1), replay.shape[-1], rgb.reshape(-1), casts, debug, sw.reshape(-1))
+    return rgb, casts, sw

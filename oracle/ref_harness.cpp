@@ -243,11 +243,13 @@ void refh_camera_ray(const float *m16, float focal, float cx, float cy, float ps
 // (test/src/TracingTestHelpers.hpp:97-112); the light table follows
 // Renderer::calculateLightWeights (src/Renderer.cpp:113-152) with the
 // reference's radiantExitance and luminance. Uniforms are replayed from
-// `replay` ([pixel][sample][stride]); out_rgb receives each sample's colour.
+// `replay` ([pixel][sample][stride]); out_rgb receives each sample's colour
+// and out_w (may be NULL) its sample count (0 or 1). debug: DebugOptions.
 void refh_render_samples(const float *pos, const int *obj_begin, const int *obj_count, const int *obj_mat,
                          const float *obj_area, int nobj, const float *mats, int nmat, const float *m16, float focal,
                          float cx, float cy, int width, int height, float psx, float psy, int sampling, int spp,
-                         const float *replay, int stride, float *out_rgb, unsigned *casts_out)
+                         const float *replay, int stride, float *out_rgb, unsigned *casts_out, int debug,
+                         float *out_w)
 {
     std::vector<Material> materials;
     for (int i = 0; i < nmat; ++i) {
@@ -331,11 +333,12 @@ void refh_render_samples(const float *pos, const int *obj_begin, const int *obj_
                 sampleColor(Vec2f{(float)x, (float)y}, pixel, stats, cam, static_cast<PixelSampling>(sampling),
                             std::span<const TriangleMesh>{objects}, info, std::span<const Material>{materials},
                             std::span<const AliasEntry>{light.entries.hostPtr(), light.entries.size()},
-                            DebugOptions::Off, rng);
+                            static_cast<DebugOptions>(debug), rng);
                 float *o = out_rgb + ((size_t)s2 * npix + pix) * 3;
                 o[0] = pixel.x;
                 o[1] = pixel.y;
                 o[2] = pixel.z;
+                if (out_w) out_w[(size_t)s2 * npix + pix] = pixel.w;
                 casts += stats.ray_casts;
             }
             casts_out[pix] = casts;

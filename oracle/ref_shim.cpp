@@ -14,3 +14,16 @@ void cudaCheckLastError(const char *file, int line, bool abort)
         if (abort) std::exit(code);
     }
 }
+
+// checkerPattern lives in src/device/implementation.cu beside the render
+// kernel (a CUDA translation unit the harness does not build). Contract of
+// include/tracing/PathGeneration.hpp:24-29: checker cell parity of uv scaled by
+// checker_count on each axis, XOR-ed; 1 selects `bright`, 0 selects `dark`.
+#include "Utils.hpp"
+
+HD Vec4 checkerPattern(const Vec2f &uv, const int checker_count, const Vec4 dark, const Vec4 bright)
+{
+    const int cell = (int(uv.x * checker_count) % 2) ^ (int(uv.y * checker_count) % 2);
+    const float f = (float)cell;
+    return bright * f + dark * (1 - f);
+}

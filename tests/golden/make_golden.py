@@ -177,7 +177,7 @@ def render_fixture():
     replay = np.random.default_rng(7).random((w * h, spp, stride)).astype(np.float32)
     out = {}
     for sampling in (0, 1):
-        rgb, casts = po.ref_render_samples(spec, cam, spp, replay, sampling)
+        rgb, casts, _ = po.ref_render_samples(spec, cam, spp, replay, sampling)
         out[f"rgb_{sampling}"] = rgb
         out[f"casts_{sampling}"] = casts
     np.savez_compressed(OUT / "render_pin.npz", positions=spec.positions, objects=spec.objects_array(),
@@ -185,9 +185,30 @@ def render_fixture():
                         spp=np.int32(spp), **out)
 
 
+def debug_fixture():
+    # The first-hit debug views of sampleColor / sampleColorDebug
+    # (include/tracing/PathGeneration.hpp:274-299, 393-429) on the box room,
+    # materials given distinct debug colours; camera jitter replayed.
+    spec = scenes.box_room(sphere_level=1)
+    for i, m in enumerate(spec.materials):
+        m["debug"] = (0.9 - 0.1 * i, 0.2 + 0.15 * i, 0.5, 0.0)
+    w, h, spp, stride = 16, 12, 3, 4
+    cam = scenes.camera(w, h)
+    replay = np.random.default_rng(11).random((w * h, spp, stride)).astype(np.float32)
+    out = {}
+    for view in (1, 2, 3):
+        rgb, casts, sw = po.ref_render_samples(spec, cam, spp, replay, 1, debug=view)
+        out[f"rgb_{view}"] = rgb
+        out[f"casts_{view}"] = casts
+        out[f"w_{view}"] = sw
+    np.savez_compressed(OUT / "render_debug_pin.npz", positions=spec.positions, materials=spec.materials_array(),
+                        replay=replay, width=np.int32(w), height=np.int32(h), spp=np.int32(spp), **out)
+
+
 def main():
     po.build(ref=True)
     render_fixture()
+    debug_fixture()
     tri_fixture()
     box_fixture()
     bbh_fixture()

@@ -195,3 +195,42 @@ def test_integrator_matches_reference_sample_color(oracle, golden):
         assert np.array_equal(rgb.view(np.uint32), g[f"rgb_{sampling}"].view(np.uint32))
         assert np.array_equal(casts, g[f"casts_{sampling}"])
         assert (rgb != 0).any()
+
+
+def test_create_pixels_known_values(oracle):
+    # 2 x 2 image; row 0 is the bottom row of the output
+    acc = np.array([[0, 0, 0, 0],            # never sampled: black
+                    [2, 4, 6, 2],            # averages above 1 clamp to 255
+                    [0.2, 0.2, 0.2, 1],      # linear 0.2 -> 51; sRGB 0.2 -> 124
+                    [0.001, 0, 1, 1]],       # 0.001 is on the linear segment: 0.01292 * 255 -> 3
+                   np.float32)
+    g = oracle.create_pixels(acc, 2, 2, True)
+    lin = oracle.create_pixels(acc, 2, 2, False)
+    # flipped: input row 0 lands in output row 1
+    assert g[2] == 0xFF000000 and g[3] == 0xFFFFFFFF
+    assert g[0] == 0xFF000000 | (124 << 16) | (124 << 8) | 124
+    assert g[1] == 0xFF000000 | (255 << 16) | 3
+    assert lin[0] == 0xFF000000 | (51 << 16) | (51 << 8) | 51
+
+
+@pytest.mark.parametrize("view", [1, 2, 3])
+def test_debug_views_match_reference(oracle, golden, view):
+    """First-hit debug views (UV checker, barycentrics, winding order) of the
+    oracle against the reference's own sampleColor with that DebugOptions."""
+    from devilray_gb300 import scenes
+    g = golden("render_debug_pin.npz")
+    spec = scenes.box_room(sphere_level=1)
+    for i, m in enumerate(spec.materials):
+        m["debug"] = (0.9 - 0.1 * i, 0.2 + 0.15 * i, 0.5, 0.0)
+    assert np.array_equal(spec.materials_array(), g["materials"])
+    w, h, spp = int(g["width"]), int(g["height"]), int(g["spp"])
+    cam = scenes.camera(w, h)
+    sc = oracle.RenderScene(spec)
+    acc, casts, rgb = sc.render(cam, spp, rng_mode=1, trig_mode=1, cast_mode=1, tri_table_order=1,
+                                replay=g["replay"], per_sample=True, pixel_sampling=1, debug=view)
+    assert np.array_equal(rgb.view(np.uint32), g[f"rgb_{view}"].view(np.uint32))
+    assert np.array_equal(casts, g[f"casts_{view}"])
+    assert np.array_equal(acc[:, 3], g[f"w_{view}"].sum(0))
+    assert (rgb != 0).any()
+    if view == 1:
+        assert (g["w_1"] == 0).any() and (g["w_1"] == 1).any()   # misses add no sample

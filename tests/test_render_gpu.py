@@ -107,3 +107,33 @@ def test_many_light_render_bit_exact_vs_oracle(native, ctx, oracle, mode):
     assert mism.size == 0, f"{mism.size} pixels differ, e.g. {mism[:3]}: {acc[mism[:3]]} vs {oacc[mism[:3]]}"
     assert np.array_equal(casts, ocasts)
     assert (acc[:, :3] > 0).mean() > 0.08
+
+
+@pytest.mark.parametrize("layout", [2, 8])
+@pytest.mark.parametrize("view,sampling", [(1, 1), (2, 1), (3, 0), (3, 1)])
+def test_debug_views_bit_exact_vs_oracle(native, ctx, oracle, view, sampling, layout):
+    spec = scenes.box_room(sphere_level=2)
+    for i, m in enumerate(spec.materials):
+        m["debug"] = (0.9 - 0.1 * i, 0.2 + 0.15 * i, 0.5, 0.0)
+    cam = scenes.camera(40, 30)
+    scene = native.Scene.from_spec(ctx, spec, layout=layout)
+    npix = 40 * 30
+    accum = torch.zeros((npix, 4), dtype=torch.float32, device="cuda")
+    casts = torch.zeros(npix, dtype=torch.int32, device="cuda")
+    scene.render(cam, accum, casts, spp=3, pixel_sampling=sampling, seed=5, debug=view)
+    scene.render(cam, accum, casts, spp=2, sample_offset=3, pixel_sampling=sampling, seed=5, debug=view)
+    torch.cuda.synchronize()
+    acc = accum.cpu().numpy()
+    oacc, ocasts, _ = oracle_render(oracle, spec, cam, 5, pixel_sampling=sampling, seed=5, debug=view)
+    assert np.array_equal(acc.view(np.uint32), oacc.view(np.uint32))
+    assert np.array_equal(casts.cpu().numpy().astype(np.uint32), ocasts)
+    if view == 1:
+        assert (acc[:, 3] < 5).any() and (acc[:, 3] == 5).any()
+
+
+def test_debug_view_rejects_bad_value(native, ctx):
+    spec = scenes.box_room(sphere_level=1)
+    scene = native.Scene.from_spec(ctx, spec)
+    accum = torch.zeros((16, 4), dtype=torch.float32, device="cuda")
+    with pytest.raises(native.DrError):
+        scene.render(scenes.camera(4, 4), accum, spp=1, debug=7)
