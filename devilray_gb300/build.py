@@ -23,6 +23,9 @@ BUILD = PKG / "_build"
 LIB_DIR = PKG / "lib"
 LIB = LIB_DIR / "libdevilray_gb300.so"
 INCLUDE = ROOT / "include"
+CXX_SRC = PKG / "cxx"
+CXX_LIB = LIB_DIR / "libdevilray_cxx.so"
+CXX_INCLUDE = INCLUDE / "devilray"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -93,7 +96,44 @@ def build(verbose: bool = False, force: bool = False) -> Path:
         if out.returncode != 0:
             raise RuntimeError(f"link failed:\n{' '.join(cmd)}\n{out.stdout}\n{out.stderr}")
         os.replace(tmp, LIB)
+    build_cxx(force=force or bool(jobs))
     return LIB
+
+
+def _cxx() -> str:
+    return os.environ.get("CXX") or shutil.which("g++") or "g++"
+
+
+def build_cxx(force: bool = False) -> Path:
+    """The C++ interface (Renderer, Scene, GpuTris, DistributionSamplers over
+    the C ABI) as ``lib/libdevilray_cxx.so``, linked to the CUDA library."""
+    srcs = sorted(CXX_SRC.glob("*.cpp"))
+    headers = list(CXX_INCLUDE.rglob("*.hpp")) + list(INCLUDE.glob("*.h"))
+    newest = max([p.stat().st_mtime for p in srcs + headers] + [Path(__file__).stat().st_mtime])
+    if not force and CXX_LIB.exists() and CXX_LIB.stat().st_mtime >= newest:
+        return CXX_LIB
+    BUILD.mkdir(exist_ok=True)
+    flags = ["-std=c++20", "-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-I", str(INCLUDE),
+             "-I", str(CXX_INCLUDE)]
+
+    def run(src):
+        obj = BUILD / ("cxx_" + src.name + ".o")
+        cmd = [_cxx(), *flags, "-c", str(src), "-o", str(obj)]
+        out = subprocess.run(cmd, capture_output=True, text=True)
+        if out.returncode != 0:
+            raise RuntimeError(f"compile failed: {src.name}\n{' '.join(cmd)}\n{out.stdout}\n{out.stderr}")
+        return obj
+
+    with ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
+        objs = list(ex.map(run, srcs))
+    tmp = CXX_LIB.with_suffix(".so.tmp")
+    cmd = [_cxx(), "-shared", "-o", str(tmp), *map(str, objs), "-L", str(LIB_DIR), "-ldevilray_gb300",
+           "-Wl,-rpath,$ORIGIN", "-pthread"]
+    out = subprocess.run(cmd, capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError(f"link failed:\n{' '.join(cmd)}\n{out.stdout}\n{out.stderr}")
+    os.replace(tmp, CXX_LIB)
+    return CXX_LIB
 
 
 if __name__ == "__main__":

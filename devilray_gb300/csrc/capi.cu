@@ -285,6 +285,80 @@ dr_status dr_scene_get_info(const dr_scene *s, dr_scene_info *info)
     return DR_OK;
 }
 
+dr_status dr_scene_get_light_table(const dr_scene *s, dr_alias_entry *table_host, uint32_t capacity,
+                                   uint32_t *count)
+{
+    DR_CHECK_ARG(s && count, "dr_scene_get_light_table: NULL argument");
+    *count = s->num_objects;
+    if (!table_host || capacity == 0) return DR_OK;
+    DR_CHECK_ARG(capacity >= s->num_objects, "dr_scene_get_light_table: capacity below the object count");
+    if (s->num_objects == 0 || !s->d_light_table) return DR_OK;
+    DR_CUDA(cudaSetDevice(s->ctx->device));
+    DR_CUDA(cudaMemcpy(table_host, s->d_light_table, (size_t)s->num_objects * sizeof(dr_alias_entry),
+                       cudaMemcpyDeviceToHost));
+    return DR_OK;
+}
+
+dr_status dr_device_allocate(dr_context *ctx, uint64_t bytes, void **dev)
+{
+    DR_CHECK_ARG(ctx && dev, "dr_device_allocate: NULL argument");
+    *dev = nullptr;
+    if (bytes == 0) return DR_OK;
+    DR_CUDA(cudaSetDevice(ctx->device));
+    const cudaError_t e = cudaMalloc(dev, bytes);
+    if (e == cudaErrorMemoryAllocation) {
+        cudaGetLastError();
+        return fail(DR_ERR_OUT_OF_MEMORY, "dr_device_allocate: %llu bytes", (unsigned long long)bytes);
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "dr_device_allocate");
+    return DR_OK;
+}
+
+dr_status dr_device_free(dr_context *ctx, void *dev)
+{
+    DR_CHECK_ARG(ctx != nullptr, "dr_device_free: ctx is NULL");
+    if (!dev) return DR_OK;
+    DR_CUDA(cudaSetDevice(ctx->device));
+    DR_CUDA(cudaFree(dev));
+    return DR_OK;
+}
+
+dr_status dr_device_copy_from_host(dr_context *ctx, void *dev, const void *host, uint64_t bytes)
+{
+    DR_CHECK_ARG(ctx && (bytes == 0 || (dev && host)), "dr_device_copy_from_host: NULL argument");
+    if (bytes == 0) return DR_OK;
+    DR_CUDA(cudaSetDevice(ctx->device));
+    DR_CUDA(cudaMemcpy(dev, host, bytes, cudaMemcpyHostToDevice));
+    return DR_OK;
+}
+
+dr_status dr_device_copy_to_host(dr_context *ctx, void *host, const void *dev, uint64_t bytes)
+{
+    DR_CHECK_ARG(ctx && (bytes == 0 || (dev && host)), "dr_device_copy_to_host: NULL argument");
+    if (bytes == 0) return DR_OK;
+    DR_CUDA(cudaSetDevice(ctx->device));
+    DR_CUDA(cudaMemcpy(host, dev, bytes, cudaMemcpyDeviceToHost));
+    return DR_OK;
+}
+
+dr_status dr_device_zero(dr_context *ctx, void *dev, uint64_t bytes, void *stream)
+{
+    DR_CHECK_ARG(ctx && (bytes == 0 || dev), "dr_device_zero: NULL argument");
+    if (bytes == 0) return DR_OK;
+    DR_CUDA(cudaSetDevice(ctx->device));
+    DR_CUDA(cudaMemsetAsync(dev, 0, bytes, static_cast<cudaStream_t>(stream)));
+    return DR_OK;
+}
+
+dr_status dr_synchronize(dr_context *ctx, void *stream)
+{
+    DR_CHECK_ARG(ctx != nullptr, "dr_synchronize: ctx is NULL");
+    DR_CUDA(cudaSetDevice(ctx->device));
+    if (stream) DR_CUDA(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)));
+    else DR_CUDA(cudaDeviceSynchronize());
+    return check_error_word(ctx, static_cast<cudaStream_t>(stream));
+}
+
 dr_status dr_trace_closest(dr_scene *s, const dr_ray *rays, uint64_t n, dr_hit *hits, int32_t tri_mode,
                            dr_trace_counters *counters, void *stream)
 {

@@ -192,9 +192,8 @@ __global__ void __launch_bounds__(kRenderBlock) k_debug(RenderParams p, int view
     for (uint32_t k = 0; k < spp; ++k) {
         float3 o, d;
         camera_ray(p, pixel, p.sample_base + k, o, d);
-        const float4 ray[2] = {make_float4(o.x, o.y, o.z, __int_as_float(0x7f800000)), make_float4(d.x, d.y, d.z, 0.0f)};
         DevRay r;
-        const bool valid = load_ray(reinterpret_cast<const dr_ray *>(ray), 0, r);
+        const bool valid = make_dev_ray(o, d, __int_as_float(0x7f800000), r);
         float t = r.tmax;
         int32_t prim = INT_MAX;
         TraceStats st;

@@ -30,20 +30,28 @@ __host__ __device__ __forceinline__ float safe_rcp(float x)
     return 1.0f / (fabsf(x) >= 1e-30f ? x : copysignf(1e-30f, x));
 }
 
+// Ray from values (origin, direction, tmax); false for a non-finite origin or
+// direction, or a zero direction.
+__host__ __device__ __forceinline__ bool make_dev_ray(float3 o, float3 v, float tmax, DevRay &r)
+{
+    r.o = o;
+    r.tmax = tmax;
+    r.v = v;
+    r.inv = make_float3(safe_rcp(v.x), safe_rcp(v.y), safe_rcp(v.z));
+    r.ooi = make_float3(o.x * r.inv.x, o.y * r.inv.y, o.z * r.inv.z);
+    using std::isfinite;
+    const bool finite = isfinite(o.x) && isfinite(o.y) && isfinite(o.z) && isfinite(v.x) && isfinite(v.y) &&
+                        isfinite(v.z);
+    const bool nonzero = !(v.x == 0.0f && v.y == 0.0f && v.z == 0.0f);
+    return finite && nonzero;
+}
+
+// Ray i of a GLOBAL-memory dr_ray array (read through the read-only path).
 __host__ __device__ __forceinline__ bool load_ray(const dr_ray *rays, uint64_t i, DevRay &r)
 {
     const float4 *p = reinterpret_cast<const float4 *>(rays) + 2 * i;
     const float4 a = DR_LDG(p), b = DR_LDG(p + 1);
-    r.o = make_float3(a.x, a.y, a.z);
-    r.tmax = a.w;
-    r.v = make_float3(b.x, b.y, b.z);
-    r.inv = make_float3(safe_rcp(b.x), safe_rcp(b.y), safe_rcp(b.z));
-    r.ooi = make_float3(r.o.x * r.inv.x, r.o.y * r.inv.y, r.o.z * r.inv.z);
-    using std::isfinite;
-    const bool finite = isfinite(a.x) && isfinite(a.y) && isfinite(a.z) && isfinite(b.x) &&
-                        isfinite(b.y) && isfinite(b.z);
-    const bool nonzero = !(b.x == 0.0f && b.y == 0.0f && b.z == 0.0f);
-    return finite && nonzero;
+    return make_dev_ray(make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z), a.w, r);
 }
 
 // Slab test of both children of a two-box node against [0, tmax]. Boxes are

@@ -117,6 +117,13 @@ SIGNATURES = {
     "dr_trace_closest_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_int32, C.c_void_p]),
     "dr_render": (C.c_int, [C.c_void_p, C.POINTER(Camera), C.POINTER(RenderConfig), C.c_void_p, C.c_void_p,
                             C.c_void_p]),
+    "dr_synchronize": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "dr_device_allocate": (C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(C.c_void_p)]),
+    "dr_device_free": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "dr_device_copy_from_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64]),
+    "dr_device_copy_to_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64]),
+    "dr_device_zero": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]),
+    "dr_scene_get_light_table": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(C.c_uint32)]),
     "dr_framebuffer_create": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
     "dr_framebuffer_destroy": (C.c_int, [C.c_void_p]),
     "dr_framebuffer_clear": (C.c_int, [C.c_void_p, C.c_void_p]),

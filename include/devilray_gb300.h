@@ -88,8 +88,27 @@ dr_status dr_context_create(const dr_context_config *cfg, dr_context **out);
 dr_status dr_context_destroy(dr_context *ctx);
 /* Reads and clears the device error word of the context (see dr_status). */
 dr_status dr_context_check(dr_context *ctx);
+/* Waits for `stream` (NULL: the whole device), then dr_context_check. */
+dr_status dr_synchronize(dr_context *ctx, void *stream);
+
+/* Device buffers for callers without a CUDA runtime of their own: the
+ * allocate / free / copyFromHost / copyToHost of DeviceMemoryManager
+ * (src/device/DeviceMemory.cu:11-60). Copies are synchronous; dr_device_zero is
+ * asynchronous on `stream`. */
+dr_status dr_device_allocate(dr_context *ctx, uint64_t bytes, void **dev);
+dr_status dr_device_free(dr_context *ctx, void *dev);
+dr_status dr_device_copy_from_host(dr_context *ctx, void *dev, const void *host, uint64_t bytes);
+dr_status dr_device_copy_to_host(dr_context *ctx, void *host, const void *dev, uint64_t bytes);
+dr_status dr_device_zero(dr_context *ctx, void *dev, uint64_t bytes, void *stream);
 
 /* ---- materials and scene --------------------------------------------------------- */
+
+/* AliasEntry of include/tracing/DistributionSamplers.hpp:44-51, 20 bytes. */
+typedef struct dr_alias_entry {
+    float p_A, pdf_A, pdf_B;
+    int32_t A, B;
+} dr_alias_entry;
+
 
 /* Flat POD material, replacing the std::variant<TransparentMaterial, DiffuseMaterial>
  * of include/tracing/Material.hpp:9-32. 64 bytes. */
@@ -158,6 +177,12 @@ typedef struct dr_scene_info {
     double build_seconds;
 } dr_scene_info;
 dr_status dr_scene_get_info(const dr_scene *scene, dr_scene_info *info);
+/* The scene's object light table (Renderer::m_light_sampler, built as
+ * Renderer::calculateLightWeights does, src/Renderer.cpp:113-152): *count =
+ * number of objects; the table is copied when table_host is not NULL
+ * (capacity >= count). Synchronous. */
+dr_status dr_scene_get_light_table(const dr_scene *scene, dr_alias_entry *table_host, uint32_t capacity,
+                                   uint32_t *count);
 
 /* ---- traversal ------------------------------------------------------------------- */
 
@@ -252,12 +277,6 @@ dr_status dr_tonemap(const float *accum_dev, int32_t width, int32_t height, int3
                      uint32_t *rgba_dev, void *stream);
 
 /* ---- alias tables ------------------------------------------------------------------- */
-
-/* AliasEntry of include/tracing/DistributionSamplers.hpp:44-51, 20 bytes. */
-typedef struct dr_alias_entry {
-    float p_A, pdf_A, pdf_B;
-    int32_t A, B;
-} dr_alias_entry;
 
 typedef enum dr_alias_mode {
     /* The pairing of generateAliasTable (src/DistributionSamplers.cpp:39-149):
