@@ -1,6 +1,7 @@
 // capi.cu -- the C ABI entry points: context, scene and traversal.
 
 #include "dr_internal.h"
+#include "render_internal.h"
 #include "trace_kernels.cuh"
 #include "alias_kernels.cuh"
 
@@ -258,13 +259,7 @@ dr_status dr_scene_destroy(dr_scene *s)
     cudaFree(s->d_shade);
     cudaFree(s->d_light_table);
     cudaFree(s->d_tri_tables);
-    for (int k = 0; k < dr_scene::kWaveStreams; ++k) {
-        cudaFree(s->d_wave[k]);
-        if (s->wave_stream[k]) cudaStreamDestroy(s->wave_stream[k]);
-    }
-    for (int k = 0; k <= dr_scene::kWaveStreams; ++k)
-        if (s->wave_event[k]) cudaEventDestroy(s->wave_event[k]);
-    cudaFree(s->d_samples);
+    delete s->runner;
     cudaFree(s->d_stage_rays);
     cudaFree(s->d_stage_hits);
     delete s;

@@ -28,6 +28,12 @@ dr_status cuda_fail(cudaError_t e, const char *what);
         if (!(cond)) return ::dr::fail(DR_ERR_INVALID_ARGUMENT, "%s", msg);   \
     } while (0)
 
+// DR_CHECK_ARG with a printf-style message.
+#define DR_CHECK_ARGF(cond, ...)                                             \
+    do {                                                                     \
+        if (!(cond)) return ::dr::fail(DR_ERR_INVALID_ARGUMENT, __VA_ARGS__); \
+    } while (0)
+
 // Device error word bits (dr_context::d_error), set by kernels instead of
 // trapping; the host maps them to dr_status.
 enum : uint32_t {
@@ -55,6 +61,7 @@ constexpr int kLeafCountBits = 4;
 constexpr uint32_t kMaxLeafSize = (1u << kLeafCountBits) - 1;  // 15
 constexpr uint32_t kMaxTriangles = 1u << (31 - kLeafCountBits); // 2^27
 constexpr int kStackSize = 64;                                  // traversal stack entries
+constexpr uint32_t kNoRoot = 0xffffffffu;                       // root of an empty hierarchy
 constexpr int kMaxBuildDepth = 60;                              // < kStackSize
 
 inline int32_t leaf_link(uint32_t first, uint32_t count) { return ~int32_t((first << kLeafCountBits) | count); }
@@ -146,6 +153,10 @@ namespace dr {
 dr_status build_render_data(dr_scene *s, const dr_scene_desc *d);
 }  // namespace dr
 
+namespace dr {
+struct WaveRunner;
+}
+
 struct dr_scene {
     dr_context *ctx = nullptr;
     uint32_t num_tris = 0;
@@ -172,15 +183,8 @@ struct dr_scene {
     float total_radiant_power = 0.0f;
     bool lights = false;                  // some object emits
 
-    // wavefront buffers of dr_render (one set per concurrent wave stream) and
-    // the per-sample colours of a call, grown on demand
-    static constexpr int kWaveStreams = 3;
-    void *d_wave[kWaveStreams] = {};
-    size_t wave_bytes[kWaveStreams] = {};
-    cudaStream_t wave_stream[kWaveStreams] = {};
-    cudaEvent_t wave_event[kWaveStreams + 1] = {};
-    void *d_samples = nullptr;
-    size_t samples_bytes = 0;
+    // wavefront state of dr_render, created on first use
+    dr::WaveRunner *runner = nullptr;
 
     // staging for the host-buffer entry points
     void *d_stage_rays = nullptr;

@@ -18,21 +18,29 @@ constexpr uint32_t kPersistentChunk = 128;
 
 // Indices a warp reserves at once: 128 when there is plenty of work, down to
 // one per lane when few rays are left, so a small launch still spreads over
-// many warps (warp-uniform).
-__device__ __forceinline__ uint32_t persistent_chunk(uint64_t n)
+// many warps (warp-uniform). A nonzero `fixed` (a multiple of 32) overrides it.
+__device__ __forceinline__ uint32_t persistent_chunk(uint64_t n, uint32_t fixed = 0)
 {
+    if (fixed) return fixed;
     const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x / 32);
     const uint64_t per = n / (warps ? warps : 1);
     uint32_t c = per >= kPersistentChunk ? kPersistentChunk : (uint32_t)((per + 31) & ~31ull);
     return c < 32 ? 32 : c;
 }
 
-// Ray source of the public entry points: ray i of a contiguous array.
+// Ray source of the public entry points: ray i of a contiguous array, all rays
+// in one hierarchy. A source's load() gives the ray and the root node of the
+// hierarchy it is traced in (kNoRoot: nothing to traverse, the ray misses).
 struct DirectSource {
     const dr_ray *rays;
     dr_hit *hits;
     uint8_t *occluded;
-    __device__ __forceinline__ bool load(uint64_t i, DevRay &r) const { return load_ray(rays, i, r); }
+    uint32_t root;
+    __device__ __forceinline__ bool load(uint64_t i, DevRay &r, uint32_t &node) const
+    {
+        node = root;
+        return load_ray(rays, i, r);
+    }
     __device__ __forceinline__ void closest(uint64_t i, float t, int32_t prim) const
     {
         reinterpret_cast<float2 *>(hits)[i] =
@@ -46,7 +54,7 @@ template <int MODE, bool ANY, bool COUNT, class Source>
 __device__ __forceinline__ void persistent_wide(const Wide8Args &a, const Source &src, uint64_t n,
                                                 unsigned long long *counter, unsigned long long &nn,
                                                 unsigned long long &nb, unsigned long long &nt,
-                                                unsigned long long &nhits)
+                                                unsigned long long &nhits, uint32_t fixed_chunk = 0)
 {
     constexpr unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
@@ -56,7 +64,7 @@ __device__ __forceinline__ void persistent_wide(const Wide8Args &a, const Source
     uint64_t idx = 0;
     bool active = false, exhausted = false;
     uint64_t chunk_next = 0, chunk_end = 0;  // warp-uniform
-    const uint32_t chunk = persistent_chunk(n);
+    const uint32_t chunk = persistent_chunk(n, fixed_chunk);
     unsigned long long cn = 0, cb = 0, ct = 0, ch = 0;
     while (true) {
         unsigned want = __ballot_sync(FULL, !active);
@@ -78,9 +86,9 @@ __device__ __forceinline__ void persistent_wide(const Wide8Args &a, const Source
             if (take) {
                 idx = chunk_next + (uint64_t)__popc(want & lower);
                 DevRay r;
-                // an empty scene (no nodes) has nothing to traverse: every ray misses
-                if (src.load(idx, r) && a.num_nodes != 0) {
-                    wide_init<MODE>(s, r);
+                uint32_t root;
+                if (src.load(idx, r, root) && root != kNoRoot) {
+                    wide_init<MODE>(s, r, root);
                     active = true;
                 } else if (ANY) {
                     src.any(idx, false);

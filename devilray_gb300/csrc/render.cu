@@ -14,8 +14,13 @@
 // of ptmath.cuh. Uniforms: Philox4x32-10 with counter (pixel, sample, group,
 // tag) and key = seed; camera dims 0,1; bounce b: 4 + 12 b + {0,1 sphere,
 // 2 Fresnel, 3..8 light sample}.
+//
+// The same kernels serve one image (dr_render) and a batch of images of many
+// scenes (dr_batch): every slot carries its job (image), pixel and sample, and
+// the job names the hierarchy root, light tables and camera it uses.
 
 #include "dr_internal.h"
+#include "render_internal.h"
 #include "alias_kernels.cuh"
 #include "ptmath.cuh"
 #include "trace_device.cuh"
@@ -28,7 +33,6 @@ namespace {
 
 constexpr float kPi = 3.14159274f;
 constexpr uint32_t kStreamTag = 0x44526E67u;
-constexpr int kMaxDepth = 63;
 constexpr int kRenderBlock = 128;
 
 struct RenderParams {
@@ -38,28 +42,23 @@ struct RenderParams {
     const dr_material *materials;
     const dr_alias_entry *light_table;
     const dr_alias_entry *tri_tables;
-    uint32_t num_objects;
-    float total_power;
-    int lights;
-    // camera
-    float m[12];
-    float focal, cx, cy, psx, psy;
-    int width, height, pixel_sampling;
-    // wave
-    uint32_t npix, wave, sample_base, spp_wave, max_depth;
-    uint32_t seed_lo, seed_hi;
+    const RenderJob *jobs;
+    const WaveSegment *segs;   // this wave's segments
+    uint32_t nsegs;
+    uint32_t wave;             // slots of this wave
+    uint32_t wave_pix;         // accumulation threads of this wave
+    uint32_t chunk;            // persistent fetch size, 0 = adaptive
     // per-slot buffers
-    float4 *rays;      // dr_ray, 2 x float4
+    float4 *rays;              // dr_ray, 2 x float4
     float2 *hits;
     float4 *thr, *color, *prev_p, *prev_n, *pending, *shadow_rays;
     int4 *stack;
     uint32_t *casts;
+    uint32_t *slot_job, *slot_pix, *slot_sample;
     uint32_t *list[2];
     uint32_t *shadow_list;
-    uint32_t *counts;  // [0, 64): active paths per bounce, [64, 128): shadow rays per bounce
+    uint32_t *counts;          // [0, 64): active paths per bounce, [64, 128): shadow rays per bounce
     unsigned long long *work;  // persistent-kernel counters: [b] closest hit, [64 + b] shadow rays
-    float4 *accum;
-    uint32_t *pix_casts;
 };
 
 struct F3 {
@@ -106,21 +105,15 @@ __device__ __forceinline__ float cosine_pdf(F3 cur, F3 next, F3 n)
     return c > 0 ? c / kPi : 0.0f;
 }
 
-__device__ __forceinline__ void uniforms4(const RenderParams &p, uint32_t pixel, uint32_t sample, uint32_t group,
+__device__ __forceinline__ void uniforms4(const RenderJob &J, uint32_t pixel, uint32_t sample, uint32_t group,
                                           float u[4])
 {
     uint32_t o[4];
-    pt::philox4x32_10(pixel, sample, group, kStreamTag, p.seed_lo, p.seed_hi, o);
+    pt::philox4x32_10(pixel, sample, group, kStreamTag, J.seed_lo, J.seed_hi, o);
     u[0] = pt::u01(o[0]);
     u[1] = pt::u01(o[1]);
     u[2] = pt::u01(o[2]);
     u[3] = pt::u01(o[3]);
-}
-
-__device__ __forceinline__ void slot_pixel(const RenderParams &p, uint32_t slot, uint32_t &pixel, uint32_t &sample)
-{
-    pixel = slot % p.npix;
-    sample = p.sample_base + slot / p.npix;
 }
 
 // Appends `slot` to a list with one atomic per warp. Every lane of the warp
@@ -138,23 +131,38 @@ __device__ __forceinline__ void warp_append(bool keep, uint32_t slot, uint32_t *
 }
 
 // cameraRay (include/tracing/CameraRay.hpp:6-34) for sample `sample` of `pixel`.
-__device__ __forceinline__ void camera_ray(const RenderParams &p, uint32_t pixel, uint32_t sample, float3 &o, float3 &d)
+__device__ __forceinline__ void camera_ray(const RenderJob &J, uint32_t pixel, uint32_t sample, float3 &o, float3 &d)
 {
-    const int px = (int)(pixel % (uint32_t)p.width), py = (int)(pixel / (uint32_t)p.width);
+    const int px = (int)(pixel % (uint32_t)J.width), py = (int)(pixel / (uint32_t)J.width);
     float subx = 0.5f, suby = 0.5f;
-    if (p.pixel_sampling == DR_PIXEL_UNIFORM_RANDOM) {
+    if (J.pixel_sampling == DR_PIXEL_UNIFORM_RANDOM) {
         float u[4];
-        uniforms4(p, pixel, sample, 0, u);
+        uniforms4(J, pixel, sample, 0, u);
         subx = u[0];
         suby = u[1];
     }
     const float pcx = (float)px + subx, pcy = (float)py + suby;
-    const float physx = pcx * p.psx - p.cx, physy = pcy * p.psy - p.cy;
-    const float dx = physx / p.focal, dy = physy / p.focal;
+    const float physx = pcx * J.psx - J.cx, physy = pcy * J.psy - J.cy;
+    const float dx = physx / J.focal, dy = physy / J.focal;
     const F3 v = normalized(f3(dx, dy, 1.0f));
-    o = make_float3(p.m[3], p.m[7], p.m[11]);
-    d = make_float3(p.m[0] * v.x + p.m[1] * v.y + p.m[2] * v.z, p.m[4] * v.x + p.m[5] * v.y + p.m[6] * v.z,
-                    p.m[8] * v.x + p.m[9] * v.y + p.m[10] * v.z);
+    o = make_float3(J.m[3], J.m[7], J.m[11]);
+    d = make_float3(J.m[0] * v.x + J.m[1] * v.y + J.m[2] * v.z, J.m[4] * v.x + J.m[5] * v.y + J.m[6] * v.z,
+                    J.m[8] * v.x + J.m[9] * v.y + J.m[10] * v.z);
+}
+
+// Segment of the wave holding `key` in the field selected by FIELD (0: slots,
+// 1: accumulation threads); segments are in increasing order of both.
+template <int FIELD>
+__device__ __forceinline__ uint32_t find_segment(const WaveSegment *segs, uint32_t nsegs, uint32_t key)
+{
+    uint32_t lo = 0, hi = nsegs;  // first segment with begin > key, minus one
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        const uint32_t begin = FIELD == 0 ? segs[mid].slot_begin : segs[mid].pix_begin;
+        if (begin <= key) lo = mid;
+        else hi = mid;
+    }
+    return lo;
 }
 
 __global__ void __launch_bounds__(kRenderBlock) k_camera(RenderParams p)
@@ -162,10 +170,13 @@ __global__ void __launch_bounds__(kRenderBlock) k_camera(RenderParams p)
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0) p.counts[0] = p.wave;
     if (i >= p.wave) return;
-    uint32_t pixel, sample;
-    slot_pixel(p, i, pixel, sample);
+    const WaveSegment sg = p.segs[find_segment<0>(p.segs, p.nsegs, i)];
+    const RenderJob &J = p.jobs[sg.job];
+    const uint32_t local = i - sg.slot_begin;
+    const uint32_t pixel = local % sg.npix;
+    const uint32_t sample = J.sample_offset + sg.sample_rel + local / sg.npix;
     float3 o, d;
-    camera_ray(p, pixel, sample, o, d);
+    camera_ray(J, pixel, sample, o, d);
     p.rays[2 * i] = make_float4(o.x, o.y, o.z, __int_as_float(0x7f800000));
     p.rays[2 * i + 1] = make_float4(d.x, d.y, d.z, 0.0f);
     p.thr[i] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
@@ -173,6 +184,9 @@ __global__ void __launch_bounds__(kRenderBlock) k_camera(RenderParams p)
     p.prev_p[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);  // w = 0: no diffuse vertex before
     p.stack[i] = make_int4(0, 0, 0, 0);                 // w = size
     p.casts[i] = 0;
+    p.slot_job[i] = sg.job;
+    p.slot_pix[i] = pixel;
+    p.slot_sample[i] = sample;
     p.list[0][i] = i;
 }
 
@@ -183,21 +197,21 @@ __global__ void __launch_bounds__(kRenderBlock) k_camera(RenderParams p)
 // checker pattern is its dark colour 0.5 everywhere; the UV view adds a sample
 // (w + 1) only where the camera ray hits.
 template <int MODE, int LAYOUT>
-__global__ void __launch_bounds__(kRenderBlock) k_debug(RenderParams p, int view, uint32_t spp)
+__global__ void __launch_bounds__(kRenderBlock) k_debug(SceneArrays p, RenderJob J, int view)
 {
     const uint32_t pixel = blockIdx.x * blockDim.x + threadIdx.x;
-    if (pixel >= p.npix) return;
-    float4 acc = p.accum[pixel];
+    if (pixel >= J.npix) return;
+    float4 acc = J.accum[pixel];
     uint32_t casts = 0;
-    for (uint32_t k = 0; k < spp; ++k) {
+    for (uint32_t k = 0; k < J.spp; ++k) {
         float3 o, d;
-        camera_ray(p, pixel, p.sample_base + k, o, d);
+        camera_ray(J, pixel, J.sample_offset + k, o, d);
         DevRay r;
         const bool valid = make_dev_ray(o, d, __int_as_float(0x7f800000), r);
         float t = r.tmax;
         int32_t prim = INT_MAX;
         TraceStats st;
-        if (valid) scene_closest<MODE, false, LAYOUT>(p.trace, r, t, prim, st);
+        if (valid) scene_closest<MODE, false, LAYOUT>(p.trace, r, J.root, t, prim, st);
         ++casts;
         float4 color = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         bool counted = true;
@@ -233,18 +247,23 @@ __global__ void __launch_bounds__(kRenderBlock) k_debug(RenderParams p, int view
             acc = add4(acc, color);
         }
     }
-    p.accum[pixel] = acc;
-    if (p.pix_casts) p.pix_casts[pixel] += casts;
+    J.accum[pixel] = acc;
+    if (J.pix_casts) J.pix_casts[pixel] += casts;
 }
 
-// Ray sources of the persistent wide kernels: list entry i names a path slot.
+// Ray sources of the persistent wide kernels: list entry i names a path slot,
+// whose job names the hierarchy root.
 struct PathSource {
     const uint32_t *list;
     const float4 *rays;
     float2 *hits;
-    __device__ __forceinline__ bool load(uint64_t i, DevRay &r) const
+    const uint32_t *slot_job;
+    const RenderJob *jobs;
+    __device__ __forceinline__ bool load(uint64_t i, DevRay &r, uint32_t &root) const
     {
-        return load_ray(reinterpret_cast<const dr_ray *>(rays), list[i], r);
+        const uint32_t slot = list[i];
+        root = jobs[slot_job[slot]].root;
+        return load_ray(reinterpret_cast<const dr_ray *>(rays), slot, r);
     }
     __device__ __forceinline__ void closest(uint64_t i, float t, int32_t prim) const
     {
@@ -259,9 +278,13 @@ struct ShadowSource {
     const float4 *rays;
     float4 *color;
     const float4 *pending;
-    __device__ __forceinline__ bool load(uint64_t i, DevRay &r) const
+    const uint32_t *slot_job;
+    const RenderJob *jobs;
+    __device__ __forceinline__ bool load(uint64_t i, DevRay &r, uint32_t &root) const
     {
-        return load_ray(reinterpret_cast<const dr_ray *>(rays), list[i], r);
+        const uint32_t slot = list[i];
+        root = jobs[slot_job[slot]].root;
+        return load_ray(reinterpret_cast<const dr_ray *>(rays), slot, r);
     }
     __device__ __forceinline__ void closest(uint64_t, float, int32_t) const {}
     __device__ __forceinline__ void any(uint64_t i, bool occluded) const
@@ -278,21 +301,21 @@ template <int MODE>
 __global__ void __launch_bounds__(kTraceBlock) k_wave_closest_p8(RenderParams p, int b)
 {
     const Wide8Args w{p.trace.nodes8, p.trace.tri_ref, p.trace.tri_wt, p.trace.prim, p.trace.num_nodes, p.trace.error};
-    const PathSource src{p.list[b & 1], p.rays, p.hits};
+    const PathSource src{p.list[b & 1], p.rays, p.hits, p.slot_job, p.jobs};
     unsigned long long nn = 0, nb = 0, nt = 0, nh = 0;
-    persistent_wide<MODE, false, false>(w, src, p.counts[b], p.work + b, nn, nb, nt, nh);
+    persistent_wide<MODE, false, false>(w, src, p.counts[b], p.work + b, nn, nb, nt, nh, p.chunk);
 }
 
 template <int MODE>
 __global__ void __launch_bounds__(kTraceBlock) k_wave_shadow_p8(RenderParams p, int b)
 {
     const Wide8Args w{p.trace.nodes8, p.trace.tri_ref, p.trace.tri_wt, p.trace.prim, p.trace.num_nodes, p.trace.error};
-    const ShadowSource src{p.shadow_list, p.shadow_rays, p.color, p.pending};
+    const ShadowSource src{p.shadow_list, p.shadow_rays, p.color, p.pending, p.slot_job, p.jobs};
     unsigned long long nn = 0, nb = 0, nt = 0, nh = 0;
-    persistent_wide<MODE, true, false>(w, src, p.counts[64 + b], p.work + 64 + b, nn, nb, nt, nh);
+    persistent_wide<MODE, true, false>(w, src, p.counts[64 + b], p.work + 64 + b, nn, nb, nt, nh, p.chunk);
 }
 
-// Closest hit of the surviving paths of bounce b.
+// Closest hit of the surviving paths of bounce b (binary hierarchy).
 template <int MODE, int LAYOUT>
 __global__ void __launch_bounds__(kTraceBlock) k_wave_closest(RenderParams p, int b)
 {
@@ -305,7 +328,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_wave_closest(RenderParams p, in
         float t = r.tmax;
         int32_t prim = INT_MAX;
         TraceStats st;
-        if (valid) scene_closest<MODE, false, LAYOUT>(p.trace, r, t, prim, st);
+        if (valid) scene_closest<MODE, false, LAYOUT>(p.trace, r, p.jobs[p.slot_job[slot]].root, t, prim, st);
         p.hits[slot] = prim != INT_MAX ? make_float2(t, __int_as_float(prim))
                                        : make_float2(__int_as_float(0x7f800000), __int_as_float(-1));
     }
@@ -322,7 +345,6 @@ __global__ void __launch_bounds__(kRenderBlock) k_shade(RenderParams p, int b)
     const uint32_t count = p.counts[b];
     const uint32_t *list = p.list[b & 1];
     uint32_t *next_list = p.list[(b + 1) & 1];
-    const bool last = b + 1 >= (int)p.max_depth;
     // warp-uniform loop so that every lane reaches the ballots
     const uint32_t warp_first = (blockIdx.x * blockDim.x + (threadIdx.x & ~31u));
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -333,6 +355,7 @@ __global__ void __launch_bounds__(kRenderBlock) k_shade(RenderParams p, int b)
         if (i < count) {
             slot = list[i];
             p.casts[slot] += 1;
+            const RenderJob &J = p.jobs[p.slot_job[slot]];
             const float2 h = p.hits[slot];
             const int prim = __float_as_int(h.y);
             if (prim >= 0) {
@@ -353,11 +376,10 @@ __global__ void __launch_bounds__(kRenderBlock) k_shade(RenderParams p, int b)
                 float4 thr = p.thr[slot];
                 float4 col = p.color[slot];
                 const float4 pp4 = p.prev_p[slot];
-                uint32_t pixel, sample;
-                slot_pixel(p, slot, pixel, sample);
+                const uint32_t pixel = p.slot_pix[slot], sample = p.slot_sample[slot];
                 float u[12];
                 const uint32_t g = 1u + 3u * (uint32_t)b;
-                uniforms4(p, pixel, sample, g, u);
+                uniforms4(J, pixel, sample, g, u);
                 F3 normal = n;
                 F3 new_o, new_v;
                 if (M.kind == DR_MAT_DIFFUSE) {
@@ -372,20 +394,20 @@ __global__ void __launch_bounds__(kRenderBlock) k_shade(RenderParams p, int b)
                         const F3 pp = f3(pp4.x, pp4.y, pp4.z), pn = f3(pn4.x, pn4.y, pn4.z);
                         const float pdf_bsdf = cosine_pdf(pp, hp, pn);
                         const float L = luminance(mul4s(E, kPi));
-                        const float pdf_area = L / p.total_power;
+                        const float pdf_area = L / J.total_power;
                         const float pdf_nee = pdf_area * area_to_solid_angle(pp, hp, n);
                         if (pdf_bsdf + pdf_nee > 0)
                             col = add4(col, mul4s(mul4(E, thr), power_heuristic(pdf_bsdf, pdf_nee)));
                     }
                     // next-event estimation: samplePointOnLights (:234-272) and
                     // evaluateDirectLighting (:336-361); visibility is the shadow ray
-                    if (p.lights) {
-                        uniforms4(p, pixel, sample, g + 1, u + 4);
-                        uniforms4(p, pixel, sample, g + 2, u + 8);
+                    if (J.lights) {
+                        uniforms4(J, pixel, sample, g + 1, u + 4);
+                        uniforms4(J, pixel, sample, g + 2, u + 8);
                         int32_t oi, ti;
                         float opdf, tpdf;
-                        alias_sample(p.light_table, p.num_objects, u[3], u[4], oi, opdf);
-                        const dr_object ob = p.objects[oi];
+                        alias_sample(p.light_table + J.obj_base, J.num_objects, u[3], u[4], oi, opdf);
+                        const dr_object ob = p.objects[J.obj_base + oi];
                         alias_sample(p.tri_tables + ob.tri_begin, ob.tri_count, u[5], u[6], ti, tpdf);
                         const int lt = (int)ob.tri_begin + ti;
                         const float4 l0 = __ldg(p.shade + 3 * lt), l1 = __ldg(p.shade + 3 * lt + 1),
@@ -491,7 +513,7 @@ __global__ void __launch_bounds__(kRenderBlock) k_shade(RenderParams p, int b)
                 p.rays[2 * slot + 1] = make_float4(new_v.x, new_v.y, new_v.z, 0.0f);
                 p.thr[slot] = thr;
                 p.color[slot] = col;
-                keep = !last;
+                keep = b + 1 < (int)J.max_depth;
             }
         }
         warp_append(keep, slot, next_list, p.counts + b + 1);
@@ -508,43 +530,31 @@ __global__ void __launch_bounds__(kTraceBlock) k_wave_shadow(RenderParams p, int
         const uint32_t slot = p.shadow_list[i];
         DevRay r;
         const bool valid = load_ray(reinterpret_cast<const dr_ray *>(p.shadow_rays), slot, r);
-        const bool occluded = valid && scene_any<MODE, LAYOUT>(p.trace, r);
+        const bool occluded = valid && scene_any<MODE, LAYOUT>(p.trace, r, p.jobs[p.slot_job[slot]].root);
         if (!occluded) p.color[slot] = add4(p.color[slot], p.pending[slot]);
     }
 }
 
-// Copies the finished wave into the per-sample buffers of the call:
-// sample_color[sample - first][pixel], sample_casts[...].
-__global__ void __launch_bounds__(256) k_store_wave(RenderParams p, float4 *sample_color, uint32_t *sample_casts,
-                                                    uint32_t first_sample)
+// Buffers::color update of the reference (pixel.w++; pixel = pixel + color) for
+// the wave's samples: one thread per (segment, pixel) adds the segment's samples
+// in sample order. Waves run this pass one after another.
+__global__ void __launch_bounds__(256) k_accumulate_wave(RenderParams p)
 {
-    const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
-    if (slot >= p.wave) return;
-    uint32_t pixel, sample;
-    slot_pixel(p, slot, pixel, sample);
-    const size_t o = (size_t)(sample - first_sample) * p.npix + pixel;
-    sample_color[o] = p.color[slot];
-    sample_casts[o] = p.casts[slot];
-}
-
-// Buffers::color update of the reference (pixel.w++; pixel = pixel + color),
-// the samples of a pixel added in sample order.
-__global__ void __launch_bounds__(256) k_accumulate_samples(float4 *accum, uint32_t *pix_casts,
-                                                            const float4 *sample_color, const uint32_t *sample_casts,
-                                                            uint32_t npix, uint32_t nsamples)
-{
-    const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
-    if (pix >= npix) return;
-    float4 acc = accum[pix];
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= p.wave_pix) return;
+    const WaveSegment sg = p.segs[find_segment<1>(p.segs, p.nsegs, t)];
+    const RenderJob &J = p.jobs[sg.job];
+    const uint32_t pix = t - sg.pix_begin;
+    float4 acc = J.accum[pix];
     uint32_t casts = 0;
-    for (uint32_t s = 0; s < nsamples; ++s) {
-        const size_t o = (size_t)s * npix + pix;
+    for (uint32_t s = 0; s < sg.nsamples; ++s) {
+        const uint32_t slot = sg.slot_begin + s * sg.npix + pix;
         acc.w = acc.w + 1.0f;
-        acc = add4(acc, sample_color[o]);
-        casts += sample_casts[o];
+        acc = add4(acc, p.color[slot]);
+        casts += p.casts[slot];
     }
-    accum[pix] = acc;
-    if (pix_casts) pix_casts[pix] += casts;
+    J.accum[pix] = acc;
+    if (J.pix_casts) J.pix_casts[pix] += casts;
 }
 
 template <typename T>
@@ -555,52 +565,256 @@ T *carve(char *&ptr, size_t count)
     return out;
 }
 
-size_t wave_bytes(uint32_t W)
+constexpr size_t kSlotBytes = 2 * 16 + 8 + 16 * 5 + 2 * 16 + 16 + 4 * 7;
+
+size_t wave_buffer_bytes(uint32_t W)
 {
-    return (size_t)W * 200 + 128 * sizeof(uint32_t) + 128 * sizeof(unsigned long long) + 18 * 256;
+    return (size_t)W * kSlotBytes + 128 * sizeof(uint32_t) + 128 * sizeof(unsigned long long) + 20 * 256;
 }
 
-// Scene, camera and output fields of the render parameters.
-RenderParams base_params(const dr_scene *s, const dr_camera *cam, const dr_render_config *cfg, float *accum_dev,
-                         uint32_t *casts_dev, uint32_t npix)
+RenderParams wave_params(const SceneArrays &sc, const RenderJob *d_jobs, void *buffer, uint32_t W, uint32_t chunk)
 {
     RenderParams p{};
-    p.trace.nodes = s->d_nodes;
-    p.trace.nodes8 = s->d_nodes8;
-    p.trace.layout = (int)s->layout;
-    p.trace.tri_ref = s->d_tri_ref;
-    p.trace.tri_wt = s->d_tri_wt;
-    p.trace.prim = s->d_prim;
-    p.trace.num_nodes = s->num_nodes;
-    p.trace.error = s->ctx->d_error;
-    p.shade = s->d_shade;
-    p.objects = s->d_objects;
-    p.materials = s->d_materials;
-    p.light_table = s->d_light_table;
-    p.tri_tables = s->d_tri_tables;
-    p.num_objects = s->num_objects;
-    p.total_power = s->total_radiant_power;
-    p.lights = s->lights ? 1 : 0;
-    for (int r = 0; r < 3; ++r)
-        for (int c = 0; c < 4; ++c) p.m[r * 4 + c] = cam->transform[r * 4 + c];
-    p.focal = cam->focal_length;
-    p.cx = cam->center[0];
-    p.cy = cam->center[1];
-    p.psx = cam->pixel_size[0];
-    p.psy = cam->pixel_size[1];
-    p.width = cam->width;
-    p.height = cam->height;
-    p.pixel_sampling = cfg->pixel_sampling;
-    p.npix = npix;
-    p.max_depth = cfg->max_depth;
-    p.seed_lo = (uint32_t)cfg->seed;
-    p.seed_hi = (uint32_t)(cfg->seed >> 32);
-    p.accum = reinterpret_cast<float4 *>(accum_dev);
-    p.pix_casts = casts_dev;
+    p.trace = sc.trace;
+    p.shade = sc.shade;
+    p.objects = sc.objects;
+    p.materials = sc.materials;
+    p.light_table = sc.light_table;
+    p.tri_tables = sc.tri_tables;
+    p.jobs = d_jobs;
+    p.chunk = chunk;
+    char *ptr = static_cast<char *>(buffer);
+    p.rays = carve<float4>(ptr, (size_t)W * 2);
+    p.hits = carve<float2>(ptr, W);
+    p.thr = carve<float4>(ptr, W);
+    p.color = carve<float4>(ptr, W);
+    p.prev_p = carve<float4>(ptr, W);
+    p.prev_n = carve<float4>(ptr, W);
+    p.pending = carve<float4>(ptr, W);
+    p.shadow_rays = carve<float4>(ptr, (size_t)W * 2);
+    p.stack = carve<int4>(ptr, W);
+    p.casts = carve<uint32_t>(ptr, W);
+    p.slot_job = carve<uint32_t>(ptr, W);
+    p.slot_pix = carve<uint32_t>(ptr, W);
+    p.slot_sample = carve<uint32_t>(ptr, W);
+    p.list[0] = carve<uint32_t>(ptr, W);
+    p.list[1] = carve<uint32_t>(ptr, W);
+    p.shadow_list = carve<uint32_t>(ptr, W);
+    p.counts = carve<uint32_t>(ptr, 128);
+    p.work = carve<unsigned long long>(ptr, 128);
     return p;
 }
 
 }  // namespace
+
+WavePlan plan_waves(const std::vector<RenderJob> &jobs, uint32_t wave_paths)
+{
+    WavePlan plan;
+    uint32_t W = std::max<uint32_t>(wave_paths, 1);
+    for (const RenderJob &j : jobs) {
+        if (j.spp) W = std::max(W, j.npix);
+        plan.max_depth = std::max(plan.max_depth, j.spp ? j.max_depth : 0u);
+    }
+    uint32_t used = 0, pix = 0;
+    plan.wave_first.push_back(0);
+    auto close_wave = [&] {
+        if (used == 0) return;
+        plan.wave_first.push_back((uint32_t)plan.segs.size());
+        plan.wave_slots.push_back(used);
+        plan.wave_pix.push_back(pix);
+        plan.max_slots = std::max(plan.max_slots, used);
+        used = 0;
+        pix = 0;
+    };
+    for (uint32_t j = 0; j < jobs.size(); ++j) {
+        const RenderJob &J = jobs[j];
+        uint32_t s = 0;
+        while (s < J.spp) {
+            uint32_t fit = (W - used) / J.npix;
+            if (fit == 0) {
+                close_wave();
+                fit = W / J.npix;
+            }
+            const uint32_t k = std::min(fit, J.spp - s);
+            plan.segs.push_back(WaveSegment{j, used, pix, J.npix, s, k});
+            used += k * J.npix;
+            pix += J.npix;
+            s += k;
+        }
+    }
+    close_wave();
+    return plan;
+}
+
+WaveRunner::~WaveRunner()
+{
+    for (int k = 0; k < kMaxWaveStreams; ++k) {
+        cudaFree(d_wave[k]);
+        if (stream[k]) cudaStreamDestroy(stream[k]);
+        if (acc_done[k]) cudaEventDestroy(acc_done[k]);
+    }
+    if (fork) cudaEventDestroy(fork);
+    cudaFree(d_jobs);
+    cudaFree(d_segs);
+}
+
+dr_status WaveRunner::prepare(const std::vector<RenderJob> &jobs, const WavePlan &plan, const WaveConfig &cfg,
+                              cudaStream_t st)
+{
+    const uint32_t nwaves = (uint32_t)plan.wave_slots.size();
+    const int K = (int)std::max<uint32_t>(1, std::min<uint32_t>({cfg.streams, (uint32_t)kMaxWaveStreams, nwaves}));
+    const size_t need = wave_buffer_bytes(plan.max_slots);
+    bool grow = jobs.size() > jobs_capacity || plan.segs.size() > segs_capacity;
+    for (int k = 0; k < K; ++k) grow = grow || wave_bytes[k] < need;
+    if (grow) {
+        // buffers may still be in use by earlier work on any stream
+        DR_CUDA(cudaDeviceSynchronize());
+        for (int k = 0; k < K; ++k)
+            if (wave_bytes[k] < need) {
+                cudaFree(d_wave[k]);
+                d_wave[k] = nullptr;
+                wave_bytes[k] = 0;
+                DR_CUDA(cudaMalloc(&d_wave[k], need));
+                wave_bytes[k] = need;
+            }
+        if (jobs.size() > jobs_capacity) {
+            cudaFree(d_jobs);
+            d_jobs = nullptr;
+            jobs_capacity = 0;
+            DR_CUDA(cudaMalloc(&d_jobs, jobs.size() * sizeof(RenderJob)));
+            jobs_capacity = jobs.size();
+        }
+        if (plan.segs.size() > segs_capacity) {
+            cudaFree(d_segs);
+            d_segs = nullptr;
+            segs_capacity = 0;
+            DR_CUDA(cudaMalloc(&d_segs, plan.segs.size() * sizeof(WaveSegment)));
+            segs_capacity = plan.segs.size();
+        }
+    }
+    for (int k = 0; k < K; ++k) {
+        if (!stream[k]) DR_CUDA(cudaStreamCreateWithFlags(&stream[k], cudaStreamNonBlocking));
+        if (!acc_done[k]) DR_CUDA(cudaEventCreateWithFlags(&acc_done[k], cudaEventDisableTiming));
+    }
+    if (!fork) DR_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+    // the tables may still be read by the waves of an earlier call
+    for (int k = 0; k < kMaxWaveStreams; ++k)
+        if (acc_done[k]) DR_CUDA(cudaStreamWaitEvent(st, acc_done[k], 0));
+    // pageable copies are staged before the call returns
+    DR_CUDA(cudaMemcpyAsync(d_jobs, jobs.data(), jobs.size() * sizeof(RenderJob), cudaMemcpyHostToDevice, st));
+    DR_CUDA(cudaMemcpyAsync(d_segs, plan.segs.data(), plan.segs.size() * sizeof(WaveSegment), cudaMemcpyHostToDevice,
+                            st));
+    return DR_OK;
+}
+
+dr_status WaveRunner::enqueue(const SceneArrays &sc, const WavePlan &plan, const WaveConfig &cfg, int tri_mode,
+                              cudaStream_t st)
+{
+    const uint32_t nwaves = (uint32_t)plan.wave_slots.size();
+    if (nwaves == 0) return DR_OK;
+    const int K = (int)std::max<uint32_t>(1, std::min<uint32_t>({cfg.streams, (uint32_t)kMaxWaveStreams, nwaves}));
+    const int sms = ctx->num_sms;
+    static int p8_per_sm = 0;
+    if (p8_per_sm == 0) {
+        int b = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_wave_closest_p8<0>, kTraceBlock, 0) != cudaSuccess || b <= 0)
+            b = 4;
+        p8_per_sm = b;
+    }
+    const bool wt = tri_mode == DR_TRI_WATERTIGHT, wide = sc.trace.layout == 8;
+    DR_CUDA(cudaEventRecord(fork, st));
+    for (int k = 0; k < K; ++k) DR_CUDA(cudaStreamWaitEvent(stream[k], fork, 0));
+    for (uint32_t w = 0; w < nwaves; ++w) {
+        const int k = (int)(w % (uint32_t)K);
+        cudaStream_t ws = stream[k];
+        RenderParams q = wave_params(sc, d_jobs, d_wave[k], plan.max_slots, cfg.chunk);
+        q.segs = d_segs + plan.wave_first[w];
+        q.nsegs = plan.wave_first[w + 1] - plan.wave_first[w];
+        q.wave = plan.wave_slots[w];
+        q.wave_pix = plan.wave_pix[w];
+        const uint32_t W = q.wave;
+        const unsigned trace_grid = (unsigned)std::min<uint64_t>((W + kTraceBlock - 1) / kTraceBlock, (uint64_t)sms * 16);
+        const unsigned shade_grid = (unsigned)std::min<uint64_t>((W + kRenderBlock - 1) / kRenderBlock, (uint64_t)sms * 16);
+        const unsigned pgrid = (unsigned)std::min<uint64_t>((W + kTraceBlock - 1) / kTraceBlock, (uint64_t)sms * p8_per_sm);
+        DR_CUDA(cudaMemsetAsync(q.counts, 0, 128 * sizeof(uint32_t), ws));
+        DR_CUDA(cudaMemsetAsync(q.work, 0, 128 * sizeof(unsigned long long), ws));
+        k_camera<<<(W + kRenderBlock - 1) / kRenderBlock, kRenderBlock, 0, ws>>>(q);
+        for (int b = 0; b < (int)plan.max_depth; ++b) {
+            if (wide) {
+                if (wt) k_wave_closest_p8<1><<<pgrid, kTraceBlock, 0, ws>>>(q, b);
+                else k_wave_closest_p8<0><<<pgrid, kTraceBlock, 0, ws>>>(q, b);
+            } else {
+                if (wt) k_wave_closest<1, 2><<<trace_grid, kTraceBlock, 0, ws>>>(q, b);
+                else k_wave_closest<0, 2><<<trace_grid, kTraceBlock, 0, ws>>>(q, b);
+            }
+            k_shade<<<shade_grid, kRenderBlock, 0, ws>>>(q, b);
+            if (wide) {
+                if (wt) k_wave_shadow_p8<1><<<pgrid, kTraceBlock, 0, ws>>>(q, b);
+                else k_wave_shadow_p8<0><<<pgrid, kTraceBlock, 0, ws>>>(q, b);
+            } else {
+                if (wt) k_wave_shadow<1, 2><<<trace_grid, kTraceBlock, 0, ws>>>(q, b);
+                else k_wave_shadow<0, 2><<<trace_grid, kTraceBlock, 0, ws>>>(q, b);
+            }
+        }
+        // images receive the waves in order
+        if (w > 0) DR_CUDA(cudaStreamWaitEvent(ws, acc_done[(w - 1) % (uint32_t)K], 0));
+        k_accumulate_wave<<<(q.wave_pix + 255) / 256, 256, 0, ws>>>(q);
+        DR_CUDA(cudaGetLastError());
+        DR_CUDA(cudaEventRecord(acc_done[k], ws));
+    }
+    for (int k = 0; k < K; ++k) DR_CUDA(cudaStreamWaitEvent(st, acc_done[k], 0));
+    return DR_OK;
+}
+
+SceneArrays scene_arrays(const dr_scene *s)
+{
+    SceneArrays a{};
+    a.trace.nodes = s->d_nodes;
+    a.trace.nodes8 = s->d_nodes8;
+    a.trace.layout = (int)s->layout;
+    a.trace.tri_ref = s->d_tri_ref;
+    a.trace.tri_wt = s->d_tri_wt;
+    a.trace.prim = s->d_prim;
+    a.trace.num_nodes = s->num_nodes;
+    a.trace.error = s->ctx->d_error;
+    a.shade = s->d_shade;
+    a.objects = s->d_objects;
+    a.materials = s->d_materials;
+    a.light_table = s->d_light_table;
+    a.tri_tables = s->d_tri_tables;
+    return a;
+}
+
+RenderJob make_job(const dr_scene *s, const dr_camera *cam, const dr_render_config *cfg, float *accum,
+                   uint32_t *casts)
+{
+    RenderJob J{};
+    J.accum = reinterpret_cast<float4 *>(accum);
+    J.pix_casts = casts;
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 4; ++c) J.m[r * 4 + c] = cam->transform[r * 4 + c];
+    J.focal = cam->focal_length;
+    J.cx = cam->center[0];
+    J.cy = cam->center[1];
+    J.psx = cam->pixel_size[0];
+    J.psy = cam->pixel_size[1];
+    J.width = cam->width;
+    J.height = cam->height;
+    J.pixel_sampling = cfg->pixel_sampling;
+    J.npix = (uint32_t)((uint64_t)cam->width * (uint64_t)cam->height);
+    J.root = scene_root(s->num_nodes);
+    J.obj_base = 0;
+    J.num_objects = s->num_objects;
+    J.total_power = s->total_radiant_power;
+    J.lights = s->lights ? 1 : 0;
+    J.seed_lo = (uint32_t)cfg->seed;
+    J.seed_hi = (uint32_t)(cfg->seed >> 32);
+    J.sample_offset = cfg->sample_offset;
+    J.max_depth = cfg->max_depth;
+    J.spp = cfg->spp;
+    return J;
+}
+
 }  // namespace dr
 
 using namespace dr;
@@ -610,7 +824,8 @@ extern "C" dr_status dr_render(dr_scene *s, const dr_camera *cam, const dr_rende
 {
     DR_CHECK_ARG(s && cam && cfg && accum_dev, "dr_render: NULL argument");
     DR_CHECK_ARG(cam->width > 0 && cam->height > 0, "dr_render: empty image");
-    DR_CHECK_ARG(cfg->max_depth >= 1 && cfg->max_depth <= (uint32_t)kMaxDepth, "dr_render: max_depth must be in [1, 63]");
+    DR_CHECK_ARG(cfg->max_depth >= 1 && cfg->max_depth <= (uint32_t)kMaxRenderDepth,
+                 "dr_render: max_depth must be in [1, 63]");
     DR_CHECK_ARG(cfg->tri_mode == DR_TRI_REFERENCE || cfg->tri_mode == DR_TRI_WATERTIGHT, "dr_render: bad tri_mode");
     DR_CHECK_ARG((reinterpret_cast<uintptr_t>(accum_dev) & 15) == 0, "dr_render: accum must be 16-byte aligned");
     DR_CHECK_ARG(cfg->debug >= DR_DEBUG_OFF && cfg->debug <= DR_DEBUG_WINDING_ORDER, "dr_render: bad debug view");
@@ -618,142 +833,34 @@ extern "C" dr_status dr_render(dr_scene *s, const dr_camera *cam, const dr_rende
     DR_CUDA(cudaSetDevice(s->ctx->device));
     auto st = static_cast<cudaStream_t>(stream);
     const uint64_t npix64 = (uint64_t)cam->width * (uint64_t)cam->height;
-    DR_CHECK_ARG(npix64 < (1ull << 31), "dr_render: image too large");
-    const uint32_t npix = (uint32_t)npix64;
+    DR_CHECK_ARG(npix64 < (1ull << 31) / 16, "dr_render: image too large");
+    const RenderJob job = make_job(s, cam, cfg, accum_dev, casts_dev);
+    const SceneArrays sc = scene_arrays(s);
     if (cfg->debug != DR_DEBUG_OFF) {
-        RenderParams p = base_params(s, cam, cfg, accum_dev, casts_dev, npix);
-        p.sample_base = cfg->sample_offset;
-        const unsigned grid = (npix + kRenderBlock - 1) / kRenderBlock;
+        const unsigned grid = (job.npix + kRenderBlock - 1) / kRenderBlock;
         const bool wt = cfg->tri_mode == DR_TRI_WATERTIGHT;
         if (s->layout == 8) {
-            if (wt) k_debug<1, 8><<<grid, kRenderBlock, 0, st>>>(p, cfg->debug, cfg->spp);
-            else k_debug<0, 8><<<grid, kRenderBlock, 0, st>>>(p, cfg->debug, cfg->spp);
+            if (wt) k_debug<1, 8><<<grid, kRenderBlock, 0, st>>>(sc, job, cfg->debug);
+            else k_debug<0, 8><<<grid, kRenderBlock, 0, st>>>(sc, job, cfg->debug);
         } else {
-            if (wt) k_debug<1, 2><<<grid, kRenderBlock, 0, st>>>(p, cfg->debug, cfg->spp);
-            else k_debug<0, 2><<<grid, kRenderBlock, 0, st>>>(p, cfg->debug, cfg->spp);
+            if (wt) k_debug<1, 2><<<grid, kRenderBlock, 0, st>>>(sc, job, cfg->debug);
+            else k_debug<0, 2><<<grid, kRenderBlock, 0, st>>>(sc, job, cfg->debug);
         }
         DR_CUDA(cudaGetLastError());
         return DR_OK;
     }
-    const uint32_t target = cfg->wave_paths ? cfg->wave_paths : (1u << 21);
-    const uint32_t spp_wave = std::max<uint32_t>(1, std::min<uint32_t>(cfg->spp, target / npix));
-    const uint32_t W = npix * spp_wave;
-    const uint32_t nwaves_total = (cfg->spp + spp_wave - 1) / spp_wave;
-    const int K = (int)std::min<uint32_t>(dr_scene::kWaveStreams, nwaves_total);
-    const size_t need = wave_bytes(W);
-    // samples held at once: whole waves, at most ~2 GiB of per-sample colours
-    const uint64_t per_sample = (uint64_t)npix * (sizeof(float4) + sizeof(uint32_t));
-    uint32_t chunk_spp = (uint32_t)std::max<uint64_t>(spp_wave, std::min<uint64_t>(cfg->spp, (2ull << 30) / per_sample));
-    chunk_spp = std::max<uint32_t>(spp_wave, chunk_spp / spp_wave * spp_wave);
-    const size_t samples_need = (size_t)std::min(chunk_spp, cfg->spp) * per_sample + 512;
-    bool grow = s->samples_bytes < samples_need;
-    for (int k = 0; k < K; ++k) grow = grow || s->wave_bytes[k] < need;
-    if (grow) {
-        DR_CUDA(cudaDeviceSynchronize());
-        for (int k = 0; k < K; ++k)
-            if (s->wave_bytes[k] < need) {
-                cudaFree(s->d_wave[k]);
-                s->d_wave[k] = nullptr;
-                s->wave_bytes[k] = 0;
-                DR_CUDA(cudaMalloc(&s->d_wave[k], need));
-                s->wave_bytes[k] = need;
-            }
-        if (s->samples_bytes < samples_need) {
-            cudaFree(s->d_samples);
-            s->d_samples = nullptr;
-            s->samples_bytes = 0;
-            DR_CUDA(cudaMalloc(&s->d_samples, samples_need));
-            s->samples_bytes = samples_need;
-        }
+    WaveConfig wc;
+    if (cfg->wave_paths) wc.wave_paths = cfg->wave_paths;
+    if (cfg->streams) wc.streams = cfg->streams;
+    wc.chunk = cfg->chunk;
+    const std::vector<RenderJob> jobs{job};
+    const WavePlan plan = plan_waves(jobs, wc.wave_paths);
+    if (!s->runner) {
+        s->runner = new (std::nothrow) WaveRunner;
+        if (!s->runner) return fail(DR_ERR_OUT_OF_MEMORY, "dr_render: host allocation failed");
+        s->runner->ctx = s->ctx;
     }
-    for (int k = 0; k < K; ++k)
-        if (!s->wave_stream[k]) DR_CUDA(cudaStreamCreateWithFlags(&s->wave_stream[k], cudaStreamNonBlocking));
-    for (int k = 0; k <= K; ++k)
-        if (!s->wave_event[k]) DR_CUDA(cudaEventCreateWithFlags(&s->wave_event[k], cudaEventDisableTiming));
-    const RenderParams p = base_params(s, cam, cfg, accum_dev, casts_dev, npix);
-    RenderParams ps[dr_scene::kWaveStreams];
-    for (int k = 0; k < K; ++k) {
-        ps[k] = p;
-        char *ptr = static_cast<char *>(s->d_wave[k]);
-        ps[k].rays = carve<float4>(ptr, (size_t)W * 2);
-        ps[k].hits = carve<float2>(ptr, W);
-        ps[k].thr = carve<float4>(ptr, W);
-        ps[k].color = carve<float4>(ptr, W);
-        ps[k].prev_p = carve<float4>(ptr, W);
-        ps[k].prev_n = carve<float4>(ptr, W);
-        ps[k].pending = carve<float4>(ptr, W);
-        ps[k].shadow_rays = carve<float4>(ptr, (size_t)W * 2);
-        ps[k].stack = carve<int4>(ptr, W);
-        ps[k].casts = carve<uint32_t>(ptr, W);
-        ps[k].list[0] = carve<uint32_t>(ptr, W);
-        ps[k].list[1] = carve<uint32_t>(ptr, W);
-        ps[k].shadow_list = carve<uint32_t>(ptr, W);
-        ps[k].counts = carve<uint32_t>(ptr, 128);
-        ps[k].work = carve<unsigned long long>(ptr, 128);
-    }
-    char *sp = static_cast<char *>(s->d_samples);
-    float4 *sample_color = carve<float4>(sp, (size_t)std::min(chunk_spp, cfg->spp) * npix);
-    uint32_t *sample_casts = carve<uint32_t>(sp, (size_t)std::min(chunk_spp, cfg->spp) * npix);
-
-    const int sms = s->ctx->num_sms;
-    const unsigned trace_grid = (unsigned)std::min<uint64_t>((W + kTraceBlock - 1) / kTraceBlock, (uint64_t)sms * 16);
-    const unsigned shade_grid = (unsigned)std::min<uint64_t>((W + kRenderBlock - 1) / kRenderBlock, (uint64_t)sms * 16);
-    // persistent wide kernels: one resident set of blocks
-    static int p8_per_sm = 0;
-    if (p8_per_sm == 0) {
-        int b = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_wave_closest_p8<0>, kTraceBlock, 0) != cudaSuccess || b <= 0)
-            b = 4;
-        p8_per_sm = b;
-    }
-    const unsigned pgrid = (unsigned)std::min<uint64_t>((W + kTraceBlock - 1) / kTraceBlock, (uint64_t)sms * p8_per_sm);
-    // Waves run on K streams so that the short, latency-bound late bounces of
-    // one wave overlap the full early bounces of the next; each wave writes its
-    // samples' colours, and one ordered pass per chunk adds them to the image.
-    const bool wt = cfg->tri_mode == DR_TRI_WATERTIGHT, wide = s->layout == 8;
-    for (uint32_t chunk0 = 0; chunk0 < cfg->spp; chunk0 += chunk_spp) {
-        const uint32_t chunk_n = std::min(chunk_spp, cfg->spp - chunk0);
-        DR_CUDA(cudaEventRecord(s->wave_event[K], st));
-        for (int k = 0; k < K; ++k) DR_CUDA(cudaStreamWaitEvent(s->wave_stream[k], s->wave_event[K], 0));
-        int wave_index = 0;
-        for (uint32_t done = 0; done < chunk_n; done += spp_wave, ++wave_index) {
-            const int k = wave_index % K;
-            cudaStream_t ws = s->wave_stream[k];
-            RenderParams &q = ps[k];
-            q.spp_wave = std::min(spp_wave, chunk_n - done);
-            q.wave = npix * q.spp_wave;
-            q.sample_base = cfg->sample_offset + chunk0 + done;
-            DR_CUDA(cudaMemsetAsync(q.counts, 0, 128 * sizeof(uint32_t), ws));
-            DR_CUDA(cudaMemsetAsync(q.work, 0, 128 * sizeof(unsigned long long), ws));
-            k_camera<<<(q.wave + kRenderBlock - 1) / kRenderBlock, kRenderBlock, 0, ws>>>(q);
-            for (int b = 0; b < (int)cfg->max_depth; ++b) {
-                if (wide) {
-                    if (wt) k_wave_closest_p8<1><<<pgrid, kTraceBlock, 0, ws>>>(q, b);
-                    else k_wave_closest_p8<0><<<pgrid, kTraceBlock, 0, ws>>>(q, b);
-                } else {
-                    if (wt) k_wave_closest<1, 2><<<trace_grid, kTraceBlock, 0, ws>>>(q, b);
-                    else k_wave_closest<0, 2><<<trace_grid, kTraceBlock, 0, ws>>>(q, b);
-                }
-                k_shade<<<shade_grid, kRenderBlock, 0, ws>>>(q, b);
-                if (wide) {
-                    if (wt) k_wave_shadow_p8<1><<<pgrid, kTraceBlock, 0, ws>>>(q, b);
-                    else k_wave_shadow_p8<0><<<pgrid, kTraceBlock, 0, ws>>>(q, b);
-                } else {
-                    if (wt) k_wave_shadow<1, 2><<<trace_grid, kTraceBlock, 0, ws>>>(q, b);
-                    else k_wave_shadow<0, 2><<<trace_grid, kTraceBlock, 0, ws>>>(q, b);
-                }
-            }
-            k_store_wave<<<(q.wave + 255) / 256, 256, 0, ws>>>(q, sample_color, sample_casts,
-                                                             cfg->sample_offset + chunk0);
-            DR_CUDA(cudaGetLastError());
-        }
-        for (int k = 0; k < K; ++k) {
-            DR_CUDA(cudaEventRecord(s->wave_event[k], s->wave_stream[k]));
-            DR_CUDA(cudaStreamWaitEvent(st, s->wave_event[k], 0));
-        }
-        k_accumulate_samples<<<(npix + 255) / 256, 256, 0, st>>>(p.accum, p.pix_casts, sample_color, sample_casts, npix,
-                                                                 chunk_n);
-        DR_CUDA(cudaGetLastError());
-    }
-    return DR_OK;
+    dr_status r = s->runner->prepare(jobs, plan, wc, st);
+    if (r != DR_OK) return r;
+    return s->runner->enqueue(sc, plan, wc, cfg->tri_mode, st);
 }

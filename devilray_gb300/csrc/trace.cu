@@ -45,7 +45,7 @@ k_trace_closest(TraceArgs a)
         const bool valid = load_ray(a.rays, i, r);
         float best_t = r.tmax;
         int32_t best_prim = INT_MAX;
-        if (valid) scene_closest<MODE, COUNT, LAYOUT>(a, r, best_t, best_prim, st);
+        if (valid) scene_closest<MODE, COUNT, LAYOUT>(a, r, scene_root(a.num_nodes), best_t, best_prim, st);
         float2 out;
         if (best_prim != INT_MAX) {
             out = make_float2(best_t, __int_as_float(best_prim));
@@ -66,7 +66,7 @@ k_trace_any(TraceArgs a)
     if (i >= a.n) return;
     DevRay r;
     const bool valid = load_ray(a.rays, i, r);
-    a.occluded[i] = (valid && scene_any<MODE, LAYOUT>(a, r)) ? 1 : 0;
+    a.occluded[i] = (valid && scene_any<MODE, LAYOUT>(a, r, scene_root(a.num_nodes))) ? 1 : 0;
 }
 
 // Persistent kernels for the compressed 8-wide layout.
@@ -74,7 +74,7 @@ template <int MODE, bool COUNT>
 __global__ void __launch_bounds__(kTraceBlock) k_trace_closest_p8(TraceArgs a)
 {
     const Wide8Args w{a.nodes8, a.tri_ref, a.tri_wt, a.prim, a.num_nodes, a.error};
-    const DirectSource src{a.rays, a.hits, nullptr};
+    const DirectSource src{a.rays, a.hits, nullptr, scene_root(a.num_nodes)};
     unsigned long long nn = 0, nb = 0, nt = 0, nh = 0;
     persistent_wide<MODE, false, COUNT>(w, src, a.n, a.work, nn, nb, nt, nh);
     if (COUNT) add_counters(a.counters, nn, nb, nt, nh);
@@ -84,7 +84,7 @@ template <int MODE>
 __global__ void __launch_bounds__(kTraceBlock) k_trace_any_p8(TraceArgs a)
 {
     const Wide8Args w{a.nodes8, a.tri_ref, a.tri_wt, a.prim, a.num_nodes, a.error};
-    const DirectSource src{a.rays, nullptr, a.occluded};
+    const DirectSource src{a.rays, nullptr, a.occluded, scene_root(a.num_nodes)};
     unsigned long long nn = 0, nb = 0, nt = 0, nh = 0;
     persistent_wide<MODE, true, false>(w, src, a.n, a.work, nn, nb, nt, nh);
 }

@@ -20,17 +20,17 @@ struct TraceStats {
 };
 
 template <int MODE, bool COUNT>
-__device__ __forceinline__ void closest_hit(const TraceArgs &a, const DevRay &r, float &best_t, int32_t &best_prim,
-                                            TraceStats &st)
+__device__ __forceinline__ void closest_hit(const TraceArgs &a, const DevRay &r, uint32_t root, float &best_t,
+                                            int32_t &best_prim, TraceStats &st)
 {
     best_t = r.tmax;
     best_prim = INT_MAX;
-    if (a.num_nodes == 0) return;
+    if (root == kNoRoot) return;
     WtSetup w;
     if (MODE == 1) w = wt_setup(r.v);
     int32_t stack[kStackSize];
     int sp = 0;
-    int32_t cur = 0;
+    int32_t cur = (int32_t)root;
     while (true) {
         if (cur >= 0) {
             const float4 *np = reinterpret_cast<const float4 *>(a.nodes + cur);
@@ -83,14 +83,14 @@ __device__ __forceinline__ void closest_hit(const TraceArgs &a, const DevRay &r,
 
 // Any hit with t <= tmax.
 template <int MODE>
-__device__ __forceinline__ bool any_hit(const TraceArgs &a, const DevRay &r)
+__device__ __forceinline__ bool any_hit(const TraceArgs &a, const DevRay &r, uint32_t root)
 {
-    if (a.num_nodes == 0) return false;
+    if (root == kNoRoot) return false;
     WtSetup w;
     if (MODE == 1) w = wt_setup(r.v);
     int32_t stack[kStackSize];
     int sp = 0;
-    int32_t cur = 0;
+    int32_t cur = (int32_t)root;
     const float tmax = r.tmax;
     while (true) {
         if (cur >= 0) {
@@ -133,28 +133,31 @@ __device__ __forceinline__ bool any_hit(const TraceArgs &a, const DevRay &r)
 
 // Closest / any hit in the scene's layout.
 template <int MODE, bool COUNT, int LAYOUT>
-__device__ __forceinline__ void scene_closest(const TraceArgs &a, const DevRay &r, float &best_t, int32_t &best_prim,
-                                              TraceStats &st)
+__device__ __forceinline__ void scene_closest(const TraceArgs &a, const DevRay &r, uint32_t root, float &best_t,
+                                              int32_t &best_prim, TraceStats &st)
 {
     if (LAYOUT == 8) {
         const Wide8Args w{a.nodes8, a.tri_ref, a.tri_wt, a.prim, a.num_nodes, a.error};
-        if (COUNT) wide_traverse<MODE, false>(w, r, best_t, best_prim, &st.nodes, &st.boxes, &st.tris);
-        else wide_traverse<MODE, false>(w, r, best_t, best_prim, nullptr, nullptr, nullptr);
+        if (COUNT) wide_traverse<MODE, false>(w, r, root, best_t, best_prim, &st.nodes, &st.boxes, &st.tris);
+        else wide_traverse<MODE, false>(w, r, root, best_t, best_prim, nullptr, nullptr, nullptr);
     } else {
-        closest_hit<MODE, COUNT>(a, r, best_t, best_prim, st);
+        closest_hit<MODE, COUNT>(a, r, root, best_t, best_prim, st);
     }
 }
 
 template <int MODE, int LAYOUT>
-__device__ __forceinline__ bool scene_any(const TraceArgs &a, const DevRay &r)
+__device__ __forceinline__ bool scene_any(const TraceArgs &a, const DevRay &r, uint32_t root)
 {
     if (LAYOUT == 8) {
         const Wide8Args w{a.nodes8, a.tri_ref, a.tri_wt, a.prim, a.num_nodes, a.error};
         float t;
         int32_t prim;
-        return wide_traverse<MODE, true>(w, r, t, prim, nullptr, nullptr, nullptr);
+        return wide_traverse<MODE, true>(w, r, root, t, prim, nullptr, nullptr, nullptr);
     }
-    return any_hit<MODE>(a, r);
+    return any_hit<MODE>(a, r, root);
 }
+
+// Root of a single-scene hierarchy.
+__host__ __device__ __forceinline__ uint32_t scene_root(uint32_t num_nodes) { return num_nodes ? 0u : kNoRoot; }
 
 }  // namespace dr

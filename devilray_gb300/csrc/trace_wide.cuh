@@ -145,14 +145,14 @@ struct WideState {
 };
 
 template <int MODE>
-__host__ __device__ __forceinline__ void wide_init(WideState &s, const DevRay &r)
+__host__ __device__ __forceinline__ void wide_init(WideState &s, const DevRay &r, uint32_t root)
 {
     s.r = r;
     if (MODE == 1) s.w = wt_setup(r.v);
     s.oct = ray_octant(r);
     s.best_t = r.tmax;
     s.best_prim = INT_MAX;
-    s.node = 0;
+    s.node = root;
     s.group = make_uint2(0, 0);
     s.sp = 0;
     s.have_node = true;
@@ -221,20 +221,21 @@ __host__ __device__ __forceinline__ bool wide_step(const Wide8Args &a, WideState
 
 // Node group on the stack: x = child_base, y = (internal hit mask << 8) | imask.
 template <int MODE, bool ANY>
-__host__ __device__ __forceinline__ bool wide_traverse(const Wide8Args &a, const DevRay &r, float &best_t,
-                                                       int32_t &best_prim, unsigned long long *nodes_out,
-                                                       unsigned long long *boxes_out, unsigned long long *tris_out)
+__host__ __device__ __forceinline__ bool wide_traverse(const Wide8Args &a, const DevRay &r, uint32_t root,
+                                                       float &best_t, int32_t &best_prim,
+                                                       unsigned long long *nodes_out, unsigned long long *boxes_out,
+                                                       unsigned long long *tris_out)
 {
     best_t = r.tmax;
     best_prim = INT_MAX;
-    if (a.num_nodes == 0) return false;
+    if (root == kNoRoot) return false;
     WtSetup w;
     if (MODE == 1) w = wt_setup(r.v);
     const uint32_t oct = ray_octant(r);
     uint2 stack[kWideStack];
     int sp = 0;
     // the root is visited directly
-    uint32_t node = 0;
+    uint32_t node = root;
     bool have_node = true;
     uint2 group = make_uint2(0, 0);
     unsigned long long nn = 0, nb = 0, nt = 0;

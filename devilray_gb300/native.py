@@ -81,7 +81,24 @@ class Camera(C.Structure):
 class RenderConfig(C.Structure):
     _fields_ = [("max_depth", C.c_uint32), ("spp", C.c_uint32), ("sample_offset", C.c_uint32),
                 ("pixel_sampling", C.c_int32), ("seed", C.c_uint64), ("tri_mode", C.c_int32),
-                ("wave_paths", C.c_uint32), ("flags", C.c_uint32), ("debug", C.c_int32)]
+                ("wave_paths", C.c_uint32), ("flags", C.c_uint32), ("debug", C.c_int32),
+                ("streams", C.c_uint32), ("chunk", C.c_uint32)]
+
+
+class Job(C.Structure):
+    _fields_ = [("scene", C.c_void_p), ("camera", Camera), ("config", RenderConfig), ("accum_dev", C.c_void_p),
+                ("casts_dev", C.c_void_p)]
+
+
+class BatchConfig(C.Structure):
+    _fields_ = [("wave_paths", C.c_uint32), ("streams", C.c_uint32), ("chunk", C.c_uint32),
+                ("use_graph", C.c_uint32)]
+
+
+class BatchInfo(C.Structure):
+    _fields_ = [("num_jobs", C.c_uint32), ("num_waves", C.c_uint32), ("max_wave_paths", C.c_uint32),
+                ("layout", C.c_uint32), ("graph_nodes", C.c_uint64), ("paths_per_render", C.c_uint64),
+                ("device_bytes", C.c_uint64), ("streams", C.c_uint32), ("chunk", C.c_uint32)]
 
 
 def make_camera(cam: dict) -> Camera:
@@ -131,6 +148,11 @@ SIGNATURES = {
     "dr_framebuffer_read": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_uint64)]),
     "dr_framebuffer_tonemap": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
     "dr_tonemap": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
+    "dr_batch_create": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.POINTER(C.c_void_p)]),
+    "dr_batch_render": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "dr_batch_get_info": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "dr_batch_destroy": (C.c_int, [C.c_void_p]),
+    "dr_render_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
     "dr_alias_build_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_int32]),
     "dr_alias_build": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_int32, C.c_void_p]),
     "dr_alias_build_noalloc": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
@@ -304,9 +326,10 @@ class Scene:
     # -- rendering --
     def render(self, cam: dict, accum_dev, casts_dev=None, spp: int = 1, max_depth: int = 10,
                sample_offset: int = 0, pixel_sampling: int = 1, seed: int = 0, tri_mode: int = DR_TRI_REFERENCE,
-               wave_paths: int = 0, debug: int = 0, stream=None):
+               wave_paths: int = 0, debug: int = 0, streams: int = 0, chunk: int = 0, stream=None):
         c = make_camera(cam)
-        cfg = RenderConfig(max_depth, spp, sample_offset, pixel_sampling, seed, tri_mode, wave_paths, 0, debug)
+        cfg = RenderConfig(max_depth, spp, sample_offset, pixel_sampling, seed, tri_mode, wave_paths, 0, debug,
+                           streams, chunk)
         check(load().dr_render(self.handle, C.byref(c), C.byref(cfg), _ptr(accum_dev), _ptr(casts_dev),
                                _stream_ptr(stream)))
 
@@ -364,6 +387,60 @@ class Framebuffer:
         out = np.zeros(self.width * self.height, np.uint32)
         check(load().dr_framebuffer_tonemap(self.handle, 1 if gamma else 0, _ptr(out)))
         return out
+
+
+def make_job(scene: "Scene", cam: dict, accum_dev, casts_dev=None, spp: int = 1, max_depth: int = 10,
+             sample_offset: int = 0, pixel_sampling: int = 1, seed: int = 0,
+             tri_mode: int = DR_TRI_REFERENCE) -> Job:
+    j = Job()
+    j.scene = scene.handle.value if isinstance(scene.handle, C.c_void_p) else scene.handle
+    j.camera = make_camera(cam)
+    j.config = RenderConfig(max_depth, spp, sample_offset, pixel_sampling, seed, tri_mode, 0, 0, 0, 0, 0)
+    j.accum_dev = _ptr(accum_dev)
+    j.casts_dev = _ptr(casts_dev) if casts_dev is not None else None
+    return j
+
+
+class Batch:
+    """Many images of many scenes rendered as one schedule (dr_batch)."""
+
+    def __init__(self, ctx: "Context", jobs: list, wave_paths: int = 0, streams: int = 0, chunk: int = 0,
+                 use_graph: bool = True):
+        self.ctx = ctx
+        self._jobs = (Job * len(jobs))(*jobs)
+        cfg = BatchConfig(wave_paths, streams, chunk, 1 if use_graph else 0)
+        h = C.c_void_p()
+        check(load().dr_batch_create(ctx.handle, self._jobs, len(jobs), C.byref(cfg), C.byref(h)))
+        self.handle = h.value
+
+    def render(self, sample_offsets=None, stream=None) -> None:
+        offs = None
+        if sample_offsets is not None:
+            offs = (C.c_uint32 * len(sample_offsets))(*[int(x) for x in sample_offsets])
+        check(load().dr_batch_render(self.handle, offs, _stream_ptr(stream)))
+
+    def info(self) -> BatchInfo:
+        i = BatchInfo()
+        check(load().dr_batch_get_info(self.handle, C.byref(i)))
+        return i
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            load().dr_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def render_batch(ctx: "Context", jobs: list, wave_paths: int = 0, streams: int = 0, chunk: int = 0,
+                 stream=None) -> None:
+    arr = (Job * len(jobs))(*jobs)
+    cfg = BatchConfig(wave_paths, streams, chunk, 0)
+    check(load().dr_render_batch(ctx.handle, arr, len(jobs), C.byref(cfg), _stream_ptr(stream)))
 
 
 def tonemap(accum_dev, width: int, height: int, rgba_dev, gamma: bool = True, stream=None) -> None:

@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define DR_ABI_VERSION 2
+#define DR_ABI_VERSION 3
 
 typedef enum dr_status {
     DR_OK = 0,
@@ -234,9 +234,12 @@ typedef struct dr_render_config {
     int32_t pixel_sampling;  /* dr_pixel_sampling */
     uint64_t seed;           /* Philox key */
     int32_t tri_mode;        /* dr_tri_mode */
-    uint32_t wave_paths;     /* paths in flight per wave, 0 = automatic */
+    uint32_t wave_paths;     /* paths in flight per wave, 0 = automatic (2^21) */
     uint32_t flags;          /* reserved, 0 */
     int32_t debug;           /* dr_debug_view */
+    uint32_t streams;        /* concurrent waves, 1..3, 0 = 3 */
+    uint32_t chunk;          /* rays per warp fetch of the persistent traversal
+                                (32, 64, 96 or 128), 0 = adaptive */
 } dr_render_config;
 
 /* Adds cfg->spp path samples per pixel to accum_dev (float4 per pixel, row
@@ -275,6 +278,55 @@ dr_status dr_framebuffer_tonemap(dr_framebuffer *fb, int32_t gamma_corrected, ui
  * height <= 65535. */
 dr_status dr_tonemap(const float *accum_dev, int32_t width, int32_t height, int32_t gamma_corrected,
                      uint32_t *rgba_dev, void *stream);
+
+/* ---- batched rendering ------------------------------------------------------------ */
+
+/* One image of a batch: a scene, its camera, its render settings (spp,
+ * max_depth, pixel_sampling, seed, tri_mode; sample_offset of the first render;
+ * debug must be DR_DEBUG_OFF) and its device outputs (as dr_render). */
+typedef struct dr_job {
+    dr_scene *scene;
+    dr_camera camera;
+    dr_render_config config;
+    float *accum_dev;
+    uint32_t *casts_dev;
+} dr_job;
+
+typedef struct dr_batch_config {
+    uint32_t wave_paths;     /* path slots per wave, 0 = 2^21 (at least one sample of the largest image) */
+    uint32_t streams;        /* concurrent waves, 1..3, 0 = 3 */
+    uint32_t chunk;          /* persistent traversal fetch (32..128, multiple of 32), 0 = adaptive */
+    uint32_t use_graph;      /* 1: capture the schedule into a CUDA graph on the first render */
+} dr_batch_config;
+
+typedef struct dr_batch dr_batch;
+
+typedef struct dr_batch_info {
+    uint32_t num_jobs, num_waves, max_wave_paths, layout;
+    uint64_t graph_nodes;       /* nodes of the captured graph, 0 before the first render */
+    uint64_t paths_per_render;  /* sum of width * height * spp */
+    uint64_t device_bytes;      /* concatenated scene arrays */
+    uint32_t streams, chunk;
+} dr_batch_info;
+
+/* Many images of many scenes (uneven sizes) traced as one schedule: the scenes
+ * are concatenated on the device, each wave of path slots mixes images, and one
+ * persistent traversal launch per bounce serves every scene in the wave. Scenes
+ * must share a hierarchy layout and outlive nothing: the batch keeps its own
+ * copy. Synchronous. */
+dr_status dr_batch_create(dr_context *ctx, const dr_job *jobs, uint32_t njobs, const dr_batch_config *cfg,
+                          dr_batch **out);
+/* Adds every job's spp samples to its image; job j starts at sample_offsets[j]
+ * (NULL: its config.sample_offset on the first render, then after the previous
+ * render's samples). The first render captures the schedule into a CUDA graph
+ * (use_graph), later renders replay it. Asynchronous on `stream`; renders of one
+ * batch run one after another. */
+dr_status dr_batch_render(dr_batch *batch, const uint32_t *sample_offsets, void *stream);
+dr_status dr_batch_get_info(const dr_batch *batch, dr_batch_info *info);
+dr_status dr_batch_destroy(dr_batch *batch);
+/* dr_batch_create + one dr_batch_render without a graph + dr_batch_destroy. Synchronous. */
+dr_status dr_render_batch(dr_context *ctx, const dr_job *jobs, uint32_t njobs, const dr_batch_config *cfg,
+                          void *stream);
 
 /* ---- alias tables ------------------------------------------------------------------- */
 

@@ -1,0 +1,138 @@
+"""Batched rendering (dr_batch): many images of many scenes in one schedule.
+
+Each image of a batch must equal, bit for bit, the image dr_render makes of
+the same scene, camera and settings alone; so must the path-ray counts. The
+batch's schedule knobs (wave size, streams, traversal fetch size) and the
+graph capture change timing only, never a pixel.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from devilray_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+def _scenes(native, ctx, layout):
+    a = native.Scene.from_spec(ctx, scenes.box_room(sphere_level=2), layout=layout)
+    b = native.Scene.from_spec(ctx, scenes.many_light(6 * 1280, 40, seed=3, half=6.0), layout=layout)
+    c = native.Scene.from_spec(ctx, scenes.box_room(sphere_level=1), layout=layout)
+    return a, b, c
+
+
+def _job_specs():
+    # (scene index, camera, spp, max_depth, seed, sampling)
+    return [
+        (0, scenes.camera(40, 30), 5, 8, 1, 1),
+        (1, scenes.outside_camera(33, 17, distance=20.0, half=6.0), 4, 12, 2, 1),
+        (0, scenes.camera(24, 20, fov_half_width=0.3), 3, 6, 3, 0),
+        (2, scenes.camera(64, 48), 2, 12, 4, 1),
+        (1, scenes.outside_camera(16, 16, distance=30.0, half=6.0), 7, 5, 5, 1),
+    ]
+
+
+def _alone(native, scene, cam, spp, depth, seed, sampling, offset=0):
+    n = cam["width"] * cam["height"]
+    acc = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+    casts = torch.zeros(n, dtype=torch.int32, device="cuda")
+    scene.render(cam, acc, casts, spp=spp, max_depth=depth, seed=seed, pixel_sampling=sampling,
+                 sample_offset=offset)
+    torch.cuda.synchronize()
+    return acc.cpu().numpy(), casts.cpu().numpy()
+
+
+def _batch_buffers(native, scs, specs):
+    jobs, outs = [], []
+    for (si, cam, spp, depth, seed, sampling) in specs:
+        n = cam["width"] * cam["height"]
+        acc = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+        casts = torch.zeros(n, dtype=torch.int32, device="cuda")
+        jobs.append(native.make_job(scs[si], cam, acc, casts, spp=spp, max_depth=depth, seed=seed,
+                                    pixel_sampling=sampling))
+        outs.append((acc, casts))
+    return jobs, outs
+
+
+@pytest.mark.parametrize("layout", [8, 2])
+def test_batch_images_equal_single_renders(native, ctx, layout):
+    scs = _scenes(native, ctx, layout)
+    specs = _job_specs()
+    jobs, outs = _batch_buffers(native, scs, specs)
+    native.render_batch(ctx, jobs, wave_paths=3000)   # small waves: images span waves and waves mix images
+    torch.cuda.synchronize()
+    for (si, cam, spp, depth, seed, sampling), (acc, casts) in zip(specs, outs):
+        want_acc, want_casts = _alone(native, scs[si], cam, spp, depth, seed, sampling)
+        got = acc.cpu().numpy()
+        assert np.array_equal(got.view(np.uint32), want_acc.view(np.uint32))
+        assert np.array_equal(casts.cpu().numpy(), want_casts)
+        assert got[:, 3].min() == spp and got[:, :3].sum() > 0
+
+
+@pytest.mark.parametrize("wave_paths,streams,chunk", [(0, 0, 0), (2048, 1, 32), (5000, 2, 128), (1 << 16, 3, 64)])
+def test_batch_schedule_knobs_do_not_change_pixels(native, ctx, wave_paths, streams, chunk):
+    scs = _scenes(native, ctx, 8)
+    specs = _job_specs()
+    ref_jobs, ref_outs = _batch_buffers(native, scs, specs)
+    native.render_batch(ctx, ref_jobs)
+    jobs, outs = _batch_buffers(native, scs, specs)
+    native.render_batch(ctx, jobs, wave_paths=wave_paths, streams=streams, chunk=chunk)
+    torch.cuda.synchronize()
+    for (a, c), (ra, rc) in zip(outs, ref_outs):
+        assert torch.equal(a.view(torch.int32), ra.view(torch.int32)) and torch.equal(c, rc)
+
+
+def test_batch_graph_replay_is_progressive(native, ctx):
+    """Three renders of a graph-captured batch equal one render of 3 x spp."""
+    scs = _scenes(native, ctx, 8)
+    specs = _job_specs()
+    jobs, outs = _batch_buffers(native, scs, specs)
+    b = native.Batch(ctx, jobs, wave_paths=4096, use_graph=True)
+    info0 = b.info()
+    assert info0.graph_nodes == 0 and info0.num_jobs == len(specs) and info0.num_waves > 1
+    for _ in range(3):
+        b.render()
+    torch.cuda.synchronize()
+    info = b.info()
+    assert info.graph_nodes > 0
+    assert info.paths_per_render == sum(c["width"] * c["height"] * spp for (_, c, spp, *_r) in specs)
+    for (si, cam, spp, depth, seed, sampling), (acc, casts) in zip(specs, outs):
+        want_acc, want_casts = _alone(native, scs[si], cam, 3 * spp, depth, seed, sampling)
+        assert np.array_equal(acc.cpu().numpy().view(np.uint32), want_acc.view(np.uint32))
+        assert np.array_equal(casts.cpu().numpy(), want_casts)
+    # explicit offsets: restart every job at sample 0 on cleared buffers
+    for acc, casts in outs:
+        acc.zero_()
+        casts.zero_()
+    b.render(sample_offsets=[0] * len(specs))
+    torch.cuda.synchronize()
+    si, cam, spp, depth, seed, sampling = specs[1]
+    want_acc, _ = _alone(native, scs[si], cam, spp, depth, seed, sampling)
+    assert np.array_equal(outs[1][0].cpu().numpy().view(np.uint32), want_acc.view(np.uint32))
+    b.close()
+
+
+def test_batch_with_empty_scene_and_bad_arguments(native, ctx):
+    empty = native.Scene(ctx, np.zeros((0, 9), np.float32))
+    full = native.Scene.from_spec(ctx, scenes.box_room(sphere_level=1), layout=8)
+    cam = scenes.camera(8, 8)
+    acc0 = torch.zeros((64, 4), dtype=torch.float32, device="cuda")
+    acc1 = torch.zeros((64, 4), dtype=torch.float32, device="cuda")
+    casts0 = torch.zeros(64, dtype=torch.int32, device="cuda")
+    jobs = [native.make_job(empty, cam, acc0, casts0, spp=3), native.make_job(full, cam, acc1, spp=2)]
+    native.render_batch(ctx, jobs)
+    torch.cuda.synchronize()
+    a0 = acc0.cpu().numpy()
+    assert np.all(a0[:, 3] == 3) and not a0[:, :3].any() and np.all(casts0.cpu().numpy() == 3)
+    assert acc1.cpu().numpy()[:, 3].min() == 2
+    other = native.Scene.from_spec(ctx, scenes.box_room(sphere_level=1), layout=2)
+    with pytest.raises(native.DrError):
+        native.render_batch(ctx, [native.make_job(full, cam, acc1), native.make_job(other, cam, acc0)])
+    bad = native.make_job(full, cam, acc1)
+    bad.config.debug = 1
+    with pytest.raises(native.DrError):
+        native.render_batch(ctx, [bad])
+    with pytest.raises(native.DrError):
+        native.render_batch(ctx, [])
