@@ -293,6 +293,9 @@ def run_ours(args):
         torch.cuda.empty_cache()
         line["render"] = render_section(ctx, native, local, stream, cpu=(world == 1 and not args.no_cpu_baseline),
                                         threads=os.cpu_count() or 1, layout=args.render_layout)
+    if not args.no_batch:
+        torch.cuda.empty_cache()
+        line["batch"] = batch_section(ctx, native, local, stream, scenes_n=args.batch_scenes)
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -348,6 +351,93 @@ def render_section(ctx, native, device: int, stream, cpu: bool, threads: int, la
     return out
 
 
+def batch_specs(n: int = 64, seed: int = 2024):
+    """Uneven procedural scenes: triangle counts log-uniform in [1k, 2M],
+    square resolutions from {128, 256, 512, 1024}; the many-light material mix
+    (1/64 of the triangles emissive, at least 16; the rest half diffuse, half
+    dielectric); camera outside the scene cube."""
+    from devilray_gb300 import scenes
+    rng = np.random.default_rng(seed)
+    tris = np.exp(rng.uniform(np.log(1e3), np.log(2e6), n)).astype(np.int64)
+    res = rng.choice([128, 256, 512, 1024], n)
+    out = []
+    for i in range(n):
+        spec = scenes.many_light(int(tris[i]), max(16, int(tris[i]) // 64), seed=seed + i)
+        out.append((spec, scenes.outside_camera(int(res[i]), int(res[i]))))
+    return out
+
+
+def batch_section(ctx, native, device: int, stream, scenes_n: int = 64, spp: int = 32, depth: int = 12):
+    """Batched uneven scenes: `scenes_n` scenes and cameras traced as one
+    schedule (dr_batch) captured in a CUDA graph, wave size / streams / fetch
+    size and hierarchy width picked by the autotuner; samples/s over the whole
+    batch, beside the same images rendered one dr_render call at a time."""
+    import torch
+    t0 = time.perf_counter()
+    specs = batch_specs(scenes_n)
+    gen_s = time.perf_counter() - t0
+    sizes = [s.positions.shape[0] for s, _ in specs]
+    median = int(np.argsort(sizes)[len(sizes) // 2])
+    t0 = time.perf_counter()
+    tune_scene = native.autotune(ctx, specs[median][0], specs[median][1], spp=2, max_depth=depth, reps=2)
+    tune_scene_s = time.perf_counter() - t0
+    layout = tune_scene.layout
+    t0 = time.perf_counter()
+    scs = [native.Scene.from_spec(ctx, spec, layout=layout) for spec, _ in specs]
+    build_s = time.perf_counter() - t0
+    jobs, outs = [], []
+    for i, ((spec, cam), sc) in enumerate(zip(specs, scs)):
+        n = cam["width"] * cam["height"]
+        acc = torch.zeros((n, 4), dtype=torch.float32, device=f"cuda:{device}")
+        casts = torch.zeros(n, dtype=torch.int32, device=f"cuda:{device}")
+        jobs.append(native.make_job(sc, cam, acc, casts, spp=spp, max_depth=depth, seed=i))
+        outs.append((acc, casts))
+    t0 = time.perf_counter()
+    tune = native.autotune_batch(ctx, jobs, probe_spp=1, reps=2)
+    tune_batch_s = time.perf_counter() - t0
+    b = native.Batch(ctx, jobs, wave_paths=tune.wave_paths, streams=tune.streams, chunk=tune.chunk, use_graph=True)
+    b.render(stream=stream)  # captures the graph
+    stream.synchronize()
+    times = []
+    for _ in range(2):
+        for acc, casts in outs:
+            acc.zero_()
+            casts.zero_()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        b.render(sample_offsets=[0] * len(jobs), stream=stream)
+        e1.record(stream)
+        stream.synchronize()
+        times.append(e0.elapsed_time(e1) / 1e3)
+    t = min(times)
+    info = b.info()
+    path_rays = sum(int(c.sum().item()) for _, c in outs)
+    samples = int(info.paths_per_render)
+    # the same images one dr_render call at a time (default schedule)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for (spec, cam), sc, (acc, casts) in zip(specs, scs, outs):
+        sc.render(cam, acc, casts, spp=spp, max_depth=depth, stream=stream)
+    e1.record(stream)
+    stream.synchronize()
+    t_seq = e0.elapsed_time(e1) / 1e3
+    out = {"scenes": scenes_n, "triangles_total": int(sum(sizes)), "triangles_min": int(min(sizes)),
+           "triangles_max": int(max(sizes)), "pixels_total": int(sum(c["width"] * c["height"] for _, c in specs)),
+           "spp": spp, "max_depth": depth, "layout": layout, "seconds": t, "samples_per_s": samples / t,
+           "path_mrays_per_s": path_rays / t / 1e6, "num_waves": info.num_waves,
+           "wave_paths": info.max_wave_paths, "graph_nodes": int(info.graph_nodes),
+           "sequential_dr_render_seconds": t_seq, "sequential_samples_per_s": samples / t_seq,
+           "autotune_scene": tune_scene.as_dict(), "autotune_batch": tune.as_dict(),
+           "autotune_seconds": round(tune_scene_s + tune_batch_s, 3), "scene_build_s": round(build_s, 3),
+           "scene_generation_s": round(gen_s, 3)}
+    b.close()
+    del jobs, outs, scs
+    torch.cuda.empty_cache()
+    return out
+
+
 def render_cpu_baseline(spec, cam, depth: int, threads: int, pixels: int):
     """The reference's integrator on the CPU (oracle port of sampleColor with the
     reference's per-object cast), `pixels` pixels x 1 sample; samples/s."""
@@ -391,6 +481,8 @@ def main():
     ap.add_argument("--ref-sample", type=int, default=1 << 19)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-render", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--batch-scenes", type=int, default=64)
     ap.add_argument("--layout", type=int, default=0, help="BVH layout of the trace workload: 0 default, 2, 8")
     ap.add_argument("--render-layout", type=int, default=0, help="BVH layout of the render workloads")
     args = ap.parse_args()

@@ -95,6 +95,28 @@ class BatchConfig(C.Structure):
                 ("use_graph", C.c_uint32)]
 
 
+class AutotuneConfig(C.Structure):
+    _fields_ = [("probe_spp", C.c_uint32), ("reps", C.c_uint32), ("try_layouts", C.c_uint32),
+                ("max_leaf_size", C.c_uint32)]
+
+
+class AutotuneCandidate(C.Structure):
+    _fields_ = [("layout", C.c_uint32), ("wave_paths", C.c_uint32), ("streams", C.c_uint32),
+                ("chunk", C.c_uint32), ("ms", C.c_float)]
+
+
+class AutotuneResult(C.Structure):
+    _fields_ = [("layout", C.c_uint32), ("wave_paths", C.c_uint32), ("streams", C.c_uint32),
+                ("chunk", C.c_uint32), ("best_ms", C.c_float), ("num_candidates", C.c_uint32),
+                ("candidates", AutotuneCandidate * 64)]
+
+    def as_dict(self) -> dict:
+        return {"layout": self.layout, "wave_paths": self.wave_paths, "streams": self.streams, "chunk": self.chunk,
+                "best_ms": self.best_ms,
+                "candidates": [{"layout": c.layout, "wave_paths": c.wave_paths, "streams": c.streams,
+                                "chunk": c.chunk, "ms": c.ms} for c in self.candidates[:self.num_candidates]]}
+
+
 class BatchInfo(C.Structure):
     _fields_ = [("num_jobs", C.c_uint32), ("num_waves", C.c_uint32), ("max_wave_paths", C.c_uint32),
                 ("layout", C.c_uint32), ("graph_nodes", C.c_uint64), ("paths_per_render", C.c_uint64),
@@ -153,6 +175,8 @@ SIGNATURES = {
     "dr_batch_get_info": (C.c_int, [C.c_void_p, C.c_void_p]),
     "dr_batch_destroy": (C.c_int, [C.c_void_p]),
     "dr_render_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
+    "dr_autotune": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "dr_autotune_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
     "dr_alias_build_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_int32]),
     "dr_alias_build": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_int32, C.c_void_p]),
     "dr_alias_build_noalloc": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
@@ -247,20 +271,68 @@ def alias_sample(table_dev, n: int, uniforms_dev, ndraws: int, index_dev, pdf_de
                                  _stream_ptr(stream)))
 
 
+def scene_desc(positions: np.ndarray, objects=None, materials=None, tri_material=None, tri_weight=None):
+    """dr_scene_desc over numpy/ctypes arrays; returns (desc, arrays to keep alive)."""
+    positions = np.ascontiguousarray(positions, np.float32).reshape(-1, 9)
+    desc = SceneDesc()
+    desc.positions_host = positions.ctypes.data
+    desc.num_triangles = positions.shape[0]
+    keep = [positions]
+    if objects is not None:
+        objs = (Object * len(objects))(*objects)
+        keep.append(objs)
+        desc.objects_host = C.addressof(objs)
+        desc.num_objects = len(objects)
+    if materials is not None:
+        mats = (Material * len(materials))(*materials)
+        keep.append(mats)
+        desc.materials_host = C.addressof(mats)
+        desc.num_materials = len(materials)
+    if tri_material is not None:
+        tm = np.ascontiguousarray(tri_material, np.int32)
+        keep.append(tm)
+        desc.tri_material_host = tm.ctypes.data
+    if tri_weight is not None:
+        tw = np.ascontiguousarray(tri_weight, np.float32)
+        keep.append(tw)
+        desc.tri_weight_host = tw.ctypes.data
+    return desc, keep
+
+
+def spec_parts(spec):
+    """(objects, materials) ctypes records of a devilray_gb300.scenes.SceneSpec."""
+    objs = [Object(int(b), int(c), int(m), float(a)) for (b, c, m, a) in spec.objects]
+    mats = []
+    for m in spec.materials:
+        mm = Material()
+        mm.kind, mm.ior = m["kind"], m["ior"]
+        for i in range(4):
+            mm.emission[i], mm.albedo[i], mm.debug_color[i] = m["emission"][i], m["albedo"][i], m["debug"][i]
+        mats.append(mm)
+    return objs, mats
+
+
+def autotune(ctx: "Context", spec, cam: dict, spp: int = 1, max_depth: int = 10, pixel_sampling: int = 1,
+             seed: int = 0, probe_spp: int = 0, reps: int = 2, try_layouts: bool = True) -> "AutotuneResult":
+    """dr_autotune for a SceneSpec rendered through `cam`."""
+    objs, mats = spec_parts(spec)
+    desc, keep = scene_desc(spec.positions, objs, mats)
+    c = make_camera(cam)
+    cfg = RenderConfig(max_depth, spp, 0, pixel_sampling, seed, DR_TRI_REFERENCE, 0, 0, 0, 0, 0)
+    tc = AutotuneConfig(probe_spp, reps, 1 if try_layouts else 0, 0)
+    out = AutotuneResult()
+    check(load().dr_autotune(ctx.handle, C.byref(desc), C.byref(c), C.byref(cfg), C.byref(tc), C.byref(out)))
+    del keep
+    return out
+
+
 class Scene:
     """A triangle soup uploaded with its BVH (dr_scene_create)."""
 
     @classmethod
     def from_spec(cls, ctx: "Context", spec, **kw) -> "Scene":
         """Scene from a devilray_gb300.scenes.SceneSpec (objects + materials)."""
-        objs = [Object(int(b), int(c), int(m), float(a)) for (b, c, m, a) in spec.objects]
-        mats = []
-        for m in spec.materials:
-            mm = Material()
-            mm.kind, mm.ior = m["kind"], m["ior"]
-            for i in range(4):
-                mm.emission[i], mm.albedo[i], mm.debug_color[i] = m["emission"][i], m["albedo"][i], m["debug"][i]
-            mats.append(mm)
+        objs, mats = spec_parts(spec)
         return cls(ctx, spec.positions, objects=objs, materials=mats, **kw)
 
     def __init__(self, ctx: Context, positions: np.ndarray, objects=None, materials=None,
@@ -268,28 +340,7 @@ class Scene:
                  threads: int = 0, layout: int = 0):
         self.ctx = ctx
         self.positions = np.ascontiguousarray(positions, np.float32).reshape(-1, 9)
-        desc = SceneDesc()
-        desc.positions_host = self.positions.ctypes.data
-        desc.num_triangles = self.positions.shape[0]
-        keep = [self.positions]
-        if objects is not None:
-            objs = (Object * len(objects))(*objects)
-            keep.append(objs)
-            desc.objects_host = C.addressof(objs)
-            desc.num_objects = len(objects)
-        if materials is not None:
-            mats = (Material * len(materials))(*materials)
-            keep.append(mats)
-            desc.materials_host = C.addressof(mats)
-            desc.num_materials = len(materials)
-        if tri_material is not None:
-            tm = np.ascontiguousarray(tri_material, np.int32)
-            keep.append(tm)
-            desc.tri_material_host = tm.ctypes.data
-        if tri_weight is not None:
-            tw = np.ascontiguousarray(tri_weight, np.float32)
-            keep.append(tw)
-            desc.tri_weight_host = tw.ctypes.data
+        desc, keep = scene_desc(self.positions, objects, materials, tri_material, tri_weight)
         cfg = BuildConfig(max_leaf_size, sah_bins, threads, layout)
         self.handle = C.c_void_p()
         check(load().dr_scene_create(ctx.handle, C.byref(desc), C.byref(cfg), C.byref(self.handle)))
@@ -434,6 +485,14 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def autotune_batch(ctx: "Context", jobs: list, probe_spp: int = 1, reps: int = 2) -> AutotuneResult:
+    arr = (Job * len(jobs))(*jobs)
+    tc = AutotuneConfig(probe_spp, reps, 0, 0)
+    out = AutotuneResult()
+    check(load().dr_autotune_batch(ctx.handle, arr, len(jobs), C.byref(tc), C.byref(out)))
+    return out
 
 
 def render_batch(ctx: "Context", jobs: list, wave_paths: int = 0, streams: int = 0, chunk: int = 0,

@@ -328,6 +328,38 @@ dr_status dr_batch_destroy(dr_batch *batch);
 dr_status dr_render_batch(dr_context *ctx, const dr_job *jobs, uint32_t njobs, const dr_batch_config *cfg,
                           void *stream);
 
+/* ---- autotuning ------------------------------------------------------------------- */
+
+typedef struct dr_autotune_config {
+    uint32_t probe_spp;      /* samples per probe render; 0 = min(spp, 2) (dr_autotune), 1 (batch) */
+    uint32_t reps;           /* timed renders per candidate, minimum taken; 0 = 2 */
+    uint32_t try_layouts;    /* dr_autotune: 1 = build the scene 8-wide and 2-wide and time both */
+    uint32_t max_leaf_size;  /* build setting of the probe scenes, 0 = default */
+} dr_autotune_config;
+
+typedef struct dr_autotune_candidate {
+    uint32_t layout, wave_paths, streams, chunk;
+    float ms;
+} dr_autotune_candidate;
+
+typedef struct dr_autotune_result {
+    uint32_t layout, wave_paths, streams, chunk;  /* the chosen settings */
+    float best_ms;                                 /* probe time of the chosen settings */
+    uint32_t num_candidates;
+    dr_autotune_candidate candidates[64];          /* every probe, in order */
+} dr_autotune_result;
+
+/* Picks the hierarchy width (dr_build_config.layout) and the wave schedule
+ * (dr_render_config wave_paths / streams / chunk) for rendering `desc` through
+ * `camera` with `cfg`, by coordinate descent over timed probe renders of the
+ * same samples (images do not depend on these settings). Synchronous. */
+dr_status dr_autotune(dr_context *ctx, const dr_scene_desc *desc, const dr_camera *camera,
+                      const dr_render_config *cfg, const dr_autotune_config *tc, dr_autotune_result *out);
+/* The same for a batch (dr_batch_config wave_paths / streams / chunk; the layout
+ * is the scenes'), probing the batch's images with probe_spp samples each. */
+dr_status dr_autotune_batch(dr_context *ctx, const dr_job *jobs, uint32_t njobs, const dr_autotune_config *tc,
+                            dr_autotune_result *out);
+
 /* ---- alias tables ------------------------------------------------------------------- */
 
 typedef enum dr_alias_mode {

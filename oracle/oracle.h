@@ -142,6 +142,22 @@ void or_render(const or_scene *s, const or_camera *cam, const or_render_cfg *cfg
  * gamma != 0: OutputLinearity::GammaCorrected (sRGB); 0: Linear. */
 void or_create_pixels(const float *accum, int32_t width, int32_t height, int32_t gamma, uint32_t *out);
 
+/* ---- path-guiding network (not part of the reference; restates the product's
+ * network in FP64 with BF16-rounded weights and layer inputs) ------------- */
+int32_t or_mlp_num_params(void);
+/* 12-frequency position encoding of (pos - center) / half, then dir, zero padded to 80. */
+void or_guide_encode(const float *pos, const float *dir, const float *center, float half, float *out80);
+/* inputs [n][80] -> out [n][48] */
+void or_mlp_forward(const float *params, const float *inputs, int32_t n, float *out);
+/* log q(w) of the 8-lobe vMF mixture of network output y[40] at unit direction w. */
+double or_vmf_mixture_log_pdf(const float *y, const float *w);
+/* Batch loss -sum c_i log q(dir_i | input_i) / n, c_i = weight_i / mean(weight),
+ * and its gradient for every parameter. */
+void or_mlp_loss_grad(const float *params, const float *inputs, const float *dirs, const float *weights, int32_t n,
+                      double *loss, double *grad);
+void or_adam_step(float *params, float *m, float *v, const float *grad, int32_t n, int32_t t, float lr, float beta1,
+                  float beta2, float eps);
+
 /* ---- Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) ------------------- */
 void or_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 

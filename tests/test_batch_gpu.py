@@ -136,3 +136,33 @@ def test_batch_with_empty_scene_and_bad_arguments(native, ctx):
         native.render_batch(ctx, [bad])
     with pytest.raises(native.DrError):
         native.render_batch(ctx, [])
+
+
+def test_autotune_picks_a_measured_schedule(native, ctx):
+    spec = scenes.box_room(sphere_level=2)
+    cam = scenes.camera(64, 48)
+    res = native.autotune(ctx, spec, cam, spp=4, max_depth=8, reps=1)
+    d = res.as_dict()
+    assert res.layout in (2, 8) and res.streams in (1, 2, 3) and res.chunk in (0, 32, 64, 128)
+    assert res.wave_paths in (1 << 19, 1 << 20, 1 << 21, 1 << 22, 1 << 23)
+    assert len(d["candidates"]) >= 6 and res.best_ms > 0
+    assert {c["layout"] for c in d["candidates"]} == {2, 8}
+    assert res.best_ms == min(c["ms"] for c in d["candidates"])
+    # the chosen schedule renders the same image as the defaults
+    scene = native.Scene.from_spec(ctx, spec, layout=res.layout)
+    a, ca = _alone(native, scene, cam, 4, 8, 0, 1)
+    n = cam["width"] * cam["height"]
+    acc = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+    scene.render(cam, acc, spp=4, max_depth=8, wave_paths=res.wave_paths, streams=res.streams, chunk=res.chunk)
+    torch.cuda.synchronize()
+    assert np.array_equal(acc.cpu().numpy().view(np.uint32), a.view(np.uint32))
+
+
+def test_autotune_batch(native, ctx):
+    scs = _scenes(native, ctx, 8)
+    jobs, outs = _batch_buffers(native, scs, _job_specs())
+    res = native.autotune_batch(ctx, jobs, probe_spp=1, reps=1)
+    assert res.layout == 8 and res.best_ms > 0 and res.num_candidates >= 6
+    # the jobs' own buffers are untouched by the probes
+    for acc, casts in outs:
+        assert not acc.any() and not casts.any()
