@@ -1,0 +1,854 @@
+// guiding.cu -- the path-guiding network on tensor cores: inference, one
+// training step (forward, loss gradient, backward, weight gradients) and Adam.
+//
+// Network: 80 inputs (12-frequency encoding of the normalised position, a
+// direction, zero padding) -> 4 hidden layers of 64 (ReLU) -> 48 outputs (40
+// used: the 8-lobe vMF mixture of guide_math.cuh). Weights and layer inputs
+// are BF16, every product accumulates in FP32 (mma.sync m16n8k16 on the
+// tensor cores); master weights and Adam moments are FP32.
+//
+// A warp carries 16 rows through all layers in registers: the FP32
+// accumulator fragment of one layer is, pair by pair, the BF16 A fragment of
+// the next (m16n8 C layout = m16k16 A layout of two adjacent column tiles).
+// Backward products use the transposed weights, staged in shared memory; the
+// deltas enter the tensor cores as a BF16 high part plus a BF16 remainder so
+// the propagated gradient keeps about 16 bits. Weight gradients are
+// delta^T x activations over the batch (K = rows), split over row chunks and
+// summed with atomics.
+
+#include "dr_internal.h"
+#include "guide_math.cuh"
+#include "guide_internal.h"
+
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <random>
+#include <vector>
+
+namespace dr {
+namespace {
+
+constexpr int kIn = 80, kHid = 64, kOut = 48, kLayers = 5;
+__host__ __device__ constexpr int fan_in(int l) { return l == 0 ? kIn : kHid; }
+__host__ __device__ constexpr int fan_out(int l) { return l == kLayers - 1 ? kOut : kHid; }
+
+__host__ __device__ constexpr int w_off(int l)
+{
+    int o = 0;
+    for (int i = 0; i < l; ++i) o += fan_out(i) * fan_in(i) + fan_out(i);
+    return o;
+}
+__host__ __device__ constexpr int b_off(int l) { return w_off(l) + fan_out(l) * fan_in(l); }
+constexpr int kNumParams = w_off(kLayers);
+// BF16 weights (no biases) in the same order, for the kernels
+__host__ __device__ constexpr int wb_off(int l)
+{
+    int o = 0;
+    for (int i = 0; i < l; ++i) o += fan_out(i) * fan_in(i);
+    return o;
+}
+constexpr int kNumWeights = wb_off(kLayers);
+
+// shared-memory strides (bf16 elements), padded so the 8 rows of a fragment
+// load fall in distinct banks
+constexpr int kStrideIn = kIn + 8;    // 88
+constexpr int kStrideHid = kHid + 8;  // 72
+constexpr int kStrideOutT = kOut + 8; // 56: transposed last layer [64][48]
+
+struct GuideParams {
+    float center[3];
+    float half;
+};
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
+{
+    const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<const uint32_t *>(&v);
+}
+
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1)
+{
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// Encoded input pair (columns c, c + 1; c even) of a row.
+__device__ __forceinline__ void encode_pair(const float p[3], const float d[3], int c, float &v0, float &v1)
+{
+    if (c < 72) {
+        const int a = c / 24, k = (c % 24) >> 1;
+        const float x = ldexpf(p[a], k);  // exact: scaling by a power of two
+        sincospif(x, &v0, &v1);
+    } else if (c == 72) {
+        v0 = d[0];
+        v1 = d[1];
+    } else if (c == 74) {
+        v0 = d[2];
+        v1 = 0.0f;
+    } else {
+        v0 = v1 = 0.0f;
+    }
+}
+
+// Shared-memory image of the weights: forward W_l [out][in] and, for the
+// backward pass, W_l^T [in][out] of layers 1..4.
+struct SmemWeights {
+    __nv_bfloat16 w0[kHid * kStrideIn];
+    __nv_bfloat16 w[3][kHid * kStrideHid];     // layers 1..3
+    __nv_bfloat16 w4[kOut * kStrideHid];
+    float bias[4 * kHid + kOut];
+};
+struct SmemWeightsT {
+    __nv_bfloat16 t[3][kHid * kStrideHid];     // W_l^T, l = 1..3: [in 64][out 64]
+    __nv_bfloat16 t4[kHid * kStrideOutT];      // W_4^T: [in 64][out 48]
+};
+
+__device__ void load_weights(SmemWeights &s, const __nv_bfloat16 *wb, const float *params)
+{
+    for (int i = threadIdx.x; i < kHid * kIn; i += blockDim.x) s.w0[(i / kIn) * kStrideIn + i % kIn] = wb[i];
+    for (int l = 1; l <= 3; ++l)
+        for (int i = threadIdx.x; i < kHid * kHid; i += blockDim.x)
+            s.w[l - 1][(i / kHid) * kStrideHid + i % kHid] = wb[wb_off(l) + i];
+    for (int i = threadIdx.x; i < kOut * kHid; i += blockDim.x) s.w4[(i / kHid) * kStrideHid + i % kHid] = wb[wb_off(4) + i];
+    for (int l = 0; l < kLayers; ++l)
+        for (int i = threadIdx.x; i < fan_out(l); i += blockDim.x) s.bias[l * kHid + i] = params[b_off(l) + i];
+}
+
+__device__ void load_weights_t(SmemWeightsT &s, const __nv_bfloat16 *wb)
+{
+    for (int l = 1; l <= 3; ++l)
+        for (int i = threadIdx.x; i < kHid * kHid; i += blockDim.x) {
+            const int o = i / kHid, in = i % kHid;
+            s.t[l - 1][in * kStrideHid + o] = wb[wb_off(l) + i];
+        }
+    for (int i = threadIdx.x; i < kOut * kHid; i += blockDim.x) {
+        const int o = i / kHid, in = i % kHid;
+        s.t4[in * kStrideOutT + o] = wb[wb_off(4) + i];
+    }
+}
+
+__device__ __forceinline__ uint32_t ld_pair(const __nv_bfloat16 *p) { return *reinterpret_cast<const uint32_t *>(p); }
+
+// acc[nt] += A (16 x 16 ks-slices) x B where B[k][n] = W[n][k], W row-major with
+// `stride`; NT column tiles of 8, KS k-steps of 16.
+template <int NT, int KS>
+__device__ __forceinline__ void layer_mma(float (&acc)[NT][4], const uint32_t (&a)[KS][4], const __nv_bfloat16 *W,
+                                          int stride)
+{
+    const int lane = threadIdx.x & 31, g = lane >> 2, tig = lane & 3;
+#pragma unroll
+    for (int ks = 0; ks < KS; ++ks)
+#pragma unroll
+        for (int nt = 0; nt < NT; ++nt) {
+            const __nv_bfloat16 *row = W + (8 * nt + g) * stride + 16 * ks + 2 * tig;
+            mma_bf16(acc[nt], a[ks], ld_pair(row), ld_pair(row + 8));
+        }
+}
+
+template <int NT>
+__device__ __forceinline__ void init_bias(float (&acc)[NT][4], const float *bias)
+{
+    const int tig = threadIdx.x & 3;
+#pragma unroll
+    for (int nt = 0; nt < NT; ++nt) {
+        const float b0 = bias[8 * nt + 2 * tig], b1 = bias[8 * nt + 2 * tig + 1];
+        acc[nt][0] = b0, acc[nt][1] = b1, acc[nt][2] = b0, acc[nt][3] = b1;
+    }
+}
+
+// ReLU of a 64-wide accumulator, as the A fragments of the next layer.
+__device__ __forceinline__ void relu_to_a(const float (&acc)[8][4], uint32_t (&a)[4][4])
+{
+#pragma unroll
+    for (int ks = 0; ks < 4; ++ks) {
+        const float *l = acc[2 * ks], *h = acc[2 * ks + 1];
+        a[ks][0] = pack_bf16(fmaxf(l[0], 0.0f), fmaxf(l[1], 0.0f));
+        a[ks][1] = pack_bf16(fmaxf(l[2], 0.0f), fmaxf(l[3], 0.0f));
+        a[ks][2] = pack_bf16(fmaxf(h[0], 0.0f), fmaxf(h[1], 0.0f));
+        a[ks][3] = pack_bf16(fmaxf(h[2], 0.0f), fmaxf(h[3], 0.0f));
+    }
+}
+
+// Input fragments of 16 rows (5 k-steps of 16 encoded columns).
+__device__ __forceinline__ void input_frags(const float p_g[3], const float d_g[3], const float p_h[3],
+                                            const float d_h[3], uint32_t (&a)[5][4])
+{
+    const int tig = threadIdx.x & 3;
+#pragma unroll
+    for (int ks = 0; ks < 5; ++ks) {
+        float v0, v1;
+        const int c0 = 16 * ks + 2 * tig, c1 = c0 + 8;
+        encode_pair(p_g, d_g, c0, v0, v1);
+        a[ks][0] = pack_bf16(v0, v1);
+        encode_pair(p_h, d_h, c0, v0, v1);
+        a[ks][1] = pack_bf16(v0, v1);
+        encode_pair(p_g, d_g, c1, v0, v1);
+        a[ks][2] = pack_bf16(v0, v1);
+        encode_pair(p_h, d_h, c1, v0, v1);
+        a[ks][3] = pack_bf16(v0, v1);
+    }
+}
+
+__device__ __forceinline__ void load_row(const float *pos, const float *dir, const uint32_t *list, uint32_t n, uint32_t r,
+                                         const GuideParams &gp, float p[3], float d[3], uint32_t &slot)
+{
+    slot = r < n ? (list ? list[r] : r) : 0xffffffffu;
+    if (r >= n) {
+        p[0] = p[1] = p[2] = d[0] = d[1] = d[2] = 0.0f;
+        return;
+    }
+    for (int a = 0; a < 3; ++a) {
+        const float x = (pos[3 * (size_t)slot + a] - gp.center[a]) / gp.half;
+        p[a] = fminf(1.0f, fmaxf(-1.0f, x));
+        d[a] = dir[3 * (size_t)slot + a];
+    }
+}
+
+// Forward pass of 16 rows per warp; y[slot][40] for rows r < n (slot = list[r]
+// or r). Grid-stride over 16-row tiles.
+__global__ void __launch_bounds__(128) k_guide_infer(const __nv_bfloat16 *wb, const float *params, GuideParams gp,
+                                                     const float *pos, const float *dir, const uint32_t *list,
+                                                     const uint32_t *count, uint32_t n_fixed, float *y)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    SmemWeights &s = *reinterpret_cast<SmemWeights *>(smem);
+    load_weights(s, wb, params);
+    __syncthreads();
+    const uint32_t n = count ? *count : n_fixed;
+    const int lane = threadIdx.x & 31, g = lane >> 2, tig = lane & 3;
+    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+    for (uint32_t tile = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); 16ull * tile < n; tile += warps) {
+        const uint32_t r0 = 16 * tile;
+        float pg[3], dg[3], ph[3], dh[3];
+        uint32_t sg, sh;
+        load_row(pos, dir, list, n, r0 + g, gp, pg, dg, sg);
+        load_row(pos, dir, list, n, r0 + g + 8, gp, ph, dh, sh);
+        uint32_t a0[5][4];
+        input_frags(pg, dg, ph, dh, a0);
+        float acc[8][4];
+        uint32_t a[4][4];
+        init_bias(acc, s.bias);
+        layer_mma<8, 5>(acc, a0, s.w0, kStrideIn);
+        relu_to_a(acc, a);
+#pragma unroll
+        for (int l = 1; l <= 3; ++l) {
+            init_bias(acc, s.bias + l * kHid);
+            layer_mma<8, 4>(acc, a, s.w[l - 1], kStrideHid);
+            relu_to_a(acc, a);
+        }
+        float out[6][4];
+        init_bias(out, s.bias + 4 * kHid);
+        layer_mma<6, 4>(out, a, s.w4, kStrideHid);
+#pragma unroll
+        for (int nt = 0; nt < 5; ++nt) {
+            const int c = 8 * nt + 2 * tig;
+            if (sg != 0xffffffffu)
+                *reinterpret_cast<float2 *>(y + (size_t)sg * kGuideOut + c) = make_float2(out[nt][0], out[nt][1]);
+            if (sh != 0xffffffffu)
+                *reinterpret_cast<float2 *>(y + (size_t)sh * kGuideOut + c) = make_float2(out[nt][2], out[nt][3]);
+        }
+    }
+}
+
+// ---- training -----------------------------------------------------------------
+
+struct TrainBuffers {
+    // per layer l (0..4): delta of the layer output, transposed [out][rows] (FP32),
+    // and the layer input, transposed [in][rows] (BF16)
+    float *deltaT[kLayers];
+    __nv_bfloat16 *actT[kLayers];
+    uint32_t rows;  // row stride of the transposed arrays (batch capacity)
+};
+
+// Writes a 16 x (8 NT) FP32 accumulator transposed: dst[col][row0 + row].
+template <int NT>
+__device__ __forceinline__ void store_t(float *dst, uint32_t stride, uint32_t row0, const float (&acc)[NT][4], uint32_t n,
+                                        int ncols)
+{
+    const int lane = threadIdx.x & 31, g = lane >> 2, tig = lane & 3;
+#pragma unroll
+    for (int nt = 0; nt < NT; ++nt) {
+        const int c = 8 * nt + 2 * tig;
+        if (c >= ncols) continue;
+        if (row0 + g < n) {
+            dst[(size_t)c * stride + row0 + g] = acc[nt][0];
+            dst[(size_t)(c + 1) * stride + row0 + g] = acc[nt][1];
+        }
+        if (row0 + g + 8 < n) {
+            dst[(size_t)c * stride + row0 + g + 8] = acc[nt][2];
+            dst[(size_t)(c + 1) * stride + row0 + g + 8] = acc[nt][3];
+        }
+    }
+}
+
+// Writes BF16 A fragments (KS k-steps) transposed: dst[col][row0 + row].
+template <int KS>
+__device__ __forceinline__ void store_a_t(__nv_bfloat16 *dst, uint32_t stride, uint32_t row0, const uint32_t (&a)[KS][4],
+                                          uint32_t n)
+{
+    const int lane = threadIdx.x & 31, g = lane >> 2, tig = lane & 3;
+#pragma unroll
+    for (int ks = 0; ks < KS; ++ks)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int row = g + ((q & 1) ? 8 : 0);
+            const int c = 16 * ks + 2 * tig + ((q & 2) ? 8 : 0);
+            if (row0 + row >= n) continue;
+            const uint32_t v = a[ks][q];
+            __nv_bfloat16 lo, hi;
+            const uint16_t lb = (uint16_t)(v & 0xffffu), hb = (uint16_t)(v >> 16);
+            memcpy(&lo, &lb, 2);
+            memcpy(&hi, &hb, 2);
+            dst[(size_t)c * stride + row0 + row] = lo;
+            dst[(size_t)(c + 1) * stride + row0 + row] = hi;
+        }
+}
+
+// Splits FP32 accumulators of 64 (or 48) columns into BF16 high and low A
+// fragments (KS k-steps), after masking by the ReLU of `act` (the layer's
+// output fragments) when MASK.
+template <int KS, bool MASK>
+__device__ __forceinline__ void delta_frags(float (&acc)[2 * KS][4], const uint32_t (&act)[4][4], uint32_t (&hi)[KS][4],
+                                            uint32_t (&lo)[KS][4])
+{
+#pragma unroll
+    for (int ks = 0; ks < KS; ++ks) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            // q: 0 (rows g, tile 2ks) 1 (rows g+8, tile 2ks) 2 (rows g, tile 2ks+1) 3 (rows g+8, tile 2ks+1)
+            float *c = acc[2 * ks + (q >> 1)] + ((q & 1) ? 2 : 0);
+            if (MASK) {
+                const uint32_t m = act[ks][q];
+                if ((m & 0x7fffu) == 0) c[0] = 0.0f;
+                if ((m & 0x7fff0000u) == 0) c[1] = 0.0f;
+            }
+            const __nv_bfloat162 h = __floats2bfloat162_rn(c[0], c[1]);
+            const float2 hf = __bfloat1622float2(h);
+            hi[ks][q] = *reinterpret_cast<const uint32_t *>(&h);
+            lo[ks][q] = pack_bf16(c[0] - hf.x, c[1] - hf.y);
+        }
+    }
+}
+
+// One block = 4 warps = 64 rows. Forward with stored activations, loss
+// gradient, backward deltas; writes deltaT / actT of every layer and adds the
+// batch loss. weight_mean: mean sample weight of the batch (device scalar).
+__global__ void __launch_bounds__(128) k_guide_train_fb(const __nv_bfloat16 *wb, const float *params, GuideParams gp,
+                                                        const float *pos, const float *dir, const float *sdir,
+                                                        const float *weight, uint32_t n, const float *weight_mean,
+                                                        TrainBuffers tb, float *loss)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    SmemWeights &s = *reinterpret_cast<SmemWeights *>(smem);
+    SmemWeightsT &t = *reinterpret_cast<SmemWeightsT *>(smem + sizeof(SmemWeights));
+    float *ybuf = reinterpret_cast<float *>(smem + sizeof(SmemWeights) + sizeof(SmemWeightsT));  // [4 warps][16][48]
+    load_weights(s, wb, params);
+    load_weights_t(t, wb);
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, tig = lane & 3;
+    float *yw = ybuf + warp * 16 * kOut;
+    const uint32_t r0 = 64 * blockIdx.x + 16 * warp;
+    if (r0 >= n) return;  // no block-wide barrier follows
+    float pg[3], dg[3], ph[3], dh[3];
+    uint32_t sg, sh;
+    load_row(pos, dir, nullptr, n, r0 + g, gp, pg, dg, sg);
+    load_row(pos, dir, nullptr, n, r0 + g + 8, gp, ph, dh, sh);
+    uint32_t a0[5][4], h[4][4][4];  // inputs; outputs of layers 0..3 (post-ReLU)
+    input_frags(pg, dg, ph, dh, a0);
+    float acc[8][4];
+    init_bias(acc, s.bias);
+    layer_mma<8, 5>(acc, a0, s.w0, kStrideIn);
+    relu_to_a(acc, h[0]);
+#pragma unroll
+    for (int l = 1; l <= 3; ++l) {
+        init_bias(acc, s.bias + l * kHid);
+        layer_mma<8, 4>(acc, h[l - 1], s.w[l - 1], kStrideHid);
+        relu_to_a(acc, h[l]);
+    }
+    float out[6][4];
+    init_bias(out, s.bias + 4 * kHid);
+    layer_mma<6, 4>(out, h[3], s.w4, kStrideHid);
+    // layer inputs, transposed
+    store_a_t<5>(tb.actT[0], tb.rows, r0, a0, n);
+#pragma unroll
+    for (int l = 1; l < kLayers; ++l) store_a_t<4>(tb.actT[l], tb.rows, r0, h[l - 1], n);
+    // loss gradient, one row per lane
+#pragma unroll
+    for (int nt = 0; nt < 6; ++nt) {
+        const int c = 8 * nt + 2 * tig;
+        yw[g * kOut + c] = out[nt][0];
+        yw[g * kOut + c + 1] = out[nt][1];
+        yw[(g + 8) * kOut + c] = out[nt][2];
+        yw[(g + 8) * kOut + c + 1] = out[nt][3];
+    }
+    __syncwarp();
+    float dyrow[kGuideOut];
+    if (lane < 16) {
+        const uint32_t r = r0 + lane;
+        float lq = 0.0f;
+        if (r < n) {
+            const float wm = *weight_mean;
+            const float c = wm > 0.0f ? weight[r] / wm : 0.0f;
+            lq = guide_loss_grad(yw + lane * kOut, sdir[3 * (size_t)r], sdir[3 * (size_t)r + 1], sdir[3 * (size_t)r + 2],
+                                 c / (float)n, dyrow);
+            atomicAdd(loss, -c * lq / (float)n);
+        } else {
+            for (int i = 0; i < kGuideOut; ++i) dyrow[i] = 0.0f;
+        }
+    }
+    __syncwarp();
+    if (lane < 16) {
+        for (int i = 0; i < kGuideOut; ++i) yw[lane * kOut + i] = dyrow[i];
+        for (int i = kGuideOut; i < kOut; ++i) yw[lane * kOut + i] = 0.0f;
+    }
+    __syncwarp();
+    float dy[6][4];
+#pragma unroll
+    for (int nt = 0; nt < 6; ++nt) {
+        const int c = 8 * nt + 2 * tig;
+        dy[nt][0] = yw[g * kOut + c];
+        dy[nt][1] = yw[g * kOut + c + 1];
+        dy[nt][2] = yw[(g + 8) * kOut + c];
+        dy[nt][3] = yw[(g + 8) * kOut + c + 1];
+    }
+    store_t<6>(tb.deltaT[4], tb.rows, r0, dy, n, kOut);
+    // delta of h4 = (dy W4) * relu'(h4): A = dy (K = 48), B[k][n] = W4[k][n] = W4T[n][k]
+    uint32_t dhi3[3][4], dlo3[3][4];
+    {
+        uint32_t dummy[4][4] = {};
+        delta_frags<3, false>(dy, dummy, dhi3, dlo3);
+    }
+    float dacc[8][4];
+#pragma unroll
+    for (int nt = 0; nt < 8; ++nt) dacc[nt][0] = dacc[nt][1] = dacc[nt][2] = dacc[nt][3] = 0.0f;
+    layer_mma<8, 3>(dacc, dhi3, t.t4, kStrideOutT);
+    layer_mma<8, 3>(dacc, dlo3, t.t4, kStrideOutT);
+    uint32_t dhi[4][4], dlo[4][4];
+#pragma unroll
+    for (int l = 3; l >= 1; --l) {
+        delta_frags<4, true>(dacc, h[l], dhi, dlo);  // masks dacc in place by relu'(h_l)
+        store_t<8>(tb.deltaT[l], tb.rows, r0, dacc, n, kHid);
+#pragma unroll
+        for (int nt = 0; nt < 8; ++nt) dacc[nt][0] = dacc[nt][1] = dacc[nt][2] = dacc[nt][3] = 0.0f;
+        layer_mma<8, 4>(dacc, dhi, t.t[l - 1], kStrideHid);
+        layer_mma<8, 4>(dacc, dlo, t.t[l - 1], kStrideHid);
+    }
+    delta_frags<4, true>(dacc, h[0], dhi, dlo);
+    store_t<8>(tb.deltaT[0], tb.rows, r0, dacc, n, kHid);
+}
+
+// Weight gradients of layer l: dW[o][i] += sum over rows of deltaT[o][r] actT[i][r]
+// (tensor cores, K = rows; delta as BF16 high + low parts), bias gradient
+// db[o] += sum deltaT[o][r]. One warp per (16 outputs, 512-row chunk); 8 column
+// tiles of inputs per pass.
+__global__ void __launch_bounds__(32) k_guide_wgrad(int l, TrainBuffers tb, uint32_t n, float *grad)
+{
+    const int lane = threadIdx.x & 31, g = lane >> 2, tig = lane & 3;
+    const int fan_in = l == 0 ? kIn : kHid;
+    const int o0 = 16 * blockIdx.x;
+    const uint32_t k0 = 512 * blockIdx.y, k1 = min(n, k0 + 512);
+    const float *dT = tb.deltaT[l];
+    const __nv_bfloat16 *aT = tb.actT[l];
+    const uint32_t stride = tb.rows;
+    const int nin_tiles = fan_in / 8;
+    for (int nt0 = 0; nt0 < nin_tiles; nt0 += 5) {
+        const int ntiles = min(5, nin_tiles - nt0);
+        float acc[5][4] = {};
+        for (uint32_t k = k0; k < k1; k += 16) {
+            // A[m = o][k = row]: a0 (o0+g, k+2tig..+1), a1 (o0+g+8, ...), a2 (o0+g, k+8+2tig..), a3 (o0+g+8, k+8+..)
+            uint32_t ahi[4], alo[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int o = o0 + g + ((q & 1) ? 8 : 0);
+                const uint32_t kk = k + 2 * tig + ((q & 2) ? 8 : 0);
+                const float v0 = kk < k1 ? dT[(size_t)o * stride + kk] : 0.0f;
+                const float v1 = kk + 1 < k1 ? dT[(size_t)o * stride + kk + 1] : 0.0f;
+                const __nv_bfloat162 hb = __floats2bfloat162_rn(v0, v1);
+                const float2 hf = __bfloat1622float2(hb);
+                ahi[q] = *reinterpret_cast<const uint32_t *>(&hb);
+                alo[q] = pack_bf16(v0 - hf.x, v1 - hf.y);
+            }
+            for (int j = 0; j < ntiles; ++j) {
+                const int i = 8 * (nt0 + j) + g;
+                const uint32_t kk = k + 2 * tig;
+                uint32_t b0 = 0, b1 = 0;
+                const __nv_bfloat16 *col = aT + (size_t)i * stride;
+                if (kk + 1 < k1) b0 = ld_pair(col + kk);
+                else if (kk < k1) b0 = (uint32_t) * reinterpret_cast<const uint16_t *>(col + kk);
+                if (kk + 9 < k1) b1 = ld_pair(col + kk + 8);
+                else if (kk + 8 < k1) b1 = (uint32_t) * reinterpret_cast<const uint16_t *>(col + kk + 8);
+                mma_bf16(acc[j], ahi, b0, b1);
+                mma_bf16(acc[j], alo, b0, b1);
+            }
+        }
+        for (int j = 0; j < ntiles; ++j) {
+            const int i = 8 * (nt0 + j) + 2 * tig;
+            float *G = grad + w_off(l);
+            atomicAdd(&G[(o0 + g) * fan_in + i], acc[j][0]);
+            atomicAdd(&G[(o0 + g) * fan_in + i + 1], acc[j][1]);
+            atomicAdd(&G[(o0 + g + 8) * fan_in + i], acc[j][2]);
+            atomicAdd(&G[(o0 + g + 8) * fan_in + i + 1], acc[j][3]);
+        }
+    }
+    // bias gradient: lanes 0..15 sum the chunk's rows of outputs o0 + lane
+    if (lane < 16) {
+        float s = 0.0f;
+        const float *row = dT + (size_t)(o0 + lane) * stride;
+        for (uint32_t k = k0; k < k1; ++k) s += row[k];
+        atomicAdd(grad + b_off(l) + o0 + lane, s);
+    }
+}
+
+__global__ void k_guide_weight_mean(const float *w, uint32_t n, float *mean)
+{
+    __shared__ float part[256];
+    float s = 0.0f;
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) s += w[i];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) part[threadIdx.x] += part[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *mean = n ? part[0] / (float)n : 0.0f;
+}
+
+__global__ void k_guide_adam(float *params, float *m, float *v, const float *grad, int t, float lr, float b1, float b2,
+                             float eps, __nv_bfloat16 *wb)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kNumParams) return;
+    const float g = grad[i];
+    const float mi = b1 * m[i] + (1.0f - b1) * g;
+    const float vi = b2 * v[i] + (1.0f - b2) * g * g;
+    m[i] = mi;
+    v[i] = vi;
+    const float c1 = 1.0f - powf(b1, (float)t), c2 = 1.0f - powf(b2, (float)t);
+    const float p = params[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    params[i] = p;
+    // BF16 weight copy (biases stay FP32)
+    for (int l = 0; l < kLayers; ++l)
+        if (i >= w_off(l) && i < b_off(l)) wb[wb_off(l) + (i - w_off(l))] = __float2bfloat16_rn(p);
+}
+
+__global__ void k_guide_export(const float *params, __nv_bfloat16 *wb)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kNumParams) return;
+    for (int l = 0; l < kLayers; ++l)
+        if (i >= w_off(l) && i < b_off(l)) wb[wb_off(l) + (i - w_off(l))] = __float2bfloat16_rn(params[i]);
+}
+
+// The network input of each row (80 columns), as the forward pass forms it
+// before rounding to BF16.
+__global__ void k_guide_encode(GuideParams gp, const float *pos, const float *dir, uint32_t n, float *out)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n * 40u) return;
+    const uint32_t r = i / 40, c = 2 * (i % 40);
+    float p[3], d[3];
+    uint32_t slot;
+    load_row(pos, dir, nullptr, n, r, gp, p, d, slot);
+    float v0, v1;
+    encode_pair(p, d, (int)c, v0, v1);
+    out[(size_t)r * kIn + c] = v0;
+    out[(size_t)r * kIn + c + 1] = v1;
+}
+
+__global__ void k_guide_sample(const float *y, const float *u, uint32_t n, float *dir, float *pdf)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const GuideLobes L = guide_decode(y + (size_t)i * kGuideOut);
+    float wx, wy, wz;
+    guide_sample(L, u[3 * (size_t)i], u[3 * (size_t)i + 1], u[3 * (size_t)i + 2], wx, wy, wz);
+    dir[3 * (size_t)i] = wx, dir[3 * (size_t)i + 1] = wy, dir[3 * (size_t)i + 2] = wz;
+    pdf[i] = guide_pdf(L, wx, wy, wz);
+}
+
+__global__ void k_guide_pdf(const float *y, const float *dir, uint32_t n, uint32_t y_stride, float *pdf)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const GuideLobes L = guide_decode(y + (size_t)(y_stride ? i : 0) * kGuideOut);
+    pdf[i] = guide_pdf(L, dir[3 * (size_t)i], dir[3 * (size_t)i + 1], dir[3 * (size_t)i + 2]);
+}
+
+constexpr size_t kInferSmem = sizeof(SmemWeights);
+constexpr size_t kTrainSmem = sizeof(SmemWeights) + sizeof(SmemWeightsT) + 4 * 16 * kOut * sizeof(float);
+
+}  // namespace
+}  // namespace dr
+
+struct dr_guide {
+    dr_context *ctx = nullptr;
+    dr_guide_config cfg{};
+    float *params = nullptr, *m = nullptr, *v = nullptr, *grad = nullptr;
+    __nv_bfloat16 *wb = nullptr;
+    float *scalars = nullptr;  // [0] weight mean, [1] loss
+    dr::TrainBuffers tb{};
+    void *tb_mem = nullptr;
+    uint32_t capacity = 0;
+    int step = 0;
+};
+
+using namespace dr;
+
+namespace {
+
+GuideParams guide_params(const dr_guide *g)
+{
+    GuideParams p{};
+    for (int a = 0; a < 3; ++a) p.center[a] = g->cfg.center[a];
+    p.half = g->cfg.half_extent > 0.0f ? g->cfg.half_extent : 1.0f;
+    return p;
+}
+
+void free_guide(dr_guide *g)
+{
+    if (!g) return;
+    cudaFree(g->params);
+    cudaFree(g->m);
+    cudaFree(g->v);
+    cudaFree(g->grad);
+    cudaFree(g->wb);
+    cudaFree(g->scalars);
+    cudaFree(g->tb_mem);
+    delete g;
+}
+
+dr_status ensure_train_capacity(dr_guide *g, uint32_t n)
+{
+    if (n <= g->capacity) return DR_OK;
+    DR_CUDA(cudaDeviceSynchronize());
+    cudaFree(g->tb_mem);
+    g->tb_mem = nullptr;
+    g->capacity = 0;
+    const uint32_t rows = (n + 63) & ~63u;
+    size_t bytes = 0;
+    for (int l = 0; l < kLayers; ++l) bytes += (size_t)fan_out(l) * rows * 4 + (size_t)fan_in(l) * rows * 2 + 512;
+    DR_CUDA(cudaMalloc(&g->tb_mem, bytes));
+    char *p = static_cast<char *>(g->tb_mem);
+    for (int l = 0; l < kLayers; ++l) {
+        g->tb.deltaT[l] = reinterpret_cast<float *>(p);
+        p += ((size_t)fan_out(l) * rows * 4 + 255) & ~size_t(255);
+        g->tb.actT[l] = reinterpret_cast<__nv_bfloat16 *>(p);
+        p += ((size_t)fan_in(l) * rows * 2 + 255) & ~size_t(255);
+    }
+    g->tb.rows = rows;
+    g->capacity = rows;
+    return DR_OK;
+}
+
+// loss and gradients (grad buffer) of one batch
+dr_status run_gradients(dr_guide *g, const float *pos, const float *dir, const float *sdir, const float *weight,
+                        uint32_t n, cudaStream_t st)
+{
+    dr_status r = ensure_train_capacity(g, n);
+    if (r != DR_OK) return r;
+    DR_CUDA(cudaMemsetAsync(g->grad, 0, kNumParams * sizeof(float), st));
+    DR_CUDA(cudaMemsetAsync(g->scalars + 1, 0, sizeof(float), st));
+    k_guide_weight_mean<<<1, 256, 0, st>>>(weight, n, g->scalars);
+    const GuideParams gp = guide_params(g);
+    k_guide_train_fb<<<(n + 63) / 64, 128, kTrainSmem, st>>>(g->wb, g->params, gp, pos, dir, sdir, weight, n,
+                                                             g->scalars, g->tb, g->scalars + 1);
+    for (int l = 0; l < kLayers; ++l) {
+        const dim3 grid(fan_out(l) / 16, (n + 511) / 512);
+        k_guide_wgrad<<<grid, 32, 0, st>>>(l, g->tb, n, g->grad);
+    }
+    DR_CUDA(cudaGetLastError());
+    return DR_OK;
+}
+
+}  // namespace
+
+namespace dr {
+
+cudaError_t launch_guide_infer(const dr_guide *g, const float *pos, const float *dir, const uint32_t *list,
+                               const uint32_t *count, uint32_t max_rows, float *y, cudaStream_t st)
+{
+    if (max_rows == 0) return cudaSuccess;
+    const unsigned tiles = (max_rows + 15) / 16;
+    const unsigned blocks = std::min<unsigned>((tiles + 3) / 4, (unsigned)g->ctx->num_sms * 4);
+    k_guide_infer<<<blocks, 128, kInferSmem, st>>>(g->wb, g->params, guide_params(g), pos, dir, list, count, max_rows, y);
+    return cudaGetLastError();
+}
+
+dr_status guide_train_step(dr_guide *g, const float *pos, const float *dir, const float *sdir, const float *weight,
+                           uint32_t n, cudaStream_t st)
+{
+    return dr_guide_train_step(g, pos, dir, sdir, weight, n, st);
+}
+
+}  // namespace dr
+
+extern "C" {
+
+uint32_t dr_guide_num_params(void) { return (uint32_t)kNumParams; }
+
+dr_status dr_guide_create(dr_context *ctx, const dr_guide_config *cfg, dr_guide **out)
+{
+    DR_CHECK_ARG(ctx && out, "dr_guide_create: NULL argument");
+    *out = nullptr;
+    DR_CUDA(cudaSetDevice(ctx->device));
+    static bool attr = false;
+    if (!attr) {
+        DR_CUDA(cudaFuncSetAttribute(k_guide_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kInferSmem));
+        DR_CUDA(cudaFuncSetAttribute(k_guide_train_fb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTrainSmem));
+        attr = true;
+    }
+    auto *g = new (std::nothrow) dr_guide;
+    if (!g) return fail(DR_ERR_OUT_OF_MEMORY, "dr_guide_create: host allocation failed");
+    g->ctx = ctx;
+    if (cfg) g->cfg = *cfg;
+    if (g->cfg.learning_rate <= 0.0f) g->cfg.learning_rate = 1e-3f;
+    if (g->cfg.beta1 <= 0.0f) g->cfg.beta1 = 0.9f;
+    if (g->cfg.beta2 <= 0.0f) g->cfg.beta2 = 0.999f;
+    if (g->cfg.epsilon <= 0.0f) g->cfg.epsilon = 1e-8f;
+    if (g->cfg.half_extent <= 0.0f) g->cfg.half_extent = 1.0f;
+    cudaError_t e;
+    if ((e = cudaMalloc(&g->params, kNumParams * 4)) != cudaSuccess || (e = cudaMalloc(&g->m, kNumParams * 4)) != cudaSuccess ||
+        (e = cudaMalloc(&g->v, kNumParams * 4)) != cudaSuccess || (e = cudaMalloc(&g->grad, kNumParams * 4)) != cudaSuccess ||
+        (e = cudaMalloc(&g->wb, kNumWeights * 2)) != cudaSuccess || (e = cudaMalloc(&g->scalars, 16)) != cudaSuccess ||
+        (e = cudaMemset(g->m, 0, kNumParams * 4)) != cudaSuccess || (e = cudaMemset(g->v, 0, kNumParams * 4)) != cudaSuccess ||
+        (e = cudaMemset(g->scalars, 0, 16)) != cudaSuccess) {
+        free_guide(g);
+        return cuda_fail(e, "dr_guide_create");
+    }
+    // He-uniform initialisation (ReLU), last layer scaled by 0.1, zero biases
+    std::mt19937_64 rng(g->cfg.seed);
+    std::vector<float> p(kNumParams, 0.0f);
+    for (int l = 0; l < kLayers; ++l) {
+        const float bound = std::sqrt(6.0f / (float)fan_in(l)) * (l == kLayers - 1 ? 0.1f : 1.0f);
+        std::uniform_real_distribution<float> U(-bound, bound);
+        for (int i = 0; i < fan_out(l) * fan_in(l); ++i) p[w_off(l) + i] = U(rng);
+    }
+    const dr_status r = dr_guide_set_params(g, p.data(), kNumParams);
+    if (r != DR_OK) {
+        free_guide(g);
+        return r;
+    }
+    *out = g;
+    return DR_OK;
+}
+
+dr_status dr_guide_destroy(dr_guide *g)
+{
+    if (!g) return DR_OK;
+    cudaSetDevice(g->ctx->device);
+    cudaDeviceSynchronize();
+    free_guide(g);
+    return DR_OK;
+}
+
+dr_status dr_guide_set_params(dr_guide *g, const float *host, uint32_t n)
+{
+    DR_CHECK_ARG(g && host && n == (uint32_t)kNumParams, "dr_guide_set_params: bad argument");
+    DR_CUDA(cudaSetDevice(g->ctx->device));
+    DR_CUDA(cudaMemcpy(g->params, host, kNumParams * 4, cudaMemcpyHostToDevice));
+    DR_CUDA(cudaMemset(g->m, 0, kNumParams * 4));
+    DR_CUDA(cudaMemset(g->v, 0, kNumParams * 4));
+    g->step = 0;
+    k_guide_export<<<(kNumParams + 255) / 256, 256>>>(g->params, g->wb);
+    DR_CUDA(cudaGetLastError());
+    DR_CUDA(cudaDeviceSynchronize());
+    return DR_OK;
+}
+
+dr_status dr_guide_get_params(dr_guide *g, float *host, uint32_t n)
+{
+    DR_CHECK_ARG(g && host && n == (uint32_t)kNumParams, "dr_guide_get_params: bad argument");
+    DR_CUDA(cudaSetDevice(g->ctx->device));
+    DR_CUDA(cudaDeviceSynchronize());
+    DR_CUDA(cudaMemcpy(host, g->params, kNumParams * 4, cudaMemcpyDeviceToHost));
+    return DR_OK;
+}
+
+dr_status dr_guide_infer(dr_guide *g, const float *pos_dev, const float *dir_dev, uint32_t n, float *y_dev, void *stream)
+{
+    DR_CHECK_ARG(g && (n == 0 || (pos_dev && dir_dev && y_dev)), "dr_guide_infer: NULL argument");
+    if (n == 0) return DR_OK;
+    DR_CUDA(cudaSetDevice(g->ctx->device));
+    const unsigned tiles = (n + 15) / 16;
+    const unsigned blocks = std::min<unsigned>((tiles + 3) / 4, (unsigned)g->ctx->num_sms * 8);
+    k_guide_infer<<<blocks, 128, kInferSmem, static_cast<cudaStream_t>(stream)>>>(
+        g->wb, g->params, guide_params(g), pos_dev, dir_dev, nullptr, nullptr, n, y_dev);
+    DR_CUDA(cudaGetLastError());
+    return DR_OK;
+}
+
+dr_status dr_guide_gradients(dr_guide *g, const float *pos_dev, const float *dir_dev, const float *sdir_dev,
+                             const float *weight_dev, uint32_t n, float *loss_host, float *grad_host)
+{
+    DR_CHECK_ARG(g && n > 0 && pos_dev && dir_dev && sdir_dev && weight_dev, "dr_guide_gradients: bad argument");
+    DR_CUDA(cudaSetDevice(g->ctx->device));
+    dr_status r = run_gradients(g, pos_dev, dir_dev, sdir_dev, weight_dev, n, nullptr);
+    if (r != DR_OK) return r;
+    DR_CUDA(cudaDeviceSynchronize());
+    if (loss_host) DR_CUDA(cudaMemcpy(loss_host, g->scalars + 1, 4, cudaMemcpyDeviceToHost));
+    if (grad_host) DR_CUDA(cudaMemcpy(grad_host, g->grad, kNumParams * 4, cudaMemcpyDeviceToHost));
+    return DR_OK;
+}
+
+dr_status dr_guide_train_step(dr_guide *g, const float *pos_dev, const float *dir_dev, const float *sdir_dev,
+                              const float *weight_dev, uint32_t n, void *stream)
+{
+    DR_CHECK_ARG(g && pos_dev && dir_dev && sdir_dev && weight_dev, "dr_guide_train_step: NULL argument");
+    if (n == 0) return DR_OK;
+    DR_CUDA(cudaSetDevice(g->ctx->device));
+    auto st = static_cast<cudaStream_t>(stream);
+    dr_status r = run_gradients(g, pos_dev, dir_dev, sdir_dev, weight_dev, n, st);
+    if (r != DR_OK) return r;
+    ++g->step;
+    k_guide_adam<<<(kNumParams + 255) / 256, 256, 0, st>>>(g->params, g->m, g->v, g->grad, g->step, g->cfg.learning_rate,
+                                                           g->cfg.beta1, g->cfg.beta2, g->cfg.epsilon, g->wb);
+    DR_CUDA(cudaGetLastError());
+    return DR_OK;
+}
+
+dr_status dr_guide_encode(dr_guide *g, const float *pos_dev, const float *dir_dev, uint32_t n, float *out_dev)
+{
+    DR_CHECK_ARG(g && (n == 0 || (pos_dev && dir_dev && out_dev)), "dr_guide_encode: NULL argument");
+    if (n == 0) return DR_OK;
+    DR_CUDA(cudaSetDevice(g->ctx->device));
+    k_guide_encode<<<(n * 40 + 255) / 256, 256>>>(guide_params(g), pos_dev, dir_dev, n, out_dev);
+    DR_CUDA(cudaGetLastError());
+    return DR_OK;
+}
+
+dr_status dr_guide_mixture_sample(const float *y_dev, const float *u_dev, uint32_t n, float *dir_dev, float *pdf_dev,
+                                  void *stream)
+{
+    DR_CHECK_ARG(n == 0 || (y_dev && u_dev && dir_dev && pdf_dev), "dr_guide_mixture_sample: NULL argument");
+    if (n == 0) return DR_OK;
+    k_guide_sample<<<(n + 255) / 256, 256, 0, static_cast<cudaStream_t>(stream)>>>(y_dev, u_dev, n, dir_dev, pdf_dev);
+    DR_CUDA(cudaGetLastError());
+    return DR_OK;
+}
+
+dr_status dr_guide_mixture_pdf(const float *y_dev, uint32_t y_per_row, const float *dir_dev, uint32_t n, float *pdf_dev,
+                               void *stream)
+{
+    DR_CHECK_ARG(n == 0 || (y_dev && dir_dev && pdf_dev), "dr_guide_mixture_pdf: NULL argument");
+    if (n == 0) return DR_OK;
+    k_guide_pdf<<<(n + 255) / 256, 256, 0, static_cast<cudaStream_t>(stream)>>>(y_dev, dir_dev, n, y_per_row, pdf_dev);
+    DR_CUDA(cudaGetLastError());
+    return DR_OK;
+}
+
+dr_status dr_guide_last_loss(dr_guide *g, float *loss_host)
+{
+    DR_CHECK_ARG(g && loss_host, "dr_guide_last_loss: NULL argument");
+    DR_CUDA(cudaSetDevice(g->ctx->device));
+    DR_CUDA(cudaMemcpy(loss_host, g->scalars + 1, 4, cudaMemcpyDeviceToHost));
+    return DR_OK;
+}
+
+}  // extern "C"

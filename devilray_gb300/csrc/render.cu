@@ -25,6 +25,8 @@
 #include "ptmath.cuh"
 #include "trace_device.cuh"
 #include "persistent.cuh"
+#include "guide_math.cuh"
+#include "guide_internal.h"
 
 #include <algorithm>
 
@@ -59,7 +61,26 @@ struct RenderParams {
     uint32_t *shadow_list;
     uint32_t *counts;          // [0, 64): active paths per bounce, [64, 128): shadow rays per bounce
     unsigned long long *work;  // persistent-kernel counters: [b] closest hit, [64 + b] shadow rays
+    // path guiding (guided kernels only)
+    float *guide_y;            // [slot][40] network output at the slot's current vertex
+    float *guide_pos, *guide_nrm;  // [slot][3] network inputs
+    uint32_t *guide_list;      // slots with a diffuse vertex this bounce
+    uint32_t *guide_counts;    // [b] length of guide_list
+    float *prev_pdf;           // [slot] solid-angle density of the last sampled diffuse direction
+    float *rec;                // [slot][kGuideRecords][kRecFloats] training records
+    uint32_t *rec_n;           // [slot] records; bit 31: the last one waits for its radiance
+    float guide_alpha;         // probability of sampling the network's mixture
+    float *train_pos, *train_nrm, *train_dir, *train_w;  // training ring
+    uint32_t *train_head;
+    uint32_t train_cap;
 };
+
+// A training record of a diffuse vertex: position, normal, sampled
+// direction, its density, luminance of the throughput after the vertex, and
+// luminance of the path's colour when the next vertex is reached.
+constexpr int kGuideRecords = 3;
+constexpr int kRecFloats = 12;
+constexpr uint32_t kRecOpen = 0x80000000u;
 
 struct F3 {
     float x, y, z;
@@ -187,6 +208,7 @@ __global__ void __launch_bounds__(kRenderBlock) k_camera(RenderParams p)
     p.slot_job[i] = sg.job;
     p.slot_pix[i] = pixel;
     p.slot_sample[i] = sample;
+    if (p.rec_n) p.rec_n[i] = 0;
     p.list[0][i] = i;
 }
 
@@ -340,6 +362,7 @@ __device__ __forceinline__ float object_ior(const RenderParams &p, int obj)
     return m.kind == DR_MAT_DIELECTRIC ? m.ior : 1.0f;
 }
 
+template <bool GUIDED>
 __global__ void __launch_bounds__(kRenderBlock) k_shade(RenderParams p, int b)
 {
     const uint32_t count = p.counts[b];
@@ -350,12 +373,21 @@ __global__ void __launch_bounds__(kRenderBlock) k_shade(RenderParams p, int b)
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = warp_first; base < count; base += stride) {
         const uint32_t i = base + (threadIdx.x & 31);
-        bool keep = false, shadow = false;
+        bool keep = false, shadow = false, dead = false;
         uint32_t slot = 0;
         if (i < count) {
             slot = list[i];
             p.casts[slot] += 1;
             const RenderJob &J = p.jobs[p.slot_job[slot]];
+            if (GUIDED) {
+                // the radiance gathered before this vertex closes the last record
+                const uint32_t rn = p.rec_n[slot];
+                if (rn & kRecOpen) {
+                    const uint32_t r = (rn & ~kRecOpen) - 1;
+                    p.rec[((size_t)slot * kGuideRecords + r) * kRecFloats + 11] = luminance(p.color[slot]);
+                    p.rec_n[slot] = rn & ~kRecOpen;
+                }
+            }
             const float2 h = p.hits[slot];
             const int prim = __float_as_int(h.y);
             if (prim >= 0) {
@@ -392,13 +424,16 @@ __global__ void __launch_bounds__(kRenderBlock) k_shade(RenderParams p, int b)
                     } else {
                         const float4 pn4 = p.prev_n[slot];
                         const F3 pp = f3(pp4.x, pp4.y, pp4.z), pn = f3(pn4.x, pn4.y, pn4.z);
-                        const float pdf_bsdf = cosine_pdf(pp, hp, pn);
+                        // guided: the density of the direction actually sampled there
+                        const float pdf_bsdf = GUIDED ? p.prev_pdf[slot] : cosine_pdf(pp, hp, pn);
                         const float L = luminance(mul4s(E, kPi));
                         const float pdf_area = L / J.total_power;
                         const float pdf_nee = pdf_area * area_to_solid_angle(pp, hp, n);
                         if (pdf_bsdf + pdf_nee > 0)
                             col = add4(col, mul4s(mul4(E, thr), power_heuristic(pdf_bsdf, pdf_nee)));
                     }
+                    GuideLobes lobes;
+                    if (GUIDED) lobes = guide_decode(p.guide_y + (size_t)slot * kGuideOut);
                     // next-event estimation: samplePointOnLights (:234-272) and
                     // evaluateDirectLighting (:336-361); visibility is the shadow ray
                     if (J.lights) {
@@ -429,7 +464,12 @@ __global__ void __launch_bounds__(kRenderBlock) k_shade(RenderParams p, int b)
                         const float lpdf = opdf * tpdf / area;
                         lp = f3(lp.x * 1.0f + 0.0f, lp.y * 1.0f + 0.0f, lp.z * 1.0f + 0.0f);
                         const dr_material &LM = p.materials[ob.material];
-                        const float nee_pdf_bsdf = cosine_pdf(hp, lp, n);
+                        float nee_pdf_bsdf = cosine_pdf(hp, lp, n);
+                        if (GUIDED) {
+                            const F3 wl0 = normalized(sub(lp, hp));
+                            nee_pdf_bsdf = p.guide_alpha * guide_pdf(lobes, wl0.x, wl0.y, wl0.z) +
+                                           (1.0f - p.guide_alpha) * nee_pdf_bsdf;
+                        }
                         const float nee_pdf_nee = lpdf * area_to_solid_angle(hp, lp, ln);
                         const float dist = length(sub(lp, hp));
                         const F3 wl = divs(sub(lp, hp), dist);
@@ -451,15 +491,46 @@ __global__ void __launch_bounds__(kRenderBlock) k_shade(RenderParams p, int b)
                             shadow = true;
                         }
                     }
-                    // cosineWeightedHemisphereSample (DistributionSamplers.hpp:33-42)
-                    const float theta0 = 2 * kPi * u[0];
-                    const float theta1 = pt::acos(1 - 2 * u[1]);
-                    float sn0, cs0, sn1, cs1;
-                    pt::sincos(theta0, sn0, cs0);
-                    pt::sincos(theta1, sn1, cs1);
-                    const F3 sph = f3(sn1 * sn0, sn1 * cs0, cs1);
-                    new_v = normalized(add(sph, normal));
-                    thr = mul4(thr, alb);
+                    if (GUIDED && !J.lights) uniforms4(J, pixel, sample, g + 2, u + 8);
+                    bool cosine = true;
+                    if (GUIDED && u[9] < p.guide_alpha) {
+                        cosine = false;
+                        float wx, wy, wz;
+                        guide_sample(lobes, u[10], u[0], u[1], wx, wy, wz);
+                        new_v = f3(wx, wy, wz);
+                    }
+                    if (cosine) {
+                        // cosineWeightedHemisphereSample (DistributionSamplers.hpp:33-42)
+                        const float theta0 = 2 * kPi * u[0];
+                        const float theta1 = pt::acos(1 - 2 * u[1]);
+                        float sn0, cs0, sn1, cs1;
+                        pt::sincos(theta0, sn0, cs0);
+                        pt::sincos(theta1, sn1, cs1);
+                        const F3 sph = f3(sn1 * sn0, sn1 * cs0, cs1);
+                        new_v = normalized(add(sph, normal));
+                    }
+                    if (GUIDED) {
+                        // one-sample MIS over the mixture and the cosine lobe: f cos / pdf_mix
+                        const float c = dot(new_v, n);
+                        const float pdf_mix = p.guide_alpha * guide_pdf(lobes, new_v.x, new_v.y, new_v.z) +
+                                              (1.0f - p.guide_alpha) * fmaxf(c, 0.0f) / kPi;
+                        const float f = c > 0.0f && pdf_mix > 0.0f ? c / (kPi * pdf_mix) : 0.0f;
+                        thr = mul4s(mul4(thr, alb), f);
+                        p.prev_pdf[slot] = pdf_mix;
+                        if (f == 0.0f) dead = true;
+                        const uint32_t rn = p.rec_n[slot];
+                        if (!dead && rn < (uint32_t)kGuideRecords && b + 1 < (int)J.max_depth) {
+                            float *rc = p.rec + ((size_t)slot * kGuideRecords + rn) * kRecFloats;
+                            rc[0] = hp.x, rc[1] = hp.y, rc[2] = hp.z;
+                            rc[3] = n.x, rc[4] = n.y, rc[5] = n.z;
+                            rc[6] = new_v.x, rc[7] = new_v.y, rc[8] = new_v.z;
+                            rc[9] = pdf_mix;
+                            rc[10] = luminance(thr);
+                            p.rec_n[slot] = (rn + 1) | kRecOpen;
+                        }
+                    } else {
+                        thr = mul4(thr, alb);
+                    }
                     new_o = hp;
                     p.prev_p[slot] = make_float4(hp.x, hp.y, hp.z, 1.0f);
                     p.prev_n[slot] = make_float4(n.x, n.y, n.z, 0.0f);
@@ -513,11 +584,79 @@ __global__ void __launch_bounds__(kRenderBlock) k_shade(RenderParams p, int b)
                 p.rays[2 * slot + 1] = make_float4(new_v.x, new_v.y, new_v.z, 0.0f);
                 p.thr[slot] = thr;
                 p.color[slot] = col;
-                keep = b + 1 < (int)J.max_depth;
+                keep = b + 1 < (int)J.max_depth && !dead;
             }
         }
         warp_append(keep, slot, next_list, p.counts + b + 1);
         warp_append(shadow, slot, p.shadow_list, p.counts + 64 + b);
+    }
+}
+
+// Network inputs of the bounce's diffuse vertices (hit point, normal facing
+// the incoming ray, as the shading computes them) and their slot list.
+__global__ void __launch_bounds__(kRenderBlock) k_guide_prepare(RenderParams p, int b)
+{
+    const uint32_t count = p.counts[b];
+    const uint32_t *list = p.list[b & 1];
+    const uint32_t warp_first = (blockIdx.x * blockDim.x + (threadIdx.x & ~31u));
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t base = warp_first; base < count; base += stride) {
+        const uint32_t i = base + (threadIdx.x & 31);
+        bool diffuse = false;
+        uint32_t slot = 0;
+        if (i < count) {
+            slot = list[i];
+            const float2 h = p.hits[slot];
+            const int prim = __float_as_int(h.y);
+            if (prim >= 0) {
+                const float4 s0 = __ldg(p.shade + 3 * prim), s1 = __ldg(p.shade + 3 * prim + 1),
+                             s2 = __ldg(p.shade + 3 * prim + 2);
+                const dr_material &M = p.materials[__float_as_int(s2.z)];
+                if (M.kind == DR_MAT_DIFFUSE) {
+                    diffuse = true;
+                    const float4 r0 = p.rays[2 * slot], r1 = p.rays[2 * slot + 1];
+                    const F3 ro = f3(r0.x, r0.y, r0.z), rv = f3(r1.x, r1.y, r1.z);
+                    const F3 A = f3(s0.x, s0.y, s0.z), B = f3(s0.w, s1.x, s1.y), C = f3(s1.z, s1.w, s2.x);
+                    F3 n = normalized(cross(sub(A, B), sub(A, C)));
+                    if (dot(n, rv) > 0) n = mul(n, -1.0f);
+                    const F3 hp = add(ro, mul(rv, h.x));
+                    float *gp = p.guide_pos + 3 * (size_t)slot, *gn = p.guide_nrm + 3 * (size_t)slot;
+                    gp[0] = hp.x, gp[1] = hp.y, gp[2] = hp.z;
+                    gn[0] = n.x, gn[1] = n.y, gn[2] = n.z;
+                }
+            }
+        }
+        warp_append(diffuse, slot, p.guide_list, p.guide_counts + b);
+    }
+}
+
+// Training samples of the finished wave: for each closed record, the
+// radiance that arrived along the sampled direction, L = (colour at the end -
+// colour when the next vertex was reached) / throughput after the vertex, and
+// the weight L cos / pdf of that direction (target density L cos). Appended
+// to the training ring.
+__global__ void __launch_bounds__(256) k_guide_collect(RenderParams p)
+{
+    const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= p.wave) return;
+    const uint32_t rn = p.rec_n[slot];
+    const uint32_t n = (rn & ~kRecOpen) - ((rn & kRecOpen) ? 1u : 0u);
+    if (n == 0) return;
+    const float cf = luminance(p.color[slot]);
+    for (uint32_t r = 0; r < n; ++r) {
+        const float *rc = p.rec + ((size_t)slot * kGuideRecords + r) * kRecFloats;
+        const float T = rc[10], cn = rc[11];
+        const float L = (cf - cn) / T;
+        const float c = rc[3] * rc[6] + rc[4] * rc[7] + rc[5] * rc[8];
+        const float w = L * fmaxf(c, 0.0f) / rc[9];
+        if (!(T > 0.0f) || !(w > 0.0f) || !isfinite(w)) continue;
+        const uint32_t at = atomicAdd(p.train_head, 1u) % p.train_cap;
+        for (int a = 0; a < 3; ++a) {
+            p.train_pos[3 * (size_t)at + a] = rc[a];
+            p.train_nrm[3 * (size_t)at + a] = rc[3 + a];
+            p.train_dir[3 * (size_t)at + a] = rc[6 + a];
+        }
+        p.train_w[at] = w;
     }
 }
 
@@ -567,12 +706,16 @@ T *carve(char *&ptr, size_t count)
 
 constexpr size_t kSlotBytes = 2 * 16 + 8 + 16 * 5 + 2 * 16 + 16 + 4 * 7;
 
-size_t wave_buffer_bytes(uint32_t W)
+constexpr size_t kGuideSlotBytes = kGuideOut * 4 + 3 * 4 + 3 * 4 + 4 + 4 + kGuideRecords * kRecFloats * 4 + 4;
+
+size_t wave_buffer_bytes(uint32_t W, bool guided)
 {
-    return (size_t)W * kSlotBytes + 128 * sizeof(uint32_t) + 128 * sizeof(unsigned long long) + 20 * 256;
+    return (size_t)W * (kSlotBytes + (guided ? kGuideSlotBytes : 0)) + 192 * sizeof(uint32_t) +
+           128 * sizeof(unsigned long long) + 28 * 256;
 }
 
-RenderParams wave_params(const SceneArrays &sc, const RenderJob *d_jobs, void *buffer, uint32_t W, uint32_t chunk)
+RenderParams wave_params(const SceneArrays &sc, const RenderJob *d_jobs, void *buffer, uint32_t W, uint32_t chunk,
+                         bool guided)
 {
     RenderParams p{};
     p.trace = sc.trace;
@@ -602,6 +745,16 @@ RenderParams wave_params(const SceneArrays &sc, const RenderJob *d_jobs, void *b
     p.shadow_list = carve<uint32_t>(ptr, W);
     p.counts = carve<uint32_t>(ptr, 128);
     p.work = carve<unsigned long long>(ptr, 128);
+    if (guided) {
+        p.guide_y = carve<float>(ptr, (size_t)W * kGuideOut);
+        p.guide_pos = carve<float>(ptr, (size_t)W * 3);
+        p.guide_nrm = carve<float>(ptr, (size_t)W * 3);
+        p.guide_list = carve<uint32_t>(ptr, W);
+        p.prev_pdf = carve<float>(ptr, W);
+        p.rec = carve<float>(ptr, (size_t)W * kGuideRecords * kRecFloats);
+        p.rec_n = carve<uint32_t>(ptr, W);
+        p.guide_counts = carve<uint32_t>(ptr, 64);
+    }
     return p;
 }
 
@@ -656,15 +809,17 @@ WaveRunner::~WaveRunner()
     if (fork) cudaEventDestroy(fork);
     cudaFree(d_jobs);
     cudaFree(d_segs);
+    cudaFree(d_train);
 }
 
 dr_status WaveRunner::prepare(const std::vector<RenderJob> &jobs, const WavePlan &plan, const WaveConfig &cfg,
-                              cudaStream_t st)
+                              cudaStream_t st, const GuideRun *gr)
 {
     const uint32_t nwaves = (uint32_t)plan.wave_slots.size();
-    const int K = (int)std::max<uint32_t>(1, std::min<uint32_t>({cfg.streams, (uint32_t)kMaxWaveStreams, nwaves}));
-    const size_t need = wave_buffer_bytes(plan.max_slots);
-    bool grow = jobs.size() > jobs_capacity || plan.segs.size() > segs_capacity;
+    const int K = gr ? 1 : (int)std::max<uint32_t>(1, std::min<uint32_t>({cfg.streams, (uint32_t)kMaxWaveStreams, nwaves}));
+    const size_t need = wave_buffer_bytes(plan.max_slots, gr != nullptr);
+    const uint32_t train_need = gr ? std::max<uint32_t>(1, gr->batch) * std::max<uint32_t>(1, gr->steps) : 0;
+    bool grow = jobs.size() > jobs_capacity || plan.segs.size() > segs_capacity || train_need > train_cap;
     for (int k = 0; k < K; ++k) grow = grow || wave_bytes[k] < need;
     if (grow) {
         // buffers may still be in use by earlier work on any stream
@@ -691,6 +846,15 @@ dr_status WaveRunner::prepare(const std::vector<RenderJob> &jobs, const WavePlan
             DR_CUDA(cudaMalloc(&d_segs, plan.segs.size() * sizeof(WaveSegment)));
             segs_capacity = plan.segs.size();
         }
+        if (train_need > train_cap) {
+            cudaFree(d_train);
+            d_train = nullptr;
+            train_cap = 0;
+            const size_t bytes = (size_t)train_need * 10 * sizeof(float) + 4 * 256;
+            DR_CUDA(cudaMalloc(&d_train, bytes));
+            DR_CUDA(cudaMemset(d_train, 0, bytes));
+            train_cap = train_need;
+        }
     }
     for (int k = 0; k < K; ++k) {
         if (!stream[k]) DR_CUDA(cudaStreamCreateWithFlags(&stream[k], cudaStreamNonBlocking));
@@ -708,11 +872,23 @@ dr_status WaveRunner::prepare(const std::vector<RenderJob> &jobs, const WavePlan
 }
 
 dr_status WaveRunner::enqueue(const SceneArrays &sc, const WavePlan &plan, const WaveConfig &cfg, int tri_mode,
-                              cudaStream_t st)
+                              cudaStream_t st, const GuideRun *gr)
 {
     const uint32_t nwaves = (uint32_t)plan.wave_slots.size();
     if (nwaves == 0) return DR_OK;
-    const int K = (int)std::max<uint32_t>(1, std::min<uint32_t>({cfg.streams, (uint32_t)kMaxWaveStreams, nwaves}));
+    // a guided render trains between waves: one wave at a time
+    const int K = gr ? 1 : (int)std::max<uint32_t>(1, std::min<uint32_t>({cfg.streams, (uint32_t)kMaxWaveStreams, nwaves}));
+    // training ring (SoA): positions, normals, directions, weights, head counter
+    float *t_pos = nullptr, *t_nrm = nullptr, *t_dir = nullptr, *t_w = nullptr;
+    uint32_t *t_head = nullptr;
+    if (gr) {
+        char *ptr = static_cast<char *>(d_train);
+        t_pos = carve<float>(ptr, (size_t)train_cap * 3);
+        t_nrm = carve<float>(ptr, (size_t)train_cap * 3);
+        t_dir = carve<float>(ptr, (size_t)train_cap * 3);
+        t_w = carve<float>(ptr, train_cap);
+        t_head = carve<uint32_t>(ptr, 1);
+    }
     const int sms = ctx->num_sms;
     static int p8_per_sm = 0;
     if (p8_per_sm == 0) {
@@ -727,7 +903,13 @@ dr_status WaveRunner::enqueue(const SceneArrays &sc, const WavePlan &plan, const
     for (uint32_t w = 0; w < nwaves; ++w) {
         const int k = (int)(w % (uint32_t)K);
         cudaStream_t ws = stream[k];
-        RenderParams q = wave_params(sc, d_jobs, d_wave[k], plan.max_slots, cfg.chunk);
+        RenderParams q = wave_params(sc, d_jobs, d_wave[k], plan.max_slots, cfg.chunk, gr != nullptr);
+        if (gr) {
+            q.guide_alpha = gr->alpha;
+            q.train_pos = t_pos, q.train_nrm = t_nrm, q.train_dir = t_dir, q.train_w = t_w;
+            q.train_head = t_head;
+            q.train_cap = train_cap;
+        }
         q.segs = d_segs + plan.wave_first[w];
         q.nsegs = plan.wave_first[w + 1] - plan.wave_first[w];
         q.wave = plan.wave_slots[w];
@@ -738,6 +920,7 @@ dr_status WaveRunner::enqueue(const SceneArrays &sc, const WavePlan &plan, const
         const unsigned pgrid = (unsigned)std::min<uint64_t>((W + kTraceBlock - 1) / kTraceBlock, (uint64_t)sms * p8_per_sm);
         DR_CUDA(cudaMemsetAsync(q.counts, 0, 128 * sizeof(uint32_t), ws));
         DR_CUDA(cudaMemsetAsync(q.work, 0, 128 * sizeof(unsigned long long), ws));
+        if (gr) DR_CUDA(cudaMemsetAsync(q.guide_counts, 0, 64 * sizeof(uint32_t), ws));
         k_camera<<<(W + kRenderBlock - 1) / kRenderBlock, kRenderBlock, 0, ws>>>(q);
         for (int b = 0; b < (int)plan.max_depth; ++b) {
             if (wide) {
@@ -747,7 +930,14 @@ dr_status WaveRunner::enqueue(const SceneArrays &sc, const WavePlan &plan, const
                 if (wt) k_wave_closest<1, 2><<<trace_grid, kTraceBlock, 0, ws>>>(q, b);
                 else k_wave_closest<0, 2><<<trace_grid, kTraceBlock, 0, ws>>>(q, b);
             }
-            k_shade<<<shade_grid, kRenderBlock, 0, ws>>>(q, b);
+            if (gr) {
+                k_guide_prepare<<<shade_grid, kRenderBlock, 0, ws>>>(q, b);
+                DR_CUDA(launch_guide_infer(gr->guide, q.guide_pos, q.guide_nrm, q.guide_list, q.guide_counts + b, W,
+                                           q.guide_y, ws));
+                k_shade<true><<<shade_grid, kRenderBlock, 0, ws>>>(q, b);
+            } else {
+                k_shade<false><<<shade_grid, kRenderBlock, 0, ws>>>(q, b);
+            }
             if (wide) {
                 if (wt) k_wave_shadow_p8<1><<<pgrid, kTraceBlock, 0, ws>>>(q, b);
                 else k_wave_shadow_p8<0><<<pgrid, kTraceBlock, 0, ws>>>(q, b);
@@ -758,8 +948,16 @@ dr_status WaveRunner::enqueue(const SceneArrays &sc, const WavePlan &plan, const
         }
         // images receive the waves in order
         if (w > 0) DR_CUDA(cudaStreamWaitEvent(ws, acc_done[(w - 1) % (uint32_t)K], 0));
+        if (gr && gr->train) k_guide_collect<<<(W + 255) / 256, 256, 0, ws>>>(q);
         k_accumulate_wave<<<(q.wave_pix + 255) / 256, 256, 0, ws>>>(q);
         DR_CUDA(cudaGetLastError());
+        if (gr && gr->train)
+            for (uint32_t t = 0; t < gr->steps; ++t) {
+                const size_t o = (size_t)t * gr->batch;
+                const dr_status ts = guide_train_step(gr->guide, t_pos + 3 * o, t_nrm + 3 * o, t_dir + 3 * o, t_w + o,
+                                                      gr->batch, ws);
+                if (ts != DR_OK) return ts;
+            }
         DR_CUDA(cudaEventRecord(acc_done[k], ws));
     }
     for (int k = 0; k < K; ++k) DR_CUDA(cudaStreamWaitEvent(st, acc_done[k], 0));
@@ -863,4 +1061,44 @@ extern "C" dr_status dr_render(dr_scene *s, const dr_camera *cam, const dr_rende
     dr_status r = s->runner->prepare(jobs, plan, wc, st);
     if (r != DR_OK) return r;
     return s->runner->enqueue(sc, plan, wc, cfg->tri_mode, st);
+}
+
+extern "C" dr_status dr_render_guided(dr_scene *s, const dr_camera *cam, const dr_render_config *cfg, dr_guide *guide,
+                                      const dr_guided_config *gcfg, float *accum_dev, uint32_t *casts_dev, void *stream)
+{
+    DR_CHECK_ARG(s && cam && cfg && guide && accum_dev, "dr_render_guided: NULL argument");
+    DR_CHECK_ARG(cam->width > 0 && cam->height > 0, "dr_render_guided: empty image");
+    DR_CHECK_ARG(cfg->max_depth >= 1 && cfg->max_depth <= (uint32_t)kMaxRenderDepth,
+                 "dr_render_guided: max_depth must be in [1, 63]");
+    DR_CHECK_ARG(cfg->tri_mode == DR_TRI_REFERENCE || cfg->tri_mode == DR_TRI_WATERTIGHT, "dr_render_guided: bad tri_mode");
+    DR_CHECK_ARG(cfg->debug == DR_DEBUG_OFF, "dr_render_guided: debug views are not guided");
+    DR_CHECK_ARG((reinterpret_cast<uintptr_t>(accum_dev) & 15) == 0, "dr_render_guided: accum must be 16-byte aligned");
+    GuideRun gr;
+    gr.guide = guide;
+    if (gcfg) {
+        DR_CHECK_ARG(gcfg->alpha >= 0.0f && gcfg->alpha < 1.0f, "dr_render_guided: alpha must be in [0, 1)");
+        gr.alpha = gcfg->alpha;
+        gr.train = gcfg->train != 0;
+        if (gcfg->train_batch) gr.batch = gcfg->train_batch;
+        if (gcfg->train_steps) gr.steps = gcfg->train_steps;
+    }
+    if (cfg->spp == 0) return DR_OK;
+    DR_CUDA(cudaSetDevice(s->ctx->device));
+    auto st = static_cast<cudaStream_t>(stream);
+    const uint64_t npix64 = (uint64_t)cam->width * (uint64_t)cam->height;
+    DR_CHECK_ARG(npix64 < (1ull << 31) / 16, "dr_render_guided: image too large");
+    WaveConfig wc;
+    if (cfg->wave_paths) wc.wave_paths = cfg->wave_paths;
+    wc.streams = 1;
+    wc.chunk = cfg->chunk;
+    const std::vector<RenderJob> jobs{make_job(s, cam, cfg, accum_dev, casts_dev)};
+    const WavePlan plan = plan_waves(jobs, wc.wave_paths);
+    if (!s->runner) {
+        s->runner = new (std::nothrow) WaveRunner;
+        if (!s->runner) return fail(DR_ERR_OUT_OF_MEMORY, "dr_render_guided: host allocation failed");
+        s->runner->ctx = s->ctx;
+    }
+    dr_status r = s->runner->prepare(jobs, plan, wc, st, &gr);
+    if (r != DR_OK) return r;
+    return s->runner->enqueue(scene_arrays(s), plan, wc, cfg->tri_mode, st, &gr);
 }

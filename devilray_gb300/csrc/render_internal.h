@@ -74,6 +74,16 @@ struct WaveConfig {
     uint32_t chunk = 0;              // rays per warp fetch of the persistent traversal, 0 = adaptive
 };
 
+// Path guiding of a render: the network, the mixture probability, and online
+// training after every wave (steps x batch rows of the newest samples).
+struct GuideRun {
+    dr_guide *guide = nullptr;
+    float alpha = 0.5f;
+    bool train = true;
+    uint32_t batch = 16384;
+    uint32_t steps = 4;
+};
+
 // Packs the samples of `jobs` (their npix and spp) into waves.
 WavePlan plan_waves(const std::vector<RenderJob> &jobs, uint32_t wave_paths);
 
@@ -90,15 +100,18 @@ struct WaveRunner {
     size_t jobs_capacity = 0;
     WaveSegment *d_segs = nullptr;
     size_t segs_capacity = 0;
+    bool guided = false;              // slot buffers carry the guiding state
+    void *d_train = nullptr;          // training ring (guided renders)
+    uint32_t train_cap = 0;
 
     ~WaveRunner();
     // Allocates buffers for `plan` and uploads jobs and segments (on `st`).
     dr_status prepare(const std::vector<RenderJob> &jobs, const WavePlan &plan, const WaveConfig &cfg,
-                      cudaStream_t st);
+                      cudaStream_t st, const GuideRun *guide = nullptr);
     // Enqueues the whole schedule on `st` (forks to the wave streams and joins
     // back). Capturable into a CUDA graph: no allocation, no host sync.
     dr_status enqueue(const SceneArrays &scene, const WavePlan &plan, const WaveConfig &cfg, int tri_mode,
-                      cudaStream_t st);
+                      cudaStream_t st, const GuideRun *guide = nullptr);
 };
 
 SceneArrays scene_arrays(const dr_scene *s);

@@ -177,6 +177,22 @@ SIGNATURES = {
     "dr_render_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
     "dr_autotune": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "dr_autotune_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
+    "dr_guide_num_params": (C.c_uint32, []),
+    "dr_guide_create": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]),
+    "dr_guide_destroy": (C.c_int, [C.c_void_p]),
+    "dr_guide_set_params": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
+    "dr_guide_get_params": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
+    "dr_guide_encode": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
+    "dr_guide_infer": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
+    "dr_guide_gradients": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32,
+                                     C.c_void_p, C.c_void_p]),
+    "dr_guide_train_step": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32,
+                                      C.c_void_p]),
+    "dr_guide_last_loss": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "dr_guide_mixture_sample": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "dr_guide_mixture_pdf": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
+    "dr_render_guided": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                   C.c_void_p, C.c_void_p]),
     "dr_alias_build_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_int32]),
     "dr_alias_build": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_int32, C.c_void_p]),
     "dr_alias_build_noalloc": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
@@ -384,6 +400,16 @@ class Scene:
         check(load().dr_render(self.handle, C.byref(c), C.byref(cfg), _ptr(accum_dev), _ptr(casts_dev),
                                _stream_ptr(stream)))
 
+    def render_guided(self, guide: "Guide", cam: dict, accum_dev, casts_dev=None, spp: int = 1,
+                      max_depth: int = 10, sample_offset: int = 0, pixel_sampling: int = 1, seed: int = 0,
+                      alpha: float = 0.5, train: bool = True, train_batch: int = 0, train_steps: int = 0,
+                      wave_paths: int = 0, stream=None):
+        c = make_camera(cam)
+        cfg = RenderConfig(max_depth, spp, sample_offset, pixel_sampling, seed, DR_TRI_REFERENCE, wave_paths, 0, 0, 0, 0)
+        g = GuidedConfig(alpha, 1 if train else 0, train_batch, train_steps)
+        check(load().dr_render_guided(self.handle, C.byref(c), C.byref(cfg), guide.handle, C.byref(g), _ptr(accum_dev),
+                                      _ptr(casts_dev), _stream_ptr(stream)))
+
     # -- traversal on host buffers --
     def trace_closest_host(self, rays: np.ndarray, hits: np.ndarray | None = None,
                            tri_mode: int = DR_TRI_REFERENCE, stream=None) -> np.ndarray:
@@ -500,6 +526,70 @@ def render_batch(ctx: "Context", jobs: list, wave_paths: int = 0, streams: int =
     arr = (Job * len(jobs))(*jobs)
     cfg = BatchConfig(wave_paths, streams, chunk, 0)
     check(load().dr_render_batch(ctx.handle, arr, len(jobs), C.byref(cfg), _stream_ptr(stream)))
+
+
+class GuidedConfig(C.Structure):
+    _fields_ = [("alpha", C.c_float), ("train", C.c_uint32), ("train_batch", C.c_uint32), ("train_steps", C.c_uint32)]
+
+
+class GuideConfig(C.Structure):
+    _fields_ = [("seed", C.c_uint64), ("learning_rate", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float),
+                ("epsilon", C.c_float), ("center", C.c_float * 3), ("half_extent", C.c_float)]
+
+
+class Guide:
+    """The path-guiding network (dr_guide)."""
+
+    def __init__(self, ctx: "Context", seed: int = 0, learning_rate: float = 1e-3, center=(0.0, 0.0, 0.0),
+                 half_extent: float = 1.0):
+        self.ctx = ctx
+        cfg = GuideConfig(seed, learning_rate, 0.9, 0.999, 1e-8, (C.c_float * 3)(*center), half_extent)
+        h = C.c_void_p()
+        check(load().dr_guide_create(ctx.handle, C.byref(cfg), C.byref(h)))
+        self.handle = h.value
+        self.num_params = int(load().dr_guide_num_params())
+
+    def params(self) -> np.ndarray:
+        out = np.zeros(self.num_params, np.float32)
+        check(load().dr_guide_get_params(self.handle, _ptr(out), self.num_params))
+        return out
+
+    def set_params(self, p: np.ndarray) -> None:
+        p = np.ascontiguousarray(p, np.float32)
+        check(load().dr_guide_set_params(self.handle, _ptr(p), self.num_params))
+
+    def encode(self, pos_dev, dir_dev, n: int, out_dev) -> None:
+        check(load().dr_guide_encode(self.handle, _ptr(pos_dev), _ptr(dir_dev), n, _ptr(out_dev)))
+
+    def infer(self, pos_dev, dir_dev, n: int, y_dev, stream=None) -> None:
+        check(load().dr_guide_infer(self.handle, _ptr(pos_dev), _ptr(dir_dev), n, _ptr(y_dev), _stream_ptr(stream)))
+
+    def gradients(self, pos_dev, dir_dev, sdir_dev, w_dev, n: int):
+        loss = C.c_float()
+        grad = np.zeros(self.num_params, np.float32)
+        check(load().dr_guide_gradients(self.handle, _ptr(pos_dev), _ptr(dir_dev), _ptr(sdir_dev), _ptr(w_dev), n,
+                                        C.byref(loss), _ptr(grad)))
+        return float(loss.value), grad
+
+    def train_step(self, pos_dev, dir_dev, sdir_dev, w_dev, n: int, stream=None) -> None:
+        check(load().dr_guide_train_step(self.handle, _ptr(pos_dev), _ptr(dir_dev), _ptr(sdir_dev), _ptr(w_dev), n,
+                                         _stream_ptr(stream)))
+
+    def last_loss(self) -> float:
+        v = C.c_float()
+        check(load().dr_guide_last_loss(self.handle, C.byref(v)))
+        return float(v.value)
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            load().dr_guide_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def tonemap(accum_dev, width: int, height: int, rgba_dev, gamma: bool = True, stream=None) -> None:

@@ -360,6 +360,74 @@ dr_status dr_autotune(dr_context *ctx, const dr_scene_desc *desc, const dr_camer
 dr_status dr_autotune_batch(dr_context *ctx, const dr_job *jobs, uint32_t njobs, const dr_autotune_config *tc,
                             dr_autotune_result *out);
 
+/* ---- path guiding ------------------------------------------------------------------ */
+
+/* A small network that proposes directions at diffuse vertices: 80 inputs
+ * (12-frequency sin/cos encoding of the position normalised by center and
+ * half_extent, a unit direction, zero padding), 4 hidden layers of 64 (ReLU),
+ * 40 outputs = an 8-lobe von Mises-Fisher mixture (per lobe: logit,
+ * log-concentration clamped to [-4, 7], unnormalised mean direction). BF16
+ * weights, FP32 accumulation on tensor cores; FP32 master weights trained with
+ * Adam on the loss -sum c_i log q(d_i | x_i) / n, c_i = weight_i / mean(weight). */
+typedef struct dr_guide dr_guide;
+
+typedef struct dr_guide_config {
+    uint64_t seed;            /* weight initialisation (He-uniform; last layer x 0.1) */
+    float learning_rate;      /* 0 = 1e-3 */
+    float beta1, beta2, epsilon;  /* Adam; 0 = 0.9, 0.999, 1e-8 */
+    float center[3];          /* position normalisation */
+    float half_extent;        /* 0 = 1 */
+} dr_guide_config;
+
+uint32_t dr_guide_num_params(void);
+dr_status dr_guide_create(dr_context *ctx, const dr_guide_config *cfg, dr_guide **out);
+dr_status dr_guide_destroy(dr_guide *guide);
+/* FP32 master parameters, per layer W [out][in] then b [out] (layer fan-ins 80,
+ * 64, 64, 64, 64; fan-outs 64, 64, 64, 64, 48). Setting resets Adam. Synchronous. */
+dr_status dr_guide_set_params(dr_guide *guide, const float *params_host, uint32_t n);
+dr_status dr_guide_get_params(dr_guide *guide, float *params_host, uint32_t n);
+/* Network input of each row (pos, dir: 3 floats per row; out: 80 floats per row). */
+dr_status dr_guide_encode(dr_guide *guide, const float *pos_dev, const float *dir_dev, uint32_t n, float *out_dev);
+/* Network output y (40 floats per row). Asynchronous on `stream`. */
+dr_status dr_guide_infer(dr_guide *guide, const float *pos_dev, const float *dir_dev, uint32_t n, float *y_dev,
+                         void *stream);
+/* Loss and gradient of every parameter for a batch (sampled directions sdir,
+ * 3 floats per row; sample weights); nothing is updated. Synchronous. */
+dr_status dr_guide_gradients(dr_guide *guide, const float *pos_dev, const float *dir_dev, const float *sdir_dev,
+                             const float *weight_dev, uint32_t n, float *loss_host, float *grad_host);
+/* One Adam step on a batch. Asynchronous on `stream`. */
+dr_status dr_guide_train_step(dr_guide *guide, const float *pos_dev, const float *dir_dev, const float *sdir_dev,
+                              const float *weight_dev, uint32_t n, void *stream);
+/* The mixture of network outputs y (40 floats per row): a direction drawn
+ * from uniforms u (3 per row: lobe, cosine, azimuth) and its density; or the
+ * density of given unit directions (y_per_row = 0: one y for every row). */
+dr_status dr_guide_mixture_sample(const float *y_dev, const float *u_dev, uint32_t n, float *dir_dev, float *pdf_dev,
+                                  void *stream);
+dr_status dr_guide_mixture_pdf(const float *y_dev, uint32_t y_per_row, const float *dir_dev, uint32_t n,
+                               float *pdf_dev, void *stream);
+/* Loss of the last dr_guide_gradients / dr_guide_train_step batch. Synchronous. */
+dr_status dr_guide_last_loss(dr_guide *guide, float *loss_host);
+
+typedef struct dr_guided_config {
+    float alpha;              /* probability of drawing a diffuse direction from the network (0 <= alpha < 1) */
+    uint32_t train;           /* 1: collect samples and train after every wave */
+    uint32_t train_batch;     /* rows per training step, 0 = 16384 */
+    uint32_t train_steps;     /* Adam steps after every wave, 0 = 4 */
+} dr_guided_config;
+
+/* dr_render with path guiding: at each diffuse vertex the network's mixture
+ * (inputs: hit point, normal facing the incoming ray) proposes the next
+ * direction with probability alpha, the cosine lobe otherwise, and the
+ * estimator divides by the mixture density alpha q + (1 - alpha) cos / pi
+ * (one-sample MIS), which also enters the MIS weights of next-event estimation
+ * and of emission hits, so the image stays unbiased for any network. With
+ * `train`, every finished wave's diffuse vertices (first 3 of each path) give
+ * training samples (incident radiance along the sampled direction) and the
+ * network takes train_steps Adam steps. Waves run one at a time. Asynchronous
+ * on `stream`. */
+dr_status dr_render_guided(dr_scene *scene, const dr_camera *camera, const dr_render_config *cfg, dr_guide *guide,
+                           const dr_guided_config *gcfg, float *accum_dev, uint32_t *casts_dev, void *stream);
+
 /* ---- alias tables ------------------------------------------------------------------- */
 
 typedef enum dr_alias_mode {

@@ -400,3 +400,62 @@ def ref_render_samples(spec, cam: dict, spp: int, replay: np.ndarray, sampling: 
                           float(cam["cy"]), w, h, float(cam["psx"]), float(cam["psy"]), sampling, spp,
                           replay.reshape(-1), replay.shape[-1], rgb.reshape(-1), casts, debug, sw.reshape(-1))
     return rgb, casts, sw
+
+
+# ---- path-guiding network (FP64 restatement) --------------------------------
+
+def _guide_lib():
+    L = lib()
+    if not getattr(L, "_guide_bound", False):
+        L.or_mlp_num_params.restype = C.c_int32
+        L.or_guide_encode.argtypes = [_f32p, _f32p, _f32p, C.c_float, _f32p]
+        L.or_mlp_forward.argtypes = [_f32p, _f32p, C.c_int32, _f32p]
+        L.or_vmf_mixture_log_pdf.argtypes = [_f32p, _f32p]
+        L.or_vmf_mixture_log_pdf.restype = C.c_double
+        L.or_mlp_loss_grad.argtypes = [_f32p, _f32p, _f32p, _f32p, C.c_int32, C.POINTER(C.c_double),
+                                       np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")]
+        L.or_adam_step.argtypes = [_f32p, _f32p, _f32p, _f32p, C.c_int32, C.c_int32, C.c_float, C.c_float,
+                                   C.c_float, C.c_float]
+        L._guide_bound = True
+    return L
+
+
+def mlp_num_params() -> int:
+    return int(_guide_lib().or_mlp_num_params())
+
+
+def guide_encode(pos, dirs, center, half) -> np.ndarray:
+    pos, dirs = _f32(pos).reshape(-1, 3), _f32(dirs).reshape(-1, 3)
+    out = np.zeros((pos.shape[0], 80), np.float32)
+    c = _f32(center)
+    for i in range(pos.shape[0]):
+        row = np.zeros(80, np.float32)
+        _guide_lib().or_guide_encode(np.ascontiguousarray(pos[i]), np.ascontiguousarray(dirs[i]), c, float(half), row)
+        out[i] = row
+    return out
+
+
+def mlp_forward(params, inputs) -> np.ndarray:
+    inputs = _f32(inputs).reshape(-1, 80)
+    out = np.zeros((inputs.shape[0], 48), np.float32)
+    _guide_lib().or_mlp_forward(_f32(params), inputs, inputs.shape[0], out)
+    return out
+
+
+def vmf_mixture_log_pdf(y, w) -> float:
+    return float(_guide_lib().or_vmf_mixture_log_pdf(_f32(y).reshape(-1)[:40].copy(), _f32(w)))
+
+
+def mlp_loss_grad(params, inputs, dirs, weights):
+    inputs = _f32(inputs).reshape(-1, 80)
+    grad = np.zeros(mlp_num_params(), np.float64)
+    loss = C.c_double()
+    _guide_lib().or_mlp_loss_grad(_f32(params), inputs, _f32(dirs).reshape(-1), _f32(weights), inputs.shape[0],
+                                  C.byref(loss), grad)
+    return loss.value, grad
+
+
+def adam_step(params, m, v, grad, t, lr=1e-3, b1=0.9, b2=0.999, eps=1e-8):
+    p, m, v = _f32(params).copy(), _f32(m).copy(), _f32(v).copy()
+    _guide_lib().or_adam_step(p, m, v, _f32(grad), p.size, int(t), lr, b1, b2, eps)
+    return p, m, v
