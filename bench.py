@@ -296,6 +296,9 @@ def run_ours(args):
     if not args.no_batch:
         torch.cuda.empty_cache()
         line["batch"] = batch_section(ctx, native, local, stream, scenes_n=args.batch_scenes)
+    if not args.no_guided:
+        torch.cuda.empty_cache()
+        line["guided"] = guided_section(ctx, native, local, stream, ref_spp=args.guided_ref_spp)
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -438,6 +441,103 @@ def batch_section(ctx, native, device: int, stream, scenes_n: int = 64, spp: int
     return out
 
 
+def guided_section(ctx, native, device: int, stream, width: int = 480, height: int = 270, spp: int = 256,
+                   depth: int = 16, ref_spp: int = 65536, hd_spp: int = 16):
+    """Learned path guiding on the occluded-light scene (the many-light
+    geometry, emitters only above an occluding slab): RMSE of the guided and of
+    the plain MIS tracer against a converged render (the plain tracer,
+    `ref_spp` samples accumulated in FP64), at equal samples and at equal time
+    (training included), plus guided samples/s at 1920x1080."""
+    import torch
+    from devilray_gb300 import scenes
+    spec = scenes.occluded_light()
+    scene = native.Scene.from_spec(ctx, spec)
+    cam = scenes.lower_camera(width, height)
+    npix = width * height
+    dev = f"cuda:{device}"
+    acc = torch.zeros((npix, 4), dtype=torch.float32, device=dev)
+
+    def image(a):
+        return (a[:, :3].double() / a[:, 3:4].double())
+
+    # converged reference: chunks of 1024 samples, summed in FP64
+    t0 = time.perf_counter()
+    ref = torch.zeros((npix, 4), dtype=torch.float64, device=dev)
+    for off in range(0, ref_spp, 1024):
+        acc.zero_()
+        scene.render(cam, acc, spp=min(1024, ref_spp - off), max_depth=depth, sample_offset=off, seed=12345,
+                     stream=stream)
+        stream.synchronize()
+        ref += acc.double()
+    ref_img = ref[:, :3] / ref[:, 3:4]
+    ref_s = time.perf_counter() - t0
+
+    def rmse(img):
+        return float(torch.sqrt(torch.mean((img - ref_img) ** 2)).item())
+
+    def timed(fn):
+        acc.zero_()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        stream.synchronize()
+        return e0.elapsed_time(e1) / 1e3
+
+    t_plain = timed(lambda: scene.render(cam, acc, spp=spp, max_depth=depth, seed=1, stream=stream))
+    rmse_plain = rmse(image(acc))
+    pos = spec.positions.reshape(-1, 3)
+    lo, hi = pos.min(0), pos.max(0)
+    guide = native.Guide(ctx, seed=1, center=tuple(float(x) for x in (lo + hi) / 2),
+                         half_extent=float((hi - lo).max() / 2))
+    wave = npix * 2  # two samples per wave: a training round every two samples
+    t_guided = timed(lambda: scene.render_guided(guide, cam, acc, spp=spp, max_depth=depth, seed=2, alpha=0.5,
+                                                 train=True, train_batch=16384, train_steps=4, wave_paths=wave,
+                                                 stream=stream))
+    rmse_guided = rmse(image(acc))
+    loss = guide.last_loss()
+    # equal time: the plain tracer with the samples it renders in the guided time
+    spp_eq = max(1, int(round(spp * t_guided / t_plain)))
+    t_eq = timed(lambda: scene.render(cam, acc, spp=spp_eq, max_depth=depth, seed=3, stream=stream))
+    rmse_eq = rmse(image(acc))
+    # the trained network's estimator on its own (no further training), equal samples
+    t_trained = timed(lambda: scene.render_guided(guide, cam, acc, spp=spp, max_depth=depth, seed=4, alpha=0.5,
+                                                  train=False, wave_paths=wave, stream=stream))
+    rmse_trained = rmse(image(acc))
+    # 1080p throughput of the guided tracer (training on)
+    hd = scenes.lower_camera(1920, 1080)
+    hd_acc = torch.zeros((1920 * 1080, 4), dtype=torch.float32, device=dev)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    scene.render_guided(guide, hd, hd_acc, spp=hd_spp, max_depth=depth, seed=5, alpha=0.5, train=True,
+                        train_batch=16384, train_steps=4, stream=stream)
+    e1.record(stream)
+    stream.synchronize()
+    t_hd = e0.elapsed_time(e1) / 1e3
+    e0.record(stream)
+    scene.render(hd, hd_acc, spp=hd_spp, max_depth=depth, seed=6, stream=stream)
+    e1.record(stream)
+    stream.synchronize()
+    t_hd_plain = e0.elapsed_time(e1) / 1e3
+    out = {"scene": "occluded_light (2^20 triangles, 65,536 emitters above a slab)", "width": width,
+           "height": height, "max_depth": depth, "reference_spp": ref_spp, "reference_accumulation": "fp64",
+           "reference_seconds": round(ref_s, 2), "spp": spp, "alpha": 0.5,
+           "plain": {"rmse": rmse_plain, "seconds": t_plain},
+           "guided": {"rmse": rmse_guided, "seconds": t_guided, "final_loss": loss,
+                      "training": "4 Adam steps x 16384 samples after every 2 spp"},
+           "plain_equal_time": {"rmse": rmse_eq, "spp": spp_eq, "seconds": t_eq},
+           "guided_trained_equal_spp": {"rmse": rmse_trained, "seconds": t_trained},
+           "rmse_ratio_equal_spp": rmse_plain / rmse_guided, "rmse_ratio_equal_time": rmse_eq / rmse_guided,
+           "hd_1080p": {"spp": hd_spp, "guided_samples_per_s": 1920 * 1080 * hd_spp / t_hd,
+                        "plain_samples_per_s": 1920 * 1080 * hd_spp / t_hd_plain}}
+    guide.close()
+    del scene, acc, ref, hd_acc
+    torch.cuda.empty_cache()
+    return out
+
+
 def render_cpu_baseline(spec, cam, depth: int, threads: int, pixels: int):
     """The reference's integrator on the CPU (oracle port of sampleColor with the
     reference's per-object cast), `pixels` pixels x 1 sample; samples/s."""
@@ -482,6 +582,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-render", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-guided", action="store_true")
+    ap.add_argument("--guided-ref-spp", type=int, default=65536)
     ap.add_argument("--batch-scenes", type=int, default=64)
     ap.add_argument("--layout", type=int, default=0, help="BVH layout of the trace workload: 0 default, 2, 8")
     ap.add_argument("--render-layout", type=int, default=0, help="BVH layout of the render workloads")

@@ -257,6 +257,201 @@ __global__ void __launch_bounds__(128) k_guide_infer(const __nv_bfloat16 *wb, co
     }
 }
 
+
+// ---- inference on the 5th-generation tensor cores (tcgen05) -------------------
+//
+// One CTA of 128 threads carries tiles of 128 rows (the M of one tcgen05.mma)
+// through the network: layer inputs and weights sit in shared memory in the
+// canonical K-major layout without swizzle, the one elected thread issues the
+// K/16 MMAs of a layer into a 128 x N FP32 accumulator in tensor memory and
+// commits them to an mbarrier, and each warp reads its 32 rows back with
+// tcgen05.ld for the bias / ReLU / BF16 epilogue, which writes the next
+// layer's input. Same arithmetic as k_guide_infer (BF16 products, FP32 sums).
+
+constexpr int kTcRows = 128;
+
+// Byte offset of element (r, c) of an R x K BF16 matrix in the canonical
+// K-major layout: core matrices of 8 rows x 8 columns (8 rows of 16 bytes);
+// column chunk j (columns 8j..8j+7) of all R rows is contiguous.
+__device__ __forceinline__ uint32_t canon_off(int r, int c, int R) { return (uint32_t)((c >> 3) * R * 16 + r * 16 + (c & 7) * 2); }
+
+// Shared-memory matrix descriptor: start address, leading byte offset (between
+// core matrices adjacent along K) and stride byte offset (between core
+// matrices adjacent along M or N), all >> 4; version 1 (bits 46-47); no swizzle.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
+{
+    return (uint64_t)((saddr >> 4) & 0x3fffu) | ((uint64_t)((lbo >> 4) & 0x3fffu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3fffu) << 32) | (1ull << 46);
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both
+// K-major, N >> 3 at bit 17, M >> 4 at bit 24.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Bounded wait on an mbarrier phase; false after the iteration limit.
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase)
+{
+    for (uint32_t it = 0; it < (1u << 22); ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(mbar), "r"(phase)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
+{
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// Shared memory of k_guide_infer_tc (byte offsets). The operand regions are
+// padded so that every core matrix a descriptor can name stays inside them.
+constexpr uint32_t kTcW0 = 0;                        // 64 x 80
+constexpr uint32_t kTcW1 = kTcW0 + 64 * 80 * 2;      // 3 x 64 x 64
+constexpr uint32_t kTcW4 = kTcW1 + 3 * 64 * 64 * 2;  // 48 x 64
+constexpr uint32_t kTcA = kTcW4 + 48 * 64 * 2 + 4096;  // 128 x 80 input / 128 x 64 hidden
+constexpr uint32_t kTcBias = kTcA + 65536;
+constexpr uint32_t kTcBar = kTcBias + (4 * kHid + kOut) * 4;
+constexpr uint32_t kTcSmem = kTcBar + 16;
+
+__global__ void __launch_bounds__(128) k_guide_infer_tc(const __nv_bfloat16 *wb, const float *params, GuideParams gp,
+                                                        const float *pos, const float *dir, const uint32_t *list,
+                                                        const uint32_t *count, uint32_t n_fixed, float *y,
+                                                        uint32_t *error)
+{
+    extern __shared__ __align__(1024) unsigned char smem[];
+    const int tid = threadIdx.x, warp = tid >> 5;
+    // weights in the canonical layout (B operands: N = outputs, K = inputs)
+    for (int i = tid; i < kHid * kIn; i += 128)
+        *reinterpret_cast<__nv_bfloat16 *>(smem + kTcW0 + canon_off(i / kIn, i % kIn, kHid)) = wb[i];
+    for (int l = 1; l <= 3; ++l)
+        for (int i = tid; i < kHid * kHid; i += 128)
+            *reinterpret_cast<__nv_bfloat16 *>(smem + kTcW1 + (l - 1) * kHid * kHid * 2 + canon_off(i / kHid, i % kHid, kHid)) =
+                wb[wb_off(l) + i];
+    for (int i = tid; i < kOut * kHid; i += 128)
+        *reinterpret_cast<__nv_bfloat16 *>(smem + kTcW4 + canon_off(i / kHid, i % kHid, kOut)) = wb[wb_off(4) + i];
+    float *bias = reinterpret_cast<float *>(smem + kTcBias);
+    for (int l = 0; l < kLayers; ++l)
+        for (int i = tid; i < fan_out(l); i += 128) bias[l * kHid + i] = params[b_off(l) + i];
+    const uint32_t mbar = smem_u32(smem + kTcBar);
+    const uint32_t tslot = smem_u32(smem + kTcBar + 8);
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mbar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;\n" ::"r"(tslot) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t taddr = *reinterpret_cast<volatile uint32_t *>(smem + kTcBar + 8);
+    const uint32_t a_base = smem_u32(smem + kTcA);
+    const uint32_t w_base[kLayers] = {smem_u32(smem + kTcW0), smem_u32(smem + kTcW1), smem_u32(smem + kTcW1 + 8192),
+                                      smem_u32(smem + kTcW1 + 16384), smem_u32(smem + kTcW4)};
+    const uint32_t n = count ? *count : n_fixed;
+    uint32_t phase = 0;
+    bool ok = true;
+    for (uint32_t tile = blockIdx.x; ok && (uint64_t)tile * kTcRows < n; tile += gridDim.x) {
+        const uint32_t r = tile * kTcRows + tid;
+        float p[3], d[3];
+        uint32_t slot;
+        load_row(pos, dir, list, n, r, gp, p, d, slot);
+        // input row: 10 chunks of 8 encoded columns
+#pragma unroll
+        for (int j = 0; j < kIn / 8; ++j) {
+            uint32_t q[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                float v0, v1;
+                encode_pair(p, d, 8 * j + 2 * k, v0, v1);
+                q[k] = pack_bf16(v0, v1);
+            }
+            *reinterpret_cast<uint4 *>(smem + kTcA + canon_off(tid, 8 * j, kTcRows)) = make_uint4(q[0], q[1], q[2], q[3]);
+        }
+        for (int l = 0; l < kLayers; ++l) {
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+            asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+            __syncthreads();
+            const int K = fan_in(l), N = fan_out(l);
+            if (tid == 0) {
+                asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                const uint32_t idesc = idesc_bf16(kTcRows, N);
+                for (int s2 = 0; s2 < K / 16; ++s2) {
+                    const uint64_t ad = smem_desc(a_base + (uint32_t)s2 * 2 * kTcRows * 16, kTcRows * 16, 128);
+                    const uint64_t bd = smem_desc(w_base[l] + (uint32_t)s2 * 2 * N * 16, (uint32_t)N * 16, 128);
+                    asm volatile(
+                        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(taddr),
+                        "l"(ad), "l"(bd), "r"(idesc), "r"(s2));
+                }
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mbar)
+                             : "memory");
+            }
+            // one decision for the whole block: every thread waited (bounded) on the same phase
+            if (!__syncthreads_and(mbar_wait(mbar, phase) ? 1 : 0)) {
+                if (tid == 0) atomicOr(error, ERR_TIMEOUT);
+                ok = false;
+                break;
+            }
+            phase ^= 1u;
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const uint32_t lane_addr = taddr + ((uint32_t)(warp * 32) << 16);
+            float v[64];
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                float t[16];
+                tmem_ld16(lane_addr + 16 * c, t);
+#pragma unroll
+                for (int i = 0; i < 16; ++i) v[16 * c + i] = t[i];
+            }
+            asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+            const float *b = bias + l * kHid;
+            if (l < kLayers - 1) {
+#pragma unroll
+                for (int j = 0; j < kHid / 8; ++j) {
+                    uint32_t q[4];
+#pragma unroll
+                    for (int k = 0; k < 4; ++k)
+                        q[k] = pack_bf16(fmaxf(v[8 * j + 2 * k] + b[8 * j + 2 * k], 0.0f),
+                                         fmaxf(v[8 * j + 2 * k + 1] + b[8 * j + 2 * k + 1], 0.0f));
+                    *reinterpret_cast<uint4 *>(smem + kTcA + canon_off(tid, 8 * j, kTcRows)) =
+                        make_uint4(q[0], q[1], q[2], q[3]);
+                }
+            } else if (slot != 0xffffffffu) {
+                float4 *dst = reinterpret_cast<float4 *>(y + (size_t)slot * kGuideOut);
+#pragma unroll
+                for (int j = 0; j < kGuideOut / 4; ++j)
+                    dst[j] = make_float4(v[4 * j] + b[4 * j], v[4 * j + 1] + b[4 * j + 1], v[4 * j + 2] + b[4 * j + 2],
+                                         v[4 * j + 3] + b[4 * j + 3]);
+            }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        __syncthreads();
+    }
+    if (!ok) mbar_wait(mbar, phase);  // MMAs still in flight: wait again (bounded) before freeing their memory
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;\n" ::"r"(taddr) : "memory");
+}
+
 // ---- training -----------------------------------------------------------------
 
 struct TrainBuffers {
@@ -675,9 +870,17 @@ cudaError_t launch_guide_infer(const dr_guide *g, const float *pos, const float 
                                const uint32_t *count, uint32_t max_rows, float *y, cudaStream_t st)
 {
     if (max_rows == 0) return cudaSuccess;
-    const unsigned tiles = (max_rows + 15) / 16;
-    const unsigned blocks = std::min<unsigned>((tiles + 3) / 4, (unsigned)g->ctx->num_sms * 4);
-    k_guide_infer<<<blocks, 128, kInferSmem, st>>>(g->wb, g->params, guide_params(g), pos, dir, list, count, max_rows, y);
+    if (g->cfg.infer_kernel == DR_GUIDE_INFER_TCGEN05) {
+        const unsigned tiles = (max_rows + kTcRows - 1) / kTcRows;
+        const unsigned blocks = std::min<unsigned>(tiles, (unsigned)g->ctx->num_sms * 2);
+        k_guide_infer_tc<<<blocks, 128, kTcSmem, st>>>(g->wb, g->params, guide_params(g), pos, dir, list, count,
+                                                       max_rows, y, g->ctx->d_error);
+    } else {
+        const unsigned tiles = (max_rows + 15) / 16;
+        const unsigned blocks = std::min<unsigned>((tiles + 3) / 4, (unsigned)g->ctx->num_sms * 4);
+        k_guide_infer<<<blocks, 128, kInferSmem, st>>>(g->wb, g->params, guide_params(g), pos, dir, list, count,
+                                                       max_rows, y);
+    }
     return cudaGetLastError();
 }
 
@@ -702,6 +905,7 @@ dr_status dr_guide_create(dr_context *ctx, const dr_guide_config *cfg, dr_guide 
     if (!attr) {
         DR_CUDA(cudaFuncSetAttribute(k_guide_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kInferSmem));
         DR_CUDA(cudaFuncSetAttribute(k_guide_train_fb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTrainSmem));
+        DR_CUDA(cudaFuncSetAttribute(k_guide_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem));
         attr = true;
     }
     auto *g = new (std::nothrow) dr_guide;
@@ -713,6 +917,10 @@ dr_status dr_guide_create(dr_context *ctx, const dr_guide_config *cfg, dr_guide 
     if (g->cfg.beta2 <= 0.0f) g->cfg.beta2 = 0.999f;
     if (g->cfg.epsilon <= 0.0f) g->cfg.epsilon = 1e-8f;
     if (g->cfg.half_extent <= 0.0f) g->cfg.half_extent = 1.0f;
+    if (g->cfg.infer_kernel > DR_GUIDE_INFER_MMA_SYNC) {
+        free_guide(g);
+        return fail(DR_ERR_INVALID_ARGUMENT, "dr_guide_create: unknown inference kernel");
+    }
     cudaError_t e;
     if ((e = cudaMalloc(&g->params, kNumParams * 4)) != cudaSuccess || (e = cudaMalloc(&g->m, kNumParams * 4)) != cudaSuccess ||
         (e = cudaMalloc(&g->v, kNumParams * 4)) != cudaSuccess || (e = cudaMalloc(&g->grad, kNumParams * 4)) != cudaSuccess ||
@@ -776,11 +984,7 @@ dr_status dr_guide_infer(dr_guide *g, const float *pos_dev, const float *dir_dev
     DR_CHECK_ARG(g && (n == 0 || (pos_dev && dir_dev && y_dev)), "dr_guide_infer: NULL argument");
     if (n == 0) return DR_OK;
     DR_CUDA(cudaSetDevice(g->ctx->device));
-    const unsigned tiles = (n + 15) / 16;
-    const unsigned blocks = std::min<unsigned>((tiles + 3) / 4, (unsigned)g->ctx->num_sms * 8);
-    k_guide_infer<<<blocks, 128, kInferSmem, static_cast<cudaStream_t>(stream)>>>(
-        g->wb, g->params, guide_params(g), pos_dev, dir_dev, nullptr, nullptr, n, y_dev);
-    DR_CUDA(cudaGetLastError());
+    DR_CUDA(launch_guide_infer(g, pos_dev, dir_dev, nullptr, nullptr, n, y_dev, static_cast<cudaStream_t>(stream)));
     return DR_OK;
 }
 

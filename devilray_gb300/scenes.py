@@ -258,6 +258,64 @@ def many_light(num_triangles: int = 1 << 20, num_emitters: int = 65536, seed: in
     return s
 
 
+def occluded_light(num_triangles: int = 1 << 20, num_emitters: int = 65536, seed: int = 0,
+                   half: float = CUBE_HALF, light_y: float = 0.4, slab_y: float = 0.3,
+                   slab_extent: float = 0.7, enclose: bool = True) -> SceneSpec:
+    """The guided configuration: the many-light scene with its emitters only on
+    spheres whose centre lies above `light_y` * half, and a diffuse occluding
+    slab (albedo 0.8, two triangles) at height `slab_y` * half covering
+    `slab_extent` of the cube's width in x and z, so light reaches the
+    spheres below mostly through the gaps at the slab's edges, off a floor
+    and a back wall (`enclose`): indirect light dominates the camera's view of
+    the lower region."""
+    soup, centres, radii = incoherent_soup(num_triangles, seed=seed, half=half)
+    per = 1280
+    rng = np.random.default_rng(seed + 17)
+    n = soup.shape[0]
+    nsph = (n + per - 1) // per
+    upper = np.flatnonzero(centres[:nsph, 1] > light_y * half)
+    candidates = np.concatenate([np.arange(k * per, min(n, (k + 1) * per)) for k in upper]) if upper.size else \
+        np.arange(0)
+    num_emitters = min(num_emitters, candidates.size)
+    emissive = np.zeros(n, bool)
+    emissive[rng.permutation(candidates)[:num_emitters]] = True
+    radiance = np.exp(rng.normal(0.0, 1.5, n)).astype(np.float32)
+    kind = rng.random(nsph) < 0.5
+    albedo = rng.uniform(0.2, 0.8, nsph)
+    ior = rng.uniform(1.3, 1.7, nsph)
+    s = SceneSpec()
+    for k in range(nsph):
+        tris = np.arange(k * per, min(n, (k + 1) * per))
+        body = tris[~emissive[tris]]
+        if body.size:
+            m = s.add_material(material(0, albedo=(albedo[k],) * 3) if kind[k] else material(1, ior=ior[k]))
+            s.add_object(soup[body], m)
+        for t in tris[emissive[tris]]:
+            L = float(radiance[t])
+            m = s.add_material(material(0, emission=(L, L, L)))
+            s.add_object(soup[t:t + 1], m)
+    e = slab_extent * half
+    slab = quad((0.0, slab_y * half, 0.0), (0.0, -1.0, 0.0), (1.0, 0.0, 0.0), 2 * e)
+    grey = s.add_material(material(0, albedo=(0.8, 0.8, 0.8)))
+    s.add_object(slab, grey)
+    if enclose:
+        # a floor and a back wall catch the light that passes the slab's edges
+        # and scatter it under the slab
+        s.add_object(quad((0.0, -1.1 * half, 0.0), (0.0, 1.0, 0.0), (1.0, 0.0, 0.0), 3.0 * half), grey)
+        s.add_object(quad((0.0, 0.0, 1.1 * half), (0.0, 0.0, -1.0), (1.0, 0.0, 0.0), 3.0 * half), grey)
+    return s
+
+
+def lower_camera(width: int, height: int, distance: float = 150.0, half: float = CUBE_HALF,
+                 look_y: float = -0.3) -> dict:
+    """Camera on the -z axis outside the cube, aimed at height look_y * half so
+    the region below the slab of occluded_light fills the view."""
+    m = np.eye(4, dtype=np.float32)
+    m[1, 3] = look_y * half
+    m[2, 3] = -distance
+    return camera(width, height, focal=1.0, fov_half_width=0.62 * half / distance * 1.6, transform=m)
+
+
 def outside_camera(width: int, height: int, distance: float = 150.0, half: float = CUBE_HALF) -> dict:
     """Camera on the -z axis outside the cube, looking at its centre."""
     m = np.eye(4, dtype=np.float32)

@@ -377,7 +377,13 @@ typedef struct dr_guide_config {
     float beta1, beta2, epsilon;  /* Adam; 0 = 0.9, 0.999, 1e-8 */
     float center[3];          /* position normalisation */
     float half_extent;        /* 0 = 1 */
+    uint32_t infer_kernel;    /* dr_guide_infer_kernel */
 } dr_guide_config;
+
+typedef enum dr_guide_infer_kernel {
+    DR_GUIDE_INFER_TCGEN05 = 0,   /* tcgen05.mma, accumulators in tensor memory (default) */
+    DR_GUIDE_INFER_MMA_SYNC = 1   /* warp-level mma.sync, accumulators in registers */
+} dr_guide_infer_kernel;
 
 uint32_t dr_guide_num_params(void);
 dr_status dr_guide_create(dr_context *ctx, const dr_guide_config *cfg, dr_guide **out);
