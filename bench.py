@@ -491,9 +491,9 @@ def guided_section(ctx, native, device: int, stream, width: int = 480, height: i
     lo, hi = pos.min(0), pos.max(0)
     guide = native.Guide(ctx, seed=1, center=tuple(float(x) for x in (lo + hi) / 2),
                          half_extent=float((hi - lo).max() / 2))
-    wave = npix * 2  # two samples per wave: a training round every two samples
+    wave = npix * 8  # eight samples per wave: a training round of 8 steps after each
     t_guided = timed(lambda: scene.render_guided(guide, cam, acc, spp=spp, max_depth=depth, seed=2, alpha=0.5,
-                                                 train=True, train_batch=16384, train_steps=4, wave_paths=wave,
+                                                 train=True, train_batch=16384, train_steps=8, wave_paths=wave,
                                                  stream=stream))
     rmse_guided = rmse(image(acc))
     loss = guide.last_loss()
@@ -512,7 +512,7 @@ def guided_section(ctx, native, device: int, stream, width: int = 480, height: i
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
     scene.render_guided(guide, hd, hd_acc, spp=hd_spp, max_depth=depth, seed=5, alpha=0.5, train=True,
-                        train_batch=16384, train_steps=4, stream=stream)
+                        train_batch=16384, train_steps=8, stream=stream)
     e1.record(stream)
     stream.synchronize()
     t_hd = e0.elapsed_time(e1) / 1e3
@@ -521,12 +521,13 @@ def guided_section(ctx, native, device: int, stream, width: int = 480, height: i
     e1.record(stream)
     stream.synchronize()
     t_hd_plain = e0.elapsed_time(e1) / 1e3
-    out = {"scene": "occluded_light (2^20 triangles, 65,536 emitters above a slab)", "width": width,
+    out = {"scene": "occluded_light (2^20 triangles, 65,536 emitters above a slab, floor and walls)",
+           "width": width,
            "height": height, "max_depth": depth, "reference_spp": ref_spp, "reference_accumulation": "fp64",
            "reference_seconds": round(ref_s, 2), "spp": spp, "alpha": 0.5,
            "plain": {"rmse": rmse_plain, "seconds": t_plain},
            "guided": {"rmse": rmse_guided, "seconds": t_guided, "final_loss": loss,
-                      "training": "4 Adam steps x 16384 samples after every 2 spp"},
+                      "training": "8 Adam steps x 16384 samples after every 8 spp"},
            "plain_equal_time": {"rmse": rmse_eq, "spp": spp_eq, "seconds": t_eq},
            "guided_trained_equal_spp": {"rmse": rmse_trained, "seconds": t_trained},
            "rmse_ratio_equal_spp": rmse_plain / rmse_guided, "rmse_ratio_equal_time": rmse_eq / rmse_guided,

@@ -10,6 +10,9 @@ namespace dr {
 cudaError_t launch_guide_infer(const dr_guide *g, const float *pos, const float *dir, const uint32_t *list,
                                const uint32_t *count, uint32_t max_rows, float *y, cudaStream_t st);
 
+// Adam steps the network has taken (enqueued).
+uint32_t guide_steps(const dr_guide *g);
+
 // One Adam step on rows [0, n) of the given arrays.
 dr_status guide_train_step(dr_guide *g, const float *pos, const float *dir, const float *sdir, const float *weight,
                            uint32_t n, cudaStream_t st);

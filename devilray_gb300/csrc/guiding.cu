@@ -534,10 +534,10 @@ __device__ __forceinline__ void delta_frags(float (&acc)[2 * KS][4], const uint3
 
 // One block = 4 warps = 64 rows. Forward with stored activations, loss
 // gradient, backward deltas; writes deltaT / actT of every layer and adds the
-// batch loss. weight_mean: mean sample weight of the batch (device scalar).
+// batch loss. weight_sum: sum of the batch's sample weights (device scalar).
 __global__ void __launch_bounds__(128) k_guide_train_fb(const __nv_bfloat16 *wb, const float *params, GuideParams gp,
                                                         const float *pos, const float *dir, const float *sdir,
-                                                        const float *weight, uint32_t n, const float *weight_mean,
+                                                        const float *weight, uint32_t n, const float *weight_sum,
                                                         TrainBuffers tb, float *loss)
 {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -589,7 +589,7 @@ __global__ void __launch_bounds__(128) k_guide_train_fb(const __nv_bfloat16 *wb,
         const uint32_t r = r0 + lane;
         float lq = 0.0f;
         if (r < n) {
-            const float wm = *weight_mean;
+            const float wm = *weight_sum / (float)n;
             const float c = wm > 0.0f ? weight[r] / wm : 0.0f;
             lq = guide_loss_grad(yw + lane * kOut, sdir[3 * (size_t)r], sdir[3 * (size_t)r + 1], sdir[3 * (size_t)r + 2],
                                  c / (float)n, dyrow);
@@ -641,21 +641,25 @@ __global__ void __launch_bounds__(128) k_guide_train_fb(const __nv_bfloat16 *wb,
 
 // Weight gradients of layer l: dW[o][i] += sum over rows of deltaT[o][r] actT[i][r]
 // (tensor cores, K = rows; delta as BF16 high + low parts), bias gradient
-// db[o] += sum deltaT[o][r]. One warp per (16 outputs, 512-row chunk); 8 column
-// tiles of inputs per pass.
-__global__ void __launch_bounds__(32) k_guide_wgrad(int l, TrainBuffers tb, uint32_t n, float *grad)
+// db[o] += sum deltaT[o][r]. Each warp computes one 16 x 8 tile (16 outputs,
+// 8 inputs) over a chunk of kWgradRows rows and adds it with atomics; block x
+// = (output tile, group of 4 input tiles), block y = row chunk.
+constexpr uint32_t kWgradRows = 256;
+
+__global__ void __launch_bounds__(128) k_guide_wgrad(int l, TrainBuffers tb, uint32_t n, float *grad)
 {
-    const int lane = threadIdx.x & 31, g = lane >> 2, tig = lane & 3;
-    const int fan_in = l == 0 ? kIn : kHid;
-    const int o0 = 16 * blockIdx.x;
-    const uint32_t k0 = 512 * blockIdx.y, k1 = min(n, k0 + 512);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, tig = lane & 3;
+    const int fan_in_l = l == 0 ? kIn : kHid;
+    const int in_tiles = fan_in_l / 8, groups = (in_tiles + 3) / 4;
+    const int o0 = 16 * (blockIdx.x / groups);
+    const int it = 4 * (blockIdx.x % groups) + warp;
+    const uint32_t k0 = kWgradRows * blockIdx.y, k1 = min(n, k0 + kWgradRows);
     const float *dT = tb.deltaT[l];
     const __nv_bfloat16 *aT = tb.actT[l];
     const uint32_t stride = tb.rows;
-    const int nin_tiles = fan_in / 8;
-    for (int nt0 = 0; nt0 < nin_tiles; nt0 += 5) {
-        const int ntiles = min(5, nin_tiles - nt0);
-        float acc[5][4] = {};
+    if (it < in_tiles) {
+        float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        const __nv_bfloat16 *col = aT + (size_t)(8 * it + g) * stride;
         for (uint32_t k = k0; k < k1; k += 16) {
             // A[m = o][k = row]: a0 (o0+g, k+2tig..+1), a1 (o0+g+8, ...), a2 (o0+g, k+8+2tig..), a3 (o0+g+8, k+8+..)
             uint32_t ahi[4], alo[4];
@@ -670,49 +674,40 @@ __global__ void __launch_bounds__(32) k_guide_wgrad(int l, TrainBuffers tb, uint
                 ahi[q] = *reinterpret_cast<const uint32_t *>(&hb);
                 alo[q] = pack_bf16(v0 - hf.x, v1 - hf.y);
             }
-            for (int j = 0; j < ntiles; ++j) {
-                const int i = 8 * (nt0 + j) + g;
-                const uint32_t kk = k + 2 * tig;
-                uint32_t b0 = 0, b1 = 0;
-                const __nv_bfloat16 *col = aT + (size_t)i * stride;
-                if (kk + 1 < k1) b0 = ld_pair(col + kk);
-                else if (kk < k1) b0 = (uint32_t) * reinterpret_cast<const uint16_t *>(col + kk);
-                if (kk + 9 < k1) b1 = ld_pair(col + kk + 8);
-                else if (kk + 8 < k1) b1 = (uint32_t) * reinterpret_cast<const uint16_t *>(col + kk + 8);
-                mma_bf16(acc[j], ahi, b0, b1);
-                mma_bf16(acc[j], alo, b0, b1);
-            }
+            // B[k = row][n = input]: b0 (rows k+2tig..+1, input 8it+g), b1 (rows k+8+2tig..)
+            const uint32_t kk = k + 2 * tig;
+            uint32_t b0 = 0, b1 = 0;
+            if (kk + 1 < k1) b0 = ld_pair(col + kk);
+            else if (kk < k1) b0 = (uint32_t) * reinterpret_cast<const uint16_t *>(col + kk);
+            if (kk + 9 < k1) b1 = ld_pair(col + kk + 8);
+            else if (kk + 8 < k1) b1 = (uint32_t) * reinterpret_cast<const uint16_t *>(col + kk + 8);
+            mma_bf16(acc, ahi, b0, b1);
+            mma_bf16(acc, alo, b0, b1);
         }
-        for (int j = 0; j < ntiles; ++j) {
-            const int i = 8 * (nt0 + j) + 2 * tig;
-            float *G = grad + w_off(l);
-            atomicAdd(&G[(o0 + g) * fan_in + i], acc[j][0]);
-            atomicAdd(&G[(o0 + g) * fan_in + i + 1], acc[j][1]);
-            atomicAdd(&G[(o0 + g + 8) * fan_in + i], acc[j][2]);
-            atomicAdd(&G[(o0 + g + 8) * fan_in + i + 1], acc[j][3]);
-        }
+        float *G = grad + w_off(l);
+        const int i = 8 * it + 2 * tig;
+        atomicAdd(&G[(o0 + g) * fan_in_l + i], acc[0]);
+        atomicAdd(&G[(o0 + g) * fan_in_l + i + 1], acc[1]);
+        atomicAdd(&G[(o0 + g + 8) * fan_in_l + i], acc[2]);
+        atomicAdd(&G[(o0 + g + 8) * fan_in_l + i + 1], acc[3]);
     }
-    // bias gradient: lanes 0..15 sum the chunk's rows of outputs o0 + lane
-    if (lane < 16) {
-        float s = 0.0f;
+    // bias gradient: in the first input-tile group, warp 0's lanes 0..15 sum the
+    // chunk's rows of outputs o0 + lane
+    if (blockIdx.x % groups == 0 && warp == 0 && lane < 16) {
+        float sum = 0.0f;
         const float *row = dT + (size_t)(o0 + lane) * stride;
-        for (uint32_t k = k0; k < k1; ++k) s += row[k];
-        atomicAdd(grad + b_off(l) + o0 + lane, s);
+        for (uint32_t k = k0; k < k1; ++k) sum += row[k];
+        atomicAdd(grad + b_off(l) + o0 + lane, sum);
     }
 }
 
-__global__ void k_guide_weight_mean(const float *w, uint32_t n, float *mean)
+// Sum of the sample weights into *sum (zeroed before).
+__global__ void k_guide_weight_sum(const float *w, uint32_t n, float *sum)
 {
-    __shared__ float part[256];
-    float s = 0.0f;
-    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) s += w[i];
-    part[threadIdx.x] = s;
-    __syncthreads();
-    for (int o = 128; o > 0; o >>= 1) {
-        if ((int)threadIdx.x < o) part[threadIdx.x] += part[threadIdx.x + o];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) *mean = n ? part[0] / (float)n : 0.0f;
+    float v = 0.0f;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) v += w[i];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(sum, v);
 }
 
 __global__ void k_guide_adam(float *params, float *m, float *v, const float *grad, int t, float lr, float b1, float b2,
@@ -787,7 +782,7 @@ struct dr_guide {
     dr_guide_config cfg{};
     float *params = nullptr, *m = nullptr, *v = nullptr, *grad = nullptr;
     __nv_bfloat16 *wb = nullptr;
-    float *scalars = nullptr;  // [0] weight mean, [1] loss
+    float *scalars = nullptr;  // [0] sum of the batch's sample weights, [1] loss
     dr::TrainBuffers tb{};
     void *tb_mem = nullptr;
     uint32_t capacity = 0;
@@ -849,14 +844,15 @@ dr_status run_gradients(dr_guide *g, const float *pos, const float *dir, const f
     dr_status r = ensure_train_capacity(g, n);
     if (r != DR_OK) return r;
     DR_CUDA(cudaMemsetAsync(g->grad, 0, kNumParams * sizeof(float), st));
-    DR_CUDA(cudaMemsetAsync(g->scalars + 1, 0, sizeof(float), st));
-    k_guide_weight_mean<<<1, 256, 0, st>>>(weight, n, g->scalars);
+    DR_CUDA(cudaMemsetAsync(g->scalars, 0, 2 * sizeof(float), st));
+    k_guide_weight_sum<<<std::min<unsigned>((n + 255) / 256, 64), 256, 0, st>>>(weight, n, g->scalars);
     const GuideParams gp = guide_params(g);
     k_guide_train_fb<<<(n + 63) / 64, 128, kTrainSmem, st>>>(g->wb, g->params, gp, pos, dir, sdir, weight, n,
                                                              g->scalars, g->tb, g->scalars + 1);
     for (int l = 0; l < kLayers; ++l) {
-        const dim3 grid(fan_out(l) / 16, (n + 511) / 512);
-        k_guide_wgrad<<<grid, 32, 0, st>>>(l, g->tb, n, g->grad);
+        const int groups = (fan_in(l) / 8 + 3) / 4;
+        const dim3 grid((unsigned)(fan_out(l) / 16 * groups), (n + kWgradRows - 1) / kWgradRows);
+        k_guide_wgrad<<<grid, 128, 0, st>>>(l, g->tb, n, g->grad);
     }
     DR_CUDA(cudaGetLastError());
     return DR_OK;
@@ -883,6 +879,8 @@ cudaError_t launch_guide_infer(const dr_guide *g, const float *pos, const float 
     }
     return cudaGetLastError();
 }
+
+uint32_t guide_steps(const dr_guide *g) { return (uint32_t)g->step; }
 
 dr_status guide_train_step(dr_guide *g, const float *pos, const float *dir, const float *sdir, const float *weight,
                            uint32_t n, cudaStream_t st)

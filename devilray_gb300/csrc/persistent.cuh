@@ -66,8 +66,13 @@ __device__ __forceinline__ void persistent_wide(const Wide8Args &a, const Source
     uint64_t chunk_next = 0, chunk_end = 0;  // warp-uniform
     const uint32_t chunk = persistent_chunk(n, fixed_chunk);
     unsigned long long cn = 0, cb = 0, ct = 0, ch = 0;
+#ifndef DR_REFILL_MIN
+#define DR_REFILL_MIN 1
+#endif
     while (true) {
         unsigned want = __ballot_sync(FULL, !active);
+        // refill once enough lanes are idle (or none is busy)
+        if (DR_REFILL_MIN > 1 && want != FULL && __popc(want) < DR_REFILL_MIN) want = 0;
         while (want != 0 && !exhausted) {
             if (chunk_next == chunk_end) {
                 unsigned long long b = 0;

@@ -70,6 +70,7 @@ struct RenderParams {
     float *rec;                // [slot][kGuideRecords][kRecFloats] training records
     uint32_t *rec_n;           // [slot] records; bit 31: the last one waits for its radiance
     float guide_alpha;         // probability of sampling the network's mixture
+    int guide_target;          // training target: 0 radiance, 1 log(1 + radiance)
     float *train_pos, *train_nrm, *train_dir, *train_w;  // training ring
     uint32_t *train_head;
     uint32_t train_cap;
@@ -646,7 +647,8 @@ __global__ void __launch_bounds__(256) k_guide_collect(RenderParams p)
     for (uint32_t r = 0; r < n; ++r) {
         const float *rc = p.rec + ((size_t)slot * kGuideRecords + r) * kRecFloats;
         const float T = rc[10], cn = rc[11];
-        const float L = (cf - cn) / T;
+        float L = (cf - cn) / T;
+        if (p.guide_target == 1) L = log1pf(fmaxf(L, 0.0f));
         const float c = rc[3] * rc[6] + rc[4] * rc[7] + rc[5] * rc[8];
         const float w = L * fmaxf(c, 0.0f) / rc[9];
         if (!(T > 0.0f) || !(w > 0.0f) || !isfinite(w)) continue;
@@ -816,7 +818,7 @@ dr_status WaveRunner::prepare(const std::vector<RenderJob> &jobs, const WavePlan
                               cudaStream_t st, const GuideRun *gr)
 {
     const uint32_t nwaves = (uint32_t)plan.wave_slots.size();
-    const int K = gr ? 1 : (int)std::max<uint32_t>(1, std::min<uint32_t>({cfg.streams, (uint32_t)kMaxWaveStreams, nwaves}));
+    const int K = (int)std::max<uint32_t>(1, std::min<uint32_t>({cfg.streams, (uint32_t)kMaxWaveStreams, nwaves}));
     const size_t need = wave_buffer_bytes(plan.max_slots, gr != nullptr);
     const uint32_t train_need = gr ? std::max<uint32_t>(1, gr->batch) * std::max<uint32_t>(1, gr->steps) : 0;
     bool grow = jobs.size() > jobs_capacity || plan.segs.size() > segs_capacity || train_need > train_cap;
@@ -876,8 +878,9 @@ dr_status WaveRunner::enqueue(const SceneArrays &sc, const WavePlan &plan, const
 {
     const uint32_t nwaves = (uint32_t)plan.wave_slots.size();
     if (nwaves == 0) return DR_OK;
-    // a guided render trains between waves: one wave at a time
-    const int K = gr ? 1 : (int)std::max<uint32_t>(1, std::min<uint32_t>({cfg.streams, (uint32_t)kMaxWaveStreams, nwaves}));
+    // the waves' training steps run in wave order: they follow the ordered
+    // accumulation pass, which waits for the previous wave's
+    const int K = (int)std::max<uint32_t>(1, std::min<uint32_t>({cfg.streams, (uint32_t)kMaxWaveStreams, nwaves}));
     // training ring (SoA): positions, normals, directions, weights, head counter
     float *t_pos = nullptr, *t_nrm = nullptr, *t_dir = nullptr, *t_w = nullptr;
     uint32_t *t_head = nullptr;
@@ -906,6 +909,7 @@ dr_status WaveRunner::enqueue(const SceneArrays &sc, const WavePlan &plan, const
         RenderParams q = wave_params(sc, d_jobs, d_wave[k], plan.max_slots, cfg.chunk, gr != nullptr);
         if (gr) {
             q.guide_alpha = gr->alpha;
+            q.guide_target = (int)gr->target;
             q.train_pos = t_pos, q.train_nrm = t_nrm, q.train_dir = t_dir, q.train_w = t_w;
             q.train_head = t_head;
             q.train_cap = train_cap;
@@ -952,7 +956,7 @@ dr_status WaveRunner::enqueue(const SceneArrays &sc, const WavePlan &plan, const
         k_accumulate_wave<<<(q.wave_pix + 255) / 256, 256, 0, ws>>>(q);
         DR_CUDA(cudaGetLastError());
         if (gr && gr->train)
-            for (uint32_t t = 0; t < gr->steps; ++t) {
+            for (uint32_t t = 0; t < gr->steps && (gr->budget == 0 || guide_steps(gr->guide) < gr->budget); ++t) {
                 const size_t o = (size_t)t * gr->batch;
                 const dr_status ts = guide_train_step(gr->guide, t_pos + 3 * o, t_nrm + 3 * o, t_dir + 3 * o, t_w + o,
                                                       gr->batch, ws);
@@ -1081,6 +1085,9 @@ extern "C" dr_status dr_render_guided(dr_scene *s, const dr_camera *cam, const d
         gr.train = gcfg->train != 0;
         if (gcfg->train_batch) gr.batch = gcfg->train_batch;
         if (gcfg->train_steps) gr.steps = gcfg->train_steps;
+        gr.budget = gcfg->train_budget;
+        DR_CHECK_ARG(gcfg->target <= 1, "dr_render_guided: target must be 0 or 1");
+        gr.target = gcfg->target;
     }
     if (cfg->spp == 0) return DR_OK;
     DR_CUDA(cudaSetDevice(s->ctx->device));
@@ -1089,7 +1096,7 @@ extern "C" dr_status dr_render_guided(dr_scene *s, const dr_camera *cam, const d
     DR_CHECK_ARG(npix64 < (1ull << 31) / 16, "dr_render_guided: image too large");
     WaveConfig wc;
     if (cfg->wave_paths) wc.wave_paths = cfg->wave_paths;
-    wc.streams = 1;
+    if (cfg->streams) wc.streams = cfg->streams;
     wc.chunk = cfg->chunk;
     const std::vector<RenderJob> jobs{make_job(s, cam, cfg, accum_dev, casts_dev)};
     const WavePlan plan = plan_waves(jobs, wc.wave_paths);

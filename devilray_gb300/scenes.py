@@ -260,7 +260,7 @@ def many_light(num_triangles: int = 1 << 20, num_emitters: int = 65536, seed: in
 
 def occluded_light(num_triangles: int = 1 << 20, num_emitters: int = 65536, seed: int = 0,
                    half: float = CUBE_HALF, light_y: float = 0.4, slab_y: float = 0.3,
-                   slab_extent: float = 0.7, enclose: bool = True) -> SceneSpec:
+                   slab_extent: float = 0.7, enclose="box") -> SceneSpec:
     """The guided configuration: the many-light scene with its emitters only on
     spheres whose centre lies above `light_y` * half, and a diffuse occluding
     slab (albedo 0.8, two triangles) at height `slab_y` * half covering
@@ -299,10 +299,15 @@ def occluded_light(num_triangles: int = 1 << 20, num_emitters: int = 65536, seed
     grey = s.add_material(material(0, albedo=(0.8, 0.8, 0.8)))
     s.add_object(slab, grey)
     if enclose:
-        # a floor and a back wall catch the light that passes the slab's edges
-        # and scatter it under the slab
-        s.add_object(quad((0.0, -1.1 * half, 0.0), (0.0, 1.0, 0.0), (1.0, 0.0, 0.0), 3.0 * half), grey)
-        s.add_object(quad((0.0, 0.0, 1.1 * half), (0.0, 0.0, -1.0), (1.0, 0.0, 0.0), 3.0 * half), grey)
+        # a floor, a back wall and side walls (open towards the camera) catch the
+        # light that passes the slab's edges and scatter it under the slab
+        w = 1.15 * half
+        s.add_object(quad((0.0, -w, 0.0), (0.0, 1.0, 0.0), (1.0, 0.0, 0.0), 2 * w), grey)
+        s.add_object(quad((0.0, 0.0, w), (0.0, 0.0, -1.0), (1.0, 0.0, 0.0), 2 * w), grey)
+        if enclose == "box":
+            s.add_object(quad((-w, 0.0, 0.0), (1.0, 0.0, 0.0), (0.0, 0.0, 1.0), 2 * w), grey)
+            s.add_object(quad((w, 0.0, 0.0), (-1.0, 0.0, 0.0), (0.0, 0.0, 1.0), 2 * w), grey)
+            s.add_object(quad((0.0, w, 0.0), (0.0, -1.0, 0.0), (1.0, 0.0, 0.0), 2 * w), grey)
     return s
 
 

@@ -419,6 +419,9 @@ typedef struct dr_guided_config {
     uint32_t train;           /* 1: collect samples and train after every wave */
     uint32_t train_batch;     /* rows per training step, 0 = 16384 */
     uint32_t train_steps;     /* Adam steps after every wave, 0 = 4 */
+    uint32_t train_budget;    /* no training once the network has taken this many steps, 0 = no limit */
+    uint32_t target;          /* training target density: 0 = L cos (incident radiance L along the
+                                 sampled direction), 1 = log(1 + L) cos (less dominated by rare bright paths) */
 } dr_guided_config;
 
 /* dr_render with path guiding: at each diffuse vertex the network's mixture
@@ -429,8 +432,10 @@ typedef struct dr_guided_config {
  * and of emission hits, so the image stays unbiased for any network. With
  * `train`, every finished wave's diffuse vertices (first 3 of each path) give
  * training samples (incident radiance along the sampled direction) and the
- * network takes train_steps Adam steps. Waves run one at a time. Asynchronous
- * on `stream`. */
+ * network takes train_steps Adam steps (in wave order; waves still overlap on
+ * cfg->streams streams, and a wave may read weights that another wave's
+ * training is updating: each vertex samples and weighs with the one mixture
+ * it computed). Asynchronous on `stream`. */
 dr_status dr_render_guided(dr_scene *scene, const dr_camera *camera, const dr_render_config *cfg, dr_guide *guide,
                            const dr_guided_config *gcfg, float *accum_dev, uint32_t *casts_dev, void *stream);
 
