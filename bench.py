@@ -485,15 +485,16 @@ def guided_section(ctx, native, device: int, stream, width: int = 480, height: i
         stream.synchronize()
         return e0.elapsed_time(e1) / 1e3
 
-    t_plain = timed(lambda: scene.render(cam, acc, spp=spp, max_depth=depth, seed=1, stream=stream))
+    t_plain = timed(lambda: scene.render(cam, acc, spp=spp, max_depth=depth, seed=1, wave_paths=npix * 16,
+                                         stream=stream))
     rmse_plain = rmse(image(acc))
     pos = spec.positions.reshape(-1, 3)
     lo, hi = pos.min(0), pos.max(0)
     guide = native.Guide(ctx, seed=1, center=tuple(float(x) for x in (lo + hi) / 2),
                          half_extent=float((hi - lo).max() / 2))
-    wave = npix * 8  # eight samples per wave: a training round of 8 steps after each
+    wave = npix * 16  # the plain tracer's default wave (2^21 paths): a training round after every 16 samples
     t_guided = timed(lambda: scene.render_guided(guide, cam, acc, spp=spp, max_depth=depth, seed=2, alpha=0.5,
-                                                 train=True, train_batch=16384, train_steps=8, wave_paths=wave,
+                                                 train=True, train_batch=16384, train_steps=16, wave_paths=wave,
                                                  stream=stream))
     rmse_guided = rmse(image(acc))
     loss = guide.last_loss()
@@ -527,7 +528,7 @@ def guided_section(ctx, native, device: int, stream, width: int = 480, height: i
            "reference_seconds": round(ref_s, 2), "spp": spp, "alpha": 0.5,
            "plain": {"rmse": rmse_plain, "seconds": t_plain},
            "guided": {"rmse": rmse_guided, "seconds": t_guided, "final_loss": loss,
-                      "training": "8 Adam steps x 16384 samples after every 8 spp"},
+                      "training": "16 Adam steps x 16384 samples after every 16 spp"},
            "plain_equal_time": {"rmse": rmse_eq, "spp": spp_eq, "seconds": t_eq},
            "guided_trained_equal_spp": {"rmse": rmse_trained, "seconds": t_trained},
            "rmse_ratio_equal_spp": rmse_plain / rmse_guided, "rmse_ratio_equal_time": rmse_eq / rmse_guided,
