@@ -320,13 +320,12 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// Shared memory of k_guide_infer_tc (byte offsets). The operand regions are
-// padded so that every core matrix a descriptor can name stays inside them.
+// Shared memory of k_guide_infer_tc (byte offsets).
 constexpr uint32_t kTcW0 = 0;                        // 64 x 80
 constexpr uint32_t kTcW1 = kTcW0 + 64 * 80 * 2;      // 3 x 64 x 64
 constexpr uint32_t kTcW4 = kTcW1 + 3 * 64 * 64 * 2;  // 48 x 64
-constexpr uint32_t kTcA = kTcW4 + 48 * 64 * 2 + 4096;  // 128 x 80 input / 128 x 64 hidden
-constexpr uint32_t kTcBias = kTcA + 65536;
+constexpr uint32_t kTcA = kTcW4 + 48 * 64 * 2 + 1024;  // 128 x 80 input / 128 x 64 hidden
+constexpr uint32_t kTcBias = kTcA + kTcRows * kIn * 2;
 constexpr uint32_t kTcBar = kTcBias + (4 * kHid + kOut) * 4;
 constexpr uint32_t kTcSmem = kTcBar + 16;
 
@@ -337,15 +336,17 @@ __global__ void __launch_bounds__(128) k_guide_infer_tc(const __nv_bfloat16 *wb,
 {
     extern __shared__ __align__(1024) unsigned char smem[];
     const int tid = threadIdx.x, warp = tid >> 5;
-    // weights in the canonical layout (B operands: N = outputs, K = inputs)
-    for (int i = tid; i < kHid * kIn; i += 128)
-        *reinterpret_cast<__nv_bfloat16 *>(smem + kTcW0 + canon_off(i / kIn, i % kIn, kHid)) = wb[i];
-    for (int l = 1; l <= 3; ++l)
-        for (int i = tid; i < kHid * kHid; i += 128)
-            *reinterpret_cast<__nv_bfloat16 *>(smem + kTcW1 + (l - 1) * kHid * kHid * 2 + canon_off(i / kHid, i % kHid, kHid)) =
-                wb[wb_off(l) + i];
-    for (int i = tid; i < kOut * kHid; i += 128)
-        *reinterpret_cast<__nv_bfloat16 *>(smem + kTcW4 + canon_off(i / kHid, i % kHid, kOut)) = wb[wb_off(4) + i];
+    // weights in the canonical layout (B operands: N = outputs, K = inputs),
+    // 16-byte chunks: 8 consecutive inputs of one output row
+    for (int l = 0; l < kLayers; ++l) {
+        const int K = fan_in(l), N = fan_out(l), chunks = K / 8;
+        const uint32_t base = l == 0 ? kTcW0 : l == 4 ? kTcW4 : kTcW1 + (uint32_t)(l - 1) * kHid * kHid * 2;
+        const uint4 *src = reinterpret_cast<const uint4 *>(wb + wb_off(l));
+        for (int i = tid; i < N * chunks; i += 128) {
+            const int r = i / chunks, j = i % chunks;
+            *reinterpret_cast<uint4 *>(smem + base + canon_off(r, 8 * j, N)) = src[i];
+        }
+    }
     float *bias = reinterpret_cast<float *>(smem + kTcBias);
     for (int l = 0; l < kLayers; ++l)
         for (int i = tid; i < fan_out(l); i += 128) bias[l * kHid + i] = params[b_off(l) + i];
@@ -868,7 +869,7 @@ cudaError_t launch_guide_infer(const dr_guide *g, const float *pos, const float 
     if (max_rows == 0) return cudaSuccess;
     if (g->cfg.infer_kernel == DR_GUIDE_INFER_TCGEN05) {
         const unsigned tiles = (max_rows + kTcRows - 1) / kTcRows;
-        const unsigned blocks = std::min<unsigned>(tiles, (unsigned)g->ctx->num_sms * 2);
+        const unsigned blocks = std::min<unsigned>(tiles, (unsigned)g->ctx->num_sms * 3);
         k_guide_infer_tc<<<blocks, 128, kTcSmem, st>>>(g->wb, g->params, guide_params(g), pos, dir, list, count,
                                                        max_rows, y, g->ctx->d_error);
     } else {

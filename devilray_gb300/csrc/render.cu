@@ -70,6 +70,7 @@ struct RenderParams {
     float *rec;                // [slot][kGuideRecords][kRecFloats] training records
     uint32_t *rec_n;           // [slot] records; bit 31: the last one waits for its radiance
     float guide_alpha;         // probability of sampling the network's mixture
+    int guide_bounces;         // bounces b < guide_bounces are guided, later ones sample the cosine lobe
     int guide_target;          // training target: 0 radiance, 1 log(1 + radiance)
     float *train_pos, *train_nrm, *train_dir, *train_w;  // training ring
     uint32_t *train_head;
@@ -434,7 +435,8 @@ __global__ void __launch_bounds__(kRenderBlock) k_shade(RenderParams p, int b)
                             col = add4(col, mul4s(mul4(E, thr), power_heuristic(pdf_bsdf, pdf_nee)));
                     }
                     GuideLobes lobes;
-                    if (GUIDED) lobes = guide_decode(p.guide_y + (size_t)slot * kGuideOut);
+                    const float alpha = GUIDED && b < p.guide_bounces ? p.guide_alpha : 0.0f;
+                    if (GUIDED && alpha > 0.0f) lobes = guide_decode(p.guide_y + (size_t)slot * kGuideOut);
                     // next-event estimation: samplePointOnLights (:234-272) and
                     // evaluateDirectLighting (:336-361); visibility is the shadow ray
                     if (J.lights) {
@@ -466,10 +468,9 @@ __global__ void __launch_bounds__(kRenderBlock) k_shade(RenderParams p, int b)
                         lp = f3(lp.x * 1.0f + 0.0f, lp.y * 1.0f + 0.0f, lp.z * 1.0f + 0.0f);
                         const dr_material &LM = p.materials[ob.material];
                         float nee_pdf_bsdf = cosine_pdf(hp, lp, n);
-                        if (GUIDED) {
+                        if (GUIDED && alpha > 0.0f) {
                             const F3 wl0 = normalized(sub(lp, hp));
-                            nee_pdf_bsdf = p.guide_alpha * guide_pdf(lobes, wl0.x, wl0.y, wl0.z) +
-                                           (1.0f - p.guide_alpha) * nee_pdf_bsdf;
+                            nee_pdf_bsdf = alpha * guide_pdf(lobes, wl0.x, wl0.y, wl0.z) + (1.0f - alpha) * nee_pdf_bsdf;
                         }
                         const float nee_pdf_nee = lpdf * area_to_solid_angle(hp, lp, ln);
                         const float dist = length(sub(lp, hp));
@@ -494,7 +495,7 @@ __global__ void __launch_bounds__(kRenderBlock) k_shade(RenderParams p, int b)
                     }
                     if (GUIDED && !J.lights) uniforms4(J, pixel, sample, g + 2, u + 8);
                     bool cosine = true;
-                    if (GUIDED && u[9] < p.guide_alpha) {
+                    if (GUIDED && u[9] < alpha) {
                         cosine = false;
                         float wx, wy, wz;
                         guide_sample(lobes, u[10], u[0], u[1], wx, wy, wz);
@@ -513,14 +514,14 @@ __global__ void __launch_bounds__(kRenderBlock) k_shade(RenderParams p, int b)
                     if (GUIDED) {
                         // one-sample MIS over the mixture and the cosine lobe: f cos / pdf_mix
                         const float c = dot(new_v, n);
-                        const float pdf_mix = p.guide_alpha * guide_pdf(lobes, new_v.x, new_v.y, new_v.z) +
-                                              (1.0f - p.guide_alpha) * fmaxf(c, 0.0f) / kPi;
+                        const float pdf_mix = (alpha > 0.0f ? alpha * guide_pdf(lobes, new_v.x, new_v.y, new_v.z) : 0.0f) +
+                                              (1.0f - alpha) * fmaxf(c, 0.0f) / kPi;
                         const float f = c > 0.0f && pdf_mix > 0.0f ? c / (kPi * pdf_mix) : 0.0f;
                         thr = mul4s(mul4(thr, alb), f);
                         p.prev_pdf[slot] = pdf_mix;
                         if (f == 0.0f) dead = true;
                         const uint32_t rn = p.rec_n[slot];
-                        if (!dead && rn < (uint32_t)kGuideRecords && b + 1 < (int)J.max_depth) {
+                        if (!dead && alpha > 0.0f && rn < (uint32_t)kGuideRecords && b + 1 < (int)J.max_depth) {
                             float *rc = p.rec + ((size_t)slot * kGuideRecords + rn) * kRecFloats;
                             rc[0] = hp.x, rc[1] = hp.y, rc[2] = hp.z;
                             rc[3] = n.x, rc[4] = n.y, rc[5] = n.z;
@@ -910,6 +911,7 @@ dr_status WaveRunner::enqueue(const SceneArrays &sc, const WavePlan &plan, const
         if (gr) {
             q.guide_alpha = gr->alpha;
             q.guide_target = (int)gr->target;
+            q.guide_bounces = (int)gr->bounces;
             q.train_pos = t_pos, q.train_nrm = t_nrm, q.train_dir = t_dir, q.train_w = t_w;
             q.train_head = t_head;
             q.train_cap = train_cap;
@@ -935,9 +937,11 @@ dr_status WaveRunner::enqueue(const SceneArrays &sc, const WavePlan &plan, const
                 else k_wave_closest<0, 2><<<trace_grid, kTraceBlock, 0, ws>>>(q, b);
             }
             if (gr) {
-                k_guide_prepare<<<shade_grid, kRenderBlock, 0, ws>>>(q, b);
-                DR_CUDA(launch_guide_infer(gr->guide, q.guide_pos, q.guide_nrm, q.guide_list, q.guide_counts + b, W,
-                                           q.guide_y, ws));
+                if (b < (int)gr->bounces) {
+                    k_guide_prepare<<<shade_grid, kRenderBlock, 0, ws>>>(q, b);
+                    DR_CUDA(launch_guide_infer(gr->guide, q.guide_pos, q.guide_nrm, q.guide_list, q.guide_counts + b,
+                                               W, q.guide_y, ws));
+                }
                 k_shade<true><<<shade_grid, kRenderBlock, 0, ws>>>(q, b);
             } else {
                 k_shade<false><<<shade_grid, kRenderBlock, 0, ws>>>(q, b);
@@ -1088,6 +1092,7 @@ extern "C" dr_status dr_render_guided(dr_scene *s, const dr_camera *cam, const d
         gr.budget = gcfg->train_budget;
         DR_CHECK_ARG(gcfg->target <= 1, "dr_render_guided: target must be 0 or 1");
         gr.target = gcfg->target;
+        gr.bounces = gcfg->bounces ? gcfg->bounces : 64;
     }
     if (cfg->spp == 0) return DR_OK;
     DR_CUDA(cudaSetDevice(s->ctx->device));

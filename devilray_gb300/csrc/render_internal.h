@@ -85,6 +85,7 @@ struct GuideRun {
     uint32_t budget = 0;  // total Adam steps of the network after which training stops, 0 = none
     uint32_t streams = 1; // concurrent waves; training of the waves runs one after another
     uint32_t target = 0;  // training target: 0 radiance, 1 log(1 + radiance)
+    uint32_t bounces = 64;  // bounces b < bounces are guided
 };
 
 // Packs the samples of `jobs` (their npix and spp) into waves.

@@ -260,14 +260,14 @@ def many_light(num_triangles: int = 1 << 20, num_emitters: int = 65536, seed: in
 
 def occluded_light(num_triangles: int = 1 << 20, num_emitters: int = 65536, seed: int = 0,
                    half: float = CUBE_HALF, light_y: float = 0.4, slab_y: float = 0.3,
-                   slab_extent: float = 0.7, enclose="box") -> SceneSpec:
+                   slab_extent: float = 0.7, enclose="box", room_albedo: float = 0.4) -> SceneSpec:
     """The guided configuration: the many-light scene with its emitters only on
     spheres whose centre lies above `light_y` * half, and a diffuse occluding
     slab (albedo 0.8, two triangles) at height `slab_y` * half covering
     `slab_extent` of the cube's width in x and z, so light reaches the
     spheres below mostly through the gaps at the slab's edges, off a floor
-    and a back wall (`enclose`): indirect light dominates the camera's view of
-    the lower region."""
+    and walls (`enclose`, albedo `room_albedo`): indirect light dominates the
+    camera's view of the lower region."""
     soup, centres, radii = incoherent_soup(num_triangles, seed=seed, half=half)
     per = 1280
     rng = np.random.default_rng(seed + 17)
@@ -296,7 +296,7 @@ def occluded_light(num_triangles: int = 1 << 20, num_emitters: int = 65536, seed
             s.add_object(soup[t:t + 1], m)
     e = slab_extent * half
     slab = quad((0.0, slab_y * half, 0.0), (0.0, -1.0, 0.0), (1.0, 0.0, 0.0), 2 * e)
-    grey = s.add_material(material(0, albedo=(0.8, 0.8, 0.8)))
+    grey = s.add_material(material(0, albedo=(room_albedo,) * 3))
     s.add_object(slab, grey)
     if enclose:
         # a floor, a back wall and side walls (open towards the camera) catch the

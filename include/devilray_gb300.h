@@ -422,6 +422,8 @@ typedef struct dr_guided_config {
     uint32_t train_budget;    /* no training once the network has taken this many steps, 0 = no limit */
     uint32_t target;          /* training target density: 0 = L cos (incident radiance L along the
                                  sampled direction), 1 = log(1 + L) cos (less dominated by rare bright paths) */
+    uint32_t bounces;         /* guide the vertices of bounces 0 .. bounces-1 only (later ones sample the
+                                 cosine lobe, no network evaluation), 0 = all */
 } dr_guided_config;
 
 /* dr_render with path guiding: at each diffuse vertex the network's mixture

@@ -49,14 +49,15 @@ def test_alpha_zero_reproduces_the_plain_image(native, ctx):
     assert np.median(rel) < 1e-5 and rel.max() < 2e-3, (np.median(rel), rel.max())
 
 
-def test_untrained_guide_is_unbiased(native, ctx):
+@pytest.mark.parametrize("bounces", [0, 1])
+def test_untrained_guide_is_unbiased(native, ctx, bounces):
     spec = scenes.box_room(sphere_level=2)
     scene = native.Scene.from_spec(ctx, spec)
     cam = scenes.camera(24, 18)
     g = _guide_for(native, ctx, spec, seed=11)
     a, _ = _render(native, scene, cam, 2048, 6, 1)
     b, _ = _render(native, scene, cam, 2048, 6, 2)
-    gi, _ = _render(native, scene, cam, 2048, 6, 3, guide=g, alpha=0.5, train=False)
+    gi, _ = _render(native, scene, cam, 2048, 6, 3, guide=g, alpha=0.5, train=False, bounces=bounces)
     noise = np.sqrt(np.mean((a - b) ** 2))
     assert np.sqrt(np.mean((gi - a) ** 2)) < 3.0 * noise
     ma, mb, mg = a.mean(), b.mean(), gi.mean()
