@@ -16,6 +16,19 @@ namespace dr {
 
 constexpr uint32_t kPersistentChunk = 128;
 
+// A warp refills its idle lanes once at least this many are idle (or all are):
+// fewer, fuller refills (measured on the incoherent workload: 1 -> 3.68,
+// 4 -> 3.78, 8 -> 3.78, 16 -> 3.54 Grays/s).
+#ifndef DR_REFILL_MIN
+#define DR_REFILL_MIN 8
+#endif
+// A lane postpones its leaf triangles while fewer than this many lanes of its
+// warp have triangles to test (0: never).
+#ifndef DR_POSTPONE_MIN
+#define DR_POSTPONE_MIN 0
+#endif
+
+
 // Indices a warp reserves at once: 128 when there is plenty of work, down to
 // one per lane when few rays are left, so a small launch still spreads over
 // many warps (warp-uniform). A nonzero `fixed` (a multiple of 32) overrides it.
@@ -66,12 +79,6 @@ __device__ __forceinline__ void persistent_wide(const Wide8Args &a, const Source
     uint64_t chunk_next = 0, chunk_end = 0;  // warp-uniform
     const uint32_t chunk = persistent_chunk(n, fixed_chunk);
     unsigned long long cn = 0, cb = 0, ct = 0, ch = 0;
-// A warp refills its idle lanes once at least this many are idle (or all are):
-// fewer, fuller refills (measured on the incoherent workload: 1 -> 3.68,
-// 4 -> 3.78, 8 -> 3.78, 16 -> 3.54 Grays/s).
-#ifndef DR_REFILL_MIN
-#define DR_REFILL_MIN 8
-#endif
     while (true) {
         unsigned want = __ballot_sync(FULL, !active);
         // refill once enough lanes are idle (or none is busy)
@@ -112,17 +119,35 @@ __device__ __forceinline__ void persistent_wide(const Wide8Args &a, const Source
             if (exhausted) break;
             continue;
         }
-        if (active) {
-            bool found = false;
-            if (wide_step<MODE, ANY>(a, s, stack, found, cn, cb, ct)) {
-                if (ANY) {
-                    src.any(idx, found);
-                } else {
-                    src.closest(idx, s.best_t, s.best_prim);
-                    if (s.best_prim != INT_MAX) ++ch;
-                }
-                active = false;
+        // 1. node test
+        if (active && s.have_node) wide_visit<MODE>(a, s, cn, cb);
+        // 2. leaf triangles: tested now when enough lanes of the warp have some
+        //    (or the lane has no node to go to); otherwise pushed as a group and
+        //    tested when popped (Ylitie, Karras and Laine 2017, triangle
+        //    postponing). Results do not depend on the order of the tests.
+        const bool has_tri = active && s.tmask != 0;
+        const unsigned tri_lanes = __ballot_sync(FULL, has_tri);
+        bool done = false, found = false;
+        if (has_tri) {
+            const bool postpone = DR_POSTPONE_MIN > 0 && __popc(tri_lanes) < DR_POSTPONE_MIN &&
+                                  (s.group.y >> 8) != 0 && s.sp < kWideStack - 8;
+            if (postpone) {
+                stack[s.sp++] = make_uint2(s.tbase, s.tmask | kTriGroupFlag);
+                s.tmask = 0;
+            } else if (wide_triangles<MODE, ANY>(a, s, ct)) {
+                done = found = true;
             }
+        }
+        // 3. next node
+        if (active && !done && s.tmask == 0) done = wide_advance<ANY>(a, s, stack);
+        if (active && done) {
+            if (ANY) {
+                src.any(idx, found);
+            } else {
+                src.closest(idx, s.best_t, s.best_prim);
+                if (s.best_prim != INT_MAX) ++ch;
+            }
+            active = false;
         }
     }
     if (COUNT) {

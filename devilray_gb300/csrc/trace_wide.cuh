@@ -142,6 +142,7 @@ struct WideState {
     uint2 group;
     int sp;
     bool have_node;
+    uint32_t tbase, tmask;  // triangles waiting to be tested (persistent kernels)
 };
 
 template <int MODE>
@@ -156,37 +157,46 @@ __host__ __device__ __forceinline__ void wide_init(WideState &s, const DevRay &r
     s.group = make_uint2(0, 0);
     s.sp = 0;
     s.have_node = true;
+    s.tbase = 0;
+    s.tmask = 0;
 }
 
-// One node (its 8 boxes and its leaf triangles) of the ray's traversal.
-// Returns true when the ray is finished (no node left, or a hit for ANY).
-template <int MODE, bool ANY>
-__host__ __device__ __forceinline__ bool wide_step(const Wide8Args &a, WideState &s, uint2 *stack, bool &found,
-                                                   unsigned long long &nn, unsigned long long &nb,
-                                                   unsigned long long &nt)
+// Stack entry of a postponed triangle group: y carries this flag above the
+// triangle mask (node groups keep y < 2^16).
+constexpr uint32_t kTriGroupFlag = 0x80000000u;
+
+// Node test of the persistent kernels: the node's internal hits become the
+// current group, its hit leaf triangles the pending triangle group.
+template <int MODE>
+__device__ __forceinline__ void wide_visit(const Wide8Args &a, WideState &s, unsigned long long &nn,
+                                           unsigned long long &nb)
 {
-    uint32_t tri_base = 0, tri_mask = 0;
-    if (s.have_node) {
-        uint32_t child_base, imask, hit_int, nbx;
-        wide_node_test(a.nodes + s.node, s.r, s.oct, s.best_t, child_base, imask, hit_int, tri_base, tri_mask, nbx);
-        ++nn;
-        nb += nbx;
-        s.group = make_uint2(child_base, (hit_int << 8) | imask);
-        s.have_node = false;
-    }
-    while (tri_mask) {
-        const int b = lowest_bit(tri_mask);
-        tri_mask &= tri_mask - 1u;
-        const uint32_t k = tri_base + (uint32_t)b;
+    uint32_t child_base, imask, hit_int, nbx, tri_base, tri_mask;
+    wide_node_test(a.nodes + s.node, s.r, s.oct, s.best_t, child_base, imask, hit_int, tri_base, tri_mask, nbx);
+    ++nn;
+    nb += nbx;
+    s.group = make_uint2(child_base, (hit_int << 8) | imask);
+    s.tbase = tri_base;
+    s.tmask = tri_mask;
+    s.have_node = false;
+}
+
+// Tests the pending triangles; true when an any-hit query is answered.
+template <int MODE, bool ANY>
+__device__ __forceinline__ bool wide_triangles(const Wide8Args &a, WideState &s, unsigned long long &nt)
+{
+    uint32_t m = s.tmask;
+    s.tmask = 0;
+    while (m) {
+        const int b = lowest_bit(m);
+        m &= m - 1u;
+        const uint32_t k = s.tbase + (uint32_t)b;
         ++nt;
         float t;
         const bool ok = MODE == 1 ? tri_test_wt(a.tri_wt, k, s.r, s.w, ANY ? s.r.tmax : s.best_t, t)
                                   : tri_test_ref(a.tri_ref, k, s.r, ANY ? s.r.tmax : s.best_t, t);
         if (ok) {
-            if (ANY) {
-                found = true;
-                return true;
-            }
+            if (ANY) return true;
             const int32_t prim = DR_LD(a.prim + k);
             if (t < s.best_t || prim < s.best_prim) {
                 s.best_t = t;
@@ -194,9 +204,23 @@ __host__ __device__ __forceinline__ bool wide_step(const Wide8Args &a, WideState
             }
         }
     }
+    return false;
+}
+
+// Next node: from the current group, else from the stack (a popped triangle
+// group becomes pending and is tested first). True when the ray is finished.
+template <bool ANY>
+__device__ __forceinline__ bool wide_advance(const Wide8Args &a, WideState &s, uint2 *stack)
+{
     if ((s.group.y >> 8) == 0) {
         if (s.sp == 0) return true;
-        s.group = stack[--s.sp];
+        const uint2 e = stack[--s.sp];
+        if (e.y & kTriGroupFlag) {
+            s.tbase = e.x;
+            s.tmask = e.y & ~kTriGroupFlag;
+            return false;
+        }
+        s.group = e;
     }
     const uint32_t hits = s.group.y >> 8;
     const int k = lowest_bit(hits);
@@ -208,9 +232,7 @@ __host__ __device__ __forceinline__ bool wide_step(const Wide8Args &a, WideState
     s.group.y = (rest << 8) | imask;
     if (rest) {
         if (s.sp >= kWideStack) {
-#if defined(__CUDA_ARCH__)
             atomicOr(a.error, ERR_STACK_OVERFLOW);
-#endif
             return true;
         }
         stack[s.sp++] = s.group;
