@@ -417,6 +417,26 @@ def batch_section(ctx, native, device: int, stream, scenes_n: int = 64, spp: int
     info = b.info()
     path_rays = sum(int(c.sum().item()) for _, c in outs)
     samples = int(info.paths_per_render)
+    # the same scenes built on the device (linear BVH, binary layout): build time
+    # and the batch's samples/s with those hierarchies
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    dscs = [native.Scene.from_spec(ctx, spec, builder=1) for spec, _ in specs]
+    torch.cuda.synchronize()
+    dev_build_s = time.perf_counter() - t0
+    djobs = [native.make_job(sc, cam, acc, casts, spp=spp, max_depth=depth, seed=i)
+             for i, ((spec, cam), sc, (acc, casts)) in enumerate(zip(specs, dscs, outs))]
+    db = native.Batch(ctx, djobs, wave_paths=tune.wave_paths, streams=tune.streams, chunk=tune.chunk, use_graph=True)
+    db.render(stream=stream)
+    stream.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    db.render(sample_offsets=[0] * len(djobs), stream=stream)
+    e1.record(stream)
+    stream.synchronize()
+    t_dev = e0.elapsed_time(e1) / 1e3
+    db.close()
+    del dscs, djobs
     # the same images one dr_render call at a time (default schedule)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -434,6 +454,8 @@ def batch_section(ctx, native, device: int, stream, scenes_n: int = 64, spp: int
            "sequential_dr_render_seconds": t_seq, "sequential_samples_per_s": samples / t_seq,
            "autotune_scene": tune_scene.as_dict(), "autotune_batch": tune.as_dict(),
            "autotune_seconds": round(tune_scene_s + tune_batch_s, 3), "scene_build_s": round(build_s, 3),
+           "device_lbvh": {"scene_build_s": round(dev_build_s, 3), "samples_per_s": samples / t_dev,
+                           "note": "the same 64 scenes built on the device (linear BVH, binary layout)"},
            "scene_generation_s": round(gen_s, 3)}
     b.close()
     del jobs, outs, scs

@@ -194,9 +194,37 @@ dr_status dr_scene_create(dr_context *ctx, const dr_scene_desc *desc, const dr_b
         bp.threads = cfg->threads;
     }
     const float slack = scene_slack(mag);
-    const uint32_t layout = (cfg && cfg->layout == 2) ? 2u : 8u;
+    const bool device_build = cfg && cfg->builder == DR_BUILD_DEVICE_LBVH;
+    if (cfg && cfg->builder != DR_BUILD_HOST_SAH && cfg->builder != DR_BUILD_DEVICE_LBVH)
+        return fail(DR_ERR_INVALID_ARGUMENT, "dr_scene_create: unknown builder");
+    if (device_build && cfg->layout == 8)
+        return fail(DR_ERR_INVALID_ARGUMENT, "dr_scene_create: the device build makes the binary layout");
+    const uint32_t layout = device_build || (cfg && cfg->layout == 2) ? 2u : 8u;
     if (cfg && cfg->layout != 0 && cfg->layout != 2 && cfg->layout != 8)
         return fail(DR_ERR_INVALID_ARGUMENT, "dr_scene_create: layout must be 0, 2 or 8");
+    if (device_build && n > 0) {
+        auto *s = new (std::nothrow) dr_scene;
+        if (!s) return fail(DR_ERR_OUT_OF_MEMORY, "host allocation failed");
+        s->ctx = ctx;
+        s->num_tris = n;
+        s->layout = 2;
+        s->slack = slack;
+        dr_status r = build_lbvh_device(s, desc->positions_host, n, slack);
+        cudaError_t e = cudaSuccess;
+        if (r == DR_OK && desc->materials_host && desc->num_materials) {
+            if ((e = upload(&s->d_materials, desc->materials_host, desc->num_materials, s->device_bytes)) != cudaSuccess)
+                r = cuda_fail(e, "dr_scene_create upload materials");
+            s->num_materials = desc->num_materials;
+        }
+        if (r == DR_OK) r = build_render_data(s, desc);
+        if (r != DR_OK) {
+            dr_scene_destroy(s);
+            return r;
+        }
+        s->build_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+        *out = s;
+        return DR_OK;
+    }
     Bvh2 bvh2;
     Bvh8 bvh8;
     const std::vector<uint32_t> *order;

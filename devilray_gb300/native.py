@@ -64,7 +64,7 @@ class SceneDesc(C.Structure):
 
 class BuildConfig(C.Structure):
     _fields_ = [("max_leaf_size", C.c_uint32), ("sah_bins", C.c_uint32), ("threads", C.c_uint32),
-                ("layout", C.c_uint32)]
+                ("layout", C.c_uint32), ("builder", C.c_uint32)]
 
 
 class SceneInfo(C.Structure):
@@ -353,11 +353,11 @@ class Scene:
 
     def __init__(self, ctx: Context, positions: np.ndarray, objects=None, materials=None,
                  tri_material=None, tri_weight=None, max_leaf_size: int = 0, sah_bins: int = 0,
-                 threads: int = 0, layout: int = 0):
+                 threads: int = 0, layout: int = 0, builder: int = 0):
         self.ctx = ctx
         self.positions = np.ascontiguousarray(positions, np.float32).reshape(-1, 9)
         desc, keep = scene_desc(self.positions, objects, materials, tri_material, tri_weight)
-        cfg = BuildConfig(max_leaf_size, sah_bins, threads, layout)
+        cfg = BuildConfig(max_leaf_size, sah_bins, threads, layout, builder)
         self.handle = C.c_void_p()
         check(load().dr_scene_create(ctx.handle, C.byref(desc), C.byref(cfg), C.byref(self.handle)))
         self._keep = keep

@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define DR_ABI_VERSION 3
+#define DR_ABI_VERSION 4
 
 typedef enum dr_status {
     DR_OK = 0,
@@ -148,11 +148,17 @@ typedef struct dr_scene_desc {
     const float *tri_weight_host;
 } dr_scene_desc;
 
+typedef enum dr_builder {
+    DR_BUILD_HOST_SAH = 0,     /* binned SAH on the host (threads), either layout */
+    DR_BUILD_DEVICE_LBVH = 1   /* linear BVH on the device (Morton order, one triangle per leaf); binary layout */
+} dr_builder;
+
 typedef struct dr_build_config {
     uint32_t max_leaf_size;  /* 0 = default (tuned) */
     uint32_t sah_bins;       /* 0 = default */
     uint32_t threads;        /* host build threads, 0 = all cores */
     uint32_t layout;         /* 0 = default, 2 = binary, 8 = compressed 8-wide */
+    uint32_t builder;        /* dr_builder */
 } dr_build_config;
 
 typedef struct dr_scene dr_scene;

@@ -182,3 +182,50 @@ def test_read_bandwidth_probe(native, ctx):
     buf = torch.ones(8 * 1024 * 1024, dtype=torch.float32, device="cuda")
     gbs = ctx.read_bandwidth(buf, buf.numel() * 4, reps=5)
     assert 100.0 < gbs < 1e6
+
+
+@pytest.mark.parametrize("n,dup", [(1, 0), (2, 0), (3, 0), (100, 0), (4096, 0), (1 << 18, 0), (5000, 3)])
+def test_device_lbvh_build_matches_host_build(native, ctx, oracle, n, dup):
+    """The device linear BVH (DR_BUILD_DEVICE_LBVH) gives the same hits, bit for
+    bit, as the host binned-SAH build and the oracle; `dup` repeats every
+    triangle (equal Morton codes)."""
+    soup, _, _ = scenes.incoherent_soup(n, seed=n + 3)
+    if dup:
+        soup = np.repeat(soup, dup, axis=0)
+    rays = scenes.incoherent_rays(20000, seed=5)
+    dev = native.Scene(ctx, soup, builder=1)
+    host = native.Scene(ctx, soup, layout=2)
+    assert dev.info().layout == 2 and dev.info().num_nodes == max(1, len(soup) - 1)
+    d_rays = torch.from_numpy(rays).cuda()
+    out = []
+    for sc in (dev, host):
+        h = torch.empty((len(rays), 2), dtype=torch.int32, device="cuda")
+        sc.trace_closest(d_rays, len(rays), h)
+        occ = torch.empty(len(rays), dtype=torch.uint8, device="cuda")
+        sc.trace_any(d_rays, len(rays), occ)
+        torch.cuda.synchronize()
+        out.append((h.cpu().numpy(), occ.cpu().numpy()))
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+    if len(soup) <= 4096:
+        t, prim = oracle.BBH(soup).trace_canonical(rays, slack=host.info().slack)
+        assert np.array_equal(out[0][0][:, 1], prim)
+    ctx.check()
+
+
+def test_device_lbvh_render_matches_host(native, ctx):
+    spec = scenes.box_room(sphere_level=2)
+    cam = scenes.camera(32, 24)
+    outs = []
+    for kw in ({"builder": 1}, {"layout": 2}):
+        sc = native.Scene.from_spec(ctx, spec, **kw)
+        acc = torch.zeros((32 * 24, 4), dtype=torch.float32, device="cuda")
+        sc.render(cam, acc, spp=4, max_depth=8)
+        torch.cuda.synchronize()
+        outs.append(acc.cpu().numpy())
+    assert np.array_equal(outs[0].view(np.uint32), outs[1].view(np.uint32))
+
+
+def test_device_lbvh_rejects_wide_layout(native, ctx):
+    soup, _, _ = scenes.incoherent_soup(100, seed=1)
+    with pytest.raises(native.DrError):
+        native.Scene(ctx, soup, builder=1, layout=8)
