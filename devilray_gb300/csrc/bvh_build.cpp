@@ -255,8 +255,10 @@ struct Flattener {
 float scene_slack(float mag)
 {
     // 2^-14 of the scene magnitude: two orders above the FP32 rounding of
-    // hit points, slab times and triangle-plane distances for rays whose
-    // origins lie within a few hundred scene radii.
+    // hit points, triangle-plane distances and the box-coordinate terms of the
+    // slab times. The part of the slab-time error that grows with the distance
+    // of the ray origin is covered by the relative margin of the box tests
+    // (kBoxFarScale).
     const float m = std::max(mag, 1.0f / 1024.0f);
     return std::ldexp(m, -14);
 }

@@ -16,6 +16,13 @@ namespace dr {
 
 constexpr uint32_t kPersistentChunk = 128;
 
+// Resident blocks per SM the persistent kernels are compiled for (8 blocks of
+// 128 threads: at most 64 registers per thread).
+#ifndef DR_P8_MIN_BLOCKS
+#define DR_P8_MIN_BLOCKS 8
+#endif
+constexpr int kP8MinBlocks = DR_P8_MIN_BLOCKS;
+
 // A warp refills its idle lanes once at least this many are idle (or all are):
 // fewer, fuller refills (measured on the incoherent workload: 1 -> 3.68,
 // 4 -> 3.78, 8 -> 3.78, 16 -> 3.54 Grays/s).

@@ -322,7 +322,7 @@ struct ShadowSource {
 };
 
 template <int MODE>
-__global__ void __launch_bounds__(kTraceBlock) k_wave_closest_p8(RenderParams p, int b)
+__global__ void __launch_bounds__(kTraceBlock, kP8MinBlocks) k_wave_closest_p8(RenderParams p, int b)
 {
     const Wide8Args w{p.trace.nodes8, p.trace.tri_ref, p.trace.tri_wt, p.trace.prim, p.trace.num_nodes, p.trace.error};
     const PathSource src{p.list[b & 1], p.rays, p.hits, p.slot_job, p.jobs};
@@ -331,7 +331,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_wave_closest_p8(RenderParams p,
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(kTraceBlock) k_wave_shadow_p8(RenderParams p, int b)
+__global__ void __launch_bounds__(kTraceBlock, kP8MinBlocks) k_wave_shadow_p8(RenderParams p, int b)
 {
     const Wide8Args w{p.trace.nodes8, p.trace.tri_ref, p.trace.tri_wt, p.trace.prim, p.trace.num_nodes, p.trace.error};
     const ShadowSource src{p.shadow_list, p.shadow_rays, p.color, p.pending, p.slot_job, p.jobs};
@@ -821,6 +821,11 @@ dr_status WaveRunner::prepare(const std::vector<RenderJob> &jobs, const WavePlan
     const uint32_t nwaves = (uint32_t)plan.wave_slots.size();
     const int K = (int)std::max<uint32_t>(1, std::min<uint32_t>({cfg.streams, (uint32_t)kMaxWaveStreams, nwaves}));
     const size_t need = wave_buffer_bytes(plan.max_slots, gr != nullptr);
+    // occupancy of the persistent kernels, queried here so enqueue (which may
+    // be under stream capture) only reads the cache
+    for (const void *k : {(const void *)k_wave_closest_p8<0>, (const void *)k_wave_closest_p8<1>,
+                          (const void *)k_wave_shadow_p8<0>, (const void *)k_wave_shadow_p8<1>})
+        resident_blocks(k, kTraceBlock);
     const uint32_t train_need = gr ? std::max<uint32_t>(1, gr->batch) * std::max<uint32_t>(1, gr->steps) : 0;
     bool grow = jobs.size() > jobs_capacity || plan.segs.size() > segs_capacity || train_need > train_cap;
     for (int k = 0; k < K; ++k) grow = grow || wave_bytes[k] < need;
@@ -894,14 +899,11 @@ dr_status WaveRunner::enqueue(const SceneArrays &sc, const WavePlan &plan, const
         t_head = carve<uint32_t>(ptr, 1);
     }
     const int sms = ctx->num_sms;
-    static int p8_per_sm = 0;
-    if (p8_per_sm == 0) {
-        int b = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_wave_closest_p8<0>, kTraceBlock, 0) != cudaSuccess || b <= 0)
-            b = 4;
-        p8_per_sm = b;
-    }
     const bool wt = tri_mode == DR_TRI_WATERTIGHT, wide = sc.trace.layout == 8;
+    const int closest_per_sm = resident_blocks(wt ? (const void *)k_wave_closest_p8<1> : (const void *)k_wave_closest_p8<0>,
+                                               kTraceBlock);
+    const int shadow_per_sm = resident_blocks(wt ? (const void *)k_wave_shadow_p8<1> : (const void *)k_wave_shadow_p8<0>,
+                                              kTraceBlock);
     DR_CUDA(cudaEventRecord(fork, st));
     for (int k = 0; k < K; ++k) DR_CUDA(cudaStreamWaitEvent(stream[k], fork, 0));
     for (uint32_t w = 0; w < nwaves; ++w) {
@@ -923,7 +925,9 @@ dr_status WaveRunner::enqueue(const SceneArrays &sc, const WavePlan &plan, const
         const uint32_t W = q.wave;
         const unsigned trace_grid = (unsigned)std::min<uint64_t>((W + kTraceBlock - 1) / kTraceBlock, (uint64_t)sms * 16);
         const unsigned shade_grid = (unsigned)std::min<uint64_t>((W + kRenderBlock - 1) / kRenderBlock, (uint64_t)sms * 16);
-        const unsigned pgrid = (unsigned)std::min<uint64_t>((W + kTraceBlock - 1) / kTraceBlock, (uint64_t)sms * p8_per_sm);
+        const uint64_t trace_blocks = (W + kTraceBlock - 1) / kTraceBlock;
+        const unsigned pgrid = (unsigned)std::min<uint64_t>(trace_blocks, (uint64_t)sms * closest_per_sm);
+        const unsigned sgrid = (unsigned)std::min<uint64_t>(trace_blocks, (uint64_t)sms * shadow_per_sm);
         DR_CUDA(cudaMemsetAsync(q.counts, 0, 128 * sizeof(uint32_t), ws));
         DR_CUDA(cudaMemsetAsync(q.work, 0, 128 * sizeof(unsigned long long), ws));
         if (gr) DR_CUDA(cudaMemsetAsync(q.guide_counts, 0, 64 * sizeof(uint32_t), ws));
@@ -947,8 +951,8 @@ dr_status WaveRunner::enqueue(const SceneArrays &sc, const WavePlan &plan, const
                 k_shade<false><<<shade_grid, kRenderBlock, 0, ws>>>(q, b);
             }
             if (wide) {
-                if (wt) k_wave_shadow_p8<1><<<pgrid, kTraceBlock, 0, ws>>>(q, b);
-                else k_wave_shadow_p8<0><<<pgrid, kTraceBlock, 0, ws>>>(q, b);
+                if (wt) k_wave_shadow_p8<1><<<sgrid, kTraceBlock, 0, ws>>>(q, b);
+                else k_wave_shadow_p8<0><<<sgrid, kTraceBlock, 0, ws>>>(q, b);
             } else {
                 if (wt) k_wave_shadow<1, 2><<<trace_grid, kTraceBlock, 0, ws>>>(q, b);
                 else k_wave_shadow<0, 2><<<trace_grid, kTraceBlock, 0, ws>>>(q, b);

@@ -11,6 +11,9 @@
 #include "persistent.cuh"
 
 #include <algorithm>
+#include <mutex>
+#include <utility>
+#include <vector>
 
 namespace dr {
 
@@ -71,7 +74,7 @@ k_trace_any(TraceArgs a)
 
 // Persistent kernels for the compressed 8-wide layout.
 template <int MODE, bool COUNT>
-__global__ void __launch_bounds__(kTraceBlock) k_trace_closest_p8(TraceArgs a)
+__global__ void __launch_bounds__(kTraceBlock, kP8MinBlocks) k_trace_closest_p8(TraceArgs a)
 {
     const Wide8Args w{a.nodes8, a.tri_ref, a.tri_wt, a.prim, a.num_nodes, a.error};
     const DirectSource src{a.rays, a.hits, nullptr, scene_root(a.num_nodes)};
@@ -81,7 +84,7 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_closest_p8(TraceArgs a)
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(kTraceBlock) k_trace_any_p8(TraceArgs a)
+__global__ void __launch_bounds__(kTraceBlock, kP8MinBlocks) k_trace_any_p8(TraceArgs a)
 {
     const Wide8Args w{a.nodes8, a.tri_ref, a.tri_wt, a.prim, a.num_nodes, a.error};
     const DirectSource src{a.rays, nullptr, a.occluded, scene_root(a.num_nodes)};
@@ -89,15 +92,27 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace_any_p8(TraceArgs a)
     persistent_wide<MODE, true, false>(w, src, a.n, a.work, nn, nb, nt, nh);
 }
 
+int resident_blocks(const void *kernel, int block_threads)
+{
+    // one entry per kernel: kernels of the same signature differ in registers
+    static std::mutex mu;
+    static std::vector<std::pair<const void *, int>> cache;
+    std::lock_guard<std::mutex> lock(mu);
+    for (const auto &e : cache)
+        if (e.first == kernel) return e.second;
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, block_threads, 0) != cudaSuccess || b <= 0) {
+        cudaGetLastError();
+        b = 4;
+    }
+    cache.emplace_back(kernel, b);
+    return b;
+}
+
 template <typename K>
 unsigned persistent_grid(K kernel, int num_sms, uint64_t n)
 {
-    static int per_sm = 0;  // resident blocks per SM of this kernel
-    if (per_sm == 0) {
-        int b = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, kTraceBlock, 0) != cudaSuccess || b <= 0) b = 4;
-        per_sm = b;
-    }
+    const int per_sm = resident_blocks((const void *)kernel, kTraceBlock);
     const uint64_t need = (n + kTraceBlock - 1) / kTraceBlock;
     return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(need, (uint64_t)num_sms * per_sm));
 }

@@ -26,6 +26,8 @@ struct TraceArgs {
 };
 
 // Launch helpers dispatch on a.layout (2 or 8) and the triangle mode.
+// Resident blocks per SM of `kernel` at `block_threads` threads (cached per kernel).
+int resident_blocks(const void *kernel, int block_threads);
 cudaError_t launch_trace_closest(const TraceArgs &a, int mode, bool count, cudaStream_t s);
 cudaError_t launch_trace_any(const TraceArgs &a, int mode, cudaStream_t s);
 

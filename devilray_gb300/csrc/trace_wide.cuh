@@ -14,6 +14,7 @@
 #include "tri_device.cuh"
 
 #include <climits>
+#include <cstring>
 
 #if defined(__CUDA_ARCH__)
 #define DR_LD(p) __ldg(p)
@@ -39,6 +40,14 @@ constexpr int kWideStack = 64;
 #ifndef DR_NODE_SELECTS
 #define DR_NODE_SELECTS 0
 #endif
+// Slab times from byte permutes folded into one FMA per plane (slab_axis).
+#ifndef DR_FAST_SLAB
+#define DR_FAST_SLAB 1
+#endif
+// Three-input min/max instructions in the box test.
+#ifndef DR_MINMAX3
+#define DR_MINMAX3 1
+#endif
 
 // Byte j of w as a float. On the device: a byte permute builds the FP32 bit
 // pattern of 2^23 + byte, and one exact subtraction removes 2^23 (avoids the
@@ -49,6 +58,43 @@ __host__ __device__ __forceinline__ float byte_f(uint32_t w, int j)
     return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7440u | (uint32_t)j)) - 8388608.0f;
 #else
     return (float)((w >> (8 * j)) & 0xffu);
+#endif
+}
+
+// 2^23 + 256 * (byte j of w), exactly, as a float: one byte permute, no
+// conversion and no subtraction (the offset is folded into the slab constants).
+__host__ __device__ __forceinline__ float byte_q(uint32_t w, int j)
+{
+#if defined(__CUDA_ARCH__)
+    return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7404u | ((uint32_t)j << 4)));
+#else
+    const uint32_t bits = 0x4B000000u | (((w >> (8 * j)) & 0xffu) << 8);
+    float f;
+    memcpy(&f, &bits, 4);
+    return f;
+#endif
+}
+
+// Three-input minimum and maximum (one instruction each on sm_100 and later).
+__host__ __device__ __forceinline__ float max3f(float a, float b, float c)
+{
+#if defined(__CUDA_ARCH__) && DR_MINMAX3
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+#else
+    return fmaxf(fmaxf(a, b), c);
+#endif
+}
+
+__host__ __device__ __forceinline__ float min3f(float a, float b, float c)
+{
+#if defined(__CUDA_ARCH__) && DR_MINMAX3
+    float r;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
+#else
+    return fminf(fminf(a, b), c);
 #endif
 }
 
@@ -65,6 +111,26 @@ __host__ __device__ __forceinline__ float bits_f(uint32_t u)
     float f;
     memcpy(&f, &u, 4);
     return f;
+}
+
+// Slab constants of one axis for the folded evaluation t = fma(byte_q, A, B):
+// with a = grid step * 1/d and b = (node origin - o) * 1/d, the plain slab time
+// of grid plane q is fl(q * a + b). Here A = a / 256 (exact) and
+// B = fl(b - 2^15 a) -+ off, so that byte_q(q) * A + B = q * a + b + (B - X)
+// where X = b - 2^15 a exactly. The rounding of X is at most 2^-24 |X| and that
+// of B at most 2^-24 |B|, so off = 2^-21 |fl(X)| + 1e-30 keeps the near time at
+// or below, and the far time at or above, the plain times (rounding is
+// monotonic): every box the plain test accepts is accepted, and the traversal
+// result is unchanged.
+struct SlabAxis {
+    float a, near_b, far_b;
+};
+
+__host__ __device__ __forceinline__ SlabAxis slab_axis(float a, float b)
+{
+    const float x = fmaf(-32768.0f, a, b);
+    const float off = fmaf(fabsf(x), 0x1p-21f, 1e-30f);
+    return SlabAxis{a * 0.00390625f, x - off, x + off};
 }
 
 // Tests the 8 child boxes of `node` against [0, tmax]; returns the internal
@@ -86,6 +152,9 @@ __host__ __device__ __forceinline__ void wide_node_test(const Bvh8Node *node, co
     // slab time of grid coordinate q on each axis: t = q * a + b
     const float ax = sx * r.inv.x, ay = sy * r.inv.y, az = sz * r.inv.z;
     const float bx = (px - r.o.x) * r.inv.x, by = (py - r.o.y) * r.inv.y, bz = (pz - r.o.z) * r.inv.z;
+#if DR_FAST_SLAB
+    const SlabAxis cx = slab_axis(ax, bx), cy = slab_axis(ay, by), cz = slab_axis(az, bz);
+#endif
     // near/far words by direction sign
     const bool fx = r.inv.x < 0.0f, fy = r.inv.y < 0.0f, fz = r.inv.z < 0.0f;
     const uint32_t nx0 = fx ? wx.z : wx.x, nx1 = fx ? wx.w : wx.y, fx0 = fx ? wx.x : wx.z, fx1 = fx ? wx.y : wx.w;
@@ -100,11 +169,17 @@ __host__ __device__ __forceinline__ void wide_node_test(const Bvh8Node *node, co
         const uint32_t wnx = s < 4 ? nx0 : nx1, wfx = s < 4 ? fx0 : fx1;
         const uint32_t wny = s < 4 ? ny0 : ny1, wfy = s < 4 ? fy0 : fy1;
         const uint32_t wnz = s < 4 ? nz0 : nz1, wfz = s < 4 ? fz0 : fz1;
+#if DR_FAST_SLAB
+        const float tnx = fmaf(byte_q(wnx, j), cx.a, cx.near_b), tfx = fmaf(byte_q(wfx, j), cx.a, cx.far_b);
+        const float tny = fmaf(byte_q(wny, j), cy.a, cy.near_b), tfy = fmaf(byte_q(wfy, j), cy.a, cy.far_b);
+        const float tnz = fmaf(byte_q(wnz, j), cz.a, cz.near_b), tfz = fmaf(byte_q(wfz, j), cz.a, cz.far_b);
+#else
         const float tnx = fmaf(byte_f(wnx, j), ax, bx), tfx = fmaf(byte_f(wfx, j), ax, bx);
         const float tny = fmaf(byte_f(wny, j), ay, by), tfy = fmaf(byte_f(wfy, j), ay, by);
         const float tnz = fmaf(byte_f(wnz, j), az, bz), tfz = fmaf(byte_f(wfz, j), az, bz);
-        const float tmin = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, 0.0f));
-        const float tmx = fminf(fminf(tfx, tfy), fminf(tfz, tmax));
+#endif
+        const float tmin = fmaxf(max3f(tnx, tny, tnz), 0.0f);
+        const float tmx = fminf(min3f(tfx, tfy, tfz), tmax) * kBoxFarScale;
         const uint32_t meta = ((s < 4 ? w1.z : w1.w) >> (8 * j)) & 0xffu;
         if (meta != 0) ++boxes;
 #if DR_NODE_SELECTS

@@ -54,8 +54,17 @@ __host__ __device__ __forceinline__ bool load_ray(const dr_ray *rays, uint64_t i
     return make_dev_ray(make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z), a.w, r);
 }
 
+// Relative margin of the box tests: a child counts as hit when its entry time
+// is at most kBoxFarScale x its exit time. The FP32 slab times carry an error
+// of a few ulps of |t| (the reciprocal, the origin term and the final
+// rounding); a margin of 2^-19 |t| covers it at any distance of the ray origin,
+// and the slack of the stored boxes covers the part proportional to the box
+// coordinates. Boxes accepted in excess only cost extra visits.
+constexpr float kBoxFarScale = 1.0f + 0x1p-19f;
+
 // Slab test of both children of a two-box node against [0, tmax]. Boxes are
-// stored widened (conservative), so the FMA form of the slab times is safe.
+// stored widened (conservative) and the exit time carries kBoxFarScale, so
+// the FMA form of the slab times is safe.
 __host__ __device__ __forceinline__ void intersect_children(const float4 c0xy, const float4 c1xy, const float4 cz,
                                                    const DevRay &r, float tmax,
                                                    float &t0, float &t1, bool &h0, bool &h1)
@@ -70,8 +79,8 @@ __host__ __device__ __forceinline__ void intersect_children(const float4 c0xy, c
     const float hi0 = fminf(fminf(fmaxf(a0, a1), fmaxf(b0, b1)), fminf(fmaxf(d0, d1), tmax));
     const float lo1 = fmaxf(fmaxf(fminf(e0, e1), fminf(f0, f1)), fmaxf(fminf(g0, g1), 0.0f));
     const float hi1 = fminf(fminf(fmaxf(e0, e1), fmaxf(f0, f1)), fminf(fmaxf(g0, g1), tmax));
-    h0 = lo0 <= hi0;
-    h1 = lo1 <= hi1;
+    h0 = lo0 <= hi0 * kBoxFarScale;
+    h1 = lo1 <= hi1 * kBoxFarScale;
     t0 = lo0;
     t1 = lo1;
 }

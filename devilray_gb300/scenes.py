@@ -260,7 +260,8 @@ def many_light(num_triangles: int = 1 << 20, num_emitters: int = 65536, seed: in
 
 def occluded_light(num_triangles: int = 1 << 20, num_emitters: int = 65536, seed: int = 0,
                    half: float = CUBE_HALF, light_y: float = 0.4, slab_y: float = 0.3,
-                   slab_extent: float = 0.7, enclose="box", room_albedo: float = 0.4) -> SceneSpec:
+                   slab_extent: float = 0.7, enclose="box", room_albedo: float = 0.4,
+                   dielectric_fraction: float = 0.5) -> SceneSpec:
     """The guided configuration: the many-light scene with its emitters only on
     spheres whose centre lies above `light_y` * half, and a diffuse occluding
     slab (albedo 0.8, two triangles) at height `slab_y` * half covering
@@ -280,7 +281,7 @@ def occluded_light(num_triangles: int = 1 << 20, num_emitters: int = 65536, seed
     emissive = np.zeros(n, bool)
     emissive[rng.permutation(candidates)[:num_emitters]] = True
     radiance = np.exp(rng.normal(0.0, 1.5, n)).astype(np.float32)
-    kind = rng.random(nsph) < 0.5
+    kind = rng.random(nsph) < 1.0 - dielectric_fraction
     albedo = rng.uniform(0.2, 0.8, nsph)
     ior = rng.uniform(1.3, 1.7, nsph)
     s = SceneSpec()

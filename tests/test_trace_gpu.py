@@ -103,6 +103,48 @@ def test_any_hit_matches_oracle(native, ctx, oracle, mode, layout):
     assert 0.05 < occ.mean() < 0.95
 
 
+def grazing_rays(soup, n, seed):
+    """Rays aimed exactly at triangle vertices and edge midpoints (so they graze
+    the boxes of the hierarchy), from origins 1 to 10^4 scene units away, a
+    quarter of them along a coordinate axis (two direction components 0)."""
+    rng = np.random.default_rng(seed)
+    tri = soup.reshape(-1, 3, 3).astype(np.float64)
+    k = rng.integers(0, len(tri), n)
+    a, b = rng.integers(0, 3, n), rng.integers(0, 3, n)
+    mid = rng.random(n) < 0.3
+    target = np.where(mid[:, None], 0.5 * (tri[k, a] + tri[k, b]), tri[k, a])
+    d = rng.normal(size=(n, 3))
+    axis = rng.random(n) < 0.25
+    ax = np.zeros((n, 3))
+    ax[np.arange(n), rng.integers(0, 3, n)] = rng.choice([-1.0, 1.0], n)
+    d = np.where(axis[:, None], ax, d / np.linalg.norm(d, axis=1, keepdims=True))
+    dist = 10.0 ** rng.uniform(0, 4, n)
+    r8 = np.zeros((n, 8), np.float32)
+    r8[:, 0:3] = (target - d * dist[:, None]).astype(np.float32)
+    r8[:, 3] = np.inf
+    r8[:, 4:7] = d.astype(np.float32)
+    return r8
+
+
+@pytest.mark.parametrize("layout", [2, 8])
+@pytest.mark.parametrize("mode", [0, 1])
+def test_grazing_rays_match_brute_force(native, ctx, oracle, layout, mode):
+    """The box tests are conservative: rays that pass exactly through vertices
+    and edges (the faces of the quantised child boxes) from near and far find
+    the brute-force closest hit."""
+    half = scenes.density_half(6000)
+    soup, _, _ = scenes.incoherent_soup(6000, seed=21, half=half)
+    rays = grazing_rays(soup, 40000, seed=22)
+    scene = native.Scene(ctx, soup, layout=layout)
+    t, prim, _ = gpu_closest(native, scene, rays, mode)
+    tb, pb = oracle.trace_brute(soup, rays, tri_mode=mode)
+    assert (pb >= 0).mean() > 0.5
+    mism = np.flatnonzero((_bits(t) != _bits(tb)) | (prim != pb))
+    assert mism.size == 0, f"{mism.size} mismatches, first {mism[:5]}: gpu {prim[mism[:5]]} brute {pb[mism[:5]]}"
+    occ = gpu_any(native, scene, rays, mode)
+    assert np.array_equal(occ.astype(bool), pb >= 0)
+
+
 @pytest.mark.parametrize("layout", [2, 8])
 def test_edge_cases(native, ctx, oracle, layout):
     unit = np.array([[0, 0, 0, 1, 0, 0, 0, 1, 0]], np.float32)
