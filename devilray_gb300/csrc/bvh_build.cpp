@@ -407,7 +407,7 @@ struct WideBuilder {
             const TreeNode *t = ch[c];
             if (!t->leaf()) {
                 imask |= 1u << s;
-                meta[s] = (uint8_t)(0x20 | s);
+                meta[s] = (uint8_t)(0x20 | (24 + s));  // hit-mask bit 24 + s
                 todo.push_back({t, next_child++});
             } else if (t->count > 0) {
                 meta[s] = (uint8_t)((((1u << t->count) - 1u) << 5) | tri_off);

@@ -40,6 +40,10 @@ constexpr int kWideStack = 64;
 #ifndef DR_NODE_SELECTS
 #define DR_NODE_SELECTS 0
 #endif
+// Hit masks from the per-slot metadata alone (no per-child internal/leaf branch).
+#ifndef DR_NODE_META_BITS
+#define DR_NODE_META_BITS 1
+#endif
 // Slab times from byte permutes folded into one FMA per plane (slab_axis).
 #ifndef DR_FAST_SLAB
 #define DR_FAST_SLAB 1
@@ -162,7 +166,7 @@ __host__ __device__ __forceinline__ void wide_node_test(const Bvh8Node *node, co
     const uint32_t nz0 = fz ? wz.z : wz.x, nz1 = fz ? wz.w : wz.y, fz0 = fz ? wz.x : wz.z, fz1 = fz ? wz.y : wz.w;
     hit_internal = 0;
     tri_mask = 0;
-    uint32_t boxes = 0;
+    uint32_t boxes = 0, hit_bits = 0;
 #pragma unroll
     for (int s = 0; s < 8; ++s) {
         const int j = s & 3;
@@ -182,7 +186,11 @@ __host__ __device__ __forceinline__ void wide_node_test(const Bvh8Node *node, co
         const float tmx = fminf(min3f(tfx, tfy, tfz), tmax) * kBoxFarScale;
         const uint32_t meta = ((s < 4 ? w1.z : w1.w) >> (8 * j)) & 0xffu;
         if (meta != 0) ++boxes;
-#if DR_NODE_SELECTS
+#if DR_NODE_META_BITS
+        // the child's bits of the node's hit mask: its triangles (bits 0-23)
+        // or, for an internal child, bit 24 + s; an empty slot has none
+        if (tmin <= tmx) hit_bits |= (meta >> 5) << (meta & 31u);
+#elif DR_NODE_SELECTS
         // the same decisions as selects (no per-child branches)
         const uint32_t hit = (tmin <= tmx && meta != 0) ? 1u : 0u;
         const uint32_t internal = (imask >> s) & 1u;
@@ -195,6 +203,15 @@ __host__ __device__ __forceinline__ void wide_node_test(const Bvh8Node *node, co
         }
 #endif
     }
+#if DR_NODE_META_BITS
+    tri_mask = hit_bits & 0x00ffffffu;
+    // internal hits from slot order to traversal order: bit s -> bit s ^ oct
+    uint32_t m = hit_bits >> 24;
+    if (oct & 1u) m = ((m & 0x55u) << 1) | ((m >> 1) & 0x55u);
+    if (oct & 2u) m = ((m & 0x33u) << 2) | ((m >> 2) & 0x33u);
+    if (oct & 4u) m = ((m & 0x0fu) << 4) | ((m >> 4) & 0x0fu);
+    hit_internal = m;
+#endif
     nboxes = boxes;
 }
 

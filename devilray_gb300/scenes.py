@@ -145,6 +145,12 @@ def quad(center, normal, right, size) -> np.ndarray:
     return np.array([np.concatenate([pts[0], pts[2], pts[1]]), np.concatenate([pts[0], pts[3], pts[2]])], np.float32)
 
 
+def rect_y(x0: float, x1: float, z0: float, z1: float, y: float) -> np.ndarray:
+    """Two triangles covering [x0, x1] x [z0, z1] at height y."""
+    a, b, c, d = (x0, y, z0), (x1, y, z0), (x1, y, z1), (x0, y, z1)
+    return np.array([a + c + b, a + d + c], np.float32)
+
+
 def material(kind=0, emission=(0, 0, 0), albedo=(0, 0, 0), ior=1.0, debug=(0.5, 0.5, 0.5)):
     return {"kind": int(kind), "ior": float(ior), "emission": tuple(emission) + (0.0,) * (4 - len(emission)),
             "albedo": tuple(albedo) + (0.0,) * (4 - len(albedo)), "debug": tuple(debug) + (0.0,) * (4 - len(debug))}
@@ -261,7 +267,7 @@ def many_light(num_triangles: int = 1 << 20, num_emitters: int = 65536, seed: in
 def occluded_light(num_triangles: int = 1 << 20, num_emitters: int = 65536, seed: int = 0,
                    half: float = CUBE_HALF, light_y: float = 0.4, slab_y: float = 0.3,
                    slab_extent: float = 0.7, enclose="box", room_albedo: float = 0.4,
-                   dielectric_fraction: float = 0.5) -> SceneSpec:
+                   dielectric_fraction: float = 0.5, slab_gap: float | None = None) -> SceneSpec:
     """The guided configuration: the many-light scene with its emitters only on
     spheres whose centre lies above `light_y` * half, and a diffuse occluding
     slab (albedo 0.8, two triangles) at height `slab_y` * half covering
@@ -295,14 +301,18 @@ def occluded_light(num_triangles: int = 1 << 20, num_emitters: int = 65536, seed
             L = float(radiance[t])
             m = s.add_material(material(0, emission=(L, L, L)))
             s.add_object(soup[t:t + 1], m)
-    e = slab_extent * half
-    slab = quad((0.0, slab_y * half, 0.0), (0.0, -1.0, 0.0), (1.0, 0.0, 0.0), 2 * e)
+    w = 1.15 * half
+    if slab_gap is None:
+        e = slab_extent * half
+        slab = quad((0.0, slab_y * half, 0.0), (0.0, -1.0, 0.0), (1.0, 0.0, 0.0), 2 * e)
+    else:
+        # the whole width of the room but a gap of slab_gap * half along the -x wall
+        slab = rect_y(-w + slab_gap * half, w, -w, w, slab_y * half)
     grey = s.add_material(material(0, albedo=(room_albedo,) * 3))
     s.add_object(slab, grey)
     if enclose:
         # a floor, a back wall and side walls (open towards the camera) catch the
         # light that passes the slab's edges and scatter it under the slab
-        w = 1.15 * half
         s.add_object(quad((0.0, -w, 0.0), (0.0, 1.0, 0.0), (1.0, 0.0, 0.0), 2 * w), grey)
         s.add_object(quad((0.0, 0.0, w), (0.0, 0.0, -1.0), (1.0, 0.0, 0.0), 2 * w), grey)
         if enclose == "box":
