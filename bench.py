@@ -298,7 +298,8 @@ def run_ours(args):
         line["batch"] = batch_section(ctx, native, local, stream, scenes_n=args.batch_scenes)
     if not args.no_guided:
         torch.cuda.empty_cache()
-        line["guided"] = guided_section(ctx, native, local, stream, ref_spp=args.guided_ref_spp)
+        line["guided"] = guided_section(ctx, native, local, stream, ref_spp=args.guided_ref_spp,
+                                        scene=args.guided_scene)
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -463,39 +464,46 @@ def batch_section(ctx, native, device: int, stream, scenes_n: int = 64, spp: int
     return out
 
 
-def guided_section(ctx, native, device: int, stream, width: int = 480, height: int = 270, spp: int = 256,
-                   depth: int = 16, ref_spp: int = 65536, hd_spp: int = 16):
+def guided_section(ctx, native, device: int, stream, width: int = 480, height: int = 270, spp: int = 1024,
+                   depth: int = 16, ref_spp: int = 65536, hd_spp: int = 16, seeds: int = 3, scene: str = "gap"):
     """Learned path guiding on the occluded-light scene (the many-light
     geometry, emitters only above an occluding slab): RMSE of the guided and of
     the plain MIS tracer against a converged render (the plain tracer,
     `ref_spp` samples accumulated in FP64), at equal samples and at equal time
-    (training included), plus guided samples/s at 1920x1080."""
+    (training included), plus guided samples/s at 1920x1080. Each RMSE is the
+    root of the mean squared error over `seeds` independent renders (the
+    guided ones each train a fresh network), because single renders of this
+    scene differ by tens of percent in squared error."""
     import torch
     from devilray_gb300 import scenes
-    spec = scenes.occluded_light()
-    scene = native.Scene.from_spec(ctx, spec)
+    scene_kw = {"gap": dict(slab_gap=0.15), "centered": {}}[scene]
+    spec = scenes.occluded_light(**scene_kw)
+    sc = native.Scene.from_spec(ctx, spec)
     cam = scenes.lower_camera(width, height)
     npix = width * height
     dev = f"cuda:{device}"
     acc = torch.zeros((npix, 4), dtype=torch.float32, device=dev)
-
-    def image(a):
-        return (a[:, :3].double() / a[:, 3:4].double())
 
     # converged reference: chunks of 1024 samples, summed in FP64
     t0 = time.perf_counter()
     ref = torch.zeros((npix, 4), dtype=torch.float64, device=dev)
     for off in range(0, ref_spp, 1024):
         acc.zero_()
-        scene.render(cam, acc, spp=min(1024, ref_spp - off), max_depth=depth, sample_offset=off, seed=12345,
-                     stream=stream)
+        sc.render(cam, acc, spp=min(1024, ref_spp - off), max_depth=depth, sample_offset=off, seed=12345,
+                  stream=stream)
         stream.synchronize()
         ref += acc.double()
     ref_img = ref[:, :3] / ref[:, 3:4]
     ref_s = time.perf_counter() - t0
+    # the share of indirect light: 1 - (image mean at depth 1) / (converged mean)
+    acc.zero_()
+    sc.render(cam, acc, spp=64, max_depth=1, seed=7, stream=stream)
+    stream.synchronize()
+    indirect = 1.0 - float((acc[:, :3].double() / acc[:, 3:4].double()).mean()) / float(ref_img.mean())
 
-    def rmse(img):
-        return float(torch.sqrt(torch.mean((img - ref_img) ** 2)).item())
+    def mse():
+        img = acc[:, :3].double() / acc[:, 3:4].double()
+        return float(torch.mean((img - ref_img) ** 2).item())
 
     def timed(fn):
         acc.zero_()
@@ -507,59 +515,79 @@ def guided_section(ctx, native, device: int, stream, width: int = 480, height: i
         stream.synchronize()
         return e0.elapsed_time(e1) / 1e3
 
-    t_plain = timed(lambda: scene.render(cam, acc, spp=spp, max_depth=depth, seed=1, wave_paths=npix * 16,
-                                         stream=stream))
-    rmse_plain = rmse(image(acc))
+    wave = npix * 16  # 16 samples per pixel per wave: a training round after every 16 spp
+    alpha, steps, batch, budget, bounces = 0.75, 16, 16384, 512, 2
+
+    def runs(fn):
+        ts, ms = [], []
+        for sd in range(seeds):
+            ts.append(timed(lambda: fn(sd)))
+            ms.append(mse())
+        return float(np.mean(ts)), float(np.mean(ms)), ms
+
+    t_plain, m_plain, m_plain_s = runs(lambda sd: sc.render(cam, acc, spp=spp, max_depth=depth, seed=100 + sd,
+                                                             wave_paths=wave, stream=stream))
     pos = spec.positions.reshape(-1, 3)
     lo, hi = pos.min(0), pos.max(0)
-    guide = native.Guide(ctx, seed=1, center=tuple(float(x) for x in (lo + hi) / 2),
-                         half_extent=float((hi - lo).max() / 2))
-    wave = npix * 16  # the plain tracer's default wave (2^21 paths): a training round after every 16 samples
-    t_guided = timed(lambda: scene.render_guided(guide, cam, acc, spp=spp, max_depth=depth, seed=2, alpha=0.5,
-                                                 train=True, train_batch=16384, train_steps=16, bounces=2,
-                                                 wave_paths=wave, stream=stream))
-    rmse_guided = rmse(image(acc))
-    loss = guide.last_loss()
+    center = tuple(float(x) for x in (lo + hi) / 2)
+    half = float((hi - lo).max() / 2)
+    guides = []
+
+    def guided(sd):
+        g = native.Guide(ctx, seed=1 + sd, center=center, half_extent=half)
+        guides.append(g)
+        sc.render_guided(g, cam, acc, spp=spp, max_depth=depth, seed=200 + sd, alpha=alpha, train=True,
+                         train_batch=batch, train_steps=steps, train_budget=budget, bounces=bounces,
+                         wave_paths=wave, stream=stream)
+
+    t_guided, m_guided, m_guided_s = runs(guided)
+    loss = guides[-1].last_loss()
     # equal time: the plain tracer with the samples it renders in the guided time
     spp_eq = max(1, int(round(spp * t_guided / t_plain)))
-    t_eq = timed(lambda: scene.render(cam, acc, spp=spp_eq, max_depth=depth, seed=3, stream=stream))
-    rmse_eq = rmse(image(acc))
-    # the trained network's estimator on its own (no further training), equal samples
-    t_trained = timed(lambda: scene.render_guided(guide, cam, acc, spp=spp, max_depth=depth, seed=4, alpha=0.5,
-                                                  train=False, bounces=2, wave_paths=wave, stream=stream))
-    rmse_trained = rmse(image(acc))
+    t_eq, m_eq, m_eq_s = runs(lambda sd: sc.render(cam, acc, spp=spp_eq, max_depth=depth, seed=300 + sd,
+                                                    wave_paths=wave, stream=stream))
+    # the trained networks on their own (no further training), equal samples
+    t_trained, m_trained, _ = runs(lambda sd: sc.render_guided(guides[sd], cam, acc, spp=spp, max_depth=depth,
+                                                                seed=400 + sd, alpha=alpha, train=False,
+                                                                bounces=bounces, wave_paths=wave, stream=stream))
     # 1080p throughput of the guided tracer (training on)
     hd = scenes.lower_camera(1920, 1080)
     hd_acc = torch.zeros((1920 * 1080, 4), dtype=torch.float32, device=dev)
+    g = native.Guide(ctx, seed=9, center=center, half_extent=half)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    scene.render_guided(guide, hd, hd_acc, spp=hd_spp, max_depth=depth, seed=5, alpha=0.5, train=True,
-                        train_batch=16384, train_steps=16, bounces=2, stream=stream)
+    sc.render_guided(g, hd, hd_acc, spp=hd_spp, max_depth=depth, seed=5, alpha=alpha, train=True,
+                     train_batch=batch, train_steps=steps, bounces=bounces, stream=stream)
     e1.record(stream)
     stream.synchronize()
     t_hd = e0.elapsed_time(e1) / 1e3
     e0.record(stream)
-    scene.render(hd, hd_acc, spp=hd_spp, max_depth=depth, seed=6, stream=stream)
+    sc.render(hd, hd_acc, spp=hd_spp, max_depth=depth, seed=6, stream=stream)
     e1.record(stream)
     stream.synchronize()
     t_hd_plain = e0.elapsed_time(e1) / 1e3
-    out = {"scene": "occluded_light (2^20 triangles, 65,536 emitters above a slab, floor and walls of albedo 0.4; "
-                    "57 % of the light indirect)",
-           "width": width,
-           "height": height, "max_depth": depth, "reference_spp": ref_spp, "reference_accumulation": "fp64",
-           "reference_seconds": round(ref_s, 2), "spp": spp, "alpha": 0.5,
-           "plain": {"rmse": rmse_plain, "seconds": t_plain},
-           "guided": {"rmse": rmse_guided, "seconds": t_guided, "final_loss": loss,
-                      "training": "16 Adam steps x 16384 samples after every 16 spp",
-                      "guided_bounces": 2},
-           "plain_equal_time": {"rmse": rmse_eq, "spp": spp_eq, "seconds": t_eq},
-           "guided_trained_equal_spp": {"rmse": rmse_trained, "seconds": t_trained},
-           "rmse_ratio_equal_spp": rmse_plain / rmse_guided, "rmse_ratio_equal_time": rmse_eq / rmse_guided,
+    g.close()
+    desc = {"gap": "slab over the whole room but a gap of 0.15 half-widths along one wall",
+            "centered": "centred slab over 0.7 of the width"}[scene]
+    out = {"scene": f"occluded_light (2^20 triangles, 65,536 emitters above the slab, {desc}; floor and walls of "
+                    f"albedo 0.4; half the spheres glass)",
+           "indirect_fraction": indirect, "width": width, "height": height, "max_depth": depth,
+           "reference_spp": ref_spp, "reference_accumulation": "fp64", "reference_seconds": round(ref_s, 2),
+           "spp": spp, "seeds": seeds, "alpha": alpha,
+           "plain": {"rmse": m_plain ** 0.5, "seconds": t_plain, "mse_per_seed": m_plain_s},
+           "guided": {"rmse": m_guided ** 0.5, "seconds": t_guided, "mse_per_seed": m_guided_s, "final_loss": loss,
+                      "training": f"{steps} Adam steps x {batch} samples after every 16 spp, at most {budget} steps",
+                      "guided_bounces": bounces},
+           "plain_equal_time": {"rmse": m_eq ** 0.5, "spp": spp_eq, "seconds": t_eq, "mse_per_seed": m_eq_s},
+           "guided_trained_equal_spp": {"rmse": m_trained ** 0.5, "seconds": t_trained},
+           "rmse_ratio_equal_spp": (m_plain / m_guided) ** 0.5, "rmse_ratio_equal_time": (m_eq / m_guided) ** 0.5,
+           "rmse_ratio_trained_equal_spp": (m_plain / m_trained) ** 0.5,
            "hd_1080p": {"spp": hd_spp, "guided_samples_per_s": 1920 * 1080 * hd_spp / t_hd,
                         "plain_samples_per_s": 1920 * 1080 * hd_spp / t_hd_plain}}
-    guide.close()
-    del scene, acc, ref, hd_acc
+    for g in guides:
+        g.close()
+    del sc, acc, ref, hd_acc
     torch.cuda.empty_cache()
     return out
 
@@ -610,6 +638,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-guided", action="store_true")
     ap.add_argument("--guided-ref-spp", type=int, default=65536)
+    ap.add_argument("--guided-scene", choices=["gap", "centered"], default="gap")
     ap.add_argument("--batch-scenes", type=int, default=64)
     ap.add_argument("--layout", type=int, default=0, help="BVH layout of the trace workload: 0 default, 2, 8")
     ap.add_argument("--render-layout", type=int, default=0, help="BVH layout of the render workloads")

@@ -79,7 +79,7 @@ __global__ void __launch_bounds__(kTraceBlock, kP8MinBlocks) k_trace_closest_p8(
     const Wide8Args w{a.nodes8, a.tri_ref, a.tri_wt, a.prim, a.num_nodes, a.error};
     const DirectSource src{a.rays, a.hits, nullptr, scene_root(a.num_nodes)};
     unsigned long long nn = 0, nb = 0, nt = 0, nh = 0;
-    persistent_wide<MODE, false, COUNT>(w, src, a.n, a.work, nn, nb, nt, nh);
+    persistent_wide<MODE, false, COUNT, DR_TRI_BATCH_CLOSEST != 0>(w, src, a.n, a.work, nn, nb, nt, nh);
     if (COUNT) add_counters(a.counters, nn, nb, nt, nh);
 }
 
@@ -89,7 +89,7 @@ __global__ void __launch_bounds__(kTraceBlock, kP8MinBlocks) k_trace_any_p8(Trac
     const Wide8Args w{a.nodes8, a.tri_ref, a.tri_wt, a.prim, a.num_nodes, a.error};
     const DirectSource src{a.rays, nullptr, a.occluded, scene_root(a.num_nodes)};
     unsigned long long nn = 0, nb = 0, nt = 0, nh = 0;
-    persistent_wide<MODE, true, false>(w, src, a.n, a.work, nn, nb, nt, nh);
+    persistent_wide<MODE, true, false, DR_TRI_BATCH_ANY != 0>(w, src, a.n, a.work, nn, nb, nt, nh);
 }
 
 int resident_blocks(const void *kernel, int block_threads)

@@ -86,10 +86,46 @@ __host__ __device__ __forceinline__ void intersect_children(const float4 c0xy, c
 }
 
 // testTriangleIntersection (DevilRay include/tracing/IntersectionTestsImpl.hpp:
-// 253-297) on a precomputed record {A, n, B-A, C-A}. The t of a hit and the
-// hit/miss decision are bit-identical to the reference; the test stops after t
-// when t cannot beat (best_t, best_prim) under the smaller-t-then-smaller-index
-// rule. Returns true when the triangle beats the current best.
+// 253-297) on a precomputed record {A, n, B-A, C-A} given as its three float4
+// words. The t of a hit and the hit/miss decision are bit-identical to the
+// reference; the test stops after t when t cannot beat (best_t, best_prim)
+// under the smaller-t-then-smaller-index rule. Returns true when the triangle
+// beats the current best.
+__host__ __device__ __forceinline__ bool tri_test_ref_words(const float4 r0, const float4 r1, const float4 r2,
+                                                            const DevRay &r, float best_t, float &t_out)
+{
+    float nx = r0.w, ny = r1.x, nz = r1.y;
+    const float px = r.o.x - r0.x, py = r.o.y - r0.y, pz = r.o.z - r0.z;
+    float dp = px * nx + py * ny + pz * nz;
+    if (dp < 0) {
+        nx = -nx;
+        ny = -ny;
+        nz = -nz;
+        dp = -dp;
+    }
+    const float d = -(r.v.x * nx + r.v.y * ny + r.v.z * nz);
+    if (d < 1e-7f) return false;
+    const float t = dp / d;
+    if (!(t <= best_t)) return false;
+    const float BAx = r1.z, BAy = r1.w, BAz = r2.x;
+    const float CAx = r2.y, CAy = r2.z, CAz = r2.w;
+    const float hx = r.o.x + r.v.x * t, hy = r.o.y + r.v.y * t, hz = r.o.z + r.v.z * t;
+    const float ax = hx - r0.x, ay = hy - r0.y, az = hz - r0.z;
+    // n_1 = (p - A) x (C - A), n_2 = (B - A) x (p - A), n_f = (A - B) x (A - C)
+    const float n1x = ay * CAz - az * CAy, n1y = az * CAx - ax * CAz, n1z = ax * CAy - ay * CAx;
+    const float n2x = BAy * az - BAz * ay, n2y = BAz * ax - BAx * az, n2z = BAx * ay - BAy * ax;
+    const float nfx = BAy * CAz - BAz * CAy, nfy = BAz * CAx - BAx * CAz, nfz = BAx * CAy - BAy * CAx;
+    const float s = nfx * nfx + nfy * nfy + nfz * nfz;
+    const float wB = (nfx * n1x + nfy * n1y + nfz * n1z) / s;
+    const float wC = (nfx * n2x + nfy * n2y + nfz * n2z) / s;
+    const float wA = 1 - wB - wC;
+    if (wA < 0 || wB < 0 || wC < 0) return false;
+    t_out = t;
+    return true;
+}
+
+// The same on record k of a GLOBAL-memory record array (read-only path; the
+// third word is read only when t can still beat the best).
 __host__ __device__ __forceinline__ bool tri_test_ref(const float4 *__restrict__ rec, uint32_t k, const DevRay &r,
                                              float best_t, float &t_out)
 {
@@ -108,22 +144,7 @@ __host__ __device__ __forceinline__ bool tri_test_ref(const float4 *__restrict__
     if (d < 1e-7f) return false;
     const float t = dp / d;
     if (!(t <= best_t)) return false;
-    const float4 r2 = DR_LDG(rec + 3 * k + 2);
-    const float BAx = r1.z, BAy = r1.w, BAz = r2.x;
-    const float CAx = r2.y, CAy = r2.z, CAz = r2.w;
-    const float hx = r.o.x + r.v.x * t, hy = r.o.y + r.v.y * t, hz = r.o.z + r.v.z * t;
-    const float ax = hx - r0.x, ay = hy - r0.y, az = hz - r0.z;
-    // n_1 = (p - A) x (C - A), n_2 = (B - A) x (p - A), n_f = (A - B) x (A - C)
-    const float n1x = ay * CAz - az * CAy, n1y = az * CAx - ax * CAz, n1z = ax * CAy - ay * CAx;
-    const float n2x = BAy * az - BAz * ay, n2y = BAz * ax - BAx * az, n2z = BAx * ay - BAy * ax;
-    const float nfx = BAy * CAz - BAz * CAy, nfy = BAz * CAx - BAx * CAz, nfz = BAx * CAy - BAy * CAx;
-    const float s = nfx * nfx + nfy * nfy + nfz * nfz;
-    const float wB = (nfx * n1x + nfy * n1y + nfz * n1z) / s;
-    const float wC = (nfx * n2x + nfy * n2y + nfz * n2z) / s;
-    const float wA = 1 - wB - wC;
-    if (wA < 0 || wB < 0 || wC < 0) return false;
-    t_out = t;
-    return true;
+    return tri_test_ref_words(r0, r1, DR_LDG(rec + 3 * k + 2), r, best_t, t_out);
 }
 
 // Per-ray setup of the watertight test (Woop, Benthin, Wald, JCGT 2013).
@@ -160,13 +181,11 @@ __host__ __device__ __forceinline__ WtSetup wt_setup(const float3 &d)
     return w;
 }
 
-// Watertight two-sided test on a record {A, B, C}.
-__host__ __device__ __forceinline__ bool tri_test_wt(const float4 *__restrict__ rec, uint32_t k, const DevRay &r,
-                                            const WtSetup &w, float best_t, float &t_out)
+// Watertight two-sided test on a record {A, B, C} given as its three float4 words.
+__host__ __device__ __forceinline__ bool tri_test_wt_words(const float4 r0, const float4 r1, const float4 r2,
+                                                           const DevRay &r, const WtSetup &w, float best_t,
+                                                           float &t_out)
 {
-    const float4 r0 = DR_LDG(rec + 3 * k);
-    const float4 r1 = DR_LDG(rec + 3 * k + 1);
-    const float4 r2 = DR_LDG(rec + 3 * k + 2);
     const float3 a = make_float3(r0.x - r.o.x, r0.y - r.o.y, r0.z - r.o.z);
     const float3 b = make_float3(r0.w - r.o.x, r1.x - r.o.y, r1.y - r.o.z);
     const float3 c = make_float3(r1.z - r.o.x, r1.w - r.o.y, r2.x - r.o.z);
@@ -199,6 +218,14 @@ __host__ __device__ __forceinline__ bool tri_test_wt(const float4 *__restrict__ 
     if (!(t <= best_t)) return false;
     t_out = t;
     return true;
+}
+
+// The same on record k of a GLOBAL-memory record array.
+__host__ __device__ __forceinline__ bool tri_test_wt(const float4 *__restrict__ rec, uint32_t k, const DevRay &r,
+                                            const WtSetup &w, float best_t, float &t_out)
+{
+    return tri_test_wt_words(DR_LDG(rec + 3 * k), DR_LDG(rec + 3 * k + 1), DR_LDG(rec + 3 * k + 2), r, w, best_t,
+                             t_out);
 }
 
 }  // namespace dr
