@@ -1,6 +1,7 @@
 """Small, fixed workloads for profiling single kernels (ncu, CUDA events).
 
     python -m devilray_gb300.profile_cases guide_infer [kernel]   # 0: tcgen05, 1: mma.sync
+    python -m devilray_gb300.profile_cases guide_train [rows]     # Adam steps on random samples
     python -m devilray_gb300.profile_cases render_box_room         # 256x256, 16 spp, depth 8
     python -m devilray_gb300.profile_cases batch_small             # 8 uneven scenes, graph, 2 renders
     python -m devilray_gb300.profile_cases guided [spp]            # occluded-light scene, plain vs guided
@@ -44,6 +45,33 @@ def guide_infer(kernel: int = 0, rows: int = 1 << 20) -> None:
     flop = 2 * (80 * 64 + 3 * 64 * 64 + 64 * 48) * rows
     print(f"guide_infer kernel {kernel}: {ms:.3f} ms for {rows} rows, {flop / ms / 1e9:.1f} TFLOP/s, "
           f"{rows / ms / 1e3:.1f} Mrows/s")
+    ctx.check()
+
+
+def guide_train(rows: int = 16384, steps: int = 100) -> None:
+    import torch
+    native, ctx = _ctx()
+    g = native.Guide(ctx, seed=1, half_extent=10.0)
+    rng = np.random.default_rng(0)
+
+    def unit(k):
+        d = rng.normal(size=(k, 3))
+        return torch.from_numpy((d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)).cuda()
+
+    pos = torch.from_numpy(rng.uniform(-10, 10, (rows, 3)).astype(np.float32)).cuda()
+    nrm, sdir = unit(rows), unit(rows)
+    w = torch.from_numpy(rng.exponential(1.0, rows).astype(np.float32)).cuda()
+    for _ in range(3):
+        g.train_step(pos, nrm, sdir, w, rows)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        g.train_step(pos, nrm, sdir, w, rows)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    print(f"guide_train: {ms:.4f} ms per Adam step of {rows} rows, loss {g.last_loss():.4f}")
     ctx.check()
 
 
@@ -118,5 +146,5 @@ def guided(spp: int = 32) -> None:
 if __name__ == "__main__":
     case = sys.argv[1] if len(sys.argv) > 1 else "guide_infer"
     args = [int(a) for a in sys.argv[2:]]
-    {"guide_infer": guide_infer, "render_box_room": render_box_room, "batch_small": batch_small,
-     "guided": guided}[case](*args)
+    {"guide_infer": guide_infer, "guide_train": guide_train, "render_box_room": render_box_room,
+     "batch_small": batch_small, "guided": guided}[case](*args)
