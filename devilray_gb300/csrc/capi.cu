@@ -83,7 +83,7 @@ TraceArgs trace_args(dr_scene *s)
     a.num_nodes = s->num_nodes;
     a.counters = s->ctx->d_counters;
     a.error = s->ctx->d_error;
-    a.work = reinterpret_cast<unsigned long long *>(s->ctx->d_work);
+    a.work = s->ctx->d_work + s->ctx->work_next.fetch_add(1) % kWorkCounters;
     a.num_sms = s->ctx->num_sms;
     return a;
 }
@@ -135,12 +135,13 @@ dr_status dr_context_create(const dr_context_config *cfg, dr_context **out)
         return cuda_fail(e, "cudaGetDeviceProperties");
     }
     ctx->num_sms = prop.multiProcessorCount;
-    if ((e = cudaMalloc(&ctx->d_error, 256)) != cudaSuccess || (e = cudaMemset(ctx->d_error, 0, 256)) != cudaSuccess) {
+    const size_t words = 256 + kWorkCounters * sizeof(unsigned long long);
+    if ((e = cudaMalloc(&ctx->d_error, words)) != cudaSuccess || (e = cudaMemset(ctx->d_error, 0, words)) != cudaSuccess) {
         delete ctx;
         return cuda_fail(e, "cudaMalloc(error word)");
     }
     ctx->d_counters = reinterpret_cast<unsigned long long *>(reinterpret_cast<char *>(ctx->d_error) + 64);
-    ctx->d_work = reinterpret_cast<unsigned int *>(reinterpret_cast<char *>(ctx->d_error) + 192);
+    ctx->d_work = reinterpret_cast<unsigned long long *>(reinterpret_cast<char *>(ctx->d_error) + 256);
     *out = ctx;
     return DR_OK;
 }
@@ -290,6 +291,8 @@ dr_status dr_scene_destroy(dr_scene *s)
     delete s->runner;
     cudaFree(s->d_stage_rays);
     cudaFree(s->d_stage_hits);
+    for (cudaStream_t h : s->stage_streams)
+        if (h) cudaStreamDestroy(h);
     delete s;
     return DR_OK;
 }
@@ -446,14 +449,18 @@ dr_status dr_trace_closest_host(dr_scene *s, const dr_ray *rays_host, uint64_t n
         s->stage_capacity = n;
     }
     // Pipeline in chunks: the copy-in of chunk k+1 and the copy-out of chunk
-    // k-1 overlap the traversal of chunk k (one stream per stage, ordered by
-    // events).
+    // k-1 overlap the traversal of chunk k. Chunks alternate between two
+    // compute streams, so the tail of one persistent launch overlaps the start
+    // of the next (each launch has its own work counter). Measured with one
+    // compute stream (16.8 M rays, 2^20 triangles): 4 chunks 5.11 ms,
+    // 8 chunks 5.21 ms, 16 chunks 5.87 ms.
     auto *d_rays = static_cast<dr_ray *>(s->d_stage_rays);
     auto *d_hits = static_cast<dr_hit *>(s->d_stage_hits);
     const uint64_t chunk = std::max<uint64_t>(1u << 18, (n + 7) / 8);
-    cudaStream_t copy_in, copy_out;
-    DR_CUDA(cudaStreamCreateWithFlags(&copy_in, cudaStreamNonBlocking));
-    DR_CUDA(cudaStreamCreateWithFlags(&copy_out, cudaStreamNonBlocking));
+    for (cudaStream_t &h : s->stage_streams)
+        if (!h) DR_CUDA(cudaStreamCreateWithFlags(&h, cudaStreamNonBlocking));
+    cudaStream_t copy_in = s->stage_streams[0], copy_out = s->stage_streams[1];
+    const cudaStream_t compute[2] = {st, s->stage_streams[2]};
     std::vector<cudaEvent_t> ev;
     auto new_event = [&]() {
         cudaEvent_t e;
@@ -465,30 +472,34 @@ dr_status dr_trace_closest_host(dr_scene *s, const dr_ray *rays_host, uint64_t n
     cudaEvent_t start = new_event();
     err = cudaEventRecord(start, st);
     if (err == cudaSuccess) err = cudaStreamWaitEvent(copy_in, start, 0);
-    TraceArgs a = trace_args(s);
-    for (uint64_t b = 0; b < n && err == cudaSuccess; b += chunk) {
+    if (err == cudaSuccess) err = cudaStreamWaitEvent(copy_out, start, 0);
+    if (err == cudaSuccess) err = cudaStreamWaitEvent(compute[1], start, 0);
+    uint64_t k = 0;
+    for (uint64_t b = 0; b < n && err == cudaSuccess; b += chunk, ++k) {
         const uint64_t m = std::min(chunk, n - b);
+        const cudaStream_t cs = compute[k & 1];
         err = cudaMemcpyAsync(d_rays + b, rays_host + b, m * sizeof(dr_ray), cudaMemcpyHostToDevice, copy_in);
         cudaEvent_t in_done = new_event();
         if (err == cudaSuccess) err = cudaEventRecord(in_done, copy_in);
-        if (err == cudaSuccess) err = cudaStreamWaitEvent(st, in_done, 0);
+        if (err == cudaSuccess) err = cudaStreamWaitEvent(cs, in_done, 0);
+        TraceArgs a = trace_args(s);
         a.rays = d_rays + b;
         a.hits = d_hits + b;
         a.n = m;
-        if (err == cudaSuccess) err = launch_trace_closest(a, tri_mode, false, st);
+        if (err == cudaSuccess) err = launch_trace_closest(a, tri_mode, false, cs);
         cudaEvent_t tr_done = new_event();
-        if (err == cudaSuccess) err = cudaEventRecord(tr_done, st);
+        if (err == cudaSuccess) err = cudaEventRecord(tr_done, cs);
         if (err == cudaSuccess) err = cudaStreamWaitEvent(copy_out, tr_done, 0);
         if (err == cudaSuccess)
             err = cudaMemcpyAsync(hits_host + b, d_hits + b, m * sizeof(dr_hit), cudaMemcpyDeviceToHost, copy_out);
     }
-    cudaEvent_t out_done = new_event();
+    cudaEvent_t out_done = new_event(), c1_done = new_event();
     if (err == cudaSuccess) err = cudaEventRecord(out_done, copy_out);
+    if (err == cudaSuccess) err = cudaEventRecord(c1_done, compute[1]);
     if (err == cudaSuccess) err = cudaStreamWaitEvent(st, out_done, 0);
+    if (err == cudaSuccess) err = cudaStreamWaitEvent(st, c1_done, 0);
     if (err == cudaSuccess) err = cudaStreamSynchronize(st);
     for (auto e : ev) cudaEventDestroy(e);
-    cudaStreamDestroy(copy_in);
-    cudaStreamDestroy(copy_out);
     if (err != cudaSuccess) return cuda_fail(err, "dr_trace_closest_host");
     return DR_OK;
 }

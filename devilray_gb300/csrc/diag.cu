@@ -40,7 +40,8 @@ extern "C" dr_status dr_probe_read_bandwidth(dr_context *ctx, const void *buf_de
     auto st = static_cast<cudaStream_t>(stream);
     const uint64_t n4 = bytes / 16;
     const int blocks = ctx->num_sms * 8;
-    float *sink = reinterpret_cast<float *>(ctx->d_work);
+    // a word of the context's status block that nothing else uses
+    float *sink = reinterpret_cast<float *>(reinterpret_cast<char *>(ctx->d_error) + 128);
     k_read_stream<<<blocks, 256, 0, st>>>(static_cast<const float4 *>(buf_dev), n4, 1, sink);  // warm
     cudaEvent_t a, b;
     DR_CUDA(cudaEventCreate(&a));

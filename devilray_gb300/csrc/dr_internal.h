@@ -1,6 +1,8 @@
 // dr_internal.h -- internal types of the GB300 path-tracing core.
 #pragma once
 
+#include <atomic>
+
 #include "devilray_gb300.h"
 
 #include <cuda_runtime.h>
@@ -143,10 +145,16 @@ struct dr_context {
     int num_sms = 0;
     uint32_t *d_error = nullptr;                // device error word
     unsigned long long *d_counters = nullptr;   // 8 counters
-    unsigned int *d_work = nullptr;             // persistent-kernel work counters (8)
+    unsigned long long *d_work = nullptr;       // ring of kWorkCounters persistent-kernel work counters
+    std::atomic<uint32_t> work_next{0};         // next counter of the ring
     void *scratch = nullptr;                    // grows on demand (alias builds, staging)
     size_t scratch_bytes = 0;
 };
+
+// Work counters of the public persistent traversal launches: each launch takes
+// the next counter of a ring, so launches on different streams that run at
+// the same time count separately (up to this many launches in flight).
+constexpr uint32_t kWorkCounters = 64;
 
 namespace dr {
 // Ensures ctx->scratch holds at least `bytes` (cudaMalloc when it must grow).
@@ -197,4 +205,5 @@ struct dr_scene {
     void *d_stage_rays = nullptr;
     void *d_stage_hits = nullptr;
     uint64_t stage_capacity = 0;
+    cudaStream_t stage_streams[3] = {};  // host-buffer tracing: copy in, copy out, second compute stream
 };

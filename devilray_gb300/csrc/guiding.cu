@@ -640,6 +640,264 @@ __global__ void __launch_bounds__(128) k_guide_train_fb(const __nv_bfloat16 *wb,
     store_t<8>(tb.deltaT[0], tb.rows, r0, dacc, n, kHid);
 }
 
+// ---- training on the 5th-generation tensor cores (tcgen05) ----------------------
+//
+// One CTA of 128 threads carries 128-row tiles through the forward pass, the
+// loss gradient and the backward deltas, with the same arithmetic as
+// k_guide_train_fb (BF16 operands, FP32 sums; deltas enter the tensor cores as
+// a BF16 high part plus a BF16 remainder): thread t owns row t of the tile.
+// Forward layer l: D[128 x out] = A[128 x in] W_l^T as in k_guide_infer_tc.
+// Backward layer l: D[128 x in] = delta_hi[128 x out] W_l + delta_lo W_l, with
+// W_l staged as the N = in, K = out operand. Writes deltaT / actT of every
+// layer (the weight gradients are k_guide_wgrad's) and adds the batch loss.
+
+// Shared memory of k_guide_train_tc (byte offsets; regions 1 KB aligned).
+constexpr uint32_t kTtW = 0;                                        // forward weights, as kTcW0..kTcW4
+constexpr uint32_t kTtWT1 = 41984;                                  // W_l as [in 64][out 64], l = 1..3
+constexpr uint32_t kTtWT4 = kTtWT1 + 3 * kHid * kHid * 2;           // W_4 as [in 64][out 48]
+constexpr uint32_t kTtA = kTtWT4 + kHid * kOut * 2 + 1024;          // 128 x 80 layer input / delta high part
+constexpr uint32_t kTtAlo = kTtA + kTcRows * kIn * 2;               // 128 x 64 delta low part
+constexpr uint32_t kTtBias = kTtAlo + kTcRows * kHid * 2;
+constexpr uint32_t kTtBar = kTtBias + (4 * kHid + kOut) * 4;
+constexpr uint32_t kTtSmem = kTtBar + 16;
+
+// Issues the K/16 MMAs of one product into the accumulator at taddr
+// (accumulating from the first when `acc`).
+__device__ __forceinline__ void tc_mma_chain(uint32_t taddr, uint32_t a_base, uint32_t b_base, int M, int N, int K,
+                                             bool acc)
+{
+    const uint32_t idesc = idesc_bf16(M, N);
+    for (int s2 = 0; s2 < K / 16; ++s2) {
+        const uint64_t ad = smem_desc(a_base + (uint32_t)s2 * 2 * M * 16, (uint32_t)M * 16, 128);
+        const uint64_t bd = smem_desc(b_base + (uint32_t)s2 * 2 * N * 16, (uint32_t)N * 16, 128);
+        const uint32_t en = (acc || s2 > 0) ? 1u : 0u;
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(taddr),
+            "l"(ad), "l"(bd), "r"(idesc), "r"(en));
+    }
+}
+
+__global__ void __launch_bounds__(128) k_guide_train_tc(const __nv_bfloat16 *wb, const float *params, GuideParams gp,
+                                                        const float *pos, const float *dir, const float *sdir,
+                                                        const float *weight, uint32_t n, const float *weight_sum,
+                                                        TrainBuffers tb, float *loss, uint32_t *error)
+{
+    extern __shared__ __align__(1024) unsigned char smem[];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    // forward weights (N = out, K = in) and backward weights (N = in, K = out)
+    for (int l = 0; l < kLayers; ++l) {
+        const int K = fan_in(l), N = fan_out(l), chunks = K / 8;
+        const uint32_t base = l == 0 ? kTcW0 : l == 4 ? kTcW4 : kTcW1 + (uint32_t)(l - 1) * kHid * kHid * 2;
+        const uint4 *src = reinterpret_cast<const uint4 *>(wb + wb_off(l));
+        for (int i = tid; i < N * chunks; i += 128) {
+            const int r = i / chunks, j = i % chunks;
+            *reinterpret_cast<uint4 *>(smem + kTtW + base + canon_off(r, 8 * j, N)) = src[i];
+        }
+    }
+    for (int l = 1; l < kLayers; ++l) {
+        const int O = fan_out(l);
+        const uint32_t base = l == 4 ? kTtWT4 : kTtWT1 + (uint32_t)(l - 1) * kHid * kHid * 2;
+        const __nv_bfloat16 *w = wb + wb_off(l);
+        for (int i = tid; i < O * kHid; i += 128) {
+            const int o = i / kHid, in = i % kHid;
+            *reinterpret_cast<__nv_bfloat16 *>(smem + base + canon_off(in, o, kHid)) = w[i];
+        }
+    }
+    float *bias = reinterpret_cast<float *>(smem + kTtBias);
+    for (int l = 0; l < kLayers; ++l)
+        for (int i = tid; i < fan_out(l); i += 128) bias[l * kHid + i] = params[b_off(l) + i];
+    const uint32_t mbar = smem_u32(smem + kTtBar);
+    const uint32_t tslot = smem_u32(smem + kTtBar + 8);
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mbar) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;\n" ::"r"(tslot) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t taddr = *reinterpret_cast<volatile uint32_t *>(smem + kTtBar + 8);
+    const uint32_t a_base = smem_u32(smem + kTtA), alo_base = smem_u32(smem + kTtAlo);
+    const uint32_t w_base[kLayers] = {smem_u32(smem + kTtW + kTcW0), smem_u32(smem + kTtW + kTcW1),
+                                      smem_u32(smem + kTtW + kTcW1 + 8192), smem_u32(smem + kTtW + kTcW1 + 16384),
+                                      smem_u32(smem + kTtW + kTcW4)};
+    const uint32_t wt_base[kLayers] = {0, smem_u32(smem + kTtWT1), smem_u32(smem + kTtWT1 + 8192),
+                                       smem_u32(smem + kTtWT1 + 16384), smem_u32(smem + kTtWT4)};
+    const uint32_t lane_addr = taddr + ((uint32_t)(warp * 32) << 16);
+    const float wmean = *weight_sum / (float)n;
+    uint32_t phase = 0;
+    bool ok = true;
+
+    // MMAs of one product, committed and waited for by the whole block;
+    // false (and the error flag) when the bounded wait gives up.
+    auto run = [&](auto issue) -> bool {
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            issue();
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mbar)
+                         : "memory");
+        }
+        if (!__syncthreads_and(mbar_wait(mbar, phase) ? 1 : 0)) {
+            if (tid == 0) atomicOr(error, ERR_TIMEOUT);
+            return false;
+        }
+        phase ^= 1u;
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        return true;
+    };
+    auto read_acc = [&](float (&v)[64], int ncols) {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            if (16 * c >= ncols) break;
+            float t[16];
+            tmem_ld16(lane_addr + 16 * c, t);
+#pragma unroll
+            for (int i = 0; i < 16; ++i) v[16 * c + i] = t[i];
+        }
+        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+    };
+
+    for (uint32_t tile = blockIdx.x; ok && (uint64_t)tile * kTcRows < n; tile += gridDim.x) {
+        const uint32_t r = tile * kTcRows + tid;
+        const bool live = r < n;
+        float p[3], d[3];
+        uint32_t slot;
+        load_row(pos, dir, nullptr, n, r, gp, p, d, slot);
+        // input row: encoded, into the A tile and actT[0]
+#pragma unroll
+        for (int j = 0; j < kIn / 8; ++j) {
+            uint32_t q[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                float v0, v1;
+                encode_pair(p, d, 8 * j + 2 * k, v0, v1);
+                q[k] = pack_bf16(v0, v1);
+            }
+            *reinterpret_cast<uint4 *>(smem + kTtA + canon_off(tid, 8 * j, kTcRows)) = make_uint4(q[0], q[1], q[2], q[3]);
+            if (live) {
+                const __nv_bfloat16 *e = reinterpret_cast<const __nv_bfloat16 *>(q);
+#pragma unroll
+                for (int k = 0; k < 8; ++k) tb.actT[0][(size_t)(8 * j + k) * tb.rows + r] = e[k];
+            }
+        }
+        // forward; mask[l] bit i: output i of layer l (l = 0..3) after ReLU is nonzero
+        uint64_t mask[4] = {0, 0, 0, 0};
+        float v[64];
+        for (int l = 0; l < kLayers && ok; ++l) {
+            const int K = fan_in(l), N = fan_out(l);
+            ok = run([&] { tc_mma_chain(taddr, a_base, w_base[l], kTcRows, N, K, false); });
+            if (!ok) break;
+            read_acc(v, N);
+            const float *b = bias + l * kHid;
+            if (l < kLayers - 1) {
+#pragma unroll
+                for (int j = 0; j < kHid / 8; ++j) {
+                    uint32_t q[4];
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        const float h0 = fmaxf(v[8 * j + 2 * k] + b[8 * j + 2 * k], 0.0f);
+                        const float h1 = fmaxf(v[8 * j + 2 * k + 1] + b[8 * j + 2 * k + 1], 0.0f);
+                        q[k] = pack_bf16(h0, h1);
+                        if (q[k] & 0x7fffu) mask[l] |= 1ull << (8 * j + 2 * k);
+                        if (q[k] & 0x7fff0000u) mask[l] |= 1ull << (8 * j + 2 * k + 1);
+                    }
+                    *reinterpret_cast<uint4 *>(smem + kTtA + canon_off(tid, 8 * j, kTcRows)) =
+                        make_uint4(q[0], q[1], q[2], q[3]);
+                    if (live) {
+                        const __nv_bfloat16 *e = reinterpret_cast<const __nv_bfloat16 *>(q);
+#pragma unroll
+                        for (int k = 0; k < 8; ++k) tb.actT[l + 1][(size_t)(8 * j + k) * tb.rows + r] = e[k];
+                    }
+                }
+            } else {
+                // output layer: loss gradient of the row (one row per thread)
+                float y[kOut], dy[kOut];
+#pragma unroll
+                for (int i = 0; i < kOut; ++i) {
+                    y[i] = v[i] + b[i];
+                    dy[i] = 0.0f;
+                }
+                float lterm = 0.0f;
+                if (live) {
+                    const float c = wmean > 0.0f ? weight[r] / wmean : 0.0f;
+                    const float lq = guide_loss_grad(y, sdir[3 * (size_t)r], sdir[3 * (size_t)r + 1],
+                                                     sdir[3 * (size_t)r + 2], c / (float)n, dy);
+                    lterm = -c * lq / (float)n;
+                }
+                for (int o = 16; o > 0; o >>= 1) lterm += __shfl_down_sync(0xffffffffu, lterm, o);
+                if (lane == 0) atomicAdd(loss, lterm);
+                // delta of the output layer: deltaT[4] and its BF16 parts (K = 48)
+#pragma unroll
+                for (int j = 0; j < kOut / 8; ++j) {
+                    uint32_t hi[4], lo[4];
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) {
+                        const float c0 = dy[8 * j + 2 * k], c1 = dy[8 * j + 2 * k + 1];
+                        const __nv_bfloat162 h = __floats2bfloat162_rn(c0, c1);
+                        const float2 hf = __bfloat1622float2(h);
+                        hi[k] = *reinterpret_cast<const uint32_t *>(&h);
+                        lo[k] = pack_bf16(c0 - hf.x, c1 - hf.y);
+                    }
+                    *reinterpret_cast<uint4 *>(smem + kTtA + canon_off(tid, 8 * j, kTcRows)) =
+                        make_uint4(hi[0], hi[1], hi[2], hi[3]);
+                    *reinterpret_cast<uint4 *>(smem + kTtAlo + canon_off(tid, 8 * j, kTcRows)) =
+                        make_uint4(lo[0], lo[1], lo[2], lo[3]);
+                }
+                if (live)
+                    for (int o = 0; o < kOut; ++o) tb.deltaT[4][(size_t)o * tb.rows + r] = dy[o];
+            }
+        }
+        // backward: delta of layer l-1 = (delta_l W_l) masked by the ReLU of layer l-1
+        for (int l = kLayers - 1; l >= 1 && ok; --l) {
+            const int K = fan_out(l);
+            ok = run([&] {
+                tc_mma_chain(taddr, a_base, wt_base[l], kTcRows, kHid, K, false);
+                tc_mma_chain(taddr, alo_base, wt_base[l], kTcRows, kHid, K, true);
+            });
+            if (!ok) break;
+            read_acc(v, kHid);
+            const uint64_t m = mask[l - 1];
+#pragma unroll
+            for (int j = 0; j < kHid / 8; ++j) {
+                uint32_t hi[4], lo[4];
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const int i0 = 8 * j + 2 * k;
+                    const float c0 = (m >> i0) & 1ull ? v[i0] : 0.0f;
+                    const float c1 = (m >> (i0 + 1)) & 1ull ? v[i0 + 1] : 0.0f;
+                    v[i0] = c0;
+                    v[i0 + 1] = c1;
+                    const __nv_bfloat162 h = __floats2bfloat162_rn(c0, c1);
+                    const float2 hf = __bfloat1622float2(h);
+                    hi[k] = *reinterpret_cast<const uint32_t *>(&h);
+                    lo[k] = pack_bf16(c0 - hf.x, c1 - hf.y);
+                }
+                if (l > 1) {
+                    *reinterpret_cast<uint4 *>(smem + kTtA + canon_off(tid, 8 * j, kTcRows)) =
+                        make_uint4(hi[0], hi[1], hi[2], hi[3]);
+                    *reinterpret_cast<uint4 *>(smem + kTtAlo + canon_off(tid, 8 * j, kTcRows)) =
+                        make_uint4(lo[0], lo[1], lo[2], lo[3]);
+                }
+            }
+            if (live)
+                for (int o = 0; o < kHid; ++o) tb.deltaT[l - 1][(size_t)o * tb.rows + r] = v[o];
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        __syncthreads();
+    }
+    if (!ok) mbar_wait(mbar, phase);  // MMAs still in flight: wait again (bounded) before freeing their memory
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;\n" ::"r"(taddr) : "memory");
+}
+
 // Weight gradients of all layers in one launch (layer l = block z):
 // dW[o][i] += sum over rows of deltaT[o][r] actT[i][r] (tensor cores, K = rows;
 // delta as BF16 high + low parts), bias gradient db[o] += sum deltaT[o][r].
@@ -857,8 +1115,15 @@ dr_status run_gradients(dr_guide *g, const float *pos, const float *dir, const f
     DR_CUDA(cudaMemsetAsync(g->scalars, 0, 2 * sizeof(float), st));
     k_guide_weight_sum<<<std::min<unsigned>((n + 255) / 256, 64), 256, 0, st>>>(weight, n, g->scalars);
     const GuideParams gp = guide_params(g);
-    k_guide_train_fb<<<(n + 63) / 64, 128, kTrainSmem, st>>>(g->wb, g->params, gp, pos, dir, sdir, weight, n,
-                                                             g->scalars, g->tb, g->scalars + 1);
+    if (g->cfg.infer_kernel == DR_GUIDE_INFER_TCGEN05) {
+        const unsigned tiles = (n + kTcRows - 1) / kTcRows;
+        const unsigned blocks = std::min<unsigned>(tiles, (unsigned)g->ctx->num_sms * 2);
+        k_guide_train_tc<<<blocks, 128, kTtSmem, st>>>(g->wb, g->params, gp, pos, dir, sdir, weight, n, g->scalars,
+                                                        g->tb, g->scalars + 1, g->ctx->d_error);
+    } else {
+        k_guide_train_fb<<<(n + 63) / 64, 128, kTrainSmem, st>>>(g->wb, g->params, gp, pos, dir, sdir, weight, n,
+                                                                 g->scalars, g->tb, g->scalars + 1);
+    }
     int bx = 0;
     for (int l = 0; l < kLayers; ++l) bx = std::max(bx, wgrad_blocks_x(l));
     const dim3 grid((unsigned)bx, (n + kWgradRows - 1) / kWgradRows, (unsigned)kLayers);
@@ -913,6 +1178,7 @@ dr_status dr_guide_create(dr_context *ctx, const dr_guide_config *cfg, dr_guide 
         DR_CUDA(cudaFuncSetAttribute(k_guide_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kInferSmem));
         DR_CUDA(cudaFuncSetAttribute(k_guide_train_fb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTrainSmem));
         DR_CUDA(cudaFuncSetAttribute(k_guide_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem));
+        DR_CUDA(cudaFuncSetAttribute(k_guide_train_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTtSmem));
         attr = true;
     }
     auto *g = new (std::nothrow) dr_guide;

@@ -383,7 +383,8 @@ typedef struct dr_guide_config {
     float beta1, beta2, epsilon;  /* Adam; 0 = 0.9, 0.999, 1e-8 */
     float center[3];          /* position normalisation */
     float half_extent;        /* 0 = 1 */
-    uint32_t infer_kernel;    /* dr_guide_infer_kernel */
+    uint32_t infer_kernel;    /* dr_guide_infer_kernel: the tensor-core path of inference and of the
+                                 forward/backward pass of training */
 } dr_guide_config;
 
 typedef enum dr_guide_infer_kernel {

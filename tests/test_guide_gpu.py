@@ -35,8 +35,8 @@ def _dev(a):
     return torch.from_numpy(np.ascontiguousarray(a)).cuda()
 
 
-def _guide(native, ctx, seed=1):
-    return native.Guide(ctx, seed=seed, center=CENTER, half_extent=HALF)
+def _guide(native, ctx, seed=1, kernel=0):
+    return native.Guide(ctx, seed=seed, center=CENTER, half_extent=HALF, infer_kernel=kernel)
 
 
 def _random_params(oracle, seed, scale=1.0):
@@ -85,11 +85,12 @@ def test_forward_matches_oracle(native, ctx, oracle, n):
     assert err.max() <= 2e-2 * scale and np.median(err) <= 1e-3 * scale, (err.max(), scale)
 
 
-def test_gradients_match_oracle(native, ctx, oracle):
-    g = _guide(native, ctx)
+@pytest.mark.parametrize("kernel,n", [(0, 777), (1, 777), (0, 1), (0, 128), (0, 129)])
+def test_gradients_match_oracle(native, ctx, oracle, kernel, n):
+    """kernel 0: tcgen05 training (k_guide_train_tc), 1: mma.sync (k_guide_train_fb)."""
+    g = _guide(native, ctx, kernel=kernel)
     p = _random_params(oracle, 7, scale=0.7)
     g.set_params(p)
-    n = 777
     pos, nrm, sdir, w = _batch(n, 9)
     d_pos, d_nrm, d_sdir, d_w = _dev(pos), _dev(nrm), _dev(sdir), _dev(w)
     enc = torch.zeros((n, 80), dtype=torch.float32, device="cuda")
@@ -97,6 +98,7 @@ def test_gradients_match_oracle(native, ctx, oracle):
     loss, grad = g.gradients(d_pos, d_nrm, d_sdir, d_w, n)
     want_loss, want = oracle.mlp_loss_grad(p, enc.cpu().numpy(), sdir, w)
     assert abs(loss - want_loss) <= 1e-3 * abs(want_loss)
+    ctx.check()
     off = 0
     for fi, fo in [(80, 64), (64, 64), (64, 64), (64, 64), (64, 48)]:
         for part in (fi * fo, fo):

@@ -71,11 +71,14 @@ def test_online_training_changes_the_network_and_keeps_the_image(native, ctx):
     assert spec.positions.shape[0] > 24 * 1280
     g = _guide_for(native, ctx, spec, seed=5)
     p0 = g.params()
-    guided, _ = _render(native, scene, cam, 64, 12, 4, guide=g, alpha=0.5, train=True, train_batch=4096,
+    guided, _ = _render(native, scene, cam, 256, 12, 4, guide=g, alpha=0.5, train=True, train_batch=4096,
                         train_steps=4, wave_paths=64 * 48 * 4)
     p1 = g.params()
     assert not np.array_equal(p0, p1) and np.all(np.isfinite(p1))
     assert np.isfinite(g.last_loss())
-    plain, _ = _render(native, scene, cam, 512, 12, 9)
     assert np.all(np.isfinite(guided))
-    assert abs(guided.mean() - plain.mean()) < 0.1 * plain.mean(), (guided.mean(), plain.mean())
+    # two independent plain renders of the same size give the noise of a mean
+    a, _ = _render(native, scene, cam, 256, 12, 9)
+    b, _ = _render(native, scene, cam, 256, 12, 10)
+    ref, noise = 0.5 * (a.mean() + b.mean()), abs(a.mean() - b.mean())
+    assert abs(guided.mean() - ref) < max(6.0 * noise, 0.05 * ref), (guided.mean(), a.mean(), b.mean())
