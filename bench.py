@@ -516,7 +516,7 @@ def guided_section(ctx, native, device: int, stream, width: int = 480, height: i
         return e0.elapsed_time(e1) / 1e3
 
     wave = npix * 16  # 16 samples per pixel per wave: a training round after every 16 spp
-    alpha, steps, batch, budget, bounces = 0.75, 16, 16384, 512, 2
+    alpha, steps, batch, budget, bounces = 0.75, 16, 65536, 512, 2
 
     def runs(fn):
         ts, ms = [], []
