@@ -399,7 +399,8 @@ def batch_section(ctx, native, device: int, stream, scenes_n: int = 64, spp: int
     t0 = time.perf_counter()
     tune = native.autotune_batch(ctx, jobs, probe_spp=1, reps=2)
     tune_batch_s = time.perf_counter() - t0
-    b = native.Batch(ctx, jobs, wave_paths=tune.wave_paths, streams=tune.streams, chunk=tune.chunk, use_graph=True)
+    b = native.Batch(ctx, jobs, wave_paths=tune.wave_paths, streams=tune.streams, chunk=tune.chunk, use_graph=True,
+                     stack=tune.stack)
     b.render(stream=stream)  # captures the graph
     stream.synchronize()
     times = []
@@ -427,7 +428,8 @@ def batch_section(ctx, native, device: int, stream, scenes_n: int = 64, spp: int
     dev_build_s = time.perf_counter() - t0
     djobs = [native.make_job(sc, cam, acc, casts, spp=spp, max_depth=depth, seed=i)
              for i, ((spec, cam), sc, (acc, casts)) in enumerate(zip(specs, dscs, outs))]
-    db = native.Batch(ctx, djobs, wave_paths=tune.wave_paths, streams=tune.streams, chunk=tune.chunk, use_graph=True)
+    db = native.Batch(ctx, djobs, wave_paths=tune.wave_paths, streams=tune.streams, chunk=tune.chunk, use_graph=True,
+                      stack=tune.stack)
     db.render(stream=stream)
     stream.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)

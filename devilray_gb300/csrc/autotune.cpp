@@ -1,10 +1,10 @@
 // autotune.cpp -- picks the hierarchy width and the wavefront schedule
-// (paths per wave, concurrent waves, traversal fetch size) by timing short
-// probe renders on the device.
+// (paths per wave, concurrent waves, traversal fetch size, shared-memory
+// stack depth) by timing short probe renders on the device.
 //
 // The search is coordinate descent from the defaults (8-wide, 2^21 paths per
-// wave, 3 streams, adaptive fetch): each knob in turn is set to the fastest of
-// its candidates with the others fixed. Every candidate renders the same
+// wave, 3 streams, adaptive fetch, 8 stack entries): each knob in turn is set
+// to the fastest of its candidates with the others fixed. Every candidate renders the same
 // samples, and the images do not depend on the schedule, so the probes differ
 // only in time. Timing: CUDA events on the probe stream, one warm-up render,
 // then the minimum over `reps` renders.
@@ -18,7 +18,7 @@ namespace dr {
 namespace {
 
 struct Knobs {
-    uint32_t layout, wave_paths, streams, chunk;
+    uint32_t layout, wave_paths, streams, chunk, stack;
 };
 
 struct Probe {
@@ -35,7 +35,8 @@ struct Probe {
 void record(dr_autotune_result *out, const Knobs &k, float ms)
 {
     if (out->num_candidates < sizeof(out->candidates) / sizeof(out->candidates[0]))
-        out->candidates[out->num_candidates++] = dr_autotune_candidate{k.layout, k.wave_paths, k.streams, k.chunk, ms};
+        out->candidates[out->num_candidates++] =
+            dr_autotune_candidate{k.layout, k.wave_paths, k.streams, k.chunk, k.stack, ms};
 }
 
 // Times `run` (one render enqueued on the probe stream): warm-up, then min over reps.
@@ -62,20 +63,30 @@ dr_status time_probe(Probe &p, uint32_t reps, F &&run, float &ms)
 const uint32_t kWaveCandidates[] = {1u << 19, 1u << 20, 1u << 21, 1u << 22, 1u << 23};
 const uint32_t kStreamCandidates[] = {1, 2, 3};
 const uint32_t kChunkCandidates[] = {0, 32, 64, 128};
+const uint32_t kStackCandidates[] = {8, 4, 16};
 
-// Coordinate descent over wave size, streams and fetch size for a fixed layout.
+uint32_t &knob_ref(Knobs &k, int knob)
+{
+    return knob == 0 ? k.wave_paths : knob == 1 ? k.streams : knob == 2 ? k.chunk : k.stack;
+}
+
+// Coordinate descent over wave size, streams, fetch size and stack depth for
+// a fixed layout.
 template <class Measure>
 dr_status descend(Knobs &best, float &best_ms, Measure &&measure)
 {
-    for (int knob = 0; knob < 3; ++knob) {
-        const uint32_t *cand = knob == 0 ? kWaveCandidates : knob == 1 ? kStreamCandidates : kChunkCandidates;
-        const int n = knob == 0 ? 5 : knob == 1 ? 3 : 4;
-        if (knob == 2 && best.layout != 8) break;  // the fetch size belongs to the persistent 8-wide kernels
+    for (int knob = 0; knob < 4; ++knob) {
+        const uint32_t *cand = knob == 0   ? kWaveCandidates
+                               : knob == 1 ? kStreamCandidates
+                               : knob == 2 ? kChunkCandidates
+                                           : kStackCandidates;
+        const int n = knob == 0 ? 5 : knob == 1 ? 3 : knob == 2 ? 4 : 3;
+        if (knob >= 2 && best.layout != 8) break;  // fetch size and stack belong to the persistent 8-wide kernels
         Knobs winner = best;
         for (int i = 0; i < n; ++i) {
             Knobs k = best;
-            (knob == 0 ? k.wave_paths : knob == 1 ? k.streams : k.chunk) = cand[i];
-            if (k.wave_paths == best.wave_paths && k.streams == best.streams && k.chunk == best.chunk) continue;
+            knob_ref(k, knob) = cand[i];
+            if (knob_ref(k, knob) == knob_ref(best, knob)) continue;
             float ms = 0.0f;
             const dr_status st = measure(k, ms);
             if (st != DR_OK) return st;
@@ -118,7 +129,7 @@ dr_status dr_autotune(dr_context *ctx, const dr_scene_desc *desc, const dr_camer
     dr_status st = dr_device_allocate(ctx, npix * 16, &accum);
     if (st != DR_OK) return st;
 
-    Knobs best{8, 1u << 21, 3, 0};
+    Knobs best{8, 1u << 21, 3, 0, 8};
     float best_ms = 1e30f;
     dr_scene *scenes[2] = {nullptr, nullptr};
     auto measure_on = [&](dr_scene *s, const Knobs &k, float &ms) -> dr_status {
@@ -128,6 +139,7 @@ dr_status dr_autotune(dr_context *ctx, const dr_scene_desc *desc, const dr_camer
         c.wave_paths = k.wave_paths;
         c.streams = k.streams;
         c.chunk = k.chunk;
+        c.stack = k.stack;
         const dr_status r = time_probe(p, reps, [&] { return dr_render(s, cam, &c, static_cast<float *>(accum), nullptr, p.stream); }, ms);
         if (r == DR_OK) record(out, k, ms);
         return r;
@@ -158,6 +170,7 @@ dr_status dr_autotune(dr_context *ctx, const dr_scene_desc *desc, const dr_camer
     out->wave_paths = best.wave_paths;
     out->streams = best.streams;
     out->chunk = best.chunk;
+    out->stack = best.stack;
     out->best_ms = best_ms;
     return DR_OK;
 }
@@ -185,10 +198,10 @@ dr_status dr_autotune_batch(dr_context *ctx, const dr_job *jobs, uint32_t njobs,
         probe[j].casts_dev = nullptr;
         probe[j].config.spp = probe_spp;
     }
-    Knobs best{jobs[0].scene->layout, 1u << 21, 3, 0};
+    Knobs best{jobs[0].scene->layout, 1u << 21, 3, 0, 8};
     float best_ms = 1e30f;
     auto measure = [&](const Knobs &k, float &ms) -> dr_status {
-        dr_batch_config bc{k.wave_paths, k.streams, k.chunk, 0};
+        dr_batch_config bc{k.wave_paths, k.streams, k.chunk, 0, k.stack};
         dr_batch *b = nullptr;
         dr_status r = dr_batch_create(ctx, probe.data(), njobs, &bc, &b);
         if (r != DR_OK) return r;
@@ -205,6 +218,7 @@ dr_status dr_autotune_batch(dr_context *ctx, const dr_job *jobs, uint32_t njobs,
     out->wave_paths = best.wave_paths;
     out->streams = best.streams;
     out->chunk = best.chunk;
+    out->stack = best.stack;
     out->best_ms = best_ms;
     return DR_OK;
 }

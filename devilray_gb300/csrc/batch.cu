@@ -150,6 +150,8 @@ dr_status dr_batch_create(dr_context *ctx, const dr_job *jobs, uint32_t njobs, c
     DR_CHECK_ARG(ctx && out && (njobs == 0 || jobs), "dr_batch_create: NULL argument");
     *out = nullptr;
     DR_CHECK_ARG(njobs > 0, "dr_batch_create: no jobs");
+    DR_CHECK_ARGF(!cfg || cfg->stack == 0 || cfg->stack == 4 || cfg->stack == 8 || cfg->stack == 16,
+                  "dr_batch_create: stack must be 0, 4, 8 or 16 (got %u)", cfg ? cfg->stack : 0u);
     DR_CUDA(cudaSetDevice(ctx->device));
     // distinct scenes in first-use order
     std::vector<const dr_scene *> scenes;
@@ -187,6 +189,7 @@ dr_status dr_batch_create(dr_context *ctx, const dr_job *jobs, uint32_t njobs, c
         if (cfg->streams) b->wave.streams = cfg->streams;
         b->wave.chunk = cfg->chunk;
         b->use_graph = cfg->use_graph != 0;
+        if (cfg->stack) b->wave.stack = cfg->stack;
     }
 
     // offsets

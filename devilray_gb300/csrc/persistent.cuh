@@ -101,7 +101,7 @@ struct DirectSource {
     __device__ __forceinline__ void any(uint64_t i, bool hit) const { occluded[i] = hit ? 1 : 0; }
 };
 
-template <int MODE, bool ANY, bool COUNT, bool BATCH, class Source>
+template <int MODE, bool ANY, bool COUNT, bool BATCH, int STACK = DR_SMEM_STACK, class Source>
 __device__ __forceinline__ void persistent_wide(const Wide8Args &a, const Source &src, uint64_t n,
                                                 unsigned long long *counter, unsigned long long &nn,
                                                 unsigned long long &nb, unsigned long long &nt,
@@ -111,13 +111,13 @@ __device__ __forceinline__ void persistent_wide(const Wide8Args &a, const Source
     const int lane = threadIdx.x & 31;
     const unsigned lower = (1u << lane) - 1u;
     WideState s;
-    LaneStack stack;
-#if DR_SMEM_STACK > 0
-    __shared__ uint2 s_stack[kTraceBlock / 32][DR_SMEM_STACK][32];
-    stack.shared = &s_stack[threadIdx.x >> 5][0][threadIdx.x & 31];
-#else
-    stack.shared = nullptr;
-#endif
+    LaneStackT<STACK> stack;
+    if constexpr (STACK > 0) {
+        __shared__ uint2 s_stack[kTraceBlock / 32][STACK > 0 ? STACK : 1][32];
+        stack.shared = &s_stack[threadIdx.x >> 5][0][threadIdx.x & 31];
+    } else {
+        stack.shared = nullptr;
+    }
     TriBatch *batch = nullptr;
     if constexpr (BATCH) {
         __shared__ TriBatch s_batch[kTraceBlock / 32];

@@ -321,22 +321,47 @@ struct ShadowSource {
     }
 };
 
-template <int MODE>
+// STACK: shared-memory entries of each lane's traversal stack (kStackDepths).
+template <int MODE, int STACK>
 __global__ void __launch_bounds__(kTraceBlock, kP8MinBlocks) k_wave_closest_p8(RenderParams p, int b)
 {
     const Wide8Args w{p.trace.nodes8, p.trace.tri_ref, p.trace.tri_wt, p.trace.prim, p.trace.num_nodes, p.trace.error};
     const PathSource src{p.list[b & 1], p.rays, p.hits, p.slot_job, p.jobs};
     unsigned long long nn = 0, nb = 0, nt = 0, nh = 0;
-    persistent_wide<MODE, false, false, DR_TRI_BATCH_PATHS != 0>(w, src, p.counts[b], p.work + b, nn, nb, nt, nh, p.chunk);
+    persistent_wide<MODE, false, false, DR_TRI_BATCH_PATHS != 0, STACK>(w, src, p.counts[b], p.work + b, nn, nb, nt,
+                                                                         nh, p.chunk);
 }
 
-template <int MODE>
+template <int MODE, int STACK>
 __global__ void __launch_bounds__(kTraceBlock, kP8MinBlocks) k_wave_shadow_p8(RenderParams p, int b)
 {
     const Wide8Args w{p.trace.nodes8, p.trace.tri_ref, p.trace.tri_wt, p.trace.prim, p.trace.num_nodes, p.trace.error};
     const ShadowSource src{p.shadow_list, p.shadow_rays, p.color, p.pending, p.slot_job, p.jobs};
     unsigned long long nn = 0, nb = 0, nt = 0, nh = 0;
-    persistent_wide<MODE, true, false, DR_TRI_BATCH_ANY != 0>(w, src, p.counts[64 + b], p.work + 64 + b, nn, nb, nt, nh, p.chunk);
+    persistent_wide<MODE, true, false, DR_TRI_BATCH_ANY != 0, STACK>(w, src, p.counts[64 + b], p.work + 64 + b, nn,
+                                                                      nb, nt, nh, p.chunk);
+}
+
+// The persistent traversal kernels of one (triangle test, stack depth).
+struct P8Kernels {
+    void (*closest)(RenderParams, int);
+    void (*shadow)(RenderParams, int);
+};
+
+template <int MODE, int STACK>
+constexpr P8Kernels p8_kernels()
+{
+    return P8Kernels{k_wave_closest_p8<MODE, STACK>, k_wave_shadow_p8<MODE, STACK>};
+}
+
+P8Kernels select_p8(int tri_mode, uint32_t stack)
+{
+    const bool wt = tri_mode == DR_TRI_WATERTIGHT;
+    switch (stack) {
+    case 4: return wt ? p8_kernels<1, 4>() : p8_kernels<0, 4>();
+    case 16: return wt ? p8_kernels<1, 16>() : p8_kernels<0, 16>();
+    default: return wt ? p8_kernels<1, 8>() : p8_kernels<0, 8>();
+    }
 }
 
 // Closest hit of the surviving paths of bounce b (binary hierarchy).
@@ -823,9 +848,11 @@ dr_status WaveRunner::prepare(const std::vector<RenderJob> &jobs, const WavePlan
     const size_t need = wave_buffer_bytes(plan.max_slots, gr != nullptr);
     // occupancy of the persistent kernels, queried here so enqueue (which may
     // be under stream capture) only reads the cache
-    for (const void *k : {(const void *)k_wave_closest_p8<0>, (const void *)k_wave_closest_p8<1>,
-                          (const void *)k_wave_shadow_p8<0>, (const void *)k_wave_shadow_p8<1>})
-        resident_blocks(k, kTraceBlock);
+    for (int mode = 0; mode < 2; ++mode) {
+        const P8Kernels k = select_p8(mode, cfg.stack);
+        resident_blocks((const void *)k.closest, kTraceBlock);
+        resident_blocks((const void *)k.shadow, kTraceBlock);
+    }
     const uint32_t train_need = gr ? std::max<uint32_t>(1, gr->batch) * std::max<uint32_t>(1, gr->steps) : 0;
     bool grow = jobs.size() > jobs_capacity || plan.segs.size() > segs_capacity || train_need > train_cap;
     for (int k = 0; k < K; ++k) grow = grow || wave_bytes[k] < need;
@@ -900,10 +927,9 @@ dr_status WaveRunner::enqueue(const SceneArrays &sc, const WavePlan &plan, const
     }
     const int sms = ctx->num_sms;
     const bool wt = tri_mode == DR_TRI_WATERTIGHT, wide = sc.trace.layout == 8;
-    const int closest_per_sm = resident_blocks(wt ? (const void *)k_wave_closest_p8<1> : (const void *)k_wave_closest_p8<0>,
-                                               kTraceBlock);
-    const int shadow_per_sm = resident_blocks(wt ? (const void *)k_wave_shadow_p8<1> : (const void *)k_wave_shadow_p8<0>,
-                                              kTraceBlock);
+    const P8Kernels p8 = select_p8(tri_mode, cfg.stack);
+    const int closest_per_sm = resident_blocks((const void *)p8.closest, kTraceBlock);
+    const int shadow_per_sm = resident_blocks((const void *)p8.shadow, kTraceBlock);
     DR_CUDA(cudaEventRecord(fork, st));
     for (int k = 0; k < K; ++k) DR_CUDA(cudaStreamWaitEvent(stream[k], fork, 0));
     for (uint32_t w = 0; w < nwaves; ++w) {
@@ -934,8 +960,7 @@ dr_status WaveRunner::enqueue(const SceneArrays &sc, const WavePlan &plan, const
         k_camera<<<(W + kRenderBlock - 1) / kRenderBlock, kRenderBlock, 0, ws>>>(q);
         for (int b = 0; b < (int)plan.max_depth; ++b) {
             if (wide) {
-                if (wt) k_wave_closest_p8<1><<<pgrid, kTraceBlock, 0, ws>>>(q, b);
-                else k_wave_closest_p8<0><<<pgrid, kTraceBlock, 0, ws>>>(q, b);
+                p8.closest<<<pgrid, kTraceBlock, 0, ws>>>(q, b);
             } else {
                 if (wt) k_wave_closest<1, 2><<<trace_grid, kTraceBlock, 0, ws>>>(q, b);
                 else k_wave_closest<0, 2><<<trace_grid, kTraceBlock, 0, ws>>>(q, b);
@@ -951,8 +976,7 @@ dr_status WaveRunner::enqueue(const SceneArrays &sc, const WavePlan &plan, const
                 k_shade<false><<<shade_grid, kRenderBlock, 0, ws>>>(q, b);
             }
             if (wide) {
-                if (wt) k_wave_shadow_p8<1><<<sgrid, kTraceBlock, 0, ws>>>(q, b);
-                else k_wave_shadow_p8<0><<<sgrid, kTraceBlock, 0, ws>>>(q, b);
+                p8.shadow<<<sgrid, kTraceBlock, 0, ws>>>(q, b);
             } else {
                 if (wt) k_wave_shadow<1, 2><<<trace_grid, kTraceBlock, 0, ws>>>(q, b);
                 else k_wave_shadow<0, 2><<<trace_grid, kTraceBlock, 0, ws>>>(q, b);
@@ -1063,6 +1087,9 @@ extern "C" dr_status dr_render(dr_scene *s, const dr_camera *cam, const dr_rende
     if (cfg->wave_paths) wc.wave_paths = cfg->wave_paths;
     if (cfg->streams) wc.streams = cfg->streams;
     wc.chunk = cfg->chunk;
+    DR_CHECK_ARGF(cfg->stack == 0 || cfg->stack == 4 || cfg->stack == 8 || cfg->stack == 16,
+                  "render: stack must be 0, 4, 8 or 16 (got %u)", cfg->stack);
+    if (cfg->stack) wc.stack = cfg->stack;
     const std::vector<RenderJob> jobs{job};
     const WavePlan plan = plan_waves(jobs, wc.wave_paths);
     if (!s->runner) {
@@ -1107,6 +1134,9 @@ extern "C" dr_status dr_render_guided(dr_scene *s, const dr_camera *cam, const d
     if (cfg->wave_paths) wc.wave_paths = cfg->wave_paths;
     if (cfg->streams) wc.streams = cfg->streams;
     wc.chunk = cfg->chunk;
+    DR_CHECK_ARGF(cfg->stack == 0 || cfg->stack == 4 || cfg->stack == 8 || cfg->stack == 16,
+                  "render: stack must be 0, 4, 8 or 16 (got %u)", cfg->stack);
+    if (cfg->stack) wc.stack = cfg->stack;
     const std::vector<RenderJob> jobs{make_job(s, cam, cfg, accum_dev, casts_dev)};
     const WavePlan plan = plan_waves(jobs, wc.wave_paths);
     if (!s->runner) {

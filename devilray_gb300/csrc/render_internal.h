@@ -72,6 +72,7 @@ struct WaveConfig {
     uint32_t wave_paths = 1u << 21;  // target slots per wave (at least one sample of the largest job)
     uint32_t streams = kMaxWaveStreams;
     uint32_t chunk = 0;              // rays per warp fetch of the persistent traversal, 0 = adaptive
+    uint32_t stack = 8;              // shared-memory stack entries per lane: 4, 8 or 16
 };
 
 // Path guiding of a render: the network, the mixture probability, and online

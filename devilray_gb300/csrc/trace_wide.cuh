@@ -313,33 +313,37 @@ __device__ __forceinline__ bool wide_triangles(const Wide8Args &a, WideState &s,
     return false;
 }
 
-// Traversal stack of one lane in the persistent kernels: the first
-// DR_SMEM_STACK entries in shared memory (a per-warp array, one column per
-// lane: 2 KB per warp for 8 entries), the rest in local memory. Measured on
-// the incoherent workload: local only 3.74, 8 entries 3.83, 16 entries
-// 3.82 Grays/s.
+// Traversal stack of one lane in the persistent kernels: the first S entries
+// in shared memory (a per-warp array, one column per lane: 256 B per entry
+// and warp), the rest in local memory. Measured on the incoherent workload:
+// local only 3.74, 8 entries 3.83, 16 entries 3.82 Grays/s (before the later
+// node-test changes); 4 and 8 entries 4.37 Grays/s after them. The public
+// kernels use DR_SMEM_STACK entries; the renderer's depth is a schedule knob
+// (dr_render_config.stack), chosen by the autotuner.
 #ifndef DR_SMEM_STACK
 #define DR_SMEM_STACK 8
 #endif
-struct LaneStack {
+template <int S>
+struct LaneStackT {
     uint2 *shared;  // this lane's column: entry i at shared[32 * i]
-    uint2 local[kWideStack > DR_SMEM_STACK ? kWideStack - DR_SMEM_STACK : 1];
+    uint2 local[kWideStack > S ? kWideStack - S : 1];
     __device__ __forceinline__ void put(int i, uint2 v)
     {
-        if (DR_SMEM_STACK > 0 && i < DR_SMEM_STACK) shared[32 * i] = v;
-        else local[i - DR_SMEM_STACK] = v;
+        if (S > 0 && i < S) shared[32 * i] = v;
+        else local[i - S] = v;
     }
     __device__ __forceinline__ uint2 get(int i) const
     {
-        if (DR_SMEM_STACK > 0 && i < DR_SMEM_STACK) return shared[32 * i];
-        return local[i - DR_SMEM_STACK];
+        if (S > 0 && i < S) return shared[32 * i];
+        return local[i - S];
     }
 };
+using LaneStack = LaneStackT<DR_SMEM_STACK>;
 
 // Next node: from the current group, else from the stack (a popped triangle
 // group becomes pending and is tested first). True when the ray is finished.
-template <bool ANY>
-__device__ __forceinline__ bool wide_advance(const Wide8Args &a, WideState &s, LaneStack &stack)
+template <bool ANY, class Stack>
+__device__ __forceinline__ bool wide_advance(const Wide8Args &a, WideState &s, Stack &stack)
 {
     if ((s.group.y >> 8) == 0) {
         if (s.sp == 0) return true;

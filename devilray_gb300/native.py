@@ -82,7 +82,7 @@ class RenderConfig(C.Structure):
     _fields_ = [("max_depth", C.c_uint32), ("spp", C.c_uint32), ("sample_offset", C.c_uint32),
                 ("pixel_sampling", C.c_int32), ("seed", C.c_uint64), ("tri_mode", C.c_int32),
                 ("wave_paths", C.c_uint32), ("flags", C.c_uint32), ("debug", C.c_int32),
-                ("streams", C.c_uint32), ("chunk", C.c_uint32)]
+                ("streams", C.c_uint32), ("chunk", C.c_uint32), ("stack", C.c_uint32)]
 
 
 class Job(C.Structure):
@@ -92,7 +92,7 @@ class Job(C.Structure):
 
 class BatchConfig(C.Structure):
     _fields_ = [("wave_paths", C.c_uint32), ("streams", C.c_uint32), ("chunk", C.c_uint32),
-                ("use_graph", C.c_uint32)]
+                ("use_graph", C.c_uint32), ("stack", C.c_uint32)]
 
 
 class AutotuneConfig(C.Structure):
@@ -102,19 +102,20 @@ class AutotuneConfig(C.Structure):
 
 class AutotuneCandidate(C.Structure):
     _fields_ = [("layout", C.c_uint32), ("wave_paths", C.c_uint32), ("streams", C.c_uint32),
-                ("chunk", C.c_uint32), ("ms", C.c_float)]
+                ("chunk", C.c_uint32), ("stack", C.c_uint32), ("ms", C.c_float)]
 
 
 class AutotuneResult(C.Structure):
     _fields_ = [("layout", C.c_uint32), ("wave_paths", C.c_uint32), ("streams", C.c_uint32),
-                ("chunk", C.c_uint32), ("best_ms", C.c_float), ("num_candidates", C.c_uint32),
-                ("candidates", AutotuneCandidate * 64)]
+                ("chunk", C.c_uint32), ("stack", C.c_uint32), ("best_ms", C.c_float),
+                ("num_candidates", C.c_uint32), ("candidates", AutotuneCandidate * 64)]
 
     def as_dict(self) -> dict:
         return {"layout": self.layout, "wave_paths": self.wave_paths, "streams": self.streams, "chunk": self.chunk,
-                "best_ms": self.best_ms,
+                "stack": self.stack, "best_ms": self.best_ms,
                 "candidates": [{"layout": c.layout, "wave_paths": c.wave_paths, "streams": c.streams,
-                                "chunk": c.chunk, "ms": c.ms} for c in self.candidates[:self.num_candidates]]}
+                                "chunk": c.chunk, "stack": c.stack, "ms": c.ms}
+                               for c in self.candidates[:self.num_candidates]]}
 
 
 class BatchInfo(C.Structure):
@@ -334,7 +335,7 @@ def autotune(ctx: "Context", spec, cam: dict, spp: int = 1, max_depth: int = 10,
     objs, mats = spec_parts(spec)
     desc, keep = scene_desc(spec.positions, objs, mats)
     c = make_camera(cam)
-    cfg = RenderConfig(max_depth, spp, 0, pixel_sampling, seed, DR_TRI_REFERENCE, 0, 0, 0, 0, 0)
+    cfg = RenderConfig(max_depth, spp, 0, pixel_sampling, seed, DR_TRI_REFERENCE, 0, 0, 0, 0, 0, 0)
     tc = AutotuneConfig(probe_spp, reps, 1 if try_layouts else 0, 0)
     out = AutotuneResult()
     check(load().dr_autotune(ctx.handle, C.byref(desc), C.byref(c), C.byref(cfg), C.byref(tc), C.byref(out)))
@@ -393,10 +394,10 @@ class Scene:
     # -- rendering --
     def render(self, cam: dict, accum_dev, casts_dev=None, spp: int = 1, max_depth: int = 10,
                sample_offset: int = 0, pixel_sampling: int = 1, seed: int = 0, tri_mode: int = DR_TRI_REFERENCE,
-               wave_paths: int = 0, debug: int = 0, streams: int = 0, chunk: int = 0, stream=None):
+               wave_paths: int = 0, debug: int = 0, streams: int = 0, chunk: int = 0, stack: int = 0, stream=None):
         c = make_camera(cam)
         cfg = RenderConfig(max_depth, spp, sample_offset, pixel_sampling, seed, tri_mode, wave_paths, 0, debug,
-                           streams, chunk)
+                           streams, chunk, stack)
         check(load().dr_render(self.handle, C.byref(c), C.byref(cfg), _ptr(accum_dev), _ptr(casts_dev),
                                _stream_ptr(stream)))
 
@@ -407,7 +408,7 @@ class Scene:
                       stream=None):
         c = make_camera(cam)
         cfg = RenderConfig(max_depth, spp, sample_offset, pixel_sampling, seed, DR_TRI_REFERENCE, wave_paths, 0, 0,
-                           streams, 0)
+                           streams, 0, 0)
         g = GuidedConfig(alpha, 1 if train else 0, train_batch, train_steps, train_budget, target, bounces)
         check(load().dr_render_guided(self.handle, C.byref(c), C.byref(cfg), guide.handle, C.byref(g), _ptr(accum_dev),
                                       _ptr(casts_dev), _stream_ptr(stream)))
@@ -474,7 +475,7 @@ def make_job(scene: "Scene", cam: dict, accum_dev, casts_dev=None, spp: int = 1,
     j = Job()
     j.scene = scene.handle.value if isinstance(scene.handle, C.c_void_p) else scene.handle
     j.camera = make_camera(cam)
-    j.config = RenderConfig(max_depth, spp, sample_offset, pixel_sampling, seed, tri_mode, 0, 0, 0, 0, 0)
+    j.config = RenderConfig(max_depth, spp, sample_offset, pixel_sampling, seed, tri_mode, 0, 0, 0, 0, 0, 0)
     j.accum_dev = _ptr(accum_dev)
     j.casts_dev = _ptr(casts_dev) if casts_dev is not None else None
     return j
@@ -484,10 +485,10 @@ class Batch:
     """Many images of many scenes rendered as one schedule (dr_batch)."""
 
     def __init__(self, ctx: "Context", jobs: list, wave_paths: int = 0, streams: int = 0, chunk: int = 0,
-                 use_graph: bool = True):
+                 use_graph: bool = True, stack: int = 0):
         self.ctx = ctx
         self._jobs = (Job * len(jobs))(*jobs)
-        cfg = BatchConfig(wave_paths, streams, chunk, 1 if use_graph else 0)
+        cfg = BatchConfig(wave_paths, streams, chunk, 1 if use_graph else 0, stack)
         h = C.c_void_p()
         check(load().dr_batch_create(ctx.handle, self._jobs, len(jobs), C.byref(cfg), C.byref(h)))
         self.handle = h.value
@@ -524,9 +525,9 @@ def autotune_batch(ctx: "Context", jobs: list, probe_spp: int = 1, reps: int = 2
 
 
 def render_batch(ctx: "Context", jobs: list, wave_paths: int = 0, streams: int = 0, chunk: int = 0,
-                 stream=None) -> None:
+                 stack: int = 0, stream=None) -> None:
     arr = (Job * len(jobs))(*jobs)
-    cfg = BatchConfig(wave_paths, streams, chunk, 0)
+    cfg = BatchConfig(wave_paths, streams, chunk, 0, stack)
     check(load().dr_render_batch(ctx.handle, arr, len(jobs), C.byref(cfg), _stream_ptr(stream)))
 
 

@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define DR_ABI_VERSION 4
+#define DR_ABI_VERSION 5
 
 typedef enum dr_status {
     DR_OK = 0,
@@ -246,6 +246,8 @@ typedef struct dr_render_config {
     uint32_t streams;        /* concurrent waves, 1..3, 0 = 3 */
     uint32_t chunk;          /* rays per warp fetch of the persistent traversal
                                 (32, 64, 96 or 128), 0 = adaptive */
+    uint32_t stack;          /* traversal-stack entries per lane kept in shared memory
+                                by the 8-wide kernels (4, 8 or 16), 0 = 8 */
 } dr_render_config;
 
 /* Adds cfg->spp path samples per pixel to accum_dev (float4 per pixel, row
@@ -303,6 +305,7 @@ typedef struct dr_batch_config {
     uint32_t streams;        /* concurrent waves, 1..3, 0 = 3 */
     uint32_t chunk;          /* persistent traversal fetch (32..128, multiple of 32), 0 = adaptive */
     uint32_t use_graph;      /* 1: capture the schedule into a CUDA graph on the first render */
+    uint32_t stack;          /* shared-memory traversal-stack entries per lane (4, 8 or 16), 0 = 8 */
 } dr_batch_config;
 
 typedef struct dr_batch dr_batch;
@@ -344,24 +347,24 @@ typedef struct dr_autotune_config {
 } dr_autotune_config;
 
 typedef struct dr_autotune_candidate {
-    uint32_t layout, wave_paths, streams, chunk;
+    uint32_t layout, wave_paths, streams, chunk, stack;
     float ms;
 } dr_autotune_candidate;
 
 typedef struct dr_autotune_result {
-    uint32_t layout, wave_paths, streams, chunk;  /* the chosen settings */
+    uint32_t layout, wave_paths, streams, chunk, stack;  /* the chosen settings */
     float best_ms;                                 /* probe time of the chosen settings */
     uint32_t num_candidates;
     dr_autotune_candidate candidates[64];          /* every probe, in order */
 } dr_autotune_result;
 
 /* Picks the hierarchy width (dr_build_config.layout) and the wave schedule
- * (dr_render_config wave_paths / streams / chunk) for rendering `desc` through
+ * (dr_render_config wave_paths / streams / chunk / stack) for rendering `desc` through
  * `camera` with `cfg`, by coordinate descent over timed probe renders of the
  * same samples (images do not depend on these settings). Synchronous. */
 dr_status dr_autotune(dr_context *ctx, const dr_scene_desc *desc, const dr_camera *camera,
                       const dr_render_config *cfg, const dr_autotune_config *tc, dr_autotune_result *out);
-/* The same for a batch (dr_batch_config wave_paths / streams / chunk; the layout
+/* The same for a batch (dr_batch_config wave_paths / streams / chunk / stack; the layout
  * is the scenes'), probing the batch's images with probe_spp samples each. */
 dr_status dr_autotune_batch(dr_context *ctx, const dr_job *jobs, uint32_t njobs, const dr_autotune_config *tc,
                             dr_autotune_result *out);

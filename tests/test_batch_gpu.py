@@ -71,14 +71,15 @@ def test_batch_images_equal_single_renders(native, ctx, layout):
         assert got[:, 3].min() == spp and got[:, :3].sum() > 0
 
 
-@pytest.mark.parametrize("wave_paths,streams,chunk", [(0, 0, 0), (2048, 1, 32), (5000, 2, 128), (1 << 16, 3, 64)])
-def test_batch_schedule_knobs_do_not_change_pixels(native, ctx, wave_paths, streams, chunk):
+@pytest.mark.parametrize("wave_paths,streams,chunk,stack", [(0, 0, 0, 0), (2048, 1, 32, 4), (5000, 2, 128, 16),
+                                                             (1 << 16, 3, 64, 8)])
+def test_batch_schedule_knobs_do_not_change_pixels(native, ctx, wave_paths, streams, chunk, stack):
     scs = _scenes(native, ctx, 8)
     specs = _job_specs()
     ref_jobs, ref_outs = _batch_buffers(native, scs, specs)
     native.render_batch(ctx, ref_jobs)
     jobs, outs = _batch_buffers(native, scs, specs)
-    native.render_batch(ctx, jobs, wave_paths=wave_paths, streams=streams, chunk=chunk)
+    native.render_batch(ctx, jobs, wave_paths=wave_paths, streams=streams, chunk=chunk, stack=stack)
     torch.cuda.synchronize()
     for (a, c), (ra, rc) in zip(outs, ref_outs):
         assert torch.equal(a.view(torch.int32), ra.view(torch.int32)) and torch.equal(c, rc)
@@ -144,6 +145,7 @@ def test_autotune_picks_a_measured_schedule(native, ctx):
     res = native.autotune(ctx, spec, cam, spp=4, max_depth=8, reps=1)
     d = res.as_dict()
     assert res.layout in (2, 8) and res.streams in (1, 2, 3) and res.chunk in (0, 32, 64, 128)
+    assert res.stack in (4, 8, 16)
     assert res.wave_paths in (1 << 19, 1 << 20, 1 << 21, 1 << 22, 1 << 23)
     assert len(d["candidates"]) >= 6 and res.best_ms > 0
     assert {c["layout"] for c in d["candidates"]} == {2, 8}
@@ -153,7 +155,8 @@ def test_autotune_picks_a_measured_schedule(native, ctx):
     a, ca = _alone(native, scene, cam, 4, 8, 0, 1)
     n = cam["width"] * cam["height"]
     acc = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
-    scene.render(cam, acc, spp=4, max_depth=8, wave_paths=res.wave_paths, streams=res.streams, chunk=res.chunk)
+    scene.render(cam, acc, spp=4, max_depth=8, wave_paths=res.wave_paths, streams=res.streams, chunk=res.chunk,
+                 stack=res.stack)
     torch.cuda.synchronize()
     assert np.array_equal(acc.cpu().numpy().view(np.uint32), a.view(np.uint32))
 
@@ -166,3 +169,10 @@ def test_autotune_batch(native, ctx):
     # the jobs' own buffers are untouched by the probes
     for acc, casts in outs:
         assert not acc.any() and not casts.any()
+
+
+def test_invalid_stack_depth_is_rejected(native, ctx):
+    scs = _scenes(native, ctx, 8)
+    jobs, _ = _batch_buffers(native, scs, _job_specs()[:2])
+    with pytest.raises(Exception, match="stack"):
+        native.render_batch(ctx, jobs, stack=5)
