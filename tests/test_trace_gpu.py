@@ -210,6 +210,36 @@ def test_counters_and_host_path(native, ctx, oracle, layout):
     assert info.depth < 64 and info.num_nodes > 0 and info.slack > 0
 
 
+def test_concurrent_launches_on_two_streams(native, ctx, oracle):
+    """Persistent launches on different streams run at the same time; each
+    takes its own work counter, so both results stay exact (including the
+    host-buffer path, which alternates two compute streams itself)."""
+    half = scenes.density_half(30000)
+    soup, _, _ = scenes.incoherent_soup(30000, seed=12, half=half)
+    rays_a = scenes.incoherent_rays(300000, seed=13, half=half)
+    rays_b = scenes.incoherent_rays(300000, seed=14, half=half)
+    scene = native.Scene(ctx, soup, layout=8)
+    ta, pa, _ = gpu_closest(native, scene, rays_a)
+    tb, pb, _ = gpu_closest(native, scene, rays_b)
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+    da, db = torch.from_numpy(rays_a).cuda(), torch.from_numpy(rays_b).cuda()
+    torch.cuda.synchronize()
+    for _ in range(3):
+        ha = torch.empty((len(rays_a), 2), dtype=torch.int32, device="cuda")
+        hb = torch.empty((len(rays_b), 2), dtype=torch.int32, device="cuda")
+        occ = torch.empty(len(rays_b), dtype=torch.uint8, device="cuda")
+        scene.trace_closest(da, len(rays_a), ha, stream=s1)
+        scene.trace_closest(db, len(rays_b), hb, stream=s2)
+        scene.trace_any(db, len(rays_b), occ, stream=s1)
+        torch.cuda.synchronize()
+        a, b = ha.cpu().numpy(), hb.cpu().numpy()
+        assert np.array_equal(a[:, 1], pa) and np.array_equal(a[:, 0].view(np.float32).view(np.uint32), _bits(ta))
+        assert np.array_equal(b[:, 1], pb) and np.array_equal(b[:, 0].view(np.float32).view(np.uint32), _bits(tb))
+        assert np.array_equal(occ.cpu().numpy().astype(bool), pb >= 0)
+    hits = scene.trace_closest_host(np.concatenate([rays_a, rays_b]))
+    assert np.array_equal(hits["prim"], np.concatenate([pa, pb]))
+
+
 def test_invalid_arguments_return_status(native, ctx):
     scene = native.Scene(ctx, np.array([[0, 0, 0, 1, 0, 0, 0, 1, 0]], np.float32))
     with pytest.raises(native.DrError) as e:
