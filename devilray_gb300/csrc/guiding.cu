@@ -326,27 +326,53 @@ constexpr uint32_t kTcW1 = kTcW0 + 64 * 80 * 2;      // 3 x 64 x 64
 constexpr uint32_t kTcW4 = kTcW1 + 3 * 64 * 64 * 2;  // 48 x 64
 constexpr uint32_t kTcA = kTcW4 + 48 * 64 * 2 + 1024;  // 128 x 80 input / 128 x 64 hidden
 constexpr uint32_t kTcBias = kTcA + kTcRows * kIn * 2;
-constexpr uint32_t kTcBar = kTcBias + (4 * kHid + kOut) * 4;
-constexpr uint32_t kTcSmem = kTcBar + 16;
+constexpr uint32_t kTcBar = kTcBias + (4 * kHid + kOut) * 4;  // MMA mbarrier, TMEM address, copy mbarrier
+constexpr uint32_t kTcSmem = kTcBar + 24;
 
-__global__ void __launch_bounds__(128) k_guide_infer_tc(const __nv_bfloat16 *wb, const float *params, GuideParams gp,
+// The weights as the tcgen05 kernels hold them in shared memory, kept in
+// global memory beside the BF16 copy so a CTA fetches them with one bulk
+// asynchronous copy: [0, 40960) the forward operands (kTcW0..kTcW4: W_l as
+// N = out, K = in, canonical K-major), [40960, 71680) the backward operands of
+// layers 1..4 (W_l as N = in 64, K = out).
+constexpr uint32_t kImgFwdBytes = 40960;
+constexpr uint32_t kImgBytes = kImgFwdBytes + 3 * kHid * kHid * 2 + kHid * kOut * 2;
+
+__device__ __forceinline__ void store_weight(__nv_bfloat16 *wb, unsigned char *img, int l, int idx, float p)
+{
+    const __nv_bfloat16 b = __float2bfloat16_rn(p);
+    wb[wb_off(l) + idx] = b;
+    const int o = idx / fan_in(l), in = idx % fan_in(l);
+    const uint32_t fwd = l == 0 ? kTcW0 : l == 4 ? kTcW4 : kTcW1 + (uint32_t)(l - 1) * kHid * kHid * 2;
+    *reinterpret_cast<__nv_bfloat16 *>(img + fwd + canon_off(o, in, fan_out(l))) = b;
+    if (l > 0) {
+        const uint32_t bwd = kImgFwdBytes + (uint32_t)(l - 1) * kHid * kHid * 2;
+        *reinterpret_cast<__nv_bfloat16 *>(img + bwd + canon_off(in, o, kHid)) = b;
+    }
+}
+
+// One bulk asynchronous copy of `bytes` of the weight image into shared
+// memory, completing on the mbarrier `cbar` (issued by one thread).
+__device__ __forceinline__ void fetch_weight_image(uint32_t dst, const unsigned char *img, uint32_t bytes, uint32_t cbar)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(cbar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(cbar), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(dst),
+                 "l"(img), "r"(bytes), "r"(cbar)
+                 : "memory");
+}
+
+__global__ void __launch_bounds__(128) k_guide_infer_tc(const unsigned char *img, const float *params, GuideParams gp,
                                                         const float *pos, const float *dir, const uint32_t *list,
                                                         const uint32_t *count, uint32_t n_fixed, float *y,
                                                         uint32_t *error)
 {
     extern __shared__ __align__(1024) unsigned char smem[];
     const int tid = threadIdx.x, warp = tid >> 5;
-    // weights in the canonical layout (B operands: N = outputs, K = inputs),
-    // 16-byte chunks: 8 consecutive inputs of one output row
-    for (int l = 0; l < kLayers; ++l) {
-        const int K = fan_in(l), N = fan_out(l), chunks = K / 8;
-        const uint32_t base = l == 0 ? kTcW0 : l == 4 ? kTcW4 : kTcW1 + (uint32_t)(l - 1) * kHid * kHid * 2;
-        const uint4 *src = reinterpret_cast<const uint4 *>(wb + wb_off(l));
-        for (int i = tid; i < N * chunks; i += 128) {
-            const int r = i / chunks, j = i % chunks;
-            *reinterpret_cast<uint4 *>(smem + base + canon_off(r, 8 * j, N)) = src[i];
-        }
-    }
+    // weights in the canonical layout (B operands: N = outputs, K = inputs):
+    // the forward part of the weight image, one bulk copy
+    const uint32_t cbar = smem_u32(smem + kTcBar + 16);
+    if (tid == 0) fetch_weight_image(smem_u32(smem + kTcW0), img, kImgFwdBytes, cbar);
     float *bias = reinterpret_cast<float *>(smem + kTcBias);
     for (int l = 0; l < kLayers; ++l)
         for (int i = tid; i < fan_out(l); i += 128) bias[l * kHid + i] = params[b_off(l) + i];
@@ -370,7 +396,9 @@ __global__ void __launch_bounds__(128) k_guide_infer_tc(const __nv_bfloat16 *wb,
                                       smem_u32(smem + kTcW1 + 16384), smem_u32(smem + kTcW4)};
     const uint32_t n = count ? *count : n_fixed;
     uint32_t phase = 0;
-    bool ok = true;
+    // the weights have landed (bounded wait, one decision for the block)
+    bool ok = __syncthreads_and(mbar_wait(cbar, 0) ? 1 : 0) != 0;
+    if (!ok && tid == 0) atomicOr(error, ERR_TIMEOUT);
     for (uint32_t tile = blockIdx.x; ok && (uint64_t)tile * kTcRows < n; tile += gridDim.x) {
         const uint32_t r = tile * kTcRows + tid;
         float p[3], d[3];
@@ -448,7 +476,11 @@ __global__ void __launch_bounds__(128) k_guide_infer_tc(const __nv_bfloat16 *wb,
         asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
         __syncthreads();
     }
-    if (!ok) mbar_wait(mbar, phase);  // MMAs still in flight: wait again (bounded) before freeing their memory
+    if (!ok) {
+        // MMAs or the weight copy still in flight: wait again (bounded) before freeing their memory
+        mbar_wait(mbar, phase);
+        mbar_wait(cbar, 0);
+    }
     __syncthreads();
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;\n" ::"r"(taddr) : "memory");
 }
@@ -686,15 +718,16 @@ constexpr uint32_t kTfW = kTfD + 16 * 2048;                    // forward weight
 constexpr uint32_t kTfWT1 = kTfW + 40960;                      // W_l as [in 64][out 64], l = 1..3
 constexpr uint32_t kTfWT4 = kTfWT1 + 3 * kHid * kHid * 2;      // W_4 as [in 64][out 48]
 constexpr uint32_t kTfBias = kTfWT4 + kHid * kOut * 2;
-constexpr uint32_t kTfBar = kTfBias + (4 * kHid + kOut) * 4;
-constexpr uint32_t kTfSmem = kTfBar + 16;
+constexpr uint32_t kTfBar = kTfBias + (4 * kHid + kOut) * 4;  // MMA mbarrier, TMEM address, copy mbarrier
+constexpr uint32_t kTfSmem = kTfBar + 24;
+static_assert(kTfWT1 == kTfW + kImgFwdBytes && kTfBias == kTfW + kImgBytes, "the weight image is one copy");
 // tensor-memory columns: [0, 64) the forward / backward product, then dW_l
 __host__ __device__ constexpr uint32_t tf_dcol(int l) { return l == 0 ? 64u : 160u + 80u * (uint32_t)(l - 1); }
 
 // Instruction descriptor of kind::f16 with both operands MN-major (bits 15, 16).
 __host__ __device__ constexpr uint32_t idesc_bf16_mn(int M, int N) { return idesc_bf16(M, N) | (1u << 15) | (1u << 16); }
 
-__global__ void __launch_bounds__(128) k_guide_train_fused(const __nv_bfloat16 *wb, const float *params,
+__global__ void __launch_bounds__(128) k_guide_train_fused(const unsigned char *img, const float *params,
                                                            GuideParams gp, const float *pos, const float *dir,
                                                            const float *sdir, const float *weight, uint32_t n,
                                                            const float *weight_sum, float *grad, float *loss,
@@ -702,24 +735,10 @@ __global__ void __launch_bounds__(128) k_guide_train_fused(const __nv_bfloat16 *
 {
     extern __shared__ __align__(1024) unsigned char smem[];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    for (int l = 0; l < kLayers; ++l) {
-        const int K = fan_in(l), N = fan_out(l), chunks = K / 8;
-        const uint32_t base = l == 0 ? kTcW0 : l == 4 ? kTcW4 : kTcW1 + (uint32_t)(l - 1) * kHid * kHid * 2;
-        const uint4 *src = reinterpret_cast<const uint4 *>(wb + wb_off(l));
-        for (int i = tid; i < N * chunks; i += 128) {
-            const int r = i / chunks, j = i % chunks;
-            *reinterpret_cast<uint4 *>(smem + kTfW + base + canon_off(r, 8 * j, N)) = src[i];
-        }
-    }
-    for (int l = 1; l < kLayers; ++l) {
-        const int O = fan_out(l);
-        const uint32_t base = l == 4 ? kTfWT4 : kTfWT1 + (uint32_t)(l - 1) * kHid * kHid * 2;
-        const __nv_bfloat16 *w = wb + wb_off(l);
-        for (int i = tid; i < O * kHid; i += 128) {
-            const int o = i / kHid, in = i % kHid;
-            *reinterpret_cast<__nv_bfloat16 *>(smem + base + canon_off(in, o, kHid)) = w[i];
-        }
-    }
+    // forward (N = out, K = in) and backward (N = in, K = out) weights: the
+    // weight image, one bulk copy
+    const uint32_t cbar = smem_u32(smem + kTfBar + 16);
+    if (tid == 0) fetch_weight_image(smem_u32(smem + kTfW), img, kImgBytes, cbar);
     float *bias = reinterpret_cast<float *>(smem + kTfBias);
     for (int l = 0; l < kLayers; ++l)
         for (int i = tid; i < fan_out(l); i += 128) bias[l * kHid + i] = params[b_off(l) + i];
@@ -761,7 +780,9 @@ __global__ void __launch_bounds__(128) k_guide_train_fused(const __nv_bfloat16 *
     const uint32_t lane_addr = taddr + ((uint32_t)(warp * 32) << 16);
     const float wmean = *weight_sum / (float)n;
     uint32_t phase = 0;
-    bool ok = true, first = true;
+    // the weights have landed (bounded wait, one decision for the block)
+    bool ok = __syncthreads_and(mbar_wait(cbar, 0) ? 1 : 0) != 0, first = true;
+    if (!ok && tid == 0) atomicOr(error, ERR_TIMEOUT);
 
     auto run = [&](auto issue) -> bool {
         asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
@@ -936,7 +957,11 @@ __global__ void __launch_bounds__(128) k_guide_train_fused(const __nv_bfloat16 *
             }
         }
     }
-    if (!ok) mbar_wait(mbar, phase);  // MMAs still in flight: wait again (bounded) before freeing their memory
+    if (!ok) {
+        // MMAs or the weight copy still in flight: wait again (bounded) before freeing their memory
+        mbar_wait(mbar, phase);
+        mbar_wait(cbar, 0);
+    }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;\n" ::"r"(taddr) : "memory");
@@ -1023,7 +1048,7 @@ __global__ void k_guide_weight_sum(const float *w, uint32_t n, float *sum)
 }
 
 __global__ void k_guide_adam(float *params, float *m, float *v, const float *grad, int t, float lr, float b1, float b2,
-                             float eps, __nv_bfloat16 *wb)
+                             float eps, __nv_bfloat16 *wb, unsigned char *img)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kNumParams) return;
@@ -1035,17 +1060,17 @@ __global__ void k_guide_adam(float *params, float *m, float *v, const float *gra
     const float c1 = 1.0f - powf(b1, (float)t), c2 = 1.0f - powf(b2, (float)t);
     const float p = params[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
     params[i] = p;
-    // BF16 weight copy (biases stay FP32)
+    // BF16 weight copy and weight image (biases stay FP32)
     for (int l = 0; l < kLayers; ++l)
-        if (i >= w_off(l) && i < b_off(l)) wb[wb_off(l) + (i - w_off(l))] = __float2bfloat16_rn(p);
+        if (i >= w_off(l) && i < b_off(l)) store_weight(wb, img, l, i - w_off(l), p);
 }
 
-__global__ void k_guide_export(const float *params, __nv_bfloat16 *wb)
+__global__ void k_guide_export(const float *params, __nv_bfloat16 *wb, unsigned char *img)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kNumParams) return;
     for (int l = 0; l < kLayers; ++l)
-        if (i >= w_off(l) && i < b_off(l)) wb[wb_off(l) + (i - w_off(l))] = __float2bfloat16_rn(params[i]);
+        if (i >= w_off(l) && i < b_off(l)) store_weight(wb, img, l, i - w_off(l), params[i]);
 }
 
 // The network input of each row (80 columns), as the forward pass forms it
@@ -1094,6 +1119,7 @@ struct dr_guide {
     dr_guide_config cfg{};
     float *params = nullptr, *m = nullptr, *v = nullptr, *grad = nullptr;
     __nv_bfloat16 *wb = nullptr;
+    unsigned char *img = nullptr;  // weight image of the tcgen05 kernels (kImgBytes)
     float *scalars = nullptr;  // [0] sum of the batch's sample weights, [1] loss
     dr::TrainBuffers tb{};
     void *tb_mem = nullptr;
@@ -1121,6 +1147,7 @@ void free_guide(dr_guide *g)
     cudaFree(g->v);
     cudaFree(g->grad);
     cudaFree(g->wb);
+    cudaFree(g->img);
     cudaFree(g->scalars);
     cudaFree(g->tb_mem);
     delete g;
@@ -1163,7 +1190,7 @@ dr_status run_gradients(dr_guide *g, const float *pos, const float *dir, const f
         // one CTA per SM (its shared memory and 512 tensor-memory columns)
         const unsigned tiles = (n + kTcRows - 1) / kTcRows;
         const unsigned blocks = std::min<unsigned>(tiles, (unsigned)g->ctx->num_sms);
-        k_guide_train_fused<<<blocks, 128, kTfSmem, st>>>(g->wb, g->params, gp, pos, dir, sdir, weight, n,
+        k_guide_train_fused<<<blocks, 128, kTfSmem, st>>>(g->img, g->params, gp, pos, dir, sdir, weight, n,
                                                            g->scalars, g->grad, g->scalars + 1, g->ctx->d_error);
     } else {
         k_guide_train_fb<<<(n + 63) / 64, 128, kTrainSmem, st>>>(g->wb, g->params, gp, pos, dir, sdir, weight, n,
@@ -1188,7 +1215,7 @@ cudaError_t launch_guide_infer(const dr_guide *g, const float *pos, const float 
     if (g->cfg.infer_kernel == DR_GUIDE_INFER_TCGEN05) {
         const unsigned tiles = (max_rows + kTcRows - 1) / kTcRows;
         const unsigned blocks = std::min<unsigned>(tiles, (unsigned)g->ctx->num_sms * 3);
-        k_guide_infer_tc<<<blocks, 128, kTcSmem, st>>>(g->wb, g->params, guide_params(g), pos, dir, list, count,
+        k_guide_infer_tc<<<blocks, 128, kTcSmem, st>>>(g->img, g->params, guide_params(g), pos, dir, list, count,
                                                        max_rows, y, g->ctx->d_error);
     } else {
         const unsigned tiles = (max_rows + 15) / 16;
@@ -1242,7 +1269,7 @@ dr_status dr_guide_create(dr_context *ctx, const dr_guide_config *cfg, dr_guide 
     cudaError_t e;
     if ((e = cudaMalloc(&g->params, kNumParams * 4)) != cudaSuccess || (e = cudaMalloc(&g->m, kNumParams * 4)) != cudaSuccess ||
         (e = cudaMalloc(&g->v, kNumParams * 4)) != cudaSuccess || (e = cudaMalloc(&g->grad, kNumParams * 4)) != cudaSuccess ||
-        (e = cudaMalloc(&g->wb, kNumWeights * 2)) != cudaSuccess || (e = cudaMalloc(&g->scalars, 16)) != cudaSuccess ||
+        (e = cudaMalloc(&g->wb, kNumWeights * 2)) != cudaSuccess || (e = cudaMalloc(&g->img, kImgBytes)) != cudaSuccess || (e = cudaMalloc(&g->scalars, 16)) != cudaSuccess ||
         (e = cudaMemset(g->m, 0, kNumParams * 4)) != cudaSuccess || (e = cudaMemset(g->v, 0, kNumParams * 4)) != cudaSuccess ||
         (e = cudaMemset(g->scalars, 0, 16)) != cudaSuccess) {
         free_guide(g);
@@ -1282,7 +1309,7 @@ dr_status dr_guide_set_params(dr_guide *g, const float *host, uint32_t n)
     DR_CUDA(cudaMemset(g->m, 0, kNumParams * 4));
     DR_CUDA(cudaMemset(g->v, 0, kNumParams * 4));
     g->step = 0;
-    k_guide_export<<<(kNumParams + 255) / 256, 256>>>(g->params, g->wb);
+    k_guide_export<<<(kNumParams + 255) / 256, 256>>>(g->params, g->wb, g->img);
     DR_CUDA(cudaGetLastError());
     DR_CUDA(cudaDeviceSynchronize());
     return DR_OK;
@@ -1330,7 +1357,7 @@ dr_status dr_guide_train_step(dr_guide *g, const float *pos_dev, const float *di
     if (r != DR_OK) return r;
     ++g->step;
     k_guide_adam<<<(kNumParams + 255) / 256, 256, 0, st>>>(g->params, g->m, g->v, g->grad, g->step, g->cfg.learning_rate,
-                                                           g->cfg.beta1, g->cfg.beta2, g->cfg.epsilon, g->wb);
+                                                           g->cfg.beta1, g->cfg.beta2, g->cfg.epsilon, g->wb, g->img);
     DR_CUDA(cudaGetLastError());
     return DR_OK;
 }

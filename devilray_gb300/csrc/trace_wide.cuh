@@ -40,9 +40,11 @@ constexpr int kWideStack = 64;
 #ifndef DR_NODE_SELECTS
 #define DR_NODE_SELECTS 0
 #endif
-// Hit masks from the per-slot metadata alone (no per-child internal/leaf branch).
+// Hit masks without a per-child internal/leaf branch: 1 = each child ORs its
+// metadata's hit-mask bits; 2 = each child sets its slot bit and the hit leaf
+// slots' metadata is read after the loop (measured: 4.38 -> 4.43 Grays/s).
 #ifndef DR_NODE_META_BITS
-#define DR_NODE_META_BITS 1
+#define DR_NODE_META_BITS 2
 #endif
 // Slab times from byte permutes folded into one FMA per plane (slab_axis).
 #ifndef DR_FAST_SLAB
@@ -117,6 +119,29 @@ __host__ __device__ __forceinline__ float bits_f(uint32_t u)
     return f;
 }
 
+__host__ __device__ __forceinline__ int lowest_bit(uint32_t m)
+{
+#if defined(__CUDA_ARCH__)
+    return __ffs(m) - 1;
+#else
+    return __builtin_ctz(m);
+#endif
+}
+
+__host__ __device__ __forceinline__ int popcount(uint32_t m)
+{
+#if defined(__CUDA_ARCH__)
+    return __popc(m);
+#else
+    return __builtin_popcount(m);
+#endif
+}
+
+__host__ __device__ __forceinline__ uint32_t nonzero_bytes(uint32_t x)
+{
+    return ((x & 0xffu) != 0u) + ((x & 0xff00u) != 0u) + ((x & 0xff0000u) != 0u) + ((x & 0xff000000u) != 0u);
+}
+
 // Slab constants of one axis for the folded evaluation t = fma(byte_q, A, B):
 // with a = grid step * 1/d and b = (node origin - o) * 1/d, the plain slab time
 // of grid plane q is fl(q * a + b). Here A = a / 256 (exact) and
@@ -184,9 +209,15 @@ __host__ __device__ __forceinline__ void wide_node_test(const Bvh8Node *node, co
 #endif
         const float tmin = fmaxf(max3f(tnx, tny, tnz), 0.0f);
         const float tmx = fminf(min3f(tfx, tfy, tfz), tmax) * kBoxFarScale;
+#if DR_NODE_META_BITS == 2
+        // one bit per slot; the metadata is read after the loop
+        if (tmin <= tmx) hit_bits |= 1u << s;
+#else
         const uint32_t meta = ((s < 4 ? w1.z : w1.w) >> (8 * j)) & 0xffu;
         if (meta != 0) ++boxes;
-#if DR_NODE_META_BITS
+#endif
+#if DR_NODE_META_BITS == 2
+#elif DR_NODE_META_BITS
         // the child's bits of the node's hit mask: its triangles (bits 0-23)
         // or, for an internal child, bit 24 + s; an empty slot has none
         if (tmin <= tmx) hit_bits |= (meta >> 5) << (meta & 31u);
@@ -204,9 +235,21 @@ __host__ __device__ __forceinline__ void wide_node_test(const Bvh8Node *node, co
 #endif
     }
 #if DR_NODE_META_BITS
+#if DR_NODE_META_BITS == 2
+    // leaf slots hit: their triangle bits from the metadata; empty slots have
+    // metadata 0 and add nothing
+    for (uint32_t lm = hit_bits & ~imask & 0xffu; lm != 0; lm &= lm - 1u) {
+        const uint32_t sl = (uint32_t)lowest_bit(lm);
+        const uint32_t meta = ((sl < 4 ? w1.z : w1.w) >> (8 * (sl & 3u))) & 0xffu;
+        tri_mask |= (meta >> 5) << (meta & 31u);
+    }
+    boxes = nonzero_bytes(w1.z) + nonzero_bytes(w1.w);  // read by counting builds only
+    uint32_t m = hit_bits & imask;
+#else
     tri_mask = hit_bits & 0x00ffffffu;
-    // internal hits from slot order to traversal order: bit s -> bit s ^ oct
     uint32_t m = hit_bits >> 24;
+#endif
+    // internal hits from slot order to traversal order: bit s -> bit s ^ oct
     if (oct & 1u) m = ((m & 0x55u) << 1) | ((m >> 1) & 0x55u);
     if (oct & 2u) m = ((m & 0x33u) << 2) | ((m >> 2) & 0x33u);
     if (oct & 4u) m = ((m & 0x0fu) << 4) | ((m >> 4) & 0x0fu);
@@ -218,24 +261,6 @@ __host__ __device__ __forceinline__ void wide_node_test(const Bvh8Node *node, co
 __host__ __device__ __forceinline__ uint32_t ray_octant(const DevRay &r)
 {
     return (r.v.x < 0.0f ? 1u : 0u) | (r.v.y < 0.0f ? 2u : 0u) | (r.v.z < 0.0f ? 4u : 0u);
-}
-
-__host__ __device__ __forceinline__ int lowest_bit(uint32_t m)
-{
-#if defined(__CUDA_ARCH__)
-    return __ffs(m) - 1;
-#else
-    return __builtin_ctz(m);
-#endif
-}
-
-__host__ __device__ __forceinline__ int popcount(uint32_t m)
-{
-#if defined(__CUDA_ARCH__)
-    return __popc(m);
-#else
-    return __builtin_popcount(m);
-#endif
 }
 
 // Resumable traversal state of one ray (for the persistent kernels).
