@@ -1180,8 +1180,12 @@ dr_status ensure_train_capacity(dr_guide *g, uint32_t n)
 dr_status run_gradients(dr_guide *g, const float *pos, const float *dir, const float *sdir, const float *weight,
                         uint32_t n, cudaStream_t st)
 {
-    dr_status r = ensure_train_capacity(g, n);
-    if (r != DR_OK) return r;
+    // the per-layer delta and activation buffers serve the mma.sync path only
+    // (the tcgen05 kernel keeps them on chip)
+    if (g->cfg.infer_kernel == DR_GUIDE_INFER_MMA_SYNC) {
+        const dr_status r = ensure_train_capacity(g, n);
+        if (r != DR_OK) return r;
+    }
     DR_CUDA(cudaMemsetAsync(g->grad, 0, kNumParams * sizeof(float), st));
     DR_CUDA(cudaMemsetAsync(g->scalars, 0, 2 * sizeof(float), st));
     k_guide_weight_sum<<<std::min<unsigned>((n + 255) / 256, 64), 256, 0, st>>>(weight, n, g->scalars);
