@@ -340,12 +340,15 @@ def render_section(ctx, native, device: int, stream, cpu: bool, threads: int, la
             times.append(a.elapsed_time(b) / 1e3)
         t = min(times)
         path_rays = int(casts.sum().item())
+        stats = scene.render_stats()
         entry = {"width": cam["width"], "height": cam["height"], "spp": spp, "max_depth": depth,
                  "layout": scene.info().layout,
                  "triangles": int(spec.positions.shape[0]), "objects": len(spec.objects),
                  "scene_build_s": round(build_s, 3), "seconds": t,
                  "samples_per_s": npix * spp / t, "path_mrays_per_s": path_rays / t / 1e6,
-                 "path_rays_per_sample": path_rays / (npix * spp)}
+                 "path_and_shadow_mrays_per_s": (stats.path_rays + stats.shadow_rays) / t / 1e6,
+                 "path_rays_per_sample": path_rays / (npix * spp),
+                 "shadow_rays_per_sample": stats.shadow_rays / (npix * spp)}
         if cpu:
             entry["cpu_baseline"] = render_cpu_baseline(spec, cam, depth, threads,
                                                         pixels=65536 if name == "box_room" else 1024)

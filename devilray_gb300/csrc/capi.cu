@@ -311,6 +311,20 @@ dr_status dr_scene_get_info(const dr_scene *s, dr_scene_info *info)
     return DR_OK;
 }
 
+dr_status dr_scene_get_render_stats(const dr_scene *s, dr_render_stats *stats)
+{
+    DR_CHECK_ARG(s && stats, "dr_scene_get_render_stats: NULL argument");
+    *stats = dr_render_stats{};
+    if (!s->runner || !s->runner->d_totals) return DR_OK;
+    DR_CUDA(cudaSetDevice(s->ctx->device));
+    DR_CUDA(cudaDeviceSynchronize());  // the render's streams do not synchronise with the legacy stream
+    unsigned long long t[2];
+    DR_CUDA(cudaMemcpy(t, s->runner->d_totals, sizeof t, cudaMemcpyDeviceToHost));
+    stats->path_rays = t[0];
+    stats->shadow_rays = t[1];
+    return DR_OK;
+}
+
 dr_status dr_scene_get_light_table(const dr_scene *s, dr_alias_entry *table_host, uint32_t capacity,
                                    uint32_t *count)
 {

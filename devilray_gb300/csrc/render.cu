@@ -36,6 +36,14 @@ namespace {
 constexpr float kPi = 3.14159274f;
 constexpr uint32_t kStreamTag = 0x44526E67u;
 constexpr int kRenderBlock = 128;
+// Resident blocks per SM the plain shading kernel is compiled for (at most 64
+// registers; measured on the box room, 256x256 x 16 spp: 2.99 ms with no bound
+// (138 registers), 2.60-2.64 ms at 8 blocks). The guided one is bound to 4
+// blocks (128 registers).
+#ifndef DR_SHADE_MIN_BLOCKS
+#define DR_SHADE_MIN_BLOCKS 8
+#endif
+constexpr int kShadeMinBlocks = DR_SHADE_MIN_BLOCKS;
 
 struct RenderParams {
     TraceArgs trace;
@@ -61,6 +69,7 @@ struct RenderParams {
     uint32_t *shadow_list;
     uint32_t *counts;          // [0, 64): active paths per bounce, [64, 128): shadow rays per bounce
     unsigned long long *work;  // persistent-kernel counters: [b] closest hit, [64 + b] shadow rays
+    unsigned long long *ray_totals;  // rays of the render: [0] path rays, [1] shadow rays
     // path guiding (guided kernels only)
     float *guide_y;            // [slot][40] network output at the slot's current vertex
     float *guide_pos, *guide_nrm;  // [slot][3] network inputs
@@ -390,7 +399,7 @@ __device__ __forceinline__ float object_ior(const RenderParams &p, int obj)
 }
 
 template <bool GUIDED>
-__global__ void __launch_bounds__(kRenderBlock) k_shade(RenderParams p, int b)
+__global__ void __launch_bounds__(kRenderBlock, GUIDED ? 4 : kShadeMinBlocks) k_shade(RenderParams p, int b)
 {
     const uint32_t count = p.counts[b];
     const uint32_t *list = p.list[b & 1];
@@ -722,6 +731,16 @@ __global__ void __launch_bounds__(256) k_accumulate_wave(RenderParams p)
     }
     J.accum[pix] = acc;
     if (J.pix_casts) J.pix_casts[pix] += casts;
+    if (t == 0) {
+        // the wave's traced rays: paths per bounce and shadow rays per bounce
+        unsigned long long np = 0, ns = 0;
+        for (int b = 0; b < 64; ++b) {
+            np += p.counts[b];
+            ns += p.counts[64 + b];
+        }
+        atomicAdd(p.ray_totals, np);
+        atomicAdd(p.ray_totals + 1, ns);
+    }
 }
 
 template <typename T>
@@ -838,6 +857,7 @@ WaveRunner::~WaveRunner()
     cudaFree(d_jobs);
     cudaFree(d_segs);
     cudaFree(d_train);
+    cudaFree(d_totals);
 }
 
 dr_status WaveRunner::prepare(const std::vector<RenderJob> &jobs, const WavePlan &plan, const WaveConfig &cfg,
@@ -896,6 +916,7 @@ dr_status WaveRunner::prepare(const std::vector<RenderJob> &jobs, const WavePlan
         if (!acc_done[k]) DR_CUDA(cudaEventCreateWithFlags(&acc_done[k], cudaEventDisableTiming));
     }
     if (!fork) DR_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+    if (!d_totals) DR_CUDA(cudaMalloc(&d_totals, 2 * sizeof(unsigned long long)));
     // the tables may still be read by the waves of an earlier call
     for (int k = 0; k < kMaxWaveStreams; ++k)
         if (acc_done[k]) DR_CUDA(cudaStreamWaitEvent(st, acc_done[k], 0));
@@ -930,6 +951,7 @@ dr_status WaveRunner::enqueue(const SceneArrays &sc, const WavePlan &plan, const
     const P8Kernels p8 = select_p8(tri_mode, cfg.stack);
     const int closest_per_sm = resident_blocks((const void *)p8.closest, kTraceBlock);
     const int shadow_per_sm = resident_blocks((const void *)p8.shadow, kTraceBlock);
+    DR_CUDA(cudaMemsetAsync(d_totals, 0, 2 * sizeof(unsigned long long), st));
     DR_CUDA(cudaEventRecord(fork, st));
     for (int k = 0; k < K; ++k) DR_CUDA(cudaStreamWaitEvent(stream[k], fork, 0));
     for (uint32_t w = 0; w < nwaves; ++w) {
@@ -944,6 +966,7 @@ dr_status WaveRunner::enqueue(const SceneArrays &sc, const WavePlan &plan, const
             q.train_head = t_head;
             q.train_cap = train_cap;
         }
+        q.ray_totals = d_totals;
         q.segs = d_segs + plan.wave_first[w];
         q.nsegs = plan.wave_first[w + 1] - plan.wave_first[w];
         q.wave = plan.wave_slots[w];

@@ -108,6 +108,7 @@ struct WaveRunner {
     bool guided = false;              // slot buffers carry the guiding state
     void *d_train = nullptr;          // training ring (guided renders)
     uint32_t train_cap = 0;
+    unsigned long long *d_totals = nullptr;  // rays of the last schedule: path, shadow
 
     ~WaveRunner();
     // Allocates buffers for `plan` and uploads jobs and segments (on `st`).

@@ -85,6 +85,10 @@ class RenderConfig(C.Structure):
                 ("streams", C.c_uint32), ("chunk", C.c_uint32), ("stack", C.c_uint32)]
 
 
+class RenderStats(C.Structure):
+    _fields_ = [("path_rays", C.c_uint64), ("shadow_rays", C.c_uint64)]
+
+
 class Job(C.Structure):
     _fields_ = [("scene", C.c_void_p), ("camera", Camera), ("config", RenderConfig), ("accum_dev", C.c_void_p),
                 ("casts_dev", C.c_void_p)]
@@ -164,6 +168,7 @@ SIGNATURES = {
     "dr_device_copy_to_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64]),
     "dr_device_zero": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p]),
     "dr_scene_get_light_table": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(C.c_uint32)]),
+    "dr_scene_get_render_stats": (C.c_int, [C.c_void_p, C.c_void_p]),
     "dr_framebuffer_create": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
     "dr_framebuffer_destroy": (C.c_int, [C.c_void_p]),
     "dr_framebuffer_clear": (C.c_int, [C.c_void_p, C.c_void_p]),
@@ -362,6 +367,12 @@ class Scene:
         self.handle = C.c_void_p()
         check(load().dr_scene_create(ctx.handle, C.byref(desc), C.byref(cfg), C.byref(self.handle)))
         self._keep = keep
+
+    def render_stats(self) -> RenderStats:
+        """Path and shadow rays of the last render (synchronous)."""
+        st = RenderStats()
+        check(load().dr_scene_get_render_stats(self.handle, C.byref(st)))
+        return st
 
     def info(self) -> SceneInfo:
         info = SceneInfo()

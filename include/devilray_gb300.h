@@ -190,6 +190,16 @@ dr_status dr_scene_get_info(const dr_scene *scene, dr_scene_info *info);
 dr_status dr_scene_get_light_table(const dr_scene *scene, dr_alias_entry *table_host, uint32_t capacity,
                                    uint32_t *count);
 
+typedef struct dr_render_stats {
+    uint64_t path_rays;      /* closest-hit rays of path vertices (the reference's ray_casts) */
+    uint64_t shadow_rays;    /* next-event visibility rays */
+} dr_render_stats;
+/* Ray counts of the scene's last dr_render / dr_render_guided call (zeros
+ * before the first): path rays as Renderer::getTotalCasts counts them
+ * (include/Renderer.hpp:48-69), plus the shadow rays. Synchronous: waits for
+ * the device. */
+dr_status dr_scene_get_render_stats(const dr_scene *scene, dr_render_stats *stats);
+
 /* ---- traversal ------------------------------------------------------------------- */
 
 /* Closest hit for n rays (device buffers). Replaces cast / getIntersection

@@ -47,6 +47,8 @@ def test_render_bit_exact_vs_oracle(native, ctx, oracle, depth, sampling, seed):
     assert mism.size == 0, f"{mism.size} pixels differ, e.g. {mism[:3]}: {acc[mism[:3]]} vs {oacc[mism[:3]]}"
     assert np.array_equal(casts, ocasts)
     assert acc[:, :3].sum() > 0
+    stats = scene.render_stats()
+    assert stats.path_rays == int(casts.sum()) and 0 < stats.shadow_rays <= stats.path_rays
 
 
 def test_progressive_and_waves_equal_single_call(native, ctx):
@@ -90,6 +92,8 @@ def test_scene_without_lights_renders_emission_only(native, ctx):
     acc, casts, scene = gpu_render(native, ctx, spec, cam, 4)
     assert scene.info().total_radiant_power == 0.0
     assert (acc[:, :3] == 0).all() and (acc[:, 3] == 4).all() and (casts > 0).all()
+    stats = scene.render_stats()
+    assert stats.path_rays == int(casts.sum()) and stats.shadow_rays == 0
 
 
 @pytest.mark.parametrize("mode", ["small", "wave"])
