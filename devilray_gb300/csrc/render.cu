@@ -37,9 +37,10 @@ constexpr float kPi = 3.14159274f;
 constexpr uint32_t kStreamTag = 0x44526E67u;
 constexpr int kRenderBlock = 128;
 // Resident blocks per SM the plain shading kernel is compiled for (at most 64
-// registers; measured on the box room, 256x256 x 16 spp: 2.99 ms with no bound
-// (138 registers), 2.60-2.64 ms at 8 blocks). The guided one is bound to 4
-// blocks (128 registers).
+// registers). Measured on the box room, 256x256 x 16 spp: a minimum of 1 block
+// (138 registers) 2.99 ms, the compiler's choice without a minimum (80
+// registers, 6 blocks) about 2.69 ms, 8 blocks 2.60-2.64 ms. The guided one is
+// bound to 4 blocks (at most 128 registers).
 #ifndef DR_SHADE_MIN_BLOCKS
 #define DR_SHADE_MIN_BLOCKS 8
 #endif
