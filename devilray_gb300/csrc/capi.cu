@@ -465,9 +465,10 @@ dr_status dr_trace_closest_host(dr_scene *s, const dr_ray *rays_host, uint64_t n
     // Pipeline in chunks: the copy-in of chunk k+1 and the copy-out of chunk
     // k-1 overlap the traversal of chunk k. Chunks alternate between two
     // compute streams, so the tail of one persistent launch overlaps the start
-    // of the next (each launch has its own work counter). Measured with one
-    // compute stream (16.8 M rays, 2^20 triangles): 4 chunks 5.11 ms,
-    // 8 chunks 5.21 ms, 16 chunks 5.87 ms.
+    // of the next (each launch has its own work counter). Measured (16.8 M
+    // rays, 2^20 triangles): one compute stream 5.11 / 5.21 / 5.87 ms for 4 /
+    // 8 / 16 chunks; two streams 4.76 / 4.52 / 4.55 / 4.63 / 4.89 ms for
+    // 4 / 8 / 12 / 16 / 24 chunks.
     auto *d_rays = static_cast<dr_ray *>(s->d_stage_rays);
     auto *d_hits = static_cast<dr_hit *>(s->d_stage_hits);
     const uint64_t chunk = std::max<uint64_t>(1u << 18, (n + 7) / 8);
