@@ -207,17 +207,18 @@ def camera(width: int, height: int, focal: float = 1.0, fov_half_width: float = 
             "cy": np.float32(height / 2.0) * ps, "width": int(width), "height": int(height), "psx": ps, "psy": ps}
 
 
-def box_room(sphere_level: int = 3) -> SceneSpec:
+def box_room(sphere_level: int = 3, glass_sphere: bool = True) -> SceneSpec:
     """The box room of the plain-method configuration: five axis-aligned
     quads (albedo 0.75, red/green side walls 0.6), a ceiling light quad
     (radiance 15) and a dielectric icosphere (IOR 1.5) in the middle; laid out
-    like the reference's interactive scene (renderer/src/SceneSetup.cpp:120-131)."""
+    like the reference's interactive scene (renderer/src/SceneSetup.cpp:120-131).
+    With glass_sphere=False the sphere is diffuse (albedo 0.75)."""
     s = SceneSpec()
     white = s.add_material(material(0, albedo=(0.75, 0.75, 0.75)))
     red = s.add_material(material(0, albedo=(0.6, 0.1, 0.1)))
     green = s.add_material(material(0, albedo=(0.1, 0.6, 0.1)))
     light = s.add_material(material(0, emission=(15.0, 15.0, 15.0)))
-    glass = s.add_material(material(1, ior=1.5))
+    glass = s.add_material(material(1, ior=1.5)) if glass_sphere else white
     s.add_object(quad((0, 0, 2.5), (0, 0, -1), (1, 0, 0), 1.0), white)
     s.add_object(quad((0.5, 0, 2), (-1, 0, 0), (0, 1, 0), 1.0), red)
     s.add_object(quad((-0.5, 0, 2), (1, 0, 0), (0, 1, 0), 1.0), green)
