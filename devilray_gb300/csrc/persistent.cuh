@@ -45,22 +45,26 @@ constexpr int kP8MinBlocks = DR_P8_MIN_BLOCKS;
 #endif
 // Which traversals send their leaf triangles through the warp's staged
 // triangle batch (tri_batch.cuh) instead of each lane's own loop: the public
-// closest-hit kernel, the renderer's path rays, the any-hit kernels (public
-// and shadow rays). Measured (incoherent workload: 2^20 triangles, 16.8 M
-// rays, 23 % hits; many-light 1080p render, 16 spp): closest hit 3.81 ->
-// 4.37 Grays/s with the batch; any hit 3.48 -> 3.45 ms; the render 53.0 ->
-// 55.9 ms with the path rays batched and 57.9 ms with the shadow rays too.
-// Path rays nearly all hit, and a batch delays the shrinking of their
-// closest-hit bound, so more boxes pass; the rays of the public kernel mostly
-// miss, so the batch only saves issue slots.
+// closest-hit and any-hit kernels, the renderer's path rays and shadow rays.
+// Measured (incoherent workload: 2^20 triangles, 16.8 M rays, 23 % hits;
+// many-light 1080p and box-room renders, 16 spp): closest hit 3.81 -> 4.37
+// Grays/s and any hit 3.43 -> 3.35 ms with the batch; the renders 51.9 ->
+// 53.4 ms and 2.50 -> 2.90 ms with the path rays batched, 53.0 and 2.87 ms
+// with the shadow rays batched. Path and shadow rays of a closed scene nearly
+// all hit, and the batch delays the early exits and the shrinking closest-hit
+// bound that then prune the traversal; the public rays mostly miss, so the
+// batch only saves issue slots.
 #ifndef DR_TRI_BATCH_CLOSEST
 #define DR_TRI_BATCH_CLOSEST 1
+#endif
+#ifndef DR_TRI_BATCH_ANY
+#define DR_TRI_BATCH_ANY 1
 #endif
 #ifndef DR_TRI_BATCH_PATHS
 #define DR_TRI_BATCH_PATHS 0
 #endif
-#ifndef DR_TRI_BATCH_ANY
-#define DR_TRI_BATCH_ANY 0
+#ifndef DR_TRI_BATCH_SHADOW
+#define DR_TRI_BATCH_SHADOW 0
 #endif
 // The batch is tested once it holds this many pairs, or once this many lanes
 // wait for its results (their rays have no node left). Measured: 16 -> 4.38,

@@ -348,7 +348,7 @@ __global__ void __launch_bounds__(kTraceBlock, kP8MinBlocks) k_wave_shadow_p8(Re
     const Wide8Args w{p.trace.nodes8, p.trace.tri_ref, p.trace.tri_wt, p.trace.prim, p.trace.num_nodes, p.trace.error};
     const ShadowSource src{p.shadow_list, p.shadow_rays, p.color, p.pending, p.slot_job, p.jobs};
     unsigned long long nn = 0, nb = 0, nt = 0, nh = 0;
-    persistent_wide<MODE, true, false, DR_TRI_BATCH_ANY != 0, STACK>(w, src, p.counts[64 + b], p.work + 64 + b, nn,
+    persistent_wide<MODE, true, false, DR_TRI_BATCH_SHADOW != 0, STACK>(w, src, p.counts[64 + b], p.work + 64 + b, nn,
                                                                       nb, nt, nh, p.chunk);
 }
 
