@@ -171,6 +171,7 @@ def test_edge_cases(native, ctx, oracle, layout):
     assert np.array_equal(_bits(t), _bits(tb)) and np.array_equal(prim, pb)
     assert prim[0] == 2 and prim[1] == 4 and prim[5] == -1 and prim[6] == -1 and prim[7] == -1
     assert np.isinf(t[5]) and prim[8] == -1
+    assert np.array_equal(gpu_any(native, scene, r8).astype(bool), pb >= 0)
     # tmax: a hit at exactly t == tmax counts; below it does not
     r8b = r8[:1].copy()
     r8b[0, 3] = np.float32(5.0)
