@@ -989,7 +989,12 @@ dr_status WaveRunner::enqueue(const SceneArrays &sc, const WavePlan &plan, const
                 if (wt) k_wave_closest<1, 2><<<trace_grid, kTraceBlock, 0, ws>>>(q, b);
                 else k_wave_closest<0, 2><<<trace_grid, kTraceBlock, 0, ws>>>(q, b);
             }
-            if (gr) {
+            // the guided shading kernel serves the guided bounces and the one
+            // after them (its emission weights use the mixture density of the
+            // last guided direction, and it closes that vertex's training
+            // record); later bounces sample the cosine lobe only, as the plain
+            // kernel does
+            if (gr && b <= (int)gr->bounces) {
                 if (b < (int)gr->bounces) {
                     k_guide_prepare<<<shade_grid, kRenderBlock, 0, ws>>>(q, b);
                     DR_CUDA(launch_guide_infer(gr->guide, q.guide_pos, q.guide_nrm, q.guide_list, q.guide_counts + b,
