@@ -33,9 +33,10 @@ constexpr int kP8MinBlocks = DR_P8_MIN_BLOCKS;
 
 // A warp refills its idle lanes once at least this many are idle (or all are):
 // fewer, fuller refills (measured on the incoherent workload: 1 -> 3.68,
-// 4 -> 3.78, 8 -> 3.78, 16 -> 3.54 Grays/s).
+// 4 -> 3.78, 8 -> 3.78, 16 -> 3.54 Grays/s with one node test per loop
+// iteration; with up to 4: 2 -> 4.88, 4 -> 4.89, 8 -> 4.86, 16 -> 4.41).
 #ifndef DR_REFILL_MIN
-#define DR_REFILL_MIN 8
+#define DR_REFILL_MIN 4
 #endif
 // A lane postpones its leaf triangles while fewer than this many lanes of its
 // warp have triangles to test (0: never). Measured on the incoherent workload
@@ -78,7 +79,7 @@ constexpr int kP8MinBlocks = DR_P8_MIN_BLOCKS;
 #endif
 // Node tests per loop iteration: after its node test, a lane that found no
 // leaf triangles goes on to its next node at once, up to this many nodes,
-// while at least DR_INNER_MIN_LANES lanes of the warp can do so; the warp's
+// while at least DR_INNER_MIN_LANES_* lanes of the warp can do so; the warp's
 // triangle, batch and refill steps then run once for all of them (the
 // "while-while" loop of Aila and Laine 2009). Separate counts for the
 // traversals with warp triangle batches and for those with per-lane loops.
@@ -87,7 +88,9 @@ constexpr int kP8MinBlocks = DR_P8_MIN_BLOCKS;
 //   batch steps 1 / 2 / 3 / 4 / 6 / 8: 4.43 / 4.78 / 4.83 / 4.86 / 4.72 /
 //   4.70 Grays/s closest hit, 3.36 / 3.08 / 3.05 / 2.99 / 3.08 / 3.10 ms any
 //   hit; 8 steps with at least 24 lanes 4.86, 28 lanes 4.65 Grays/s;
-//   per-lane steps 1 / 2 / 3 / 4: render 52.2 / 50.0 / 50.1 / 49.4 ms.
+//   per-lane steps 1 / 2 / 3 / 4: render 52.2 / 50.0 / 50.1 / 49.4 ms;
+//   4 batch steps with at least 12 / 16 / 20 / 24 lanes: 4.84 / 4.86 / 4.89 /
+//   4.86 Grays/s; 4 per-lane steps with 24 lanes: render 50.8 ms.
 // Results do not depend on it.
 #ifndef DR_INNER_STEPS_BATCH
 #define DR_INNER_STEPS_BATCH 4
@@ -95,8 +98,11 @@ constexpr int kP8MinBlocks = DR_P8_MIN_BLOCKS;
 #ifndef DR_INNER_STEPS_LANE
 #define DR_INNER_STEPS_LANE 4
 #endif
-#ifndef DR_INNER_MIN_LANES
-#define DR_INNER_MIN_LANES 16
+#ifndef DR_INNER_MIN_LANES_BATCH
+#define DR_INNER_MIN_LANES_BATCH 20
+#endif
+#ifndef DR_INNER_MIN_LANES_LANE
+#define DR_INNER_MIN_LANES_LANE 16
 #endif
 
 
@@ -214,7 +220,7 @@ __device__ __forceinline__ void persistent_wide(const Wide8Args &a, const Source
 #pragma unroll 1
             for (int k = 1; k < DR_INNER_STEPS_BATCH; ++k) {
                 const bool go = active && !waiting && !fin && s.tmask == 0;
-                if (__popc(__ballot_sync(FULL, go)) < DR_INNER_MIN_LANES) break;
+                if (__popc(__ballot_sync(FULL, go)) < DR_INNER_MIN_LANES_BATCH) break;
                 if (go) {
                     fin = wide_advance<ANY>(a, s, stack);
                     if (!fin && s.have_node) wide_visit<MODE>(a, s, cn, cb);
@@ -270,7 +276,7 @@ __device__ __forceinline__ void persistent_wide(const Wide8Args &a, const Source
 #pragma unroll 1
             for (int k = 1; k < DR_INNER_STEPS_LANE; ++k) {
                 const bool go = active && !fin && s.tmask == 0;
-                if (__popc(__ballot_sync(FULL, go)) < DR_INNER_MIN_LANES) break;
+                if (__popc(__ballot_sync(FULL, go)) < DR_INNER_MIN_LANES_LANE) break;
                 if (go) {
                     fin = wide_advance<ANY>(a, s, stack);
                     if (!fin && s.have_node) wide_visit<MODE>(a, s, cn, cb);
