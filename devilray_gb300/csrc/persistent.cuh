@@ -90,7 +90,9 @@ constexpr int kP8MinBlocks = DR_P8_MIN_BLOCKS;
 //   hit; 8 steps with at least 24 lanes 4.86, 28 lanes 4.65 Grays/s;
 //   per-lane steps 1 / 2 / 3 / 4: render 52.2 / 50.0 / 50.1 / 49.4 ms;
 //   4 batch steps with at least 12 / 16 / 20 / 24 lanes: 4.84 / 4.86 / 4.89 /
-//   4.86 Grays/s; 4 per-lane steps with 24 lanes: render 50.8 ms.
+//   4.86 Grays/s; 4 per-lane steps with 24 lanes: render 50.8 ms. Letting
+//   lanes with leaf triangles push them as a postponed group and go on in
+//   the extra node tests: 4.96 -> 4.63 Grays/s.
 // Results do not depend on it.
 #ifndef DR_INNER_STEPS_BATCH
 #define DR_INNER_STEPS_BATCH 4
@@ -104,6 +106,7 @@ constexpr int kP8MinBlocks = DR_P8_MIN_BLOCKS;
 #ifndef DR_INNER_MIN_LANES_LANE
 #define DR_INNER_MIN_LANES_LANE 16
 #endif
+
 
 
 // Indices a warp reserves at once: 128 when there is plenty of work, down to
