@@ -115,10 +115,14 @@ def batch_small() -> None:
 
 
 def guided(spp: int = 32) -> None:
+    """Plain and guided renders of the single-gap occluded-light scene at
+    480x270 with the benchmark's guided schedule: alpha 0.75, the first 3
+    bounces guided, 16 Adam steps of 65,536 samples after every 16-spp wave
+    (at most 512 steps), a fresh network."""
     import torch
     from devilray_gb300 import scenes
     native, ctx = _ctx()
-    spec = scenes.occluded_light()
+    spec = scenes.occluded_light(slab_gap=0.15)
     scene = native.Scene.from_spec(ctx, spec)
     cam = scenes.lower_camera(480, 270)
     n = 480 * 270
@@ -137,8 +141,9 @@ def guided(spp: int = 32) -> None:
         return time.perf_counter() - t
 
     tp = timed(lambda: scene.render(cam, acc, spp=spp, max_depth=16, seed=1, wave_paths=16 * n))
-    tg = timed(lambda: scene.render_guided(g, cam, acc, spp=spp, max_depth=16, seed=2, train=True, train_steps=16,
-                                           bounces=2, wave_paths=16 * n))
+    tg = timed(lambda: scene.render_guided(g, cam, acc, spp=spp, max_depth=16, seed=2, alpha=0.75, train=True,
+                                           train_batch=65536, train_steps=16, train_budget=512, bounces=3,
+                                           wave_paths=16 * n))
     print(f"guided: plain {tp:.3f} s, guided with training {tg:.3f} s for {spp} spp at 480x270")
     ctx.check()
 
