@@ -181,6 +181,31 @@ def test_edge_cases(native, ctx, oracle, layout):
 
 
 @pytest.mark.parametrize("layout", [2, 8])
+def test_coincident_and_zero_area_triangles_match_brute_force(native, ctx, oracle, layout):
+    """Thousands of copies of one triangle (zero-extent splits, equal costs in
+    the wide collapse), zero-area triangles and a few ordinary ones: the
+    smallest index among the coincident copies must win."""
+    rng = np.random.default_rng(11)
+    tri = np.array([[0, 0, 0, 1, 0, 0, 0, 1, 0]], np.float32)
+    copies = np.repeat(tri, 3000, axis=0)
+    points = np.repeat(np.float32([[0.25, 0.25, 0.5] * 3]), 500, axis=0)
+    centres = rng.uniform(-3, 3, size=(200, 1, 3))
+    centres[:, 0, 2] = rng.uniform(-3, -0.5, 200)  # below the copies
+    others = (centres + rng.uniform(-0.3, 0.3, size=(200, 3, 3))).reshape(200, 9).astype(np.float32)
+    soup = np.concatenate([others[:100], copies, points, others[100:]])
+    o = np.column_stack([rng.uniform(0, 0.5, 4000), rng.uniform(0, 0.5, 4000), np.full(4000, 2.0)])
+    dvec = np.column_stack([rng.normal(0, 0.05, 4000), rng.normal(0, 0.05, 4000), -np.ones(4000)])
+    r6 = np.concatenate([np.column_stack([o, dvec]), rng.uniform(-3, 3, size=(4000, 6))]).astype(np.float32)
+    r8 = rays8_from6(r6)
+    scene = native.Scene(ctx, soup, layout=layout)
+    t, prim, _ = gpu_closest(native, scene, r8)
+    tb, pb = oracle.trace_brute(soup, r8)
+    assert np.array_equal(_bits(t), _bits(tb)) and np.array_equal(prim, pb)
+    assert (prim[:4000] == 100).sum() > 3000  # the first copy
+    assert np.array_equal(gpu_any(native, scene, r8).astype(bool), pb >= 0)
+
+
+@pytest.mark.parametrize("layout", [2, 8])
 def test_empty_and_single_triangle_scenes(native, ctx, layout):
     rays = scenes.incoherent_rays(1000, seed=3)
     empty = native.Scene(ctx, np.zeros((0, 9), np.float32), layout=layout)
