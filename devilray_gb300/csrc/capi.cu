@@ -468,10 +468,29 @@ dr_status dr_trace_closest_host(dr_scene *s, const dr_ray *rays_host, uint64_t n
     // of the next (each launch has its own work counter). Measured (16.8 M
     // rays, 2^20 triangles): one compute stream 5.11 / 5.21 / 5.87 ms for 4 /
     // 8 / 16 chunks; two streams 4.76 / 4.52 / 4.55 / 4.63 / 4.89 ms for
-    // 4 / 8 / 12 / 16 / 24 chunks.
+    // 4 / 8 / 12 / 16 / 24 chunks. With the faster traversal: 8 equal chunks
+    // 4.13 ms; a first chunk of 1/32 and a second of 1/16 of the rays (the
+    // traversal starts sooner) 4.01 ms; short chunks at the end as well
+    // 4.07 ms. Reading the rays and writing the hits in place in mapped
+    // page-locked memory, in one launch: 4.82 ms.
     auto *d_rays = static_cast<dr_ray *>(s->d_stage_rays);
     auto *d_hits = static_cast<dr_hit *>(s->d_stage_hits);
-    const uint64_t chunk = std::max<uint64_t>(1u << 18, (n + 7) / 8);
+    // chunk boundaries, in 32nds of the rays: short first chunks so the
+    // traversal starts sooner (chunks under 2^18 rays join the next)
+    std::vector<uint64_t> bounds{0};
+    {
+        static const int parts[] = {1, 2, 4, 4, 4, 5, 4, 4, 4, 0};
+        int total = 0;
+        for (int i = 0; parts[i]; ++i) total += parts[i];
+        uint64_t acc = 0;
+        for (int i = 0; parts[i]; ++i) {
+            acc += (uint64_t)parts[i];
+            uint64_t e = n * acc / (uint64_t)total;
+            if (e - bounds.back() < (1u << 18) && parts[i + 1]) continue;  // too small: merge into the next
+            bounds.push_back(e);
+        }
+        if (bounds.back() != n) bounds.push_back(n);
+    }
     for (cudaStream_t &h : s->stage_streams)
         if (!h) DR_CUDA(cudaStreamCreateWithFlags(&h, cudaStreamNonBlocking));
     cudaStream_t copy_in = s->stage_streams[0], copy_out = s->stage_streams[1];
@@ -489,9 +508,9 @@ dr_status dr_trace_closest_host(dr_scene *s, const dr_ray *rays_host, uint64_t n
     if (err == cudaSuccess) err = cudaStreamWaitEvent(copy_in, start, 0);
     if (err == cudaSuccess) err = cudaStreamWaitEvent(copy_out, start, 0);
     if (err == cudaSuccess) err = cudaStreamWaitEvent(compute[1], start, 0);
-    uint64_t k = 0;
-    for (uint64_t b = 0; b < n && err == cudaSuccess; b += chunk, ++k) {
-        const uint64_t m = std::min(chunk, n - b);
+    for (size_t k = 0; k + 1 < bounds.size() && err == cudaSuccess; ++k) {
+        const uint64_t b = bounds[k], m = bounds[k + 1] - bounds[k];
+        if (m == 0) continue;
         const cudaStream_t cs = compute[k & 1];
         err = cudaMemcpyAsync(d_rays + b, rays_host + b, m * sizeof(dr_ray), cudaMemcpyHostToDevice, copy_in);
         cudaEvent_t in_done = new_event();
