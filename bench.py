@@ -308,9 +308,11 @@ def run_ours(args):
 
 def render_section(ctx, native, device: int, stream, cpu: bool, threads: int, layout: int = 0):
     """1080p samples/s on the many-light configuration (1920x1080, 64 spp,
-    depth 16, 65,536 emitters) and the box room (256x256, 16 spp, depth 8);
-    each with the reference's CPU integrator (oracle port: per-object cast,
-    reference random-number order) timed on a pixel subset."""
+    depth 16, 65,536 emitters) and the box room (256x256, 16 spp, depth 8),
+    rendered with the schedule dr_autotune picks (the default schedule's time
+    is reported beside it); each with the reference's CPU integrator (oracle
+    port: per-object cast, reference random-number order) timed on a pixel
+    subset."""
     import torch
     from devilray_gb300 import scenes
     out = {}
@@ -325,24 +327,43 @@ def render_section(ctx, native, device: int, stream, cpu: bool, threads: int, la
         npix = cam["width"] * cam["height"]
         accum = torch.zeros((npix, 4), dtype=torch.float32, device=f"cuda:{device}")
         casts = torch.zeros(npix, dtype=torch.int32, device=f"cuda:{device}")
-        scene.render(cam, accum, casts, spp=1, max_depth=depth, stream=stream)  # warm-up
-        stream.synchronize()
-        times = []
-        for r in range(reps):
-            accum.zero_()
-            casts.zero_()
-            torch.cuda.synchronize()
-            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            a.record(stream)
-            scene.render(cam, accum, casts, spp=spp, max_depth=depth, stream=stream)
-            b.record(stream)
+        # the autotuner's schedule (dr_autotune: probe renders, untimed); the
+        # images do not depend on it
+        t0 = time.perf_counter()
+        # probes of the full sample count where that is cheap (a probe with
+        # fewer samples runs smaller waves and can favour another layout)
+        probe = spp if npix * spp <= (1 << 22) else min(spp, 4)
+        tune = native.autotune(ctx, spec, cam, spp=spp, max_depth=depth, probe_spp=probe, reps=2,
+                               try_layouts=layout == 0)
+        tune_s = time.perf_counter() - t0
+        tuned = scene
+        if layout == 0 and tune.layout != scene.info().layout:
+            tuned = native.Scene.from_spec(ctx, spec, layout=tune.layout)
+        sched = dict(wave_paths=tune.wave_paths, streams=tune.streams, chunk=tune.chunk, stack=tune.stack)
+
+        def timed(sc, kw):
+            sc.render(cam, accum, casts, spp=1, max_depth=depth, stream=stream, **kw)  # warm-up
             stream.synchronize()
-            times.append(a.elapsed_time(b) / 1e3)
-        t = min(times)
+            times = []
+            for r in range(reps):
+                accum.zero_()
+                casts.zero_()
+                torch.cuda.synchronize()
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                sc.render(cam, accum, casts, spp=spp, max_depth=depth, stream=stream, **kw)
+                b.record(stream)
+                stream.synchronize()
+                times.append(a.elapsed_time(b) / 1e3)
+            return min(times)
+
+        t_default = timed(scene, {})
+        t = timed(tuned, sched)
         path_rays = int(casts.sum().item())
-        stats = scene.render_stats()
+        stats = tuned.render_stats()
         entry = {"width": cam["width"], "height": cam["height"], "spp": spp, "max_depth": depth,
-                 "layout": scene.info().layout,
+                 "layout": tuned.info().layout, "schedule": sched, "autotune_s": round(tune_s, 3),
+                 "default_schedule_seconds": t_default,
                  "triangles": int(spec.positions.shape[0]), "objects": len(spec.objects),
                  "scene_build_s": round(build_s, 3), "seconds": t,
                  "samples_per_s": npix * spp / t, "path_mrays_per_s": path_rays / t / 1e6,
@@ -353,7 +374,7 @@ def render_section(ctx, native, device: int, stream, cpu: bool, threads: int, la
             entry["cpu_baseline"] = render_cpu_baseline(spec, cam, depth, threads,
                                                         pixels=65536 if name == "box_room" else 1024)
         out[name] = entry
-        del scene, accum, casts
+        del scene, tuned, accum, casts
     torch.cuda.empty_cache()
     return out
 

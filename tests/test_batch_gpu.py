@@ -149,7 +149,10 @@ def test_autotune_picks_a_measured_schedule(native, ctx):
     assert res.wave_paths in (1 << 19, 1 << 20, 1 << 21, 1 << 22, 1 << 23)
     assert len(d["candidates"]) >= 6 and res.best_ms > 0
     assert {c["layout"] for c in d["candidates"]} == {2, 8}
-    assert res.best_ms == min(c["ms"] for c in d["candidates"])
+    # the chosen schedule is a measured one, and no candidate beat it by more
+    # than the 2 % a switch requires
+    times = [c["ms"] for c in d["candidates"]]
+    assert res.best_ms in times and min(times) >= 0.98 * res.best_ms * (1 - 1e-6)
     # the chosen schedule renders the same image as the defaults
     scene = native.Scene.from_spec(ctx, spec, layout=res.layout)
     a, ca = _alone(native, scene, cam, 4, 8, 0, 1)
