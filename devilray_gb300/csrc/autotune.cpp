@@ -2,7 +2,7 @@
 // (paths per wave, concurrent waves, traversal fetch size, shared-memory
 // stack depth) by timing short probe renders on the device.
 //
-// The search is coordinate descent from the defaults (8-wide, 2^21 paths per
+// The search is coordinate descent from the defaults (8-wide, 2^22 paths per
 // wave, 3 streams, adaptive fetch, 8 stack entries): each knob in turn is set
 // to the fastest of its candidates with the others fixed, where a candidate
 // must beat the incumbent by more than 2 %. Every candidate renders the same
@@ -138,7 +138,7 @@ dr_status dr_autotune(dr_context *ctx, const dr_scene_desc *desc, const dr_camer
     dr_status st = dr_device_allocate(ctx, npix * 16, &accum);
     if (st != DR_OK) return st;
 
-    Knobs best{8, 1u << 21, 3, 0, 8};
+    Knobs best{8, 1u << 22, 3, 0, 8};
     float best_ms = 1e30f;
     dr_scene *scenes[2] = {nullptr, nullptr};
     auto measure_on = [&](dr_scene *s, const Knobs &k, float &ms) -> dr_status {
@@ -207,7 +207,7 @@ dr_status dr_autotune_batch(dr_context *ctx, const dr_job *jobs, uint32_t njobs,
         probe[j].casts_dev = nullptr;
         probe[j].config.spp = probe_spp;
     }
-    Knobs best{jobs[0].scene->layout, 1u << 21, 3, 0, 8};
+    Knobs best{jobs[0].scene->layout, 1u << 22, 3, 0, 8};
     float best_ms = 1e30f;
     auto measure = [&](const Knobs &k, float &ms) -> dr_status {
         dr_batch_config bc{k.wave_paths, k.streams, k.chunk, 0, k.stack};

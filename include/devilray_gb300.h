@@ -250,7 +250,7 @@ typedef struct dr_render_config {
     int32_t pixel_sampling;  /* dr_pixel_sampling */
     uint64_t seed;           /* Philox key */
     int32_t tri_mode;        /* dr_tri_mode */
-    uint32_t wave_paths;     /* paths in flight per wave, 0 = automatic (2^21) */
+    uint32_t wave_paths;     /* paths in flight per wave, 0 = automatic (2^22) */
     uint32_t flags;          /* reserved, 0 */
     int32_t debug;           /* dr_debug_view */
     uint32_t streams;        /* concurrent waves, 1..3, 0 = 3 */
@@ -311,7 +311,7 @@ typedef struct dr_job {
 } dr_job;
 
 typedef struct dr_batch_config {
-    uint32_t wave_paths;     /* path slots per wave, 0 = 2^21 (at least one sample of the largest image) */
+    uint32_t wave_paths;     /* path slots per wave, 0 = 2^22 (at least one sample of the largest image) */
     uint32_t streams;        /* concurrent waves, 1..3, 0 = 3 */
     uint32_t chunk;          /* persistent traversal fetch (32..128, multiple of 32), 0 = adaptive */
     uint32_t use_graph;      /* 1: capture the schedule into a CUDA graph on the first render */
