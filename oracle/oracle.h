@@ -1,7 +1,7 @@
 /*
  * oracle.h -- CPU restatement of DevilRay's tracing path (TEST INFRASTRUCTURE).
  *
- * This library is the checker for the GB300 kernels. Only the test suite,
+ * This library is the oracle the GB300 kernels are compared against. Only the test suite,
  * the smoke check and the CPU-baseline leg of the benchmark load it; the
  * product library never links or calls it.
  *

@@ -1,6 +1,6 @@
 // oracle_alias.cpp -- CPU restatement of DevilRay's alias-table build and
 // sampling, plus the CPU restatement of the device's sweep-pairing build
-// (TEST INFRASTRUCTURE: the checker for the GB300 kernels).
+// (TEST INFRASTRUCTURE: the oracle of the GB300 kernels).
 
 #include "oracle.h"
 

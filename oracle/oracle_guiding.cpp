@@ -1,5 +1,5 @@
 // oracle_guiding.cpp -- FP64 restatement of the path-guiding network (TEST
-// INFRASTRUCTURE: the checker for the GB300 guiding kernels; never linked into
+// INFRASTRUCTURE: the oracle of the GB300 guiding kernels; never linked into
 // the product).
 //
 // The guiding distribution is not part of the reference (DevilRay has no

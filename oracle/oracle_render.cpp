@@ -1,5 +1,5 @@
 // oracle_render.cpp -- CPU restatement of DevilRay's integrator (TEST
-// INFRASTRUCTURE: the checker for the GB300 renderer; never linked into the
+// INFRASTRUCTURE: the oracle of the GB300 renderer; never linked into the
 // product).
 //
 // Restates sampleColor (include/tracing/PathGeneration.hpp:363-515) with the
@@ -324,7 +324,7 @@ void or_render(const or_scene *s, const or_camera *cam, const or_render_cfg *cfg
 
                 if (cfg->debug != 0) {
                     // first-hit debug views (PathGeneration.hpp:274-299, 393-429);
-                    // the reference's hit uv is (0, 0), so the checker is its dark colour
+                    // the reference's hit uv is (0, 0), so the UV checkerboard gives its dark colour
                     const Hit hit = castRay(*s, cfg->cast_mode, rp, rv);
                     pixel_casts += 1;
                     V4 color{0, 0, 0, 0};

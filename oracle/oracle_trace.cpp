@@ -1,6 +1,6 @@
 // oracle_trace.cpp -- CPU restatement of DevilRay's ray/triangle test, its
-// median-split BBH and its traversal (TEST INFRASTRUCTURE: the checker for the
-// GB300 kernels; never linked into the product).
+// median-split BBH and its traversal (TEST INFRASTRUCTURE: the oracle the GB300
+// kernels are compared against; never linked into the product).
 //
 // Compiled with -O2 -ffp-contract=off and no fast-math, so every FP32
 // expression below rounds exactly like the reference compiled the same way.
