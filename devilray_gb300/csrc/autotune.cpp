@@ -61,7 +61,7 @@ dr_status time_probe(Probe &p, uint32_t reps, F &&run, float &ms)
     return DR_OK;
 }
 
-const uint32_t kWaveCandidates[] = {1u << 19, 1u << 20, 1u << 21, 1u << 22, 1u << 23};
+const uint32_t kWaveCandidates[] = {1u << 19, 1u << 20, 1u << 21, 1u << 22, 1u << 23, 1u << 24};
 const uint32_t kStreamCandidates[] = {1, 2, 3};
 const uint32_t kChunkCandidates[] = {0, 32, 64, 128};
 const uint32_t kStackCandidates[] = {8, 4, 16};
@@ -89,7 +89,7 @@ dr_status descend(Knobs &best, float &best_ms, Measure &&measure)
                                : knob == 1 ? kStreamCandidates
                                : knob == 2 ? kChunkCandidates
                                            : kStackCandidates;
-        const int n = knob == 0 ? 5 : knob == 1 ? 3 : knob == 2 ? 4 : 3;
+        const int n = knob == 0 ? 6 : knob == 1 ? 3 : knob == 2 ? 4 : 3;
         if (knob >= 2 && best.layout != 8) break;  // fetch size and stack belong to the persistent 8-wide kernels
         Knobs winner = best;
         for (int i = 0; i < n; ++i) {
