@@ -36,7 +36,7 @@ NUM_TRIS = 1 << 20
 NUM_RAYS = 1 << 24
 # DRAM bytes of one full 16.8 M-ray launch of the dominant kernel, from one
 # `ncu --set full` capture of this workload (the profiles named beside them).
-NCU_TRAFFIC = {8: 936_858_880 + 130_535_936, 2: 1_652_000_000 + 152_000_000}
+NCU_TRAFFIC = {8: 931_329_536 + 130_428_416, 2: 1_652_000_000 + 152_000_000}
 NCU_PROFILE = {8: "trace_closest_p8_incoherent_1M_tris_16M_rays.md",
                2: "trace_closest_bvh2_incoherent_1M_tris_16M_rays.md"}
 METRIC = "Mrays/s closest-hit"

@@ -70,9 +70,11 @@ constexpr int kP8MinBlocks = DR_P8_MIN_BLOCKS;
 #endif
 // The batch is tested once it holds this many pairs, or once this many lanes
 // wait for its results (their rays have no node left). Measured: 16 -> 4.38,
-// 24 -> 4.37, 32 -> 4.24 Grays/s; 3, 6 or 10 waiting lanes all 4.37.
+// 24 -> 4.37, 32 -> 4.24 Grays/s; 3, 6 or 10 waiting lanes all 4.37. With up
+// to 4 node tests per iteration and the collapsed tree: 12 / 16 / 24 pairs ->
+// 4.963 / 4.956 / 4.838 Grays/s closest hit, 2.92 / 2.95 / 3.04 ms any hit.
 #ifndef DR_TRI_BATCH_FLUSH
-#define DR_TRI_BATCH_FLUSH 16
+#define DR_TRI_BATCH_FLUSH 12
 #endif
 #ifndef DR_TRI_BATCH_WAITERS
 #define DR_TRI_BATCH_WAITERS 6
