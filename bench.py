@@ -170,6 +170,21 @@ def run_reference(args):
     return 0
 
 
+def max_over_ranks(values, dist, device):
+    """Each timing's maximum over the ranks (the slowest replica sets the
+    job's time)."""
+    import torch
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t.tolist()]
+
+
+def job_rate(world: int, units_per_rank: int, steps: int, seconds: float) -> float:
+    """Whole-job millions of units per second: every replica processes its own
+    units each step (weak scaling), the job takes the slowest rank's time."""
+    return world * units_per_rank * steps / seconds / 1e6
+
+
 def run_ours(args):
     import torch
     rank, local, world = _env_rank()
@@ -236,11 +251,9 @@ def run_ours(args):
     same = torch.equal(h_hits, d_hits.cpu())
 
     if dist:
-        t = torch.tensor([total_ms, e2e_s], dtype=torch.float64, device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms, e2e_s = float(t[0]), float(t[1])
-    value = world * NUM_RAYS * args.steps / (total_ms / 1e3) / 1e6
-    e2e_value = world * NUM_RAYS * e2e_steps / e2e_s / 1e6
+        total_ms, e2e_s = max_over_ranks([total_ms, e2e_s], dist, f"cuda:{local}")
+    value = job_rate(world, NUM_RAYS, args.steps, total_ms / 1e3)
+    e2e_value = job_rate(world, NUM_RAYS, e2e_steps, e2e_s)
 
     if rank != 0:
         if dist:
