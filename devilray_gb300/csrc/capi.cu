@@ -472,7 +472,8 @@ dr_status dr_trace_closest_host(dr_scene *s, const dr_ray *rays_host, uint64_t n
     // 4.13 ms; a first chunk of 1/32 and a second of 1/16 of the rays (the
     // traversal starts sooner) 4.01 ms; short chunks at the end as well
     // 4.07 ms. Reading the rays and writing the hits in place in mapped
-    // page-locked memory, in one launch: 4.82 ms.
+    // page-locked memory, in one launch: 4.82 ms; copying the chunks in on
+    // two alternating streams: 4.43 ms.
     auto *d_rays = static_cast<dr_ray *>(s->d_stage_rays);
     auto *d_hits = static_cast<dr_hit *>(s->d_stage_hits);
     // chunk boundaries, in 32nds of the rays: short first chunks so the
