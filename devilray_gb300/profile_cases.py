@@ -91,6 +91,25 @@ def render_box_room() -> None:
     ctx.check()
 
 
+def render_many_light(spp: int = 16) -> None:
+    """Many-light 1080p: scenes.many_light() (2^20 triangles, 65,536 emitters)
+    through the outside camera, depth 16, default schedule."""
+    import torch
+    from devilray_gb300 import scenes
+    native, ctx = _ctx()
+    scene = native.Scene.from_spec(ctx, scenes.many_light())
+    cam = scenes.outside_camera(1920, 1080)
+    n = 1920 * 1080
+    acc = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+    scene.render(cam, acc, spp=1, max_depth=16)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    scene.render(cam, acc, spp=spp, max_depth=16)
+    torch.cuda.synchronize()
+    print(f"render_many_light: {time.perf_counter() - t:.4f} s for {spp} spp")
+    ctx.check()
+
+
 def batch_small() -> None:
     import torch
     from devilray_gb300 import scenes  # noqa: F401
@@ -152,4 +171,5 @@ if __name__ == "__main__":
     case = sys.argv[1] if len(sys.argv) > 1 else "guide_infer"
     args = [int(a) for a in sys.argv[2:]]
     {"guide_infer": guide_infer, "guide_train": guide_train, "render_box_room": render_box_room,
+     "render_many_light": render_many_light,
      "batch_small": batch_small, "guided": guided}[case](*args)
