@@ -392,22 +392,6 @@ def render_section(ctx, native, device: int, stream, cpu: bool, threads: int, la
     return out
 
 
-def batch_specs(n: int = 64, seed: int = 2024):
-    """Uneven procedural scenes: triangle counts log-uniform in [1k, 2M],
-    square resolutions from {128, 256, 512, 1024}; the many-light material mix
-    (1/64 of the triangles emissive, at least 16; the rest half diffuse, half
-    dielectric); camera outside the scene cube."""
-    from devilray_gb300 import scenes
-    rng = np.random.default_rng(seed)
-    tris = np.exp(rng.uniform(np.log(1e3), np.log(2e6), n)).astype(np.int64)
-    res = rng.choice([128, 256, 512, 1024], n)
-    out = []
-    for i in range(n):
-        spec = scenes.many_light(int(tris[i]), max(16, int(tris[i]) // 64), seed=seed + i)
-        out.append((spec, scenes.outside_camera(int(res[i]), int(res[i]))))
-    return out
-
-
 def batch_section(ctx, native, device: int, stream, scenes_n: int = 64, spp: int = 32, depth: int = 12):
     """Batched uneven scenes: `scenes_n` scenes and cameras traced as one
     schedule (dr_batch) captured in a CUDA graph, wave size / streams / fetch
@@ -415,7 +399,8 @@ def batch_section(ctx, native, device: int, stream, scenes_n: int = 64, spp: int
     batch, beside the same images rendered one dr_render call at a time."""
     import torch
     t0 = time.perf_counter()
-    specs = batch_specs(scenes_n)
+    from devilray_gb300 import scenes
+    specs = scenes.uneven_batch(scenes_n)
     gen_s = time.perf_counter() - t0
     sizes = [s.positions.shape[0] for s, _ in specs]
     median = int(np.argsort(sizes)[len(sizes) // 2])

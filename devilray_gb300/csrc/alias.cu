@@ -492,6 +492,121 @@ __global__ void k_sweep_assign(const float *__restrict__ w, uint32_t n, const Sw
     out[slot] = e;
 }
 
+// ---- sweep build of many small tables, one thread per table ---------------------------
+
+// The sweep build of one table by one thread: the same fixed-point quantities
+// (m_i, W, a_i = n m_i - W) as the parallel kernels above and the same
+// assignment rules, evaluated by two cursors that walk the lights and the
+// heavies in index order instead of prefix sums and binary searches. O(n), no
+// scratch memory; the table equals the parallel build's bit for bit.
+__device__ void alias_sweep_build_one(const float *__restrict__ w, uint32_t n, dr_alias_entry *__restrict__ out)
+{
+    if (n == 0) return;
+    SweepScalars s;
+    s.emax = INT_MIN;
+    for (uint32_t i = 0; i < n; ++i) {
+        const float x = clamp_weight(w[i]);
+        if (x > 0.0f) s.emax = max(s.emax, float_exponent(x));
+    }
+    int lg = 0;
+    while ((1ll << lg) < (long long)n + 1) ++lg;
+    s.lg = lg;
+    s.shift = 61 - lg - s.emax;
+    unsigned long long W = 0;
+    for (uint32_t i = 0; i < n; ++i) W += (unsigned long long)fixed_weight(w[i], s);
+    const float Wf = s.emax == INT_MIN ? 0.0f : (float)ldexp((double)W, -s.shift);
+    if (!(Wf >= 1e-5f)) {
+        const float u = 1.0f / (float)n;
+        for (uint32_t i = 0; i < n; ++i) out[i] = dr_alias_entry{1.0f, u, 0.0f, (int32_t)i, -1};
+        return;
+    }
+    const double Wd = (double)W;
+    const long long nn = (long long)n;
+    auto surplus = [&](uint32_t i) { return nn * fixed_weight(w[i], s) - (long long)W; };  // a_i
+    auto next_heavy = [&](uint32_t i) {
+        while (i < n && surplus(i) < 0) ++i;
+        return i;
+    };
+    auto next_light = [&](uint32_t i) {
+        while (i < n && surplus(i) >= 0) ++i;
+        return i;
+    };
+    // lights: alias = first heavy h whose inclusive surplus sum exceeds the
+    // deficits of the lights before this one
+    {
+        uint32_t h = next_heavy(0);
+        i128 S = h < n ? (i128)surplus(h) : (i128)0;
+        i128 D = 0;
+        for (uint32_t i = next_light(0); i < n; i = next_light(i + 1)) {
+            while (h < n && !(S > D)) {
+                h = next_heavy(h + 1);
+                if (h < n) S += (i128)surplus(h);
+            }
+            const long long m = fixed_weight(w[i], s);
+            dr_alias_entry e;
+            e.A = (int32_t)i;
+            e.p_A = (float)((double)(nn * m) / Wd);
+            e.pdf_A = pdf_of(m, W);
+            if (h < n) {
+                e.B = (int32_t)h;
+                e.pdf_B = pdf_of(fixed_weight(w[h], s), W);
+            } else {
+                e.B = -1;
+                e.pdf_B = 0.0f;
+                e.p_A = 1.0f;
+            }
+            ensure_pa_larger(e);
+            out[i] = e;
+            D += (i128)(-surplus(i));
+        }
+    }
+    // heavies: R = inclusive surplus sum - deficits of the lights before the
+    // first light not covered by it; alias = the next heavy
+    {
+        uint32_t k = next_light(0);
+        i128 Dk = 0, S = 0;
+        for (uint32_t j = next_heavy(0); j < n;) {
+            S += (i128)surplus(j);
+            while (k < n && !(Dk >= S)) {
+                Dk += (i128)(-surplus(k));
+                k = next_light(k + 1);
+            }
+            const long long R = (long long)(S - Dk);
+            const uint32_t jn = next_heavy(j + 1);
+            dr_alias_entry e;
+            e.A = (int32_t)j;
+            e.pdf_A = pdf_of(fixed_weight(w[j], s), W);
+            if (jn < n) {
+                e.p_A = (float)((double)((long long)W + R) / Wd);
+                e.B = (int32_t)jn;
+                e.pdf_B = pdf_of(fixed_weight(w[jn], s), W);
+            } else {
+                e.p_A = 1.0f;
+                e.B = -1;
+                e.pdf_B = 0.0f;
+            }
+            if (e.p_A == 1.0f) {
+                e.B = -1;
+                e.pdf_B = 0.0f;
+            }
+            ensure_pa_larger(e);
+            out[j] = e;
+            j = jn;
+        }
+    }
+}
+
+// Many independent sweep tables, one thread each (segments as k_alias_ref_segments).
+__global__ void k_alias_sweep_segments(const float *__restrict__ w, const uint32_t *__restrict__ begin,
+                                       const uint32_t *__restrict__ count, uint32_t nseg,
+                                       dr_alias_entry *__restrict__ out)
+{
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nseg) return;
+    const uint32_t b = begin[s];
+    alias_sweep_build_one(w + b, count[s], out + b);
+}
+
 // ---- sampling ------------------------------------------------------------------------------
 
 // sample() (include/tracing/DistributionSamplers.hpp:64-88) with the two
@@ -567,6 +682,14 @@ cudaError_t launch_alias_ref_segments(const float *w, uint32_t total_n, const ui
     HeapItem *heaps = reinterpret_cast<HeapItem *>(p);
     float *filtered = reinterpret_cast<float *>(heaps + 2 * (size_t)total_n);
     k_alias_ref_segments<<<(nseg + 63) / 64, 64, 0, st>>>(w, begin, count, nseg, out, heaps, filtered);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_alias_sweep_segments(const float *w, const uint32_t *begin, const uint32_t *count, uint32_t nseg,
+                                       dr_alias_entry *out, cudaStream_t st)
+{
+    if (nseg == 0) return cudaSuccess;
+    k_alias_sweep_segments<<<(nseg + 63) / 64, 64, 0, st>>>(w, begin, count, nseg, out);
     return cudaGetLastError();
 }
 

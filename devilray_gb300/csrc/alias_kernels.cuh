@@ -34,6 +34,11 @@ cudaError_t launch_alias_build(const float *w, uint32_t n, dr_alias_entry *out, 
 cudaError_t launch_alias_ref_segments(const float *w, uint32_t total_n, const uint32_t *begin, const uint32_t *count,
                                      uint32_t nseg, dr_alias_entry *out, void *scratch, size_t scratch_bytes,
                                      cudaStream_t st);
+// Sweep-mode builds of many tables, one device thread per table (any size;
+// the table equals launch_alias_build's DR_ALIAS_SWEEP table of the segment).
+constexpr uint32_t kSweepThreadMax = 1u << 16;  // larger tables: the parallel build
+cudaError_t launch_alias_sweep_segments(const float *w, const uint32_t *begin, const uint32_t *count, uint32_t nseg,
+                                       dr_alias_entry *out, cudaStream_t st);
 cudaError_t launch_alias_sample(const dr_alias_entry *table, uint32_t n, const float *u, uint64_t draws,
                                 int32_t *index, float *pdf, cudaStream_t st);
 

@@ -170,6 +170,8 @@ dr_status dr_scene_create(dr_context *ctx, const dr_scene_desc *desc, const dr_b
     const uint32_t n = desc->num_triangles;
     DR_CHECK_ARG(n == 0 || desc->positions_host, "dr_scene_create: positions_host is NULL");
     if (n >= kMaxTriangles) return fail(DR_ERR_TOO_LARGE, "dr_scene_create: %u triangles (max %u)", n, kMaxTriangles - 1);
+    DR_CHECK_ARG(desc->light_tables == DR_LIGHT_TABLES_SWEEP || desc->light_tables == DR_LIGHT_TABLES_REFERENCE,
+                 "dr_scene_create: unknown light_tables value");
     float mag = 0.0f;
     for (size_t i = 0; i < (size_t)n * 9; ++i) {
         const float v = desc->positions_host[i];

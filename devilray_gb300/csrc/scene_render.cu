@@ -4,8 +4,10 @@
 // Light selection follows the reference: an object is picked by emitted power
 // (Renderer::calculateLightWeights, src/Renderer.cpp:113-152: surface area x
 // luminance(pi x emission), normalised by the total), then a triangle of that
-// object by area (src/GpuTris.cpp:7-21). Both tables are built on the device in
-// reference mode, so they equal generateAliasTable's bit for bit.
+// object by area (src/GpuTris.cpp:7-21). Both tables are built on the device:
+// by default with the parallel sweep build (the object table of 66,356 objects
+// in a few parallel launches), or, with DR_LIGHT_TABLES_REFERENCE, in
+// reference mode, so that they equal generateAliasTable's bit for bit.
 
 #include "dr_internal.h"
 #include "alias_kernels.cuh"
@@ -132,7 +134,8 @@ dr_status build_render_data(dr_scene *s, const dr_scene_desc *d)
     }
     if (!s->lights) return DR_OK;
 
-    // device builds (reference mode: one thread per table)
+    // device builds
+    const bool ref_mode = d->light_tables == DR_LIGHT_TABLES_REFERENCE;
     float *d_w = nullptr, *d_tw = nullptr;
     uint32_t *d_seg = nullptr;
     DR_CUDA(cudaMalloc(&s->d_light_table, N * sizeof(dr_alias_entry)));
@@ -141,27 +144,47 @@ dr_status build_render_data(dr_scene *s, const dr_scene_desc *d)
     DR_CUDA(cudaMemset(s->d_tri_tables, 0, (size_t)std::max(1u, n) * sizeof(dr_alias_entry)));
     DR_CUDA(cudaMalloc(&d_w, N * sizeof(float)));
     DR_CUDA(cudaMemcpy(d_w, weights.data(), N * sizeof(float), cudaMemcpyHostToDevice));
-    const size_t need1 = alias_scratch_bytes((uint32_t)N, DR_ALIAS_REFERENCE);
-    const size_t need2 = (size_t)n * (2 * 8 + 4) + 1024;
-    dr_status st = ensure_scratch(s->ctx, std::max(need1, need2));
+    // scratch: the object table's build, the reference triangle tables' heaps,
+    // and the parallel sweep of the largest triangle table
+    size_t need = alias_scratch_bytes((uint32_t)N, ref_mode ? DR_ALIAS_REFERENCE : DR_ALIAS_SWEEP);
+    if (ref_mode) need = std::max(need, (size_t)n * (2 * 8 + 4) + 1024);
+    std::vector<uint32_t> big;  // sweep mode: segments built by the parallel kernels
+    for (size_t k = 0; k < seg_begin.size(); ++k)
+        if (!ref_mode && seg_count[k] > kSweepThreadMax) {
+            big.push_back((uint32_t)k);
+            need = std::max(need, alias_scratch_bytes(seg_count[k], DR_ALIAS_SWEEP));
+        }
+    dr_status st = ensure_scratch(s->ctx, need);
     if (st != DR_OK) {
         cudaFree(d_w);
         return st;
     }
-    e = launch_alias_build(d_w, (uint32_t)N, s->d_light_table, DR_ALIAS_REFERENCE, s->ctx->scratch,
-                           s->ctx->scratch_bytes, s->ctx->num_sms, nullptr);
+    e = launch_alias_build(d_w, (uint32_t)N, s->d_light_table, ref_mode ? DR_ALIAS_REFERENCE : DR_ALIAS_SWEEP,
+                           s->ctx->scratch, s->ctx->scratch_bytes, s->ctx->num_sms, nullptr);
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     cudaFree(d_w);
     if (e != cudaSuccess) return cuda_fail(e, "dr_scene_create: light table");
     if (!seg_begin.empty()) {
         DR_CUDA(cudaMalloc(&d_tw, (size_t)n * sizeof(float)));
         DR_CUDA(cudaMemcpy(d_tw, tri_w.data(), (size_t)n * sizeof(float), cudaMemcpyHostToDevice));
+        // sweep mode: the one-thread kernel skips the large segments (count 0)
+        std::vector<uint32_t> small_count = seg_count;
+        for (uint32_t k : big) small_count[k] = 0;
         DR_CUDA(cudaMalloc(&d_seg, seg_begin.size() * 2 * sizeof(uint32_t)));
         DR_CUDA(cudaMemcpy(d_seg, seg_begin.data(), seg_begin.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
-        DR_CUDA(cudaMemcpy(d_seg + seg_begin.size(), seg_count.data(), seg_count.size() * sizeof(uint32_t),
+        DR_CUDA(cudaMemcpy(d_seg + seg_begin.size(), small_count.data(), small_count.size() * sizeof(uint32_t),
                            cudaMemcpyHostToDevice));
-        e = launch_alias_ref_segments(d_tw, n, d_seg, d_seg + seg_begin.size(), (uint32_t)seg_begin.size(),
-                                      s->d_tri_tables, s->ctx->scratch, s->ctx->scratch_bytes, nullptr);
+        if (ref_mode)
+            e = launch_alias_ref_segments(d_tw, n, d_seg, d_seg + seg_begin.size(), (uint32_t)seg_begin.size(),
+                                          s->d_tri_tables, s->ctx->scratch, s->ctx->scratch_bytes, nullptr);
+        else
+            e = launch_alias_sweep_segments(d_tw, d_seg, d_seg + seg_begin.size(), (uint32_t)seg_begin.size(),
+                                            s->d_tri_tables, nullptr);
+        for (size_t k = 0; k < big.size() && e == cudaSuccess; ++k) {
+            const uint32_t b = seg_begin[big[k]], c = seg_count[big[k]];
+            e = launch_alias_build(d_tw + b, c, s->d_tri_tables + b, DR_ALIAS_SWEEP, s->ctx->scratch,
+                                   s->ctx->scratch_bytes, s->ctx->num_sms, nullptr);
+        }
         if (e == cudaSuccess) e = cudaDeviceSynchronize();
         cudaFree(d_tw);
         cudaFree(d_seg);

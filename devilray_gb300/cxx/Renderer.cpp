@@ -148,6 +148,9 @@ void Renderer::calculateLightWeights()
     desc.materials_host = materials.data();
     desc.num_materials = (uint32_t)materials.size();
     desc.tri_weight_host = tri_weight.data();
+    // Renderer::calculateLightWeights and convertMeshToTris build their tables
+    // with generateAliasTable: keep the reference's pairing (bit-identical tables)
+    desc.light_tables = DR_LIGHT_TABLES_REFERENCE;
     dr_scene *scene = nullptr;
     check(dr_scene_create(context(), &desc, nullptr, &scene), "Renderer::setScene");
     if (m_deviceScene) dr_scene_destroy(m_deviceScene);

@@ -23,6 +23,8 @@ STATUS_NAMES = {
 
 DR_ALIAS_REFERENCE = 0
 DR_ALIAS_SWEEP = 1
+DR_LIGHT_TABLES_SWEEP = 0
+DR_LIGHT_TABLES_REFERENCE = 1
 ALIAS_DTYPE = np.dtype([("p_A", "<f4"), ("pdf_A", "<f4"), ("pdf_B", "<f4"), ("A", "<i4"), ("B", "<i4")])
 
 DR_TRI_REFERENCE = 0
@@ -59,7 +61,8 @@ class SceneDesc(C.Structure):
     _fields_ = [("positions_host", C.c_void_p), ("num_triangles", C.c_uint32),
                 ("objects_host", C.c_void_p), ("num_objects", C.c_uint32),
                 ("materials_host", C.c_void_p), ("num_materials", C.c_uint32),
-                ("tri_material_host", C.c_void_p), ("tri_weight_host", C.c_void_p)]
+                ("tri_material_host", C.c_void_p), ("tri_weight_host", C.c_void_p),
+                ("light_tables", C.c_uint32)]
 
 
 class BuildConfig(C.Structure):
@@ -293,10 +296,13 @@ def alias_sample(table_dev, n: int, uniforms_dev, ndraws: int, index_dev, pdf_de
                                  _stream_ptr(stream)))
 
 
-def scene_desc(positions: np.ndarray, objects=None, materials=None, tri_material=None, tri_weight=None):
-    """dr_scene_desc over numpy/ctypes arrays; returns (desc, arrays to keep alive)."""
+def scene_desc(positions: np.ndarray, objects=None, materials=None, tri_material=None, tri_weight=None,
+               light_tables: int = 0):
+    """dr_scene_desc over numpy/ctypes arrays; returns (desc, arrays to keep alive).
+    light_tables: DR_LIGHT_TABLES_SWEEP (0) or DR_LIGHT_TABLES_REFERENCE (1)."""
     positions = np.ascontiguousarray(positions, np.float32).reshape(-1, 9)
     desc = SceneDesc()
+    desc.light_tables = light_tables
     desc.positions_host = positions.ctypes.data
     desc.num_triangles = positions.shape[0]
     keep = [positions]
@@ -359,10 +365,10 @@ class Scene:
 
     def __init__(self, ctx: Context, positions: np.ndarray, objects=None, materials=None,
                  tri_material=None, tri_weight=None, max_leaf_size: int = 0, sah_bins: int = 0,
-                 threads: int = 0, layout: int = 0, builder: int = 0):
+                 threads: int = 0, layout: int = 0, builder: int = 0, light_tables: int = 0):
         self.ctx = ctx
         self.positions = np.ascontiguousarray(positions, np.float32).reshape(-1, 9)
-        desc, keep = scene_desc(self.positions, objects, materials, tri_material, tri_weight)
+        desc, keep = scene_desc(self.positions, objects, materials, tri_material, tri_weight, light_tables)
         cfg = BuildConfig(max_leaf_size, sah_bins, threads, layout, builder)
         self.handle = C.c_void_p()
         check(load().dr_scene_create(ctx.handle, C.byref(desc), C.byref(cfg), C.byref(self.handle)))
@@ -378,6 +384,15 @@ class Scene:
         info = SceneInfo()
         check(load().dr_scene_get_info(self.handle, C.byref(info)))
         return info
+
+    def light_table(self) -> np.ndarray:
+        """The object light table (dr_scene_get_light_table), ALIAS_DTYPE entries."""
+        count = C.c_uint32()
+        check(load().dr_scene_get_light_table(self.handle, None, 0, C.byref(count)))
+        out = np.zeros(count.value, ALIAS_DTYPE)
+        if count.value:
+            check(load().dr_scene_get_light_table(self.handle, out.ctypes.data, count.value, C.byref(count)))
+        return out
 
     def close(self):
         if self.handle:

@@ -338,3 +338,19 @@ def outside_camera(width: int, height: int, distance: float = 150.0, half: float
     m = np.eye(4, dtype=np.float32)
     m[2, 3] = -distance
     return camera(width, height, focal=1.0, fov_half_width=0.62 * half / distance * 1.6, transform=m)
+
+
+def uneven_batch(n: int = 64, seed: int = 2024) -> list:
+    """The batched configuration: `n` procedural scenes with triangle counts
+    log-uniform in [1k, 2M] and square resolutions from {128, 256, 512, 1024};
+    the many-light material mix (1/64 of the triangles emissive, at least 16;
+    the rest half diffuse, half dielectric); each seen by a camera outside its
+    cube. Returns [(SceneSpec, camera)]."""
+    rng = np.random.default_rng(seed)
+    tris = np.exp(rng.uniform(np.log(1e3), np.log(2e6), n)).astype(np.int64)
+    res = rng.choice([128, 256, 512, 1024], n)
+    out = []
+    for i in range(n):
+        spec = many_light(int(tris[i]), max(16, int(tris[i]) // 64), seed=seed + i)
+        out.append((spec, outside_camera(int(res[i]), int(res[i]))))
+    return out

@@ -123,11 +123,18 @@ typedef struct or_render_cfg {
     int32_t replay_stride;   /* uniforms per (pixel, sample) in `replay` */
     const float *replay;     /* [pixel][sample][replay_stride] */
     int32_t debug;           /* 0 off, 1 UV checker, 2 barycentrics, 3 winding order */
+    const int64_t *pixels;   /* NULL: every pixel; else render only these pixel indices (y * width + x);
+                                outputs keep the full image's indexing */
+    int64_t num_pixels;
 } or_render_cfg;
 
 typedef struct or_scene or_scene;
+/* light_tables: 0 = every light table by or_alias_build_sweep (the GPU's
+ * default, DR_LIGHT_TABLES_SWEEP), 1 = by or_alias_build_ref (the reference's
+ * generateAliasTable pairing, DR_LIGHT_TABLES_REFERENCE). */
 or_scene *or_scene_create(const float *positions, int32_t num_tris, const or_object *objects, int32_t num_objects,
-                          const or_material *materials, int32_t num_materials, const int32_t *tri_material);
+                          const or_material *materials, int32_t num_materials, const int32_t *tri_material,
+                          int32_t light_tables);
 void or_scene_destroy(or_scene *s);
 float or_scene_total_power(const or_scene *s);
 void or_scene_light_table(const or_scene *s, or_alias_entry *out);
@@ -136,6 +143,14 @@ void or_scene_light_table(const or_scene *s, or_alias_entry *out);
  * Any output may be NULL. */
 void or_render(const or_scene *s, const or_camera *cam, const or_render_cfg *cfg, float *sample_rgb, float *accum,
                uint32_t *casts);
+
+/* FP64 restatement of the same integrator for converged reference images:
+ * adds the sum of cfg->spp sample colours of every rendered pixel to
+ * sum_rgb [height*width][3] (double). Uses max_depth, spp, sample_offset,
+ * pixel_sampling, seed, threads and pixels of cfg; closest hits over a
+ * double-precision BVH, lights drawn from double cumulative sums, std trig
+ * functions, Philox uniforms of 53 bits on a stream of their own. */
+void or_render_f64(const or_scene *s, const or_camera *cam, const or_render_cfg *cfg, double *sum_rgb);
 
 /* Renderer::createPixels (src/Renderer.cpp:51-90): accum [height*width][4]
  * (colour sums, sample count in w) to RGBA8 rows, first row = top of the image.

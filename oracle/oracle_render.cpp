@@ -23,8 +23,10 @@
 #include "oracle.h"
 #include "oracle_common.hpp"
 #include "oracle_ptmath.hpp"
+#include "oracle_scene.hpp"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <limits>
@@ -38,9 +40,6 @@ namespace {
 
 constexpr float kPi = 3.14159274f;  // std::numbers::pi_v<float> (include/Utils.hpp:27)
 
-struct V4 {
-    float x, y, z, w;
-};
 inline V4 add4(const V4 &a, const V4 &b) { return V4{a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w}; }
 inline V4 mul4(const V4 &a, const V4 &b) { return V4{a.x * b.x, a.y * b.y, a.z * b.z, a.w * b.w}; }
 inline V4 mul4s(const V4 &a, float f) { return V4{a.x * f, a.y * f, a.z * f, a.w * f}; }
@@ -67,11 +66,6 @@ inline float cosineHemispherePdf(const V3 &cur, const V3 &next, const V3 &n)
     return c > 0 ? c / kPi : 0.0f;
 }
 
-struct Mat {
-    int kind;
-    float ior;
-    V4 emission, albedo, debug;
-};
 
 inline V4 radiantExitance(const Mat &m)  // include/tracing/LightSampling.hpp:7-13
 {
@@ -116,31 +110,9 @@ struct Hit {
     int prim;
 };
 
-struct BbhDel {
-    void operator()(or_bbh *p) const { or_bbh_destroy(p); }
-};
-using BbhPtr = std::unique_ptr<or_bbh, BbhDel>;
 
 }  // namespace
 
-struct or_scene {
-    std::vector<float> pos;                 // 9 floats per triangle
-    std::vector<or_object> objects;
-    std::vector<int32_t> tri_object;        // triangle -> object
-    std::vector<Mat> mats;
-    std::vector<int32_t> tri_material;      // triangle -> material (object's unless overridden)
-    // light sampling
-    std::vector<or_alias_entry> light_table;
-    float total_power = 0.0f;
-    // per-object triangle tables, two index orders
-    std::vector<or_alias_entry> tri_table[2];
-    std::vector<int32_t> tri_table_map[2];  // [order][tri_begin + i] -> soup triangle
-    // closest hit structures
-    BbhPtr soup_bbh;
-    std::vector<BbhPtr> obj_bbh;
-    std::vector<std::vector<int32_t>> obj_order;  // per object: sorted position -> soup triangle
-    float slack = 0.0f;
-};
 
 namespace {
 
@@ -205,8 +177,10 @@ struct LightSample {
 extern "C" {
 
 or_scene *or_scene_create(const float *positions, int32_t num_tris, const or_object *objects, int32_t num_objects,
-                          const or_material *materials, int32_t num_materials, const int32_t *tri_material)
+                          const or_material *materials, int32_t num_materials, const int32_t *tri_material,
+                          int32_t light_tables)
 {
+    const auto build_table = light_tables == 1 ? or_alias_build_ref : or_alias_build_sweep;
     auto *s = new or_scene;
     s->pos.assign(positions, positions + (size_t)num_tris * 9);
     if (objects && num_objects > 0) s->objects.assign(objects, objects + num_objects);
@@ -244,7 +218,7 @@ or_scene *or_scene_create(const float *positions, int32_t num_tris, const or_obj
     }
     for (size_t i = 0; i < N; ++i) weights[i] /= total;
     s->light_table.resize(N);
-    or_alias_build_ref(weights.data(), (int32_t)N, s->light_table.data());
+    build_table(weights.data(), (int32_t)N, s->light_table.data());
     s->total_power = total;
 
     // Per-object BBHs (reference cast) and triangle tables in both orders.
@@ -268,7 +242,7 @@ or_scene *or_scene_create(const float *positions, int32_t num_tris, const or_obj
                 s->tri_table_map[ord][ob.tri_begin + k] = tri;
                 areas[k] = triangleArea(vtx(*s, tri, 0), vtx(*s, tri, 1), vtx(*s, tri, 2));
             }
-            or_alias_build_ref(areas.data(), (int32_t)ob.tri_count, s->tri_table[ord].data() + ob.tri_begin);
+            build_table(areas.data(), (int32_t)ob.tri_count, s->tri_table[ord].data() + ob.tri_begin);
         }
     }
     return s;
@@ -291,8 +265,11 @@ void or_render(const or_scene *s, const or_camera *cam, const or_render_cfg *cfg
     const Trig trig{cfg->trig_mode};
     const int order = cfg->tri_table_order;
     int threads = cfg->threads > 0 ? cfg->threads : (int)std::max(1u, std::thread::hardware_concurrency());
+    const int64_t nwork = cfg->pixels ? cfg->num_pixels : npix;
     auto work = [&](int64_t pb, int64_t pe) {
-        for (int64_t pix = pb; pix < pe; ++pix) {
+        for (int64_t wi = pb; wi < pe; ++wi) {
+            const int64_t pix = cfg->pixels ? cfg->pixels[wi] : wi;
+            if (pix < 0 || pix >= npix) continue;
             const int px = (int)(pix % W), py = (int)(pix / W);
             V4 pixel{0, 0, 0, 0};
             uint32_t pixel_casts = 0;
@@ -553,17 +530,21 @@ void or_render(const or_scene *s, const or_camera *cam, const or_render_cfg *cfg
             if (casts_out) casts_out[pix] = pixel_casts;
         }
     };
-    if (threads <= 1 || npix < 64) {
-        work(0, npix);
+    if (threads <= 1 || nwork < 64) {
+        work(0, nwork);
         return;
     }
+    // interleaved chunks of 64 work items so that expensive regions spread over the threads
     std::vector<std::thread> pool;
-    const int64_t chunk = (npix + threads - 1) / threads;
-    for (int t = 0; t < threads; ++t) {
-        const int64_t b = t * chunk, e = std::min<int64_t>(npix, b + chunk);
-        if (b >= e) break;
-        pool.emplace_back(work, b, e);
-    }
+    std::atomic<int64_t> next{0};
+    auto worker = [&]() {
+        for (;;) {
+            const int64_t b = next.fetch_add(64);
+            if (b >= nwork) break;
+            work(b, std::min<int64_t>(nwork, b + 64));
+        }
+    };
+    for (int t = 0; t < threads; ++t) pool.emplace_back(worker);
     for (auto &th : pool) th.join();
 }
 

@@ -300,7 +300,7 @@ class RenderCfg(C.Structure):
                 ("pixel_sampling", C.c_int32), ("seed", C.c_uint64), ("rng_mode", C.c_int32),
                 ("trig_mode", C.c_int32), ("cast_mode", C.c_int32), ("tri_table_order", C.c_int32),
                 ("threads", C.c_int32), ("replay_stride", C.c_int32), ("replay", C.c_void_p),
-                ("debug", C.c_int32)]
+                ("debug", C.c_int32), ("pixels", C.c_void_p), ("num_pixels", C.c_int64)]
 
 
 class Camera(C.Structure):
@@ -321,7 +321,8 @@ def make_camera(cam: dict) -> Camera:
 def _render_lib():
     L = lib()
     if not getattr(L, "_render_bound", False):
-        L.or_scene_create.argtypes = [_f32p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p]
+        L.or_scene_create.argtypes = [_f32p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p,
+                                      C.c_int32]
         L.or_scene_create.restype = C.c_void_p
         L.or_scene_destroy.argtypes = [C.c_void_p]
         L.or_scene_total_power.argtypes = [C.c_void_p]
@@ -329,20 +330,22 @@ def _render_lib():
         L.or_scene_light_table.argtypes = [C.c_void_p, C.c_void_p]
         L.or_render.argtypes = [C.c_void_p, C.POINTER(Camera), C.POINTER(RenderCfg), C.c_void_p, C.c_void_p,
                                 C.c_void_p]
+        L.or_render_f64.argtypes = [C.c_void_p, C.POINTER(Camera), C.POINTER(RenderCfg), C.c_void_p]
         L._render_bound = True
     return L
 
 
 class RenderScene:
-    """Oracle scene for the integrator restatement."""
+    """Oracle scene for the integrator restatement. light_tables: 0 = sweep
+    tables (the GPU scene's default), 1 = the reference's pairing."""
 
-    def __init__(self, spec):
+    def __init__(self, spec, light_tables: int = 0):
         L = _render_lib()
         self.pos = _f32(spec.positions).reshape(-1)
         self.objs = spec.objects_array()
         self.mats = spec.materials_array()
         self.h = L.or_scene_create(self.pos, self.pos.size // 9, self.objs.ctypes.data, len(self.objs),
-                                   self.mats.ctypes.data, len(self.mats), None)
+                                   self.mats.ctypes.data, len(self.mats), None, int(light_tables))
 
     def __del__(self):
         if getattr(self, "h", None):
@@ -361,9 +364,16 @@ class RenderScene:
     def render(self, cam: dict, spp: int, max_depth: int = 10, seed: int = 0, sample_offset: int = 0,
                pixel_sampling: int = 1, rng_mode: int = 0, trig_mode: int = 0, cast_mode: int = 0,
                tri_table_order: int = 0, replay: np.ndarray | None = None, threads: int = 0,
-               per_sample: bool = False, debug: int = 0):
+               per_sample: bool = False, debug: int = 0, pixels: np.ndarray | None = None):
+        """accum [h*w, 4], casts [h*w], per-sample rgb or None. With `pixels`
+        (pixel indices y * width + x) only those pixels are rendered; the
+        others stay zero."""
         cfg = RenderCfg(max_depth, spp, sample_offset, pixel_sampling, seed, rng_mode, trig_mode, cast_mode,
-                        tri_table_order, threads, 0, None, debug)
+                        tri_table_order, threads, 0, None, debug, None, 0)
+        if pixels is not None:
+            pixels = np.ascontiguousarray(pixels, np.int64)
+            cfg.pixels = pixels.ctypes.data
+            cfg.num_pixels = pixels.size
         if replay is not None:
             replay = _f32(replay)
             cfg.replay_stride = replay.shape[-1]
@@ -376,6 +386,23 @@ class RenderScene:
         _render_lib().or_render(self.h, C.byref(c), C.byref(cfg), rgb.ctypes.data if rgb is not None else None,
                                 accum.ctypes.data, casts.ctypes.data)
         return accum, casts, rgb
+
+
+    def render_f64(self, cam: dict, spp: int, max_depth: int = 10, seed: int = 0, sample_offset: int = 0,
+                   pixel_sampling: int = 1, threads: int = 0, pixels: np.ndarray | None = None) -> np.ndarray:
+        """FP64 restatement of the integrator: mean radiance [h*w, 3] (float64)
+        over `spp` samples per pixel (pixels outside `pixels` stay zero)."""
+        cfg = RenderCfg(max_depth, spp, sample_offset, pixel_sampling, seed, 0, 0, 0, 0, threads, 0, None, 0,
+                        None, 0)
+        if pixels is not None:
+            pixels = np.ascontiguousarray(pixels, np.int64)
+            cfg.pixels = pixels.ctypes.data
+            cfg.num_pixels = pixels.size
+        w, h = cam["width"], cam["height"]
+        out = np.zeros((h * w, 3), np.float64)
+        c = make_camera(cam)
+        _render_lib().or_render_f64(self.h, C.byref(c), C.byref(cfg), out.ctypes.data)
+        return out / float(spp)
 
 
 def ref_render_samples(spec, cam: dict, spp: int, replay: np.ndarray, sampling: int = 1, debug: int = 0):

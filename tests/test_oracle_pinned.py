@@ -188,7 +188,7 @@ def test_integrator_matches_reference_sample_color(oracle, golden):
     assert np.array_equal(spec.positions, g["positions"])
     w, h, spp = int(g["width"]), int(g["height"]), int(g["spp"])
     cam = scenes.camera(w, h)
-    sc = oracle.RenderScene(spec)
+    sc = oracle.RenderScene(spec, light_tables=1)
     for sampling in (0, 1):
         acc, casts, rgb = sc.render(cam, spp, max_depth=10, rng_mode=1, trig_mode=1, cast_mode=1, tri_table_order=1,
                                     replay=g["replay"], per_sample=True, pixel_sampling=sampling)
@@ -225,7 +225,7 @@ def test_debug_views_match_reference(oracle, golden, view):
     assert np.array_equal(spec.materials_array(), g["materials"])
     w, h, spp = int(g["width"]), int(g["height"]), int(g["spp"])
     cam = scenes.camera(w, h)
-    sc = oracle.RenderScene(spec)
+    sc = oracle.RenderScene(spec, light_tables=1)
     acc, casts, rgb = sc.render(cam, spp, rng_mode=1, trig_mode=1, cast_mode=1, tri_table_order=1,
                                 replay=g["replay"], per_sample=True, pixel_sampling=1, debug=view)
     assert np.array_equal(rgb.view(np.uint32), g[f"rgb_{view}"].view(np.uint32))
