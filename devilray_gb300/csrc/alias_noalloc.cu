@@ -12,7 +12,10 @@
 //    Larger n is rejected with DR_ERR_TOO_LARGE.
 //  * Set-up: the first call on a device looks up the device address of the
 //    array (cudaGetSymbolAddress, with that device current) and caches it;
-//    make that first call before any stream capture.
+//    make that first call before any stream capture. The cache lives as long
+//    as the process: a device reset (cudaDeviceReset) after the first call is
+//    not supported, because the array's address may change with the new
+//    context while the cached one would not.
 //  * Sharing: every call uses the same array and the array keeps the last
 //    call's contents. The build's first kernel re-initialises the running
 //    totals it reads, so stale contents never leak into a result, but calls

@@ -214,7 +214,7 @@ dr_status dr_batch_create(dr_context *ctx, const dr_job *jobs, uint32_t njobs, c
         if (count == 0) return cudaSuccess;
         const size_t bytes = count * sizeof(**p);
         b->device_bytes += bytes;
-        return cudaMalloc(reinterpret_cast<void **>(p), bytes);
+        return dev_malloc(reinterpret_cast<void **>(p), bytes);
     };
     cudaError_t e = cudaSuccess;
     if (layout == 8) e = alloc(&b->nodes8, nodes);
@@ -321,6 +321,7 @@ dr_status dr_batch_render(dr_batch *b, const uint32_t *sample_offsets, void *str
         a.trace.prim = b->prim;
         a.trace.num_nodes = b->num_nodes;
         a.trace.error = b->ctx->d_error;
+        a.trace.stack_limit = b->ctx->stack_limit;
         a.shade = b->shade;
         a.objects = b->objects;
         a.materials = b->materials;

@@ -52,7 +52,7 @@ cudaError_t upload(T **dst, const T *src, size_t count, uint64_t &bytes)
 {
     *dst = nullptr;
     if (count == 0) return cudaSuccess;
-    cudaError_t e = cudaMalloc(reinterpret_cast<void **>(dst), sizeof(T) * count);
+    cudaError_t e = dev_malloc(reinterpret_cast<void **>(dst), sizeof(T) * count);
     if (e != cudaSuccess) return e;
     bytes += sizeof(T) * count;
     return cudaMemcpy(*dst, src, sizeof(T) * count, cudaMemcpyHostToDevice);
@@ -81,14 +81,46 @@ TraceArgs trace_args(dr_scene *s)
     a.tri_wt = s->d_tri_wt;
     a.prim = s->d_prim;
     a.num_nodes = s->num_nodes;
-    a.counters = s->ctx->d_counters;
     a.error = s->ctx->d_error;
-    a.work = s->ctx->d_work + s->ctx->work_next.fetch_add(1) % kWorkCounters;
+    // each launch takes its own work counter and traversal counters, so that
+    // launches on different streams can overlap
+    const uint32_t slot = s->ctx->work_next.fetch_add(1) % kWorkCounters;
+    a.work = s->ctx->d_work + slot;
+    a.counters = s->ctx->d_counters + 8 * (size_t)slot;
     a.num_sms = s->ctx->num_sms;
+    a.stack_limit = s->ctx->stack_limit;
     return a;
 }
 
 }  // namespace
+
+// Countdown of dr_debug_fail_allocation: 0 = off, k = the k-th next allocation fails.
+static std::atomic<uint32_t> g_fail_alloc_after{0};
+
+}  // namespace dr
+
+extern "C" dr_status dr_debug_fail_allocation(uint32_t after)
+{
+    dr::g_fail_alloc_after.store(after, std::memory_order_relaxed);
+    return DR_OK;
+}
+
+namespace dr {
+
+cudaError_t dev_malloc_raw(void **p, size_t bytes)
+{
+    uint32_t k = g_fail_alloc_after.load(std::memory_order_relaxed);
+    while (k != 0) {
+        if (g_fail_alloc_after.compare_exchange_weak(k, k - 1, std::memory_order_relaxed)) {
+            if (k == 1) {
+                *p = nullptr;
+                return cudaErrorMemoryAllocation;
+            }
+            break;
+        }
+    }
+    return cudaMalloc(p, bytes);
+}
 
 dr_status ensure_scratch(dr_context *ctx, size_t bytes)
 {
@@ -98,7 +130,7 @@ dr_status ensure_scratch(dr_context *ctx, size_t bytes)
     cudaFree(ctx->scratch);
     ctx->scratch = nullptr;
     ctx->scratch_bytes = 0;
-    DR_CUDA(cudaMalloc(&ctx->scratch, want));
+    DR_CUDA(dev_malloc(&ctx->scratch, want));
     ctx->scratch_bytes = want;
     return DR_OK;
 }
@@ -135,13 +167,15 @@ dr_status dr_context_create(const dr_context_config *cfg, dr_context **out)
         return cuda_fail(e, "cudaGetDeviceProperties");
     }
     ctx->num_sms = prop.multiProcessorCount;
-    const size_t words = 256 + kWorkCounters * sizeof(unsigned long long);
-    if ((e = cudaMalloc(&ctx->d_error, words)) != cudaSuccess || (e = cudaMemset(ctx->d_error, 0, words)) != cudaSuccess) {
+    // [0, 64) error word, [128, 132) probe sink, [256, +512) work counters,
+    // then 8 traversal counters per work counter
+    const size_t words = 256 + kWorkCounters * sizeof(unsigned long long) * 9;
+    if ((e = dev_malloc(&ctx->d_error, words)) != cudaSuccess || (e = cudaMemset(ctx->d_error, 0, words)) != cudaSuccess) {
         delete ctx;
-        return cuda_fail(e, "cudaMalloc(error word)");
+        return cuda_fail(e, "allocation of the error word");
     }
-    ctx->d_counters = reinterpret_cast<unsigned long long *>(reinterpret_cast<char *>(ctx->d_error) + 64);
     ctx->d_work = reinterpret_cast<unsigned long long *>(reinterpret_cast<char *>(ctx->d_error) + 256);
+    ctx->d_counters = ctx->d_work + kWorkCounters;
     *out = ctx;
     return DR_OK;
 }
@@ -347,7 +381,7 @@ dr_status dr_device_allocate(dr_context *ctx, uint64_t bytes, void **dev)
     *dev = nullptr;
     if (bytes == 0) return DR_OK;
     DR_CUDA(cudaSetDevice(ctx->device));
-    const cudaError_t e = cudaMalloc(dev, bytes);
+    const cudaError_t e = dev_malloc(dev, bytes);
     if (e == cudaErrorMemoryAllocation) {
         cudaGetLastError();
         return fail(DR_ERR_OUT_OF_MEMORY, "dr_device_allocate: %llu bytes", (unsigned long long)bytes);
@@ -415,11 +449,11 @@ dr_status dr_trace_closest(dr_scene *s, const dr_ray *rays, uint64_t n, dr_hit *
     a.rays = rays;
     a.n = n;
     a.hits = hits;
-    if (counters) DR_CUDA(cudaMemsetAsync(s->ctx->d_counters, 0, 8 * sizeof(unsigned long long), st));
+    if (counters) DR_CUDA(cudaMemsetAsync(a.counters, 0, 8 * sizeof(unsigned long long), st));
     DR_CUDA(launch_trace_closest(a, tri_mode, counters != nullptr, st));
     if (counters) {
         unsigned long long c[8];
-        DR_CUDA(cudaMemcpyAsync(c, s->ctx->d_counters, sizeof(c), cudaMemcpyDeviceToHost, st));
+        DR_CUDA(cudaMemcpyAsync(c, a.counters, sizeof(c), cudaMemcpyDeviceToHost, st));
         DR_CUDA(cudaStreamSynchronize(st));
         counters->rays = n;
         counters->node_visits = c[0];
@@ -460,8 +494,8 @@ dr_status dr_trace_closest_host(dr_scene *s, const dr_ray *rays_host, uint64_t n
         cudaFree(s->d_stage_hits);
         s->d_stage_rays = s->d_stage_hits = nullptr;
         s->stage_capacity = 0;
-        DR_CUDA(cudaMalloc(&s->d_stage_rays, n * sizeof(dr_ray)));
-        DR_CUDA(cudaMalloc(&s->d_stage_hits, n * sizeof(dr_hit)));
+        DR_CUDA(dev_malloc(&s->d_stage_rays, n * sizeof(dr_ray)));
+        DR_CUDA(dev_malloc(&s->d_stage_hits, n * sizeof(dr_hit)));
         s->stage_capacity = n;
     }
     // Pipeline in chunks: the copy-in of chunk k+1 and the copy-out of chunk

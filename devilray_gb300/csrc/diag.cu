@@ -1,9 +1,14 @@
-// diag.cu -- diagnostic read-bandwidth probe (no counterpart in the
-// reference). It measures the roofline denominator of the traversal kernels:
-// streaming reads of a buffer that fits in L2 give the L2 read bandwidth, a
-// buffer larger than L2 gives the HBM read bandwidth.
+// diag.cu -- diagnostics without a counterpart in the reference:
+//  * the read-bandwidth probe: the roofline denominator of the traversal
+//    kernels (streaming reads of a buffer that fits in L2 give the L2 read
+//    bandwidth, a buffer larger than L2 the HBM read bandwidth);
+//  * the failure paths' test hooks: a bounded mbarrier wait made to give up,
+//    a lower cap on the traversal stack, and failed device allocations. None
+//    of them faults, traps or hangs a GPU: each makes the library take the
+//    same error path that a real timeout, overflow or out-of-memory takes.
 
 #include "dr_internal.h"
+#include "mbarrier.cuh"
 
 namespace dr {
 namespace {
@@ -26,10 +31,44 @@ __global__ void __launch_bounds__(256) k_read_stream(const float4 *__restrict__ 
     if (acc == 1234.5678f) sink[0] = acc;  // keeps the loads alive
 }
 
+// One warp waits on phase 0 of an mbarrier that expects one arrival and gets
+// none, with at most `polls` polls of the same bounded wait the product
+// kernels use; when it gives up it reports the timeout as they do. No copy and
+// no MMA is in flight on the barrier.
+__global__ void k_expire_wait(uint32_t polls, uint32_t *error)
+{
+    __shared__ __align__(8) uint64_t bar;
+    const uint32_t b = (uint32_t)__cvta_generic_to_shared(&bar);
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(b) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncwarp();
+    const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(b, 0, polls));
+    if (!ok && threadIdx.x == 0) atomicOr(error, ERR_TIMEOUT);
+}
+
 }  // namespace
 }  // namespace dr
 
 using namespace dr;
+
+extern "C" dr_status dr_debug_expire_wait(dr_context *ctx, uint32_t polls, void *stream)
+{
+    DR_CHECK_ARG(ctx, "dr_debug_expire_wait: NULL context");
+    DR_CUDA(cudaSetDevice(ctx->device));
+    k_expire_wait<<<1, 32, 0, static_cast<cudaStream_t>(stream)>>>(polls, ctx->d_error);
+    DR_CUDA(cudaGetLastError());
+    return DR_OK;
+}
+
+extern "C" dr_status dr_debug_stack_limit(dr_context *ctx, uint32_t entries)
+{
+    DR_CHECK_ARG(ctx, "dr_debug_stack_limit: NULL context");
+    DR_CHECK_ARG(entries <= 64, "dr_debug_stack_limit: at most 64 entries");
+    ctx->stack_limit = entries ? entries : 64;
+    return DR_OK;
+}
 
 extern "C" dr_status dr_probe_read_bandwidth(dr_context *ctx, const void *buf_dev, uint64_t bytes, uint32_t reps,
                                              double *gbs_out, void *stream)

@@ -36,6 +36,17 @@ dr_status cuda_fail(cudaError_t e, const char *what);
         if (!(cond)) return ::dr::fail(DR_ERR_INVALID_ARGUMENT, __VA_ARGS__); \
     } while (0)
 
+// Device allocations of the library go through dev_malloc: cudaMalloc, except
+// that dr_debug_fail_allocation can make the n-th next one fail with
+// cudaErrorMemoryAllocation, so that tests reach every allocation's error path
+// without exhausting a GPU.
+cudaError_t dev_malloc_raw(void **p, size_t bytes);
+template <typename T>
+inline cudaError_t dev_malloc(T **p, size_t bytes)
+{
+    return dev_malloc_raw(reinterpret_cast<void **>(p), bytes);
+}
+
 // Device error word bits (dr_context::d_error), set by kernels instead of
 // trapping; the host maps them to dr_status.
 enum : uint32_t {
@@ -144,11 +155,12 @@ struct dr_context {
     int device = 0;
     int num_sms = 0;
     uint32_t *d_error = nullptr;                // device error word
-    unsigned long long *d_counters = nullptr;   // 8 counters
+    unsigned long long *d_counters = nullptr;   // 8 traversal counters per work counter of the ring
     unsigned long long *d_work = nullptr;       // ring of kWorkCounters persistent-kernel work counters
     std::atomic<uint32_t> work_next{0};         // next counter of the ring
     void *scratch = nullptr;                    // grows on demand (alias builds, staging)
     size_t scratch_bytes = 0;
+    uint32_t stack_limit = 64;                  // 8-wide traversal stack entries (dr_debug_stack_limit)
 };
 
 // Work counters of the public persistent traversal launches: each launch takes

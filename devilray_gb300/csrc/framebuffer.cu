@@ -71,9 +71,9 @@ dr_status dr_framebuffer_create(dr_context *ctx, int32_t width, int32_t height, 
     fb->height = height;
     const size_t n = (size_t)width * height;
     cudaError_t e;
-    if ((e = cudaMalloc(&fb->accum, n * sizeof(float4))) != cudaSuccess ||
-        (e = cudaMalloc(&fb->casts, n * sizeof(uint32_t))) != cudaSuccess ||
-        (e = cudaMalloc(&fb->pixels, n * sizeof(uint32_t))) != cudaSuccess ||
+    if ((e = dev_malloc(&fb->accum, n * sizeof(float4))) != cudaSuccess ||
+        (e = dev_malloc(&fb->casts, n * sizeof(uint32_t))) != cudaSuccess ||
+        (e = dev_malloc(&fb->pixels, n * sizeof(uint32_t))) != cudaSuccess ||
         (e = cudaMemset(fb->accum, 0, n * sizeof(float4))) != cudaSuccess ||
         (e = cudaMemset(fb->casts, 0, n * sizeof(uint32_t))) != cudaSuccess) {
         dr_framebuffer_destroy(fb);
@@ -170,8 +170,8 @@ dr_status dr_alias_build_host(dr_context *ctx, const float *w, uint32_t n, dr_al
     DR_CUDA(cudaSetDevice(ctx->device));
     float *dw = nullptr;
     dr_alias_entry *dt = nullptr;
-    DR_CUDA(cudaMalloc(&dw, (size_t)n * sizeof(float)));
-    cudaError_t e = cudaMalloc(&dt, (size_t)n * sizeof(dr_alias_entry));
+    DR_CUDA(dev_malloc(&dw, (size_t)n * sizeof(float)));
+    cudaError_t e = dev_malloc(&dt, (size_t)n * sizeof(dr_alias_entry));
     if (e == cudaSuccess) e = cudaMemcpy(dw, w, (size_t)n * sizeof(float), cudaMemcpyHostToDevice);
     dr_status st = DR_OK;
     if (e == cudaSuccess) {

@@ -17,6 +17,7 @@
 // summed with atomics.
 
 #include "dr_internal.h"
+#include "mbarrier.cuh"
 #include "guide_math.cuh"
 #include "guide_internal.h"
 
@@ -296,16 +297,7 @@ __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)_
 // Bounded wait on an mbarrier phase; false after the iteration limit.
 __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase)
 {
-    for (uint32_t it = 0; it < (1u << 22); ++it) {
-        uint32_t done;
-        asm volatile(
-            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-            : "=r"(done)
-            : "r"(mbar), "r"(phase)
-            : "memory");
-        if (done) return true;
-    }
-    return false;
+    return mbar_wait_bounded(mbar, phase, kMbarWaitPolls);
 }
 
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
@@ -1163,7 +1155,7 @@ dr_status ensure_train_capacity(dr_guide *g, uint32_t n)
     const uint32_t rows = (n + 63) & ~63u;
     size_t bytes = 0;
     for (int l = 0; l < kLayers; ++l) bytes += (size_t)fan_out(l) * rows * 4 + (size_t)fan_in(l) * rows * 2 + 512;
-    DR_CUDA(cudaMalloc(&g->tb_mem, bytes));
+    DR_CUDA(dev_malloc(&g->tb_mem, bytes));
     char *p = static_cast<char *>(g->tb_mem);
     for (int l = 0; l < kLayers; ++l) {
         g->tb.deltaT[l] = reinterpret_cast<float *>(p);
@@ -1271,9 +1263,9 @@ dr_status dr_guide_create(dr_context *ctx, const dr_guide_config *cfg, dr_guide 
         return fail(DR_ERR_INVALID_ARGUMENT, "dr_guide_create: unknown inference kernel");
     }
     cudaError_t e;
-    if ((e = cudaMalloc(&g->params, kNumParams * 4)) != cudaSuccess || (e = cudaMalloc(&g->m, kNumParams * 4)) != cudaSuccess ||
-        (e = cudaMalloc(&g->v, kNumParams * 4)) != cudaSuccess || (e = cudaMalloc(&g->grad, kNumParams * 4)) != cudaSuccess ||
-        (e = cudaMalloc(&g->wb, kNumWeights * 2)) != cudaSuccess || (e = cudaMalloc(&g->img, kImgBytes)) != cudaSuccess || (e = cudaMalloc(&g->scalars, 16)) != cudaSuccess ||
+    if ((e = dev_malloc(&g->params, kNumParams * 4)) != cudaSuccess || (e = dev_malloc(&g->m, kNumParams * 4)) != cudaSuccess ||
+        (e = dev_malloc(&g->v, kNumParams * 4)) != cudaSuccess || (e = dev_malloc(&g->grad, kNumParams * 4)) != cudaSuccess ||
+        (e = dev_malloc(&g->wb, kNumWeights * 2)) != cudaSuccess || (e = dev_malloc(&g->img, kImgBytes)) != cudaSuccess || (e = dev_malloc(&g->scalars, 16)) != cudaSuccess ||
         (e = cudaMemset(g->m, 0, kNumParams * 4)) != cudaSuccess || (e = cudaMemset(g->v, 0, kNumParams * 4)) != cudaSuccess ||
         (e = cudaMemset(g->scalars, 0, 16)) != cudaSuccess) {
         free_guide(g);

@@ -387,10 +387,10 @@ dr_status build_lbvh_device(dr_scene *s, const float *positions_host, uint32_t n
         cudaFree(children);
         return st;
     };
-    if ((e = cudaMalloc(&pos, (size_t)n * 9 * sizeof(float))) != cudaSuccess ||
-        (e = cudaMalloc(&scratch, words * sizeof(uint32_t))) != cudaSuccess ||
-        (e = cudaMalloc(&boxes, nint * sizeof(Box6))) != cudaSuccess ||
-        (e = cudaMalloc(&children, nint * sizeof(int2))) != cudaSuccess ||
+    if ((e = dev_malloc(&pos, (size_t)n * 9 * sizeof(float))) != cudaSuccess ||
+        (e = dev_malloc(&scratch, words * sizeof(uint32_t))) != cudaSuccess ||
+        (e = dev_malloc(&boxes, nint * sizeof(Box6))) != cudaSuccess ||
+        (e = dev_malloc(&children, nint * sizeof(int2))) != cudaSuccess ||
         (e = cudaMemcpy(pos, positions_host, (size_t)n * 9 * sizeof(float), cudaMemcpyHostToDevice)) != cudaSuccess)
         return done(cuda_fail(e, "device BVH build: allocation"));
     uint32_t *keys = scratch, *vals = keys + n, *keys2 = vals + n, *vals2 = keys2 + n;
@@ -418,13 +418,13 @@ dr_status build_lbvh_device(dr_scene *s, const float *positions_host, uint32_t n
     uint32_t num_nodes = 1;
     uint32_t depth = 1;
     if (n == 1) {
-        if ((e = cudaMalloc(&s->d_nodes, sizeof(Bvh2Node))) != cudaSuccess) return done(cuda_fail(e, "device BVH build"));
+        if ((e = dev_malloc(&s->d_nodes, sizeof(Bvh2Node))) != cudaSuccess) return done(cuda_fail(e, "device BVH build"));
         k_emit_single<<<1, 1>>>(pos, slack, s->d_nodes);
     } else {
         num_nodes = n - 1;
         k_karras<<<grid_for(n - 1, 256), 256>>>(keys, (int)n, children, parent_int, parent_leaf);
         k_boxes<<<grid_for(n, 256), 256>>>(pos, vals, (int)n, children, parent_int, parent_leaf, visits, boxes, heights);
-        if ((e = cudaMalloc(&s->d_nodes, (size_t)num_nodes * sizeof(Bvh2Node))) != cudaSuccess)
+        if ((e = dev_malloc(&s->d_nodes, (size_t)num_nodes * sizeof(Bvh2Node))) != cudaSuccess)
             return done(cuda_fail(e, "device BVH build: nodes"));
         k_emit_nodes<<<grid_for(n - 1, 256), 256>>>(pos, vals, (int)n, children, boxes, slack, s->d_nodes);
         // root height (edges) + 1 = nodes on the longest root-to-leaf path
@@ -433,9 +433,9 @@ dr_status build_lbvh_device(dr_scene *s, const float *positions_host, uint32_t n
         depth += 1;
     }
     s->device_bytes += (size_t)num_nodes * sizeof(Bvh2Node);
-    if ((e = cudaMalloc(&s->d_tri_ref, (size_t)n * 3 * sizeof(float4))) != cudaSuccess ||
-        (e = cudaMalloc(&s->d_tri_wt, (size_t)n * 3 * sizeof(float4))) != cudaSuccess ||
-        (e = cudaMalloc(&s->d_prim, (size_t)n * sizeof(int32_t))) != cudaSuccess)
+    if ((e = dev_malloc(&s->d_tri_ref, (size_t)n * 3 * sizeof(float4))) != cudaSuccess ||
+        (e = dev_malloc(&s->d_tri_wt, (size_t)n * 3 * sizeof(float4))) != cudaSuccess ||
+        (e = dev_malloc(&s->d_prim, (size_t)n * sizeof(int32_t))) != cudaSuccess)
         return done(cuda_fail(e, "device BVH build: records"));
     s->device_bytes += (size_t)n * (2 * 3 * sizeof(float4) + sizeof(int32_t));
     k_records<<<grid_for(n, 256), 256>>>(pos, vals, n, s->d_tri_ref, s->d_tri_wt, s->d_prim);

@@ -262,7 +262,9 @@ __device__ __forceinline__ void persistent_wide(const Wide8Args &a, const Source
             const unsigned waiters = __ballot_sync(FULL, waiting);
             if (nbatch != 0 && (overflow || nbatch >= DR_TRI_BATCH_FLUSH || __popc(waiters) >= DR_TRI_BATCH_WAITERS ||
                                 waiters == __ballot_sync(FULL, active))) {
-                const bool hit = tb_flush<MODE, ANY>(a, *batch, nbatch, phase, s, lane, ct);
+                bool aborted = false;
+                const bool hit = tb_flush<MODE, ANY>(a, *batch, nbatch, phase, s, lane, ct, aborted);
+                if (aborted) break;  // warp-uniform: the staging copies timed out
                 nbatch = 0;
                 if (active && pend != 0) {
                     pend = 0;

@@ -335,7 +335,8 @@ struct ShadowSource {
 template <int MODE, int STACK>
 __global__ void __launch_bounds__(kTraceBlock, kP8MinBlocks) k_wave_closest_p8(RenderParams p, int b)
 {
-    const Wide8Args w{p.trace.nodes8, p.trace.tri_ref, p.trace.tri_wt, p.trace.prim, p.trace.num_nodes, p.trace.error};
+    const Wide8Args w{p.trace.nodes8, p.trace.tri_ref, p.trace.tri_wt, p.trace.prim, p.trace.num_nodes, p.trace.error,
+                      p.trace.stack_limit};
     const PathSource src{p.list[b & 1], p.rays, p.hits, p.slot_job, p.jobs};
     unsigned long long nn = 0, nb = 0, nt = 0, nh = 0;
     persistent_wide<MODE, false, false, DR_TRI_BATCH_PATHS != 0, STACK>(w, src, p.counts[b], p.work + b, nn, nb, nt,
@@ -345,7 +346,8 @@ __global__ void __launch_bounds__(kTraceBlock, kP8MinBlocks) k_wave_closest_p8(R
 template <int MODE, int STACK>
 __global__ void __launch_bounds__(kTraceBlock, kP8MinBlocks) k_wave_shadow_p8(RenderParams p, int b)
 {
-    const Wide8Args w{p.trace.nodes8, p.trace.tri_ref, p.trace.tri_wt, p.trace.prim, p.trace.num_nodes, p.trace.error};
+    const Wide8Args w{p.trace.nodes8, p.trace.tri_ref, p.trace.tri_wt, p.trace.prim, p.trace.num_nodes, p.trace.error,
+                      p.trace.stack_limit};
     const ShadowSource src{p.shadow_list, p.shadow_rays, p.color, p.pending, p.slot_job, p.jobs};
     unsigned long long nn = 0, nb = 0, nt = 0, nh = 0;
     persistent_wide<MODE, true, false, DR_TRI_BATCH_SHADOW != 0, STACK>(w, src, p.counts[64 + b], p.work + 64 + b, nn,
@@ -885,21 +887,21 @@ dr_status WaveRunner::prepare(const std::vector<RenderJob> &jobs, const WavePlan
                 cudaFree(d_wave[k]);
                 d_wave[k] = nullptr;
                 wave_bytes[k] = 0;
-                DR_CUDA(cudaMalloc(&d_wave[k], need));
+                DR_CUDA(dev_malloc(&d_wave[k], need));
                 wave_bytes[k] = need;
             }
         if (jobs.size() > jobs_capacity) {
             cudaFree(d_jobs);
             d_jobs = nullptr;
             jobs_capacity = 0;
-            DR_CUDA(cudaMalloc(&d_jobs, jobs.size() * sizeof(RenderJob)));
+            DR_CUDA(dev_malloc(&d_jobs, jobs.size() * sizeof(RenderJob)));
             jobs_capacity = jobs.size();
         }
         if (plan.segs.size() > segs_capacity) {
             cudaFree(d_segs);
             d_segs = nullptr;
             segs_capacity = 0;
-            DR_CUDA(cudaMalloc(&d_segs, plan.segs.size() * sizeof(WaveSegment)));
+            DR_CUDA(dev_malloc(&d_segs, plan.segs.size() * sizeof(WaveSegment)));
             segs_capacity = plan.segs.size();
         }
         if (train_need > train_cap) {
@@ -907,7 +909,7 @@ dr_status WaveRunner::prepare(const std::vector<RenderJob> &jobs, const WavePlan
             d_train = nullptr;
             train_cap = 0;
             const size_t bytes = (size_t)train_need * 10 * sizeof(float) + 4 * 256;
-            DR_CUDA(cudaMalloc(&d_train, bytes));
+            DR_CUDA(dev_malloc(&d_train, bytes));
             DR_CUDA(cudaMemset(d_train, 0, bytes));
             train_cap = train_need;
         }
@@ -917,7 +919,7 @@ dr_status WaveRunner::prepare(const std::vector<RenderJob> &jobs, const WavePlan
         if (!acc_done[k]) DR_CUDA(cudaEventCreateWithFlags(&acc_done[k], cudaEventDisableTiming));
     }
     if (!fork) DR_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
-    if (!d_totals) DR_CUDA(cudaMalloc(&d_totals, 2 * sizeof(unsigned long long)));
+    if (!d_totals) DR_CUDA(dev_malloc(&d_totals, 2 * sizeof(unsigned long long)));
     // the tables may still be read by the waves of an earlier call
     for (int k = 0; k < kMaxWaveStreams; ++k)
         if (acc_done[k]) DR_CUDA(cudaStreamWaitEvent(st, acc_done[k], 0));
@@ -1040,6 +1042,7 @@ SceneArrays scene_arrays(const dr_scene *s)
     a.trace.prim = s->d_prim;
     a.trace.num_nodes = s->num_nodes;
     a.trace.error = s->ctx->d_error;
+    a.trace.stack_limit = s->ctx->stack_limit;
     a.shade = s->d_shade;
     a.objects = s->d_objects;
     a.materials = s->d_materials;

@@ -35,11 +35,18 @@ cudaError_t upload_vec(T **dst, const std::vector<T> &v, uint64_t &bytes)
 {
     *dst = nullptr;
     if (v.empty()) return cudaSuccess;
-    cudaError_t e = cudaMalloc(reinterpret_cast<void **>(dst), sizeof(T) * v.size());
+    cudaError_t e = dev_malloc(reinterpret_cast<void **>(dst), sizeof(T) * v.size());
     if (e != cudaSuccess) return e;
     bytes += sizeof(T) * v.size();
     return cudaMemcpy(*dst, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice);
 }
+
+// A temporary device buffer freed when it leaves scope (also on error returns).
+template <typename T>
+struct DevTemp {
+    T *p = nullptr;
+    ~DevTemp() { cudaFree(p); }
+};
 
 }  // namespace
 
@@ -136,14 +143,15 @@ dr_status build_render_data(dr_scene *s, const dr_scene_desc *d)
 
     // device builds
     const bool ref_mode = d->light_tables == DR_LIGHT_TABLES_REFERENCE;
-    float *d_w = nullptr, *d_tw = nullptr;
-    uint32_t *d_seg = nullptr;
-    DR_CUDA(cudaMalloc(&s->d_light_table, N * sizeof(dr_alias_entry)));
-    DR_CUDA(cudaMalloc(&s->d_tri_tables, (size_t)std::max(1u, n) * sizeof(dr_alias_entry)));
-    s->device_bytes += N * sizeof(dr_alias_entry) + (size_t)n * sizeof(dr_alias_entry);
+    DevTemp<float> d_w, d_tw;
+    DevTemp<uint32_t> d_seg;
+    DR_CUDA(dev_malloc(&s->d_light_table, N * sizeof(dr_alias_entry)));
+    s->device_bytes += N * sizeof(dr_alias_entry);
+    DR_CUDA(dev_malloc(&s->d_tri_tables, (size_t)std::max(1u, n) * sizeof(dr_alias_entry)));
+    s->device_bytes += (size_t)std::max(1u, n) * sizeof(dr_alias_entry);
     DR_CUDA(cudaMemset(s->d_tri_tables, 0, (size_t)std::max(1u, n) * sizeof(dr_alias_entry)));
-    DR_CUDA(cudaMalloc(&d_w, N * sizeof(float)));
-    DR_CUDA(cudaMemcpy(d_w, weights.data(), N * sizeof(float), cudaMemcpyHostToDevice));
+    DR_CUDA(dev_malloc(&d_w.p, N * sizeof(float)));
+    DR_CUDA(cudaMemcpy(d_w.p, weights.data(), N * sizeof(float), cudaMemcpyHostToDevice));
     // scratch: the object table's build, the reference triangle tables' heaps,
     // and the parallel sweep of the largest triangle table
     size_t need = alias_scratch_bytes((uint32_t)N, ref_mode ? DR_ALIAS_REFERENCE : DR_ALIAS_SWEEP);
@@ -154,41 +162,31 @@ dr_status build_render_data(dr_scene *s, const dr_scene_desc *d)
             big.push_back((uint32_t)k);
             need = std::max(need, alias_scratch_bytes(seg_count[k], DR_ALIAS_SWEEP));
         }
-    dr_status st = ensure_scratch(s->ctx, need);
-    if (st != DR_OK) {
-        cudaFree(d_w);
-        return st;
-    }
-    e = launch_alias_build(d_w, (uint32_t)N, s->d_light_table, ref_mode ? DR_ALIAS_REFERENCE : DR_ALIAS_SWEEP,
-                           s->ctx->scratch, s->ctx->scratch_bytes, s->ctx->num_sms, nullptr);
-    if (e == cudaSuccess) e = cudaDeviceSynchronize();
-    cudaFree(d_w);
-    if (e != cudaSuccess) return cuda_fail(e, "dr_scene_create: light table");
+    const dr_status st = ensure_scratch(s->ctx, need);
+    if (st != DR_OK) return st;
+    DR_CUDA(launch_alias_build(d_w.p, (uint32_t)N, s->d_light_table, ref_mode ? DR_ALIAS_REFERENCE : DR_ALIAS_SWEEP,
+                               s->ctx->scratch, s->ctx->scratch_bytes, s->ctx->num_sms, nullptr));
+    DR_CUDA(cudaDeviceSynchronize());
     if (!seg_begin.empty()) {
-        DR_CUDA(cudaMalloc(&d_tw, (size_t)n * sizeof(float)));
-        DR_CUDA(cudaMemcpy(d_tw, tri_w.data(), (size_t)n * sizeof(float), cudaMemcpyHostToDevice));
+        DR_CUDA(dev_malloc(&d_tw.p, (size_t)n * sizeof(float)));
+        DR_CUDA(cudaMemcpy(d_tw.p, tri_w.data(), (size_t)n * sizeof(float), cudaMemcpyHostToDevice));
         // sweep mode: the one-thread kernel skips the large segments (count 0)
         std::vector<uint32_t> small_count = seg_count;
         for (uint32_t k : big) small_count[k] = 0;
-        DR_CUDA(cudaMalloc(&d_seg, seg_begin.size() * 2 * sizeof(uint32_t)));
-        DR_CUDA(cudaMemcpy(d_seg, seg_begin.data(), seg_begin.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
-        DR_CUDA(cudaMemcpy(d_seg + seg_begin.size(), small_count.data(), small_count.size() * sizeof(uint32_t),
-                           cudaMemcpyHostToDevice));
+        const size_t ns = seg_begin.size();
+        DR_CUDA(dev_malloc(&d_seg.p, ns * 2 * sizeof(uint32_t)));
+        DR_CUDA(cudaMemcpy(d_seg.p, seg_begin.data(), ns * sizeof(uint32_t), cudaMemcpyHostToDevice));
+        DR_CUDA(cudaMemcpy(d_seg.p + ns, small_count.data(), ns * sizeof(uint32_t), cudaMemcpyHostToDevice));
         if (ref_mode)
-            e = launch_alias_ref_segments(d_tw, n, d_seg, d_seg + seg_begin.size(), (uint32_t)seg_begin.size(),
-                                          s->d_tri_tables, s->ctx->scratch, s->ctx->scratch_bytes, nullptr);
+            DR_CUDA(launch_alias_ref_segments(d_tw.p, n, d_seg.p, d_seg.p + ns, (uint32_t)ns, s->d_tri_tables,
+                                              s->ctx->scratch, s->ctx->scratch_bytes, nullptr));
         else
-            e = launch_alias_sweep_segments(d_tw, d_seg, d_seg + seg_begin.size(), (uint32_t)seg_begin.size(),
-                                            s->d_tri_tables, nullptr);
-        for (size_t k = 0; k < big.size() && e == cudaSuccess; ++k) {
-            const uint32_t b = seg_begin[big[k]], c = seg_count[big[k]];
-            e = launch_alias_build(d_tw + b, c, s->d_tri_tables + b, DR_ALIAS_SWEEP, s->ctx->scratch,
-                                   s->ctx->scratch_bytes, s->ctx->num_sms, nullptr);
-        }
-        if (e == cudaSuccess) e = cudaDeviceSynchronize();
-        cudaFree(d_tw);
-        cudaFree(d_seg);
-        if (e != cudaSuccess) return cuda_fail(e, "dr_scene_create: triangle tables");
+            DR_CUDA(launch_alias_sweep_segments(d_tw.p, d_seg.p, d_seg.p + ns, (uint32_t)ns, s->d_tri_tables, nullptr));
+        for (uint32_t k : big)
+            DR_CUDA(launch_alias_build(d_tw.p + seg_begin[k], seg_count[k], s->d_tri_tables + seg_begin[k],
+                                       DR_ALIAS_SWEEP, s->ctx->scratch, s->ctx->scratch_bytes, s->ctx->num_sms,
+                                       nullptr));
+        DR_CUDA(cudaDeviceSynchronize());
     }
     return DR_OK;
 }

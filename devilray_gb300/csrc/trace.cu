@@ -76,7 +76,7 @@ k_trace_any(TraceArgs a)
 template <int MODE, bool COUNT>
 __global__ void __launch_bounds__(kTraceBlock, kP8MinBlocks) k_trace_closest_p8(TraceArgs a)
 {
-    const Wide8Args w{a.nodes8, a.tri_ref, a.tri_wt, a.prim, a.num_nodes, a.error};
+    const Wide8Args w{a.nodes8, a.tri_ref, a.tri_wt, a.prim, a.num_nodes, a.error, a.stack_limit};
     const DirectSource src{a.rays, a.hits, nullptr, scene_root(a.num_nodes)};
     unsigned long long nn = 0, nb = 0, nt = 0, nh = 0;
     persistent_wide<MODE, false, COUNT, DR_TRI_BATCH_CLOSEST != 0>(w, src, a.n, a.work, nn, nb, nt, nh);
@@ -86,7 +86,7 @@ __global__ void __launch_bounds__(kTraceBlock, kP8MinBlocks) k_trace_closest_p8(
 template <int MODE>
 __global__ void __launch_bounds__(kTraceBlock, kP8MinBlocks) k_trace_any_p8(TraceArgs a)
 {
-    const Wide8Args w{a.nodes8, a.tri_ref, a.tri_wt, a.prim, a.num_nodes, a.error};
+    const Wide8Args w{a.nodes8, a.tri_ref, a.tri_wt, a.prim, a.num_nodes, a.error, a.stack_limit};
     const DirectSource src{a.rays, nullptr, a.occluded, scene_root(a.num_nodes)};
     unsigned long long nn = 0, nb = 0, nt = 0, nh = 0;
     persistent_wide<MODE, true, false, DR_TRI_BATCH_ANY != 0>(w, src, a.n, a.work, nn, nb, nt, nh);

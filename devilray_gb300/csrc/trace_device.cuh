@@ -137,7 +137,7 @@ __device__ __forceinline__ void scene_closest(const TraceArgs &a, const DevRay &
                                               int32_t &best_prim, TraceStats &st)
 {
     if (LAYOUT == 8) {
-        const Wide8Args w{a.nodes8, a.tri_ref, a.tri_wt, a.prim, a.num_nodes, a.error};
+        const Wide8Args w{a.nodes8, a.tri_ref, a.tri_wt, a.prim, a.num_nodes, a.error, a.stack_limit};
         if (COUNT) wide_traverse<MODE, false>(w, r, root, best_t, best_prim, &st.nodes, &st.boxes, &st.tris);
         else wide_traverse<MODE, false>(w, r, root, best_t, best_prim, nullptr, nullptr, nullptr);
     } else {
@@ -149,7 +149,7 @@ template <int MODE, int LAYOUT>
 __device__ __forceinline__ bool scene_any(const TraceArgs &a, const DevRay &r, uint32_t root)
 {
     if (LAYOUT == 8) {
-        const Wide8Args w{a.nodes8, a.tri_ref, a.tri_wt, a.prim, a.num_nodes, a.error};
+        const Wide8Args w{a.nodes8, a.tri_ref, a.tri_wt, a.prim, a.num_nodes, a.error, a.stack_limit};
         float t;
         int32_t prim;
         return wide_traverse<MODE, true>(w, r, root, t, prim, nullptr, nullptr, nullptr);

@@ -23,6 +23,7 @@ struct TraceArgs {
     uint32_t *error;
     unsigned long long *work;  // persistent-kernel ray counter (zeroed before each launch)
     int num_sms;
+    uint32_t stack_limit;      // 8-wide traversal stack entries (<= kWideStack)
 };
 
 // Launch helpers dispatch on a.layout (2 or 8) and the triangle mode.

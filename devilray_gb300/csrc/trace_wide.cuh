@@ -31,6 +31,7 @@ struct Wide8Args {
     const int32_t *prim;
     uint32_t num_nodes;
     uint32_t *error;
+    uint32_t stack_limit;  // stack entries a ray may use (kWideStack; lower only for tests)
 };
 
 constexpr int kWideStack = 64;
@@ -392,7 +393,7 @@ __device__ __forceinline__ bool wide_advance(const Wide8Args &a, WideState &s, S
     s.have_node = true;
     s.group.y = (rest << 8) | imask;
     if (rest) {
-        if (s.sp >= kWideStack) {
+        if ((uint32_t)s.sp >= a.stack_limit) {
             atomicOr(a.error, ERR_STACK_OVERFLOW);
             return true;
         }
@@ -471,7 +472,7 @@ __host__ __device__ __forceinline__ bool wide_traverse(const Wide8Args &a, const
         have_node = true;
         group.y = (rest << 8) | imask;
         if (rest) {
-            if (sp >= kWideStack) {
+            if ((uint32_t)sp >= a.stack_limit) {
 #if defined(__CUDA_ARCH__)
                 atomicOr(a.error, ERR_STACK_OVERFLOW);
 #endif

@@ -11,6 +11,7 @@
 // tested, and the minimum over pairs does not depend on the order.
 #pragma once
 
+#include "mbarrier.cuh"
 #include "trace_wide.cuh"
 
 namespace dr {
@@ -68,33 +69,33 @@ __device__ __forceinline__ void tb_append(TriBatch &B, const float4 *recs, uint3
     }
 }
 
-// Bounded wait for the staging copies of the current phase.
+// Bounded wait of the whole warp for the staging copies of the current phase
+// (one decision for the warp).
 __device__ __forceinline__ bool tb_wait(TriBatch &B, uint32_t phase)
 {
-    const uint32_t bar = smem_u32(&B.bar);
-    for (uint32_t it = 0; it < (1u << 22); ++it) {
-        uint32_t done;
-        asm volatile(
-            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-            : "=r"(done)
-            : "r"(bar), "r"(phase)
-            : "memory");
-        if (done) return true;
-    }
-    return false;
+    return __all_sync(0xffffffffu, mbar_wait_bounded(smem_u32(&B.bar), phase, kMbarWaitPolls));
 }
 
 // Tests the batch's n pairs, one per lane. Closest hit: each owner lane's
 // (best_t, best_prim) takes the smallest (t, index) of its pairs. Any hit:
-// returns true for owner lanes with a hit. `phase` flips.
+// returns true for owner lanes with a hit. `phase` flips. If the staging
+// copies do not land within the wait's limit, the warp sets ERR_TIMEOUT,
+// waits once more (bounded) so that no copy is left writing its shared
+// memory, tests nothing and sets `aborted`: the caller stops the warp (the
+// rays it held keep no result; the call reports DR_ERR_TIMEOUT).
 template <int MODE, bool ANY>
 __device__ __forceinline__ bool tb_flush(const Wide8Args &a, TriBatch &B, uint32_t n, uint32_t &phase, WideState &s,
-                                         int lane, unsigned long long &nt)
+                                         int lane, unsigned long long &nt, bool &aborted)
 {
     constexpr unsigned FULL = 0xffffffffu;
     __syncwarp();
     if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(&B.bar)) : "memory");
-    if (!tb_wait(B, phase) && lane == 0) atomicOr(a.error, ERR_TIMEOUT);
+    if (!tb_wait(B, phase)) {
+        if (lane == 0) atomicOr(a.error, ERR_TIMEOUT);
+        tb_wait(B, phase);
+        aborted = true;
+        return false;
+    }
     phase ^= 1u;
     const bool have = (uint32_t)lane < n;
     const int owner = have ? (int)B.owner[lane] : lane;

@@ -209,6 +209,9 @@ SIGNATURES = {
                                   C.c_void_p]),
     "dr_probe_read_bandwidth": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_uint32, C.POINTER(C.c_double),
                                           C.c_void_p]),
+    "dr_debug_expire_wait": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p]),
+    "dr_debug_stack_limit": (C.c_int, [C.c_void_p, C.c_uint32]),
+    "dr_debug_fail_allocation": (C.c_int, [C.c_uint32]),
 }
 
 _lib = None

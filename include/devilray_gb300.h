@@ -513,8 +513,9 @@ dr_status dr_alias_build_host(dr_context *ctx, const float *weights_host, uint32
  * a fixed array inside the library (about 2.6 MB on every GPU that loads it),
  * so n is limited to 65,536 weights (DR_ERR_TOO_LARGE above that). Needs no
  * context: it runs on the current device. The first call on a device sets up
- * the array's device address; make it before any stream capture. All calls
- * share the array: calls whose work overlaps on the GPU race. */
+ * the array's device address; make it before any stream capture, and do not
+ * reset the device (cudaDeviceReset) after it. All calls share the array:
+ * calls whose work overlaps on the GPU race. */
 dr_status dr_alias_build_noalloc(const float *weights_dev, uint32_t n, dr_alias_entry *table_dev, void *stream);
 
 /* ---- diagnostics ------------------------------------------------------------------- */
@@ -526,6 +527,32 @@ dr_status dr_alias_build_noalloc(const float *weights_dev, uint32_t n, dr_alias_
  * denominator. Synchronous. */
 dr_status dr_probe_read_bandwidth(dr_context *ctx, const void *buf_dev, uint64_t bytes, uint32_t reps,
                                   double *gbs_out, void *stream);
+
+/* ---- failure-path test hooks -------------------------------------------------------- */
+/* No counterpart in the reference, which exits the process on any CUDA error
+ * (src/device/DevUtils.cu:12-22). These make the library take the error paths
+ * that a real timeout, stack overflow or out-of-memory takes, without faulting,
+ * trapping or hanging a GPU, so that tests can check the statuses. */
+
+/* One warp waits, with at most `polls` polls, on an mbarrier phase that
+ * nothing completes (no copy or MMA in flight on it), through the same
+ * bounded wait as the traversal and guiding kernels; giving up, it sets the
+ * context's timeout bit as they do. The next dr_context_check or
+ * dr_synchronize returns DR_ERR_TIMEOUT and clears it; the context stays
+ * usable. Asynchronous on `stream`. */
+dr_status dr_debug_expire_wait(dr_context *ctx, uint32_t polls, void *stream);
+
+/* Caps the stack of the context's 8-wide traversals at `entries` (1..64;
+ * 0 restores 64, the size the builders' depth limit never exceeds). A ray
+ * that needs more stops and sets the stack-overflow bit (reported as
+ * DR_ERR_STACK_OVERFLOW); its hit is not valid. */
+dr_status dr_debug_stack_limit(dr_context *ctx, uint32_t entries);
+
+/* Makes the `after`-th next device allocation of the library (after = 1:
+ * the next one) fail as cudaMalloc does when the device is out of memory;
+ * 0 turns it off. Process-wide. The failing call returns DR_ERR_OUT_OF_MEMORY
+ * and frees what it had allocated. */
+dr_status dr_debug_fail_allocation(uint32_t after);
 
 /* ---- version ----------------------------------------------------------------------- */
 

@@ -49,6 +49,28 @@ def test_noalloc_matches_allocating_build_twice(native, ctx):
         assert got.tobytes() == want.tobytes()
 
 
+def test_noalloc_allocates_no_device_memory(native, ctx):
+    """After the first call (which only looks up the array's address), further
+    calls leave the device's free memory unchanged; one of them runs on a
+    non-default stream and still equals the allocating build."""
+    rng = np.random.default_rng(7)
+    w = rng.lognormal(0.0, 1.0, 40000).astype(np.float32)
+    dw = torch.from_numpy(w).cuda()
+    out = torch.zeros(40000 * 5, dtype=torch.int32, device="cuda")
+    lib = native.load()
+    native.check(lib.dr_alias_build_noalloc(dw.data_ptr(), 40000, out.data_ptr(), None))
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    s = torch.cuda.Stream()
+    for _ in range(3):
+        native.check(lib.dr_alias_build_noalloc(dw.data_ptr(), 40000, out.data_ptr(), s.cuda_stream))
+    s.synchronize()
+    free1 = torch.cuda.mem_get_info()[0]
+    assert free1 == free0, f"free device memory changed by {free0 - free1} bytes"
+    got = out.cpu().numpy().view(native.ALIAS_DTYPE)
+    assert got.tobytes() == _allocating(native, ctx, dw, 40000).tobytes()
+
+
 def test_noalloc_rejects_sizes_beyond_its_limit(native):
     w = torch.ones(65537, dtype=torch.float32, device="cuda")
     out = torch.zeros(65537 * 5, dtype=torch.int32, device="cuda")
