@@ -363,6 +363,338 @@ __global__ void k_records(const float *pos, const uint32_t *order, uint32_t n, f
     prim[k] = (int32_t)t;
 }
 
+// ---- compressed 8-wide hierarchy: collapse of the radix tree ---------------------
+//
+// The collapse of the host build (bvh_build.cpp, WideBuilder), run on the
+// device over the radix tree: a bottom-up pass gives every binary node its
+// box and, by dynamic programming over (subtree, slots), the least surface-
+// area cost of placing the subtree in at most j child slots of a wide node
+// (Ylitie, Karras and Laine, HPG 2017); a top-down pass, one kernel pair per
+// level of wide nodes, writes the 80-byte nodes breadth first. Each level
+// counts its nodes' internal children and leaf triangles, scans the counts
+// (so the layout does not depend on thread timing) and then writes the nodes,
+// the next level's work list and the triangle order.
+
+constexpr float kWideLeafTriCost = 1.0f;
+constexpr uint32_t kWideMaxLeafTris = 3;
+
+struct WideDp {
+    float cost[8];     // cost[j - 1]: least cost of the subtree in at most j slots
+    int8_t split[8];   // split[j - 1]: the left child's share when the node is opened, 0 = one slot
+    uint8_t tris;      // triangles of the subtree, counted up to 4
+    uint8_t wide_leaf; // its one slot is a leaf slot (else an internal wide node)
+    uint8_t pad[2];
+};
+
+__device__ __forceinline__ float box_area(const Box6 &b)
+{
+    const float dx = b.hi[0] - b.lo[0], dy = b.hi[1] - b.lo[1], dz = b.hi[2] - b.lo[2];
+    if (!(dx >= 0 && dy >= 0 && dz >= 0)) return 0.0f;
+    return 2.0f * (dx * dy + dy * dz + dz * dx);
+}
+
+// The DP entry of a radix-tree leaf (one triangle).
+__device__ __forceinline__ WideDp leaf_dp(const Box6 &b)
+{
+    WideDp d;
+    const float c = kWideLeafTriCost * box_area(b);
+    for (int j = 0; j < 8; ++j) {
+        d.cost[j] = c;
+        d.split[j] = 0;
+    }
+    d.tris = 1;
+    d.wide_leaf = 1;
+    return d;
+}
+
+__device__ __forceinline__ WideDp load_dp(const WideDp *dp, int i)
+{
+    WideDp d;
+    const uint4 *p = reinterpret_cast<const uint4 *>(dp + i);
+    uint4 v[3];
+    for (int k = 0; k < 3; ++k) v[k] = __ldcg(p + k);
+    memcpy(&d, v, sizeof(WideDp));
+    return d;
+}
+
+// Bottom-up boxes and collapse costs (k_boxes plus the DP of WideBuilder::solve).
+__global__ void k_boxes_dp(const float *pos, const uint32_t *order, int n, const int2 *children, const int *parent_int,
+                           const int *parent_leaf, uint32_t *visits, Box6 *boxes, uint32_t *height, WideDp *dp)
+{
+    const int leaf = blockIdx.x * blockDim.x + threadIdx.x;
+    if (leaf >= n) return;
+    int node = parent_leaf[leaf];
+    while (node >= 0) {
+        __threadfence();
+        if (atomicAdd(visits + node, 1u) == 0) return;  // the other child is not done yet
+        __threadfence();
+        const int2 c = children[node];
+        const Box6 ba = c.x < 0 ? tri_box(pos, order[~c.x]) : load_box(boxes, c.x);
+        const Box6 bb = c.y < 0 ? tri_box(pos, order[~c.y]) : load_box(boxes, c.y);
+        const WideDp l = c.x < 0 ? leaf_dp(ba) : load_dp(dp, c.x);
+        const WideDp r = c.y < 0 ? leaf_dp(bb) : load_dp(dp, c.y);
+        Box6 u = ba;
+        for (int k = 0; k < 3; ++k) {
+            u.lo[k] = fminf(u.lo[k], bb.lo[k]);
+            u.hi[k] = fmaxf(u.hi[k], bb.hi[k]);
+        }
+        const float A = box_area(u);
+        WideDp d;
+        d.tris = (uint8_t)min(l.tris + r.tris, 4);
+        float open[9];
+        int8_t open_split[9];
+        for (int j = 2; j <= 8; ++j) {
+            open[j] = INFINITY;
+            open_split[j] = 1;
+            for (int k = 1; k < j; ++k) {
+                const float cst = l.cost[k - 1] + r.cost[j - k - 1];
+                if (cst < open[j]) {
+                    open[j] = cst;
+                    open_split[j] = (int8_t)k;
+                }
+            }
+        }
+        float one = A + open[8];
+        d.wide_leaf = 0;
+        if (d.tris <= kWideMaxLeafTris && kWideLeafTriCost * (float)d.tris * A <= one) {
+            one = kWideLeafTriCost * (float)d.tris * A;
+            d.wide_leaf = 1;
+        }
+        d.cost[0] = one;
+        d.split[0] = 0;
+        for (int j = 2; j <= 8; ++j) {
+            const bool opened = open[j] < one;
+            d.cost[j - 1] = opened ? open[j] : one;
+            d.split[j - 1] = opened ? open_split[j] : (int8_t)0;
+        }
+        d.pad[0] = d.pad[1] = 0;
+        const uint32_t ha = c.x < 0 ? 0u : __ldcg(height + c.x), hb = c.y < 0 ? 0u : __ldcg(height + c.y);
+        boxes[node] = u;
+        dp[node] = d;
+        height[node] = 1u + max(ha, hb);
+        node = node == 0 ? -1 : parent_int[node];
+    }
+}
+
+// The child slots of the wide node of internal radix node `node` (WideBuilder::
+// collect / expand): up to 8 radix subtrees, internal (>= 0) or leaves (< 0).
+__device__ int wide_children(int node, const int2 *children, const WideDp *dp, int out[8])
+{
+    const int2 c = children[node];
+    auto cost = [&](int x, int j) {  // cost of subtree x in j slots
+        if (x >= 0) return dp[x].cost[j - 1];
+        return 0.0f;  // a radix leaf costs the same for every j: the split does not depend on it
+    };
+    int k_best = 1;
+    float best = INFINITY;
+    for (int k = 1; k < 8; ++k) {
+        const float v = (c.x >= 0 ? cost(c.x, k) : 0.0f) + (c.y >= 0 ? cost(c.y, 8 - k) : 0.0f);
+        if (v < best) {
+            best = v;
+            k_best = k;
+        }
+    }
+    // explicit stack of (subtree, slots), expanded left first
+    int st_node[16], st_j[16], sp = 0, m = 0;
+    st_node[sp] = c.y, st_j[sp++] = 8 - k_best;
+    st_node[sp] = c.x, st_j[sp++] = k_best;
+    while (sp > 0) {
+        --sp;
+        const int x = st_node[sp], j = st_j[sp];
+        const int8_t sp_j = x >= 0 ? dp[x].split[j - 1] : (int8_t)0;
+        if (x < 0 || sp_j == 0) {
+            out[m++] = x;
+            continue;
+        }
+        const int2 cc = children[x];
+        st_node[sp] = cc.y, st_j[sp++] = j - sp_j;
+        st_node[sp] = cc.x, st_j[sp++] = sp_j;
+    }
+    return m;
+}
+
+__device__ __forceinline__ bool is_wide_leaf(int x, const WideDp *dp) { return x < 0 || dp[x].wide_leaf; }
+__device__ __forceinline__ uint32_t wide_tris(int x, const WideDp *dp) { return x < 0 ? 1u : dp[x].tris; }
+
+// Per task of the level: internal children and leaf triangles of its wide node.
+__global__ void k_wide_count(const int *tasks, uint32_t ntasks, const int2 *children, const WideDp *dp,
+                             uint32_t *cnt_nodes, uint32_t *cnt_tris)
+{
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntasks) return;
+    int ch[8];
+    const int m = wide_children(tasks[t], children, dp, ch);
+    uint32_t ni = 0, nt = 0;
+    for (int k = 0; k < m; ++k) {
+        if (is_wide_leaf(ch[k], dp)) nt += wide_tris(ch[k], dp);
+        else ++ni;
+    }
+    cnt_nodes[t] = ni;
+    cnt_tris[t] = nt;
+}
+
+// Triangles of radix subtree x (at most 3) in leaf order.
+__device__ int subtree_tris(int x, const int2 *children, const uint32_t *order, uint32_t out[3])
+{
+    int stack[8], sp = 0, m = 0;
+    stack[sp++] = x;
+    while (sp > 0 && m < 3) {
+        const int y = stack[--sp];
+        if (y < 0) {
+            out[m++] = order[~y];
+            continue;
+        }
+        const int2 c = children[y];
+        stack[sp++] = c.y;
+        stack[sp++] = c.x;
+    }
+    return m;
+}
+
+__device__ __forceinline__ Box6 subtree_box(int x, const float *pos, const uint32_t *order, const Box6 *boxes)
+{
+    return x < 0 ? tri_box(pos, order[~x]) : boxes[x];
+}
+
+// Writes the wide node of each task of the level (the host emit's encoding).
+__global__ void k_wide_emit(const float *pos, const uint32_t *order, const int *tasks, const uint32_t *task_node,
+                            uint32_t ntasks, const int2 *children, const WideDp *dp, const Box6 *boxes,
+                            const uint32_t *scan_nodes, const uint32_t *scan_tris, uint32_t node_base,
+                            uint32_t tri_base0, float slack, Bvh8Node *nodes, int *next_tasks,
+                            uint32_t *next_task_node, uint32_t *order8)
+{
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntasks) return;
+    int ch[8];
+    const int m = wide_children(tasks[t], children, dp, ch);
+    Box6 cb[8], u;
+    for (int a = 0; a < 3; ++a) {
+        u.lo[a] = INFINITY;
+        u.hi[a] = -INFINITY;
+    }
+    for (int k = 0; k < m; ++k) {
+        const Box6 b = subtree_box(ch[k], pos, order, boxes);
+        for (int a = 0; a < 3; ++a) {
+            cb[k].lo[a] = widen_down(b.lo[a], slack);
+            cb[k].hi[a] = widen_up(b.hi[a], slack);
+            u.lo[a] = fminf(u.lo[a], cb[k].lo[a]);
+            u.hi[a] = fmaxf(u.hi[a], cb[k].hi[a]);
+        }
+    }
+    // octant slots: greedily the (child, slot) pair whose centroid lies
+    // furthest towards the slot's corner, ties to the earlier pair
+    int child_in[8];
+    bool used[8];
+    for (int s = 0; s < 8; ++s) child_in[s] = -1;
+    for (int k = 0; k < 8; ++k) used[k] = k >= m;
+    float pc[3];
+    for (int a = 0; a < 3; ++a) pc[a] = 0.5f * (u.lo[a] + u.hi[a]);
+    for (int round = 0; round < m; ++round) {
+        float best = -INFINITY;
+        int bc = -1, bs = -1;
+        for (int k = 0; k < m; ++k) {
+            if (used[k]) continue;
+            for (int sl = 0; sl < 8; ++sl) {
+                if (child_in[sl] >= 0) continue;
+                float v = 0.0f;
+                for (int a = 0; a < 3; ++a) {
+                    const float d = ((sl >> a) & 1) ? 1.0f : -1.0f;
+                    v += d * (0.5f * (cb[k].lo[a] + cb[k].hi[a]) - pc[a]);
+                }
+                if (bc < 0 || v > best) {
+                    best = v;
+                    bc = k;
+                    bs = sl;
+                }
+            }
+        }
+        used[bc] = true;
+        child_in[bs] = bc;
+    }
+    // quantisation grid
+    uint32_t ebias[3];
+    double scale[3];
+    for (int a = 0; a < 3; ++a) {
+        const double ext = (double)u.hi[a] - (double)u.lo[a];
+        int e = -100;
+        if (ext > 0.0) e = (int)ceil(log2(ext / 255.0));
+        while (ldexp(255.0, e) < ext) ++e;
+        e = max(-126, min(127, e));
+        ebias[a] = (uint32_t)(e + 127);
+        scale[a] = ldexp(1.0, e);
+    }
+    uint32_t qlo[3][2] = {}, qhi[3][2] = {}, meta[2] = {0u, 0u};
+    for (int a = 0; a < 3; ++a) qlo[a][0] = qlo[a][1] = 0xffffffffu;  // empty slots: lo 255, hi 0
+    uint32_t imask = 0, tri_off = 0, next_child = 0;
+    const uint32_t child_base = node_base + scan_nodes[t];
+    const uint32_t tri_base = tri_base0 + scan_tris[t];
+    for (int sl = 0; sl < 8; ++sl) {
+        const int k = child_in[sl];
+        if (k < 0) continue;
+        const int w = sl >> 2, sh = 8 * (sl & 3);
+        for (int a = 0; a < 3; ++a) {
+            const double lo = floor(((double)cb[k].lo[a] - (double)u.lo[a]) / scale[a]);
+            const double hi = ceil(((double)cb[k].hi[a] - (double)u.lo[a]) / scale[a]);
+            const uint32_t ql = (uint32_t)fmax(0.0, fmin(255.0, lo)), qh = (uint32_t)fmax(0.0, fmin(255.0, hi));
+            qlo[a][w] = (qlo[a][w] & ~(0xffu << sh)) | (ql << sh);
+            qhi[a][w] |= qh << sh;
+        }
+        const int x = ch[k];
+        uint32_t mt = 0;
+        if (!is_wide_leaf(x, dp)) {
+            imask |= 1u << sl;
+            mt = 0x20u | (24u + (uint32_t)sl);
+            const uint32_t slot = scan_nodes[t] + next_child;  // position in the next level's work list
+            next_tasks[slot] = x;
+            next_task_node[slot] = child_base + next_child;
+            ++next_child;
+        } else {
+            uint32_t tr[3];
+            const int nt = subtree_tris(x, children, order, tr);
+            for (int q = 0; q < nt; ++q) order8[tri_base + tri_off + q] = tr[q];
+            mt = ((((1u << nt) - 1u) << 5) | tri_off);
+            tri_off += (uint32_t)nt;
+        }
+        meta[w] |= mt << sh;
+    }
+    Bvh8Node nd;
+    nd.w[0] = make_uint4(__float_as_uint(u.lo[0]), __float_as_uint(u.lo[1]), __float_as_uint(u.lo[2]),
+                         ebias[0] | (ebias[1] << 8) | (ebias[2] << 16) | (imask << 24));
+    nd.w[1] = make_uint4(child_base, tri_base, meta[0], meta[1]);
+    for (int a = 0; a < 3; ++a) nd.w[2 + a] = make_uint4(qlo[a][0], qlo[a][1], qhi[a][0], qhi[a][1]);
+    nodes[task_node[t]] = nd;
+}
+
+// A one-triangle scene: a root whose slot 0 is the triangle's leaf.
+__global__ void k_wide_single(const float *pos, float slack, Bvh8Node *nodes, uint32_t *order8)
+{
+    const Box6 b = tri_box(pos, 0);
+    Box6 cb;
+    for (int a = 0; a < 3; ++a) {
+        cb.lo[a] = widen_down(b.lo[a], slack);
+        cb.hi[a] = widen_up(b.hi[a], slack);
+    }
+    uint32_t ebias[3], ql[3], qh[3];
+    for (int a = 0; a < 3; ++a) {
+        const double ext = (double)cb.hi[a] - (double)cb.lo[a];
+        int e = -100;
+        if (ext > 0.0) e = (int)ceil(log2(ext / 255.0));
+        while (ldexp(255.0, e) < ext) ++e;
+        e = max(-126, min(127, e));
+        ebias[a] = (uint32_t)(e + 127);
+        const double sc = ldexp(1.0, e);
+        ql[a] = 0;
+        qh[a] = (uint32_t)fmax(0.0, fmin(255.0, ceil(((double)cb.hi[a] - (double)cb.lo[a]) / sc)));
+    }
+    Bvh8Node nd;
+    nd.w[0] = make_uint4(__float_as_uint(cb.lo[0]), __float_as_uint(cb.lo[1]), __float_as_uint(cb.lo[2]),
+                         ebias[0] | (ebias[1] << 8) | (ebias[2] << 16));
+    nd.w[1] = make_uint4(1u, 0u, 0x20u, 0u);  // slot 0: one triangle at offset 0
+    for (int a = 0; a < 3; ++a) nd.w[2 + a] = make_uint4(0xffffff00u | ql[a], 0xffffffffu, qh[a], 0u);
+    nodes[0] = nd;
+    order8[0] = 0;
+}
+
 unsigned grid_for(uint64_t n, unsigned block) { return (unsigned)std::max<uint64_t>(1, (n + block - 1) / block); }
 
 }  // namespace

@@ -18,7 +18,9 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 ORACLE_SO = HERE / "lib" / "liboracle.so"
 REF_SO = HERE / "_ref" / "libref_harness.so"
-REF_ROOT = Path(os.environ.get("DEVILRAY_REF_ROOT", "/root/reference"))
+# The DevilRay source tree: DEVILRAY_REF_ROOT when set, else the location
+# oracle/Makefile names (the recipe that reads the sources there).
+REF_ROOT_ENV = os.environ.get("DEVILRAY_REF_ROOT")
 
 _f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
 _i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
@@ -32,12 +34,13 @@ ALIAS_DTYPE = np.dtype([("p_A", "<f4"), ("pdf_A", "<f4"), ("pdf_B", "<f4"), ("A"
 def build(ref: bool | None = None, quiet: bool = True) -> None:
     """Compiles liboracle.so (and the reference harness when the sources exist)."""
     targets = ["all"]
+    root = [f"REF_ROOT={REF_ROOT_ENV}"] if REF_ROOT_ENV else []
     if ref is None:
-        ref = (REF_ROOT / "include" / "Utils.hpp").exists()
+        probe = subprocess.run(["make", "-s", "-C", str(HERE), *root, "ref-present"], capture_output=True, text=True)
+        ref = probe.returncode == 0 and probe.stdout.strip() == "yes"
     if ref:
         targets.append("ref")
-    out = subprocess.run(["make", "-C", str(HERE), f"REF_ROOT={REF_ROOT}", "-j4", *targets],
-                         capture_output=True, text=True)
+    out = subprocess.run(["make", "-C", str(HERE), *root, "-j4", *targets], capture_output=True, text=True)
     if out.returncode != 0:
         raise RuntimeError(f"oracle build failed:\n{out.stdout}\n{out.stderr}")
 
@@ -285,6 +288,39 @@ def ref_alias_build(weights) -> np.ndarray:
     out = np.zeros(n, ALIAS_DTYPE)
     out["p_A"], out["pdf_A"], out["pdf_B"], out["A"], out["B"] = pA, pdfA, pdfB, A, B
     return out
+
+
+def ref_mesh_load(path: str, normalize: bool = False):
+    """The reference's loadMesh (then normalizeMeshSize and
+    generateCoarseNormals when `normalize`): dict of points [n, 3], normals
+    [m, 3], triangles [k, 6] (a.pi, a.ni, b.pi, b.ni, c.pi, c.ni) and name, or
+    None when it throws."""
+    L = ref()
+    if not getattr(L, "_mesh_bound", False):
+        L.refh_mesh_load.argtypes = [C.c_char_p, C.c_char_p, C.c_int]
+        L.refh_mesh_load.restype = C.c_void_p
+        L.refh_mesh_free.argtypes = [C.c_void_p]
+        L.refh_mesh_sizes.argtypes = [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        L.refh_mesh_export.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_char_p, C.c_int]
+        L.refh_mesh_normalize_and_coarse_normals.argtypes = [C.c_void_p]
+        L._mesh_bound = True
+    err = C.create_string_buffer(512)
+    h = L.refh_mesh_load(path.encode(), err, 512)
+    if not h:
+        return None
+    try:
+        if normalize:
+            L.refh_mesh_normalize_and_coarse_normals(h)
+        np_, nn, nt = C.c_int(), C.c_int(), C.c_int()
+        L.refh_mesh_sizes(h, C.byref(np_), C.byref(nn), C.byref(nt))
+        pts = np.zeros((np_.value, 3), np.float32)
+        nrm = np.zeros((nn.value, 3), np.float32)
+        tri = np.zeros((nt.value, 6), np.uint32)
+        name = C.create_string_buffer(256)
+        L.refh_mesh_export(h, pts.ctypes.data, nrm.ctypes.data, tri.ctypes.data, name, 256)
+    finally:
+        L.refh_mesh_free(h)
+    return {"points": pts, "normals": nrm, "triangles": tri, "name": np.array(name.value.decode())}
 
 
 def ref_lognormal(n: int, seed: int = 42) -> np.ndarray:

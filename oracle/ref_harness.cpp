@@ -19,6 +19,10 @@
 #include "tracing/LightSampling.hpp"
 #include "tracing/DistributionSamplers.hpp"
 #include "models/BBH.hpp"
+#include "models/Mesh.hpp"
+
+#include <stdexcept>
+#include <string>
 
 // Replays caller-provided uniforms through the `.rnd()` interface the
 // reference samplers are templated on (test/src/TracingTestHelpers.hpp:45-57).
@@ -343,6 +347,64 @@ void refh_render_samples(const float *pos, const int *obj_begin, const int *obj_
             }
             casts_out[pix] = casts;
         }
+}
+
+// ---- OBJ loading (src/models/Mesh.cpp) ------------------------------------------
+
+// loadMesh on `path`; NULL when it throws, with the message in `err`.
+void *refh_mesh_load(const char *path, char *err, int err_cap)
+{
+    try {
+        return new Mesh(loadMesh(path));
+    } catch (const std::exception &e) {
+        if (err && err_cap > 0) {
+            std::strncpy(err, e.what(), (size_t)err_cap - 1);
+            err[err_cap - 1] = 0;
+        }
+        return nullptr;
+    }
+}
+
+void refh_mesh_free(void *m) { delete static_cast<Mesh *>(m); }
+
+void refh_mesh_sizes(void *m, int *np, int *nn, int *nt)
+{
+    const Mesh &mesh = *static_cast<Mesh *>(m);
+    *np = (int)mesh.points.size();
+    *nn = (int)mesh.normals.size();
+    *nt = (int)mesh.triangles.size();
+}
+
+// points [np][3], normals [nn][3], triangles [nt][6] (a.pi, a.ni, b.pi, b.ni,
+// c.pi, c.ni), the name into name (capacity name_cap).
+void refh_mesh_export(void *m, float *points, float *normals, uint32_t *tris, char *name, int name_cap)
+{
+    const Mesh &mesh = *static_cast<Mesh *>(m);
+    for (size_t i = 0; i < mesh.points.size(); ++i) {
+        points[3 * i] = mesh.points[i].x;
+        points[3 * i + 1] = mesh.points[i].y;
+        points[3 * i + 2] = mesh.points[i].z;
+    }
+    for (size_t i = 0; i < mesh.normals.size(); ++i) {
+        normals[3 * i] = mesh.normals[i].x;
+        normals[3 * i + 1] = mesh.normals[i].y;
+        normals[3 * i + 2] = mesh.normals[i].z;
+    }
+    for (size_t i = 0; i < mesh.triangles.size(); ++i) {
+        const Triangle &t = mesh.triangles[i];
+        const uint32_t v[6] = {t.a.pi, t.a.ni, t.b.pi, t.b.ni, t.c.pi, t.c.ni};
+        std::memcpy(tris + 6 * i, v, sizeof(v));
+    }
+    std::strncpy(name, mesh.name.c_str(), (size_t)name_cap - 1);
+    name[name_cap - 1] = 0;
+}
+
+// normalizeMeshSize then generateCoarseNormals on the loaded mesh.
+void refh_mesh_normalize_and_coarse_normals(void *m)
+{
+    Mesh &mesh = *static_cast<Mesh *>(m);
+    normalizeMeshSize(mesh);
+    generateCoarseNormals(mesh);
 }
 
 }  // extern "C"

@@ -434,8 +434,48 @@ void test_renderer_progressive_equals_one_call()
 
 }  // namespace
 
+// dump-mesh <obj> <out>: loadMesh, then normalizeMeshSize + generateCoarseNormals,
+// written as int32 ok, then per stage int32 np, nn, nt, the float points,
+// the float normals, the uint32 triangles (a.pi, a.ni, b.pi, b.ni, c.pi, c.ni)
+// and the name (int32 length + bytes); ok = 0 when loadMesh throws.
+int dump_mesh(const char *obj, const char *out_path)
+{
+    std::ofstream out(out_path, std::ios::binary);
+    auto i32 = [&](int32_t v) { out.write(reinterpret_cast<const char *>(&v), 4); };
+    auto stage = [&](const Mesh &m) {
+        i32((int32_t)m.points.size());
+        i32((int32_t)m.normals.size());
+        i32((int32_t)m.triangles.size());
+        out.write(reinterpret_cast<const char *>(m.points.data()), (std::streamsize)(m.points.size() * sizeof(Vec3)));
+        out.write(reinterpret_cast<const char *>(m.normals.data()), (std::streamsize)(m.normals.size() * sizeof(Vec3)));
+        for (const Triangle &t : m.triangles)
+            for (const Vertex &v : {t.a, t.b, t.c}) {
+                i32((int32_t)v.pi);
+                i32((int32_t)v.ni);
+            }
+        i32((int32_t)m.name.size());
+        out.write(m.name.data(), (std::streamsize)m.name.size());
+    };
+    Mesh m;
+    try {
+        m = loadMesh(obj);
+    } catch (const std::exception &) {
+        i32(0);
+        return 0;
+    }
+    i32(1);
+    stage(m);
+    if (!m.points.empty()) {
+        normalizeMeshSize(m);
+        generateCoarseNormals(m);
+        stage(m);
+    }
+    return 0;
+}
+
 int main(int argc, char **argv)
 {
+    if (argc == 4 && std::string(argv[1]) == "dump-mesh") return dump_mesh(argv[2], argv[3]);
     const std::string which = argc > 1 ? argv[1] : "all";
     g_dir = argc > 2 ? std::filesystem::path(argv[2]) : std::filesystem::path(".");
     std::filesystem::create_directories(g_dir);

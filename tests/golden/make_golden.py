@@ -205,14 +205,59 @@ def debug_fixture():
                         replay=replay, width=np.int32(w), height=np.int32(h), spp=np.int32(spp), **out)
 
 
+# OBJ texts of the loader's grammar and error cases (ours); the reference's
+# model files are read from its tree.
+MESH_TEXTS = {
+    "grammar": "# corners in every form\nmtllib scene.mtl\no tetra_1\nv 0 0 0\nv 1.5 0 -0.25\r\n"
+               "v 0 1 0.5 \t\nv 0.25 0.125 2\nvt 0.5 0.5\nvn 0 0 1\nvn 0.6 0.8 0\ns off\n"
+               "f 1 2 3\nf 1//2 2//2 4//1\nf 1/1/1 3/1/2 4/1/1\nf 2/1 3/1 4/1\nf 4 3\n\n",
+    "no_normals": "v -1 -1 0\nv 1 -1 0\nv 0 1 0\nv 0 0 1\nf 1 2 3\nf 1 2 4\n",
+    "quad": "v 0 0 0\nv 1 0 0\nv 1 1 0\nv 0 1 0\nf 1 2 3 4\n",
+    "unknown_tag": "v 0 0 0\nusemtl red\n",
+    "index_range": "v 0 0 0\nv 1 0 0\nv 0 1 0\nf 1 2 4\n",
+    "normal_range": "v 0 0 0\nv 1 0 0\nv 0 1 0\nvn 0 0 1\nf 1//1 2//2 3//1\n",
+    "negative_index": "v 0 0 0\nv 1 0 0\nv 0 1 0\nf -1 -2 -3\n",
+    "bad_number": "v 0 x 0\n",
+    "four_indices": "v 0 0 0\nv 1 0 0\nv 0 1 0\nf 1/1/1/1 2 3\n",
+}
+
+
+def mesh_fixture():
+    """loadMesh, then normalizeMeshSize and generateCoarseNormals, of the
+    reference (src/models/Mesh.cpp:117-243) on its three model files and on
+    the OBJ texts above; a case that throws keeps only its text and the flag."""
+    import os
+    import tempfile
+    ref_root = Path(os.environ.get("DEVILRAY_REF_ROOT", "/root/reference"))
+    cases = {name: (ref_root / "models" / f"{name}.obj").read_bytes() for name in ("ico", "cube", "suzanne")}
+    cases.update({k: v.encode() for k, v in MESH_TEXTS.items()})
+    out = {"names": np.array(list(cases.keys()))}
+    with tempfile.TemporaryDirectory() as d:
+        for name, text in cases.items():
+            path = Path(d) / f"{name}.obj"
+            path.write_bytes(text)
+            out[f"{name}_obj"] = np.frombuffer(text, np.uint8)
+            m = po.ref_mesh_load(str(path))
+            out[f"{name}_ok"] = np.int32(m is not None)
+            if m is None:
+                continue
+            for k, v in m.items():
+                out[f"{name}_{k}"] = v
+            if len(m["points"]):
+                for k, v in po.ref_mesh_load(str(path), normalize=True).items():
+                    out[f"{name}_norm_{k}"] = v
+    np.savez_compressed(OUT / "mesh.npz", **out)
+
+
+FIXTURES = {"render": lambda: (render_fixture(), debug_fixture()), "tri": tri_fixture, "box": box_fixture,
+            "bbh": bbh_fixture, "alias": alias_fixture, "mesh": mesh_fixture}
+
+
 def main():
+    """Writes every fixture, or those named on the command line."""
     po.build(ref=True)
-    render_fixture()
-    debug_fixture()
-    tri_fixture()
-    box_fixture()
-    bbh_fixture()
-    alias_fixture()
+    for name in (sys.argv[1:] or list(FIXTURES)):
+        FIXTURES[name]()
     for p in sorted(OUT.glob("*.npz")):
         print(f"{p.name}: {p.stat().st_size} bytes")
 
