@@ -462,11 +462,11 @@ def batch_section(ctx, native, device: int, stream, scenes_n: int = 64, spp: int
     info = b.info()
     path_rays = sum(int(c.sum().item()) for _, c in outs)
     samples = int(info.paths_per_render)
-    # the same scenes built on the device (linear BVH, binary layout): build time
-    # and the batch's samples/s with those hierarchies
+    # the same scenes built on the device (linear BVH collapsed into the same
+    # hierarchy width): build time and the batch's samples/s with them
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    dscs = [native.Scene.from_spec(ctx, spec, builder=1) for spec, _ in specs]
+    dscs = [native.Scene.from_spec(ctx, spec, builder=1, layout=layout) for spec, _ in specs]
     torch.cuda.synchronize()
     dev_build_s = time.perf_counter() - t0
     djobs = [native.make_job(sc, cam, acc, casts, spp=spp, max_depth=depth, seed=i)
@@ -501,7 +501,9 @@ def batch_section(ctx, native, device: int, stream, scenes_n: int = 64, spp: int
            "autotune_scene": tune_scene.as_dict(), "autotune_batch": tune.as_dict(),
            "autotune_seconds": round(tune_scene_s + tune_batch_s, 3), "scene_build_s": round(build_s, 3),
            "device_lbvh": {"scene_build_s": round(dev_build_s, 3), "samples_per_s": samples / t_dev,
-                           "note": "the same 64 scenes built on the device (linear BVH, binary layout)"},
+                           "layout": layout,
+                           "note": f"the same {scenes_n} scenes built on the device (linear BVH, collapsed into "
+                                   f"{'8-wide' if layout == 8 else 'binary'} nodes), light tables included"},
            "scene_generation_s": round(gen_s, 3)}
     b.close()
     del jobs, outs, scs

@@ -234,9 +234,8 @@ dr_status dr_scene_create(dr_context *ctx, const dr_scene_desc *desc, const dr_b
     const bool device_build = cfg && cfg->builder == DR_BUILD_DEVICE_LBVH;
     if (cfg && cfg->builder != DR_BUILD_HOST_SAH && cfg->builder != DR_BUILD_DEVICE_LBVH)
         return fail(DR_ERR_INVALID_ARGUMENT, "dr_scene_create: unknown builder");
-    if (device_build && cfg->layout == 8)
-        return fail(DR_ERR_INVALID_ARGUMENT, "dr_scene_create: the device build makes the binary layout");
-    const uint32_t layout = device_build || (cfg && cfg->layout == 2) ? 2u : 8u;
+    // the device build makes the binary layout unless the 8-wide one is asked for
+    const uint32_t layout = (device_build && cfg->layout != 8) || (cfg && cfg->layout == 2) ? 2u : 8u;
     if (cfg && cfg->layout != 0 && cfg->layout != 2 && cfg->layout != 8)
         return fail(DR_ERR_INVALID_ARGUMENT, "dr_scene_create: layout must be 0, 2 or 8");
     if (device_build && n > 0) {
@@ -244,9 +243,9 @@ dr_status dr_scene_create(dr_context *ctx, const dr_scene_desc *desc, const dr_b
         if (!s) return fail(DR_ERR_OUT_OF_MEMORY, "host allocation failed");
         s->ctx = ctx;
         s->num_tris = n;
-        s->layout = 2;
+        s->layout = layout;
         s->slack = slack;
-        dr_status r = build_lbvh_device(s, desc->positions_host, n, slack);
+        dr_status r = build_lbvh_device(s, desc->positions_host, n, slack, layout);
         cudaError_t e = cudaSuccess;
         if (r == DR_OK && desc->materials_host && desc->num_materials) {
             if ((e = upload(&s->d_materials, desc->materials_host, desc->num_materials, s->device_bytes)) != cudaSuccess)

@@ -128,12 +128,13 @@ Bvh2 build_bvh2(const float *positions, uint32_t num_tris, const BuildParams &p,
 // compressed 8-wide nodes.
 Bvh8 build_bvh8(const float *positions, uint32_t num_tris, const BuildParams &p, float slack);
 
-// Device linear-BVH build (lbvh.cu): nodes, triangle records and index map of
-// `s` from host positions (n >= 1); sets num_nodes and depth.
+// Device linear-BVH build (lbvh.cu): nodes (binary layout 2, or collapsed
+// into 8-wide nodes for layout 8), triangle records and index map of `s` from
+// host positions (n >= 1); sets num_nodes and depth.
 }  // namespace dr
 struct dr_scene;
 namespace dr {
-dr_status build_lbvh_device(dr_scene *s, const float *positions_host, uint32_t n, float slack);
+dr_status build_lbvh_device(dr_scene *s, const float *positions_host, uint32_t n, float slack, uint32_t layout);
 
 // Conservative world-space widening for a scene whose largest absolute
 // coordinate is `mag`.

@@ -13,8 +13,10 @@
 //      (ties between equal codes broken by the index);
 //   5. boxes bottom-up: the second child to arrive at a node unions both;
 //   6. the two-box node layout of the traversal (boxes widened by the scene's
-//      slack and rounded outward) and the triangle records in leaf order.
-// Leaves hold one triangle. The result is a valid hierarchy for the
+//      slack and rounded outward) and the triangle records in leaf order;
+//      or, for the 8-wide layout, the collapse of the radix tree into
+//      compressed 8-wide nodes (below).
+// Leaves of the binary layout hold one triangle, wide leaves up to three. The result is a valid hierarchy for the
 // canonical closest-hit semantics: traversal results equal the host-built
 // scene's bit for bit.
 
@@ -378,13 +380,14 @@ __global__ void k_records(const float *pos, const uint32_t *order, uint32_t n, f
 constexpr float kWideLeafTriCost = 1.0f;
 constexpr uint32_t kWideMaxLeafTris = 3;
 
-struct WideDp {
+struct alignas(16) WideDp {
     float cost[8];     // cost[j - 1]: least cost of the subtree in at most j slots
     int8_t split[8];   // split[j - 1]: the left child's share when the node is opened, 0 = one slot
     uint8_t tris;      // triangles of the subtree, counted up to 4
     uint8_t wide_leaf; // its one slot is a leaf slot (else an internal wide node)
-    uint8_t pad[2];
+    uint8_t pad[6];
 };
+static_assert(sizeof(WideDp) == 48, "WideDp is read as three 16-byte words");
 
 __device__ __forceinline__ float box_area(const Box6 &b)
 {
@@ -467,7 +470,7 @@ __global__ void k_boxes_dp(const float *pos, const uint32_t *order, int n, const
             d.cost[j - 1] = opened ? open[j] : one;
             d.split[j - 1] = opened ? open_split[j] : (int8_t)0;
         }
-        d.pad[0] = d.pad[1] = 0;
+        for (int k = 0; k < 6; ++k) d.pad[k] = 0;
         const uint32_t ha = c.x < 0 ? 0u : __ldcg(height + c.x), hb = c.y < 0 ? 0u : __ldcg(height + c.y);
         boxes[node] = u;
         dp[node] = d;
@@ -518,10 +521,14 @@ __device__ __forceinline__ uint32_t wide_tris(int x, const WideDp *dp) { return 
 
 // Per task of the level: internal children and leaf triangles of its wide node.
 __global__ void k_wide_count(const int *tasks, uint32_t ntasks, const int2 *children, const WideDp *dp,
-                             uint32_t *cnt_nodes, uint32_t *cnt_tris)
+                             uint32_t *cnt_nodes, uint32_t *cnt_tris, int num_internal)
 {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ntasks) return;
+    if (tasks[t] < 0 || tasks[t] >= num_internal) {  // never by construction; see k_wide_emit
+        cnt_nodes[t] = cnt_tris[t] = 0;
+        return;
+    }
     int ch[8];
     const int m = wide_children(tasks[t], children, dp, ch);
     uint32_t ni = 0, nt = 0;
@@ -561,10 +568,13 @@ __global__ void k_wide_emit(const float *pos, const uint32_t *order, const int *
                             uint32_t ntasks, const int2 *children, const WideDp *dp, const Box6 *boxes,
                             const uint32_t *scan_nodes, const uint32_t *scan_tris, uint32_t node_base,
                             uint32_t tri_base0, float slack, Bvh8Node *nodes, int *next_tasks,
-                            uint32_t *next_task_node, uint32_t *order8)
+                            uint32_t *next_task_node, uint32_t *order8, uint32_t max_nodes, uint32_t n)
 {
+    // every index below stays under max_nodes (wide nodes), n (work-list
+    // entries and triangles) by construction; the checks keep a miscount from
+    // writing out of bounds (the host then finds the wrong totals)
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= ntasks) return;
+    if (t >= ntasks || task_node[t] >= max_nodes || tasks[t] < 0 || tasks[t] >= (int)n - 1) return;
     int ch[8];
     const int m = wide_children(tasks[t], children, dp, ch);
     Box6 cb[8], u;
@@ -645,13 +655,16 @@ __global__ void k_wide_emit(const float *pos, const uint32_t *order, const int *
             imask |= 1u << sl;
             mt = 0x20u | (24u + (uint32_t)sl);
             const uint32_t slot = scan_nodes[t] + next_child;  // position in the next level's work list
-            next_tasks[slot] = x;
-            next_task_node[slot] = child_base + next_child;
+            if (slot < n && child_base + next_child < max_nodes) {
+                next_tasks[slot] = x;
+                next_task_node[slot] = child_base + next_child;
+            }
             ++next_child;
         } else {
             uint32_t tr[3];
             const int nt = subtree_tris(x, children, order, tr);
-            for (int q = 0; q < nt; ++q) order8[tri_base + tri_off + q] = tr[q];
+            for (int q = 0; q < nt; ++q)
+                if (tri_base + tri_off + q < n) order8[tri_base + tri_off + q] = tr[q];
             mt = ((((1u << nt) - 1u) << 5) | tri_off);
             tri_off += (uint32_t)nt;
         }
@@ -700,8 +713,9 @@ unsigned grid_for(uint64_t n, unsigned block) { return (unsigned)std::max<uint64
 }  // namespace
 
 // Builds nodes, records and the index map of `s` on the device from host
-// positions (n >= 1). Sets num_nodes and depth.
-dr_status build_lbvh_device(dr_scene *s, const float *positions_host, uint32_t n, float slack)
+// positions (n >= 1): the radix tree's binary nodes (layout 2) or its collapse
+// into compressed 8-wide nodes (layout 8). Sets num_nodes and depth.
+dr_status build_lbvh_device(dr_scene *s, const float *positions_host, uint32_t n, float slack, uint32_t layout)
 {
     cudaError_t e = cudaSuccess;
     float *pos = nullptr;
@@ -711,12 +725,20 @@ dr_status build_lbvh_device(dr_scene *s, const float *positions_host, uint32_t n
     const size_t words = (size_t)4 * n + (size_t)256 * tiles + 4 * (size_t)n + 16;
     Box6 *boxes = nullptr;
     int2 *children = nullptr;
+    WideDp *dp = nullptr;
+    int *tasks = nullptr;         // wide build: two work lists of radix nodes
+    uint32_t *wide_tmp = nullptr; // task nodes (2 lists), node and triangle counts, the triangle order
+    Bvh8Node *nodes8 = nullptr;   // wide nodes before they are copied to their final size
     const size_t nint = n > 1 ? n - 1 : 1;
     auto done = [&](dr_status st) {
         cudaFree(pos);
         cudaFree(scratch);
         cudaFree(boxes);
         cudaFree(children);
+        cudaFree(dp);
+        cudaFree(tasks);
+        cudaFree(wide_tmp);
+        cudaFree(nodes8);
         return st;
     };
     if ((e = dev_malloc(&pos, (size_t)n * 9 * sizeof(float))) != cudaSuccess ||
@@ -749,9 +771,90 @@ dr_status build_lbvh_device(dr_scene *s, const float *positions_host, uint32_t n
     if ((e = cudaGetLastError()) != cudaSuccess) return done(cuda_fail(e, "device BVH build: sort"));
     uint32_t num_nodes = 1;
     uint32_t depth = 1;
-    if (n == 1) {
+    const uint32_t *tri_order = vals;  // leaf position -> triangle of the records
+    if (layout == 8) {
+        // the triangle order of the wide leaves, then per level the work lists
+        uint32_t *order8 = nullptr;
+        if ((e = dev_malloc(&wide_tmp, ((size_t)n * 4 + 2) * sizeof(uint32_t))) != cudaSuccess ||
+            (e = dev_malloc(&nodes8, nint * sizeof(Bvh8Node))) != cudaSuccess)
+            return done(cuda_fail(e, "device BVH build: wide nodes"));
+        order8 = wide_tmp;
+        uint32_t *task_node[2] = {wide_tmp + n, wide_tmp + 2 * (size_t)n};
+        uint32_t *cnt_nodes = wide_tmp + 3 * (size_t)n;  // n + 1 entries
+        if (n == 1) {
+            k_wide_single<<<1, 1>>>(pos, slack, nodes8, order8);
+        } else {
+            uint32_t *cnt2 = nullptr;  // triangle counts, n + 1 entries
+            if ((e = dev_malloc(&dp, (n - 1) * sizeof(WideDp))) != cudaSuccess ||
+                (e = dev_malloc(&tasks, 2 * (size_t)n * sizeof(int))) != cudaSuccess ||
+                (e = dev_malloc(&cnt2, ((size_t)n + 1) * sizeof(uint32_t))) != cudaSuccess) {
+                cudaFree(cnt2);
+                return done(cuda_fail(e, "device BVH build: wide collapse"));
+            }
+            uint32_t *cnt_tris = cnt2;
+            k_karras<<<grid_for(n - 1, 256), 256>>>(keys, (int)n, children, parent_int, parent_leaf);
+            k_boxes_dp<<<grid_for(n, 256), 256>>>(pos, vals, (int)n, children, parent_int, parent_leaf, visits, boxes,
+                                                  heights, dp);
+            int *list[2] = {tasks, tasks + n};
+            if ((e = cudaMemset(tasks, 0, 2 * (size_t)n * sizeof(int))) != cudaSuccess ||
+                (e = cudaMemset(task_node[0], 0, 2 * (size_t)n * sizeof(uint32_t))) != cudaSuccess) {
+                cudaFree(cnt2);
+                return done(cuda_fail(e, "device BVH build: wide collapse"));
+            }
+            const int root = 0;
+            const uint32_t zero = 0;
+            if ((e = cudaMemcpy(list[0], &root, sizeof(int), cudaMemcpyHostToDevice)) != cudaSuccess ||
+                (e = cudaMemcpy(task_node[0], &zero, sizeof(uint32_t), cudaMemcpyHostToDevice)) != cudaSuccess) {
+                cudaFree(cnt2);
+                return done(cuda_fail(e, "device BVH build: wide collapse"));
+            }
+            uint32_t ntasks = 1, node_base = 1, tri_base = 0, levels = 0;
+            while (ntasks > 0 && e == cudaSuccess) {
+                const unsigned g = grid_for(ntasks, 128);
+                k_wide_count<<<g, 128>>>(list[0], ntasks, children, dp, cnt_nodes, cnt_tris, (int)n - 1);
+                // exclusive scans over ntasks + 1 entries: the last one becomes the level's total
+                if ((e = cudaMemset(cnt_nodes + ntasks, 0, sizeof(uint32_t))) != cudaSuccess ||
+                    (e = cudaMemset(cnt_tris + ntasks, 0, sizeof(uint32_t))) != cudaSuccess)
+                    break;
+                k_sort_scan<<<1, 1024>>>(cnt_nodes, ntasks + 1);
+                k_sort_scan<<<1, 1024>>>(cnt_tris, ntasks + 1);
+                k_wide_emit<<<g, 128>>>(pos, vals, list[0], task_node[0], ntasks, children, dp, boxes, cnt_nodes,
+                                        cnt_tris, node_base, tri_base, slack, nodes8, list[1], task_node[1], order8,
+                                        (uint32_t)nint, n);
+                uint32_t totals[2];
+                if ((e = cudaMemcpy(&totals[0], cnt_nodes + ntasks, sizeof(uint32_t), cudaMemcpyDeviceToHost)) !=
+                        cudaSuccess ||
+                    (e = cudaMemcpy(&totals[1], cnt_tris + ntasks, sizeof(uint32_t), cudaMemcpyDeviceToHost)) !=
+                        cudaSuccess)
+                    break;
+                ++levels;
+                ntasks = totals[0];
+                node_base += totals[0];
+                tri_base += totals[1];
+                std::swap(list[0], list[1]);
+                std::swap(task_node[0], task_node[1]);
+                if (levels > (uint32_t)kMaxBuildDepth || node_base > nint) break;
+            }
+            cudaFree(cnt2);
+            if (e != cudaSuccess) return done(cuda_fail(e, "device BVH build: wide collapse"));
+            if (levels > (uint32_t)kMaxBuildDepth)
+                return done(fail(DR_ERR_TOO_LARGE, "device BVH build: more than %d wide levels", kMaxBuildDepth));
+            if (tri_base != n || node_base > nint)
+                return done(fail(DR_ERR_CUDA, "device BVH build: wide collapse placed %u of %u triangles", tri_base,
+                                 n));
+            num_nodes = node_base;
+            depth = levels;
+        }
+        if ((e = dev_malloc(&s->d_nodes8, (size_t)num_nodes * sizeof(Bvh8Node))) != cudaSuccess ||
+            (e = cudaMemcpy(s->d_nodes8, nodes8, (size_t)num_nodes * sizeof(Bvh8Node), cudaMemcpyDeviceToDevice)) !=
+                cudaSuccess)
+            return done(cuda_fail(e, "device BVH build: wide nodes"));
+        s->device_bytes += (size_t)num_nodes * sizeof(Bvh8Node);
+        tri_order = order8;
+    } else if (n == 1) {
         if ((e = dev_malloc(&s->d_nodes, sizeof(Bvh2Node))) != cudaSuccess) return done(cuda_fail(e, "device BVH build"));
         k_emit_single<<<1, 1>>>(pos, slack, s->d_nodes);
+        s->device_bytes += sizeof(Bvh2Node);
     } else {
         num_nodes = n - 1;
         k_karras<<<grid_for(n - 1, 256), 256>>>(keys, (int)n, children, parent_int, parent_leaf);
@@ -763,14 +866,14 @@ dr_status build_lbvh_device(dr_scene *s, const float *positions_host, uint32_t n
         if ((e = cudaMemcpy(&depth, heights, sizeof(uint32_t), cudaMemcpyDeviceToHost)) != cudaSuccess)
             return done(cuda_fail(e, "device BVH build: depth"));
         depth += 1;
+        s->device_bytes += (size_t)num_nodes * sizeof(Bvh2Node);
     }
-    s->device_bytes += (size_t)num_nodes * sizeof(Bvh2Node);
     if ((e = dev_malloc(&s->d_tri_ref, (size_t)n * 3 * sizeof(float4))) != cudaSuccess ||
         (e = dev_malloc(&s->d_tri_wt, (size_t)n * 3 * sizeof(float4))) != cudaSuccess ||
         (e = dev_malloc(&s->d_prim, (size_t)n * sizeof(int32_t))) != cudaSuccess)
         return done(cuda_fail(e, "device BVH build: records"));
     s->device_bytes += (size_t)n * (2 * 3 * sizeof(float4) + sizeof(int32_t));
-    k_records<<<grid_for(n, 256), 256>>>(pos, vals, n, s->d_tri_ref, s->d_tri_wt, s->d_prim);
+    k_records<<<grid_for(n, 256), 256>>>(pos, tri_order, n, s->d_tri_ref, s->d_tri_wt, s->d_prim);
     if ((e = cudaDeviceSynchronize()) != cudaSuccess) return done(cuda_fail(e, "device BVH build"));
     s->num_nodes = num_nodes;
     s->depth = depth;

@@ -167,7 +167,8 @@ typedef struct dr_scene_desc {
 
 typedef enum dr_builder {
     DR_BUILD_HOST_SAH = 0,     /* binned SAH on the host (threads), either layout */
-    DR_BUILD_DEVICE_LBVH = 1   /* linear BVH on the device (Morton order, one triangle per leaf); binary layout */
+    DR_BUILD_DEVICE_LBVH = 1   /* linear BVH on the device (Morton order): the binary layout (one triangle per
+                                  leaf; layout 0 or 2) or its collapse into compressed 8-wide nodes (layout 8) */
 } dr_builder;
 
 typedef struct dr_build_config {

@@ -323,7 +323,48 @@ def test_device_lbvh_render_matches_host(native, ctx):
     assert np.array_equal(outs[0].view(np.uint32), outs[1].view(np.uint32))
 
 
-def test_device_lbvh_rejects_wide_layout(native, ctx):
-    soup, _, _ = scenes.incoherent_soup(100, seed=1)
-    with pytest.raises(native.DrError):
-        native.Scene(ctx, soup, builder=1, layout=8)
+@pytest.mark.parametrize("n,dup", [(1, 0), (2, 0), (3, 0), (9, 0), (100, 0), (4096, 0), (1 << 18, 0), (5000, 3)])
+def test_device_wide_build_matches_host_build(native, ctx, oracle, n, dup):
+    """The device build collapsed into compressed 8-wide nodes
+    (DR_BUILD_DEVICE_LBVH, layout 8) gives the same closest and any hits, bit
+    for bit, as the host-built 8-wide scene and the oracle; `dup` repeats every
+    triangle (equal Morton codes)."""
+    soup, _, _ = scenes.incoherent_soup(n, seed=n + 7)
+    if dup:
+        soup = np.repeat(soup, dup, axis=0)
+    rays = scenes.incoherent_rays(20000, seed=8)
+    rng = np.random.default_rng(n)
+    rays[:, 3] = np.where(rng.random(len(rays)) < 0.5, np.inf, rng.uniform(0, 60, len(rays))).astype(np.float32)
+    dev = native.Scene(ctx, soup, builder=1, layout=8)
+    host = native.Scene(ctx, soup, layout=8)
+    assert dev.info().layout == 8 and 1 <= dev.info().num_nodes <= max(1, len(soup) - 1)
+    assert dev.info().depth >= 1
+    d_rays = torch.from_numpy(rays).cuda()
+    out = []
+    for sc in (dev, host):
+        h = torch.empty((len(rays), 2), dtype=torch.int32, device="cuda")
+        sc.trace_closest(d_rays, len(rays), h)
+        occ = torch.empty(len(rays), dtype=torch.uint8, device="cuda")
+        sc.trace_any(d_rays, len(rays), occ)
+        torch.cuda.synchronize()
+        out.append((h.cpu().numpy(), occ.cpu().numpy()))
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+    if len(soup) <= 4096:
+        t, prim = oracle.BBH(soup).trace_canonical(rays, slack=host.info().slack)
+        assert np.array_equal(out[0][0][:, 1], prim)
+        assert np.array_equal(out[0][0][:, 0].view(np.float32).view(np.uint32), t.view(np.uint32))
+    ctx.check()
+
+
+def test_device_wide_build_renders_like_host_build(native, ctx):
+    spec = scenes.many_light(6 * 1280, 40, seed=3, half=6.0)
+    cam = scenes.outside_camera(40, 30, distance=20.0, half=6.0)
+    outs = []
+    for kw in ({"builder": 1, "layout": 8}, {"layout": 8}):
+        sc = native.Scene.from_spec(ctx, spec, **kw)
+        acc = torch.zeros((40 * 30, 4), dtype=torch.float32, device="cuda")
+        sc.render(cam, acc, spp=4, max_depth=12)
+        torch.cuda.synchronize()
+        outs.append(acc.cpu().numpy())
+    assert np.array_equal(outs[0].view(np.uint32), outs[1].view(np.uint32))
+    assert outs[0][:, :3].sum() > 0
