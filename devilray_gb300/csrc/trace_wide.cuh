@@ -51,9 +51,13 @@ constexpr int kWideStack = 64;
 #ifndef DR_FAST_SLAB
 #define DR_FAST_SLAB 1
 #endif
-// (Packed FP32 pairs, __ffma2_rn, for the near and far planes of a slot or
-// for slots j and j + 4 were measured slower: 4.86 -> 4.79 and 4.61 Grays/s,
-// the register pairs spill at 64 registers.)
+// Packed FP32 pairs (fma.rn.f32x2) for the slab FMAs of slots j and j + 4:
+// each half rounds as the scalar FMA does, so results are unchanged. At 64
+// registers the pairs spill (4.86 -> 4.61 Grays/s); the public kernels turn
+// them on with a 73-register budget (trace.cu), the renderer keeps them off.
+#ifndef DR_PACKED_SLAB
+#define DR_PACKED_SLAB 0
+#endif
 // Three-input min/max instructions in the box test.
 #ifndef DR_MINMAX3
 #define DR_MINMAX3 1
@@ -196,6 +200,31 @@ __host__ __device__ __forceinline__ void wide_node_test(const Bvh8Node *node, co
     hit_internal = 0;
     tri_mask = 0;
     uint32_t boxes = 0, hit_bits = 0;
+#if DR_PACKED_SLAB && DR_FAST_SLAB && DR_NODE_META_BITS == 2 && defined(__CUDA_ARCH__)
+    // slots j and j + 4 share byte j of the two words of each plane: their six
+    // slab FMAs and the far-time scaling run as packed FP32 pairs (each lane of
+    // a pair rounds as the scalar instruction would)
+    const float2 Ax = make_float2(cx.a, cx.a), NBx = make_float2(cx.near_b, cx.near_b),
+                 FBx = make_float2(cx.far_b, cx.far_b);
+    const float2 Ay = make_float2(cy.a, cy.a), NBy = make_float2(cy.near_b, cy.near_b),
+                 FBy = make_float2(cy.far_b, cy.far_b);
+    const float2 Az = make_float2(cz.a, cz.a), NBz = make_float2(cz.near_b, cz.near_b),
+                 FBz = make_float2(cz.far_b, cz.far_b);
+    const float2 farS = make_float2(kBoxFarScale, kBoxFarScale);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const float2 tnx = __ffma2_rn(make_float2(byte_q(nx0, j), byte_q(nx1, j)), Ax, NBx);
+        const float2 tfx = __ffma2_rn(make_float2(byte_q(fx0, j), byte_q(fx1, j)), Ax, FBx);
+        const float2 tny = __ffma2_rn(make_float2(byte_q(ny0, j), byte_q(ny1, j)), Ay, NBy);
+        const float2 tfy = __ffma2_rn(make_float2(byte_q(fy0, j), byte_q(fy1, j)), Ay, FBy);
+        const float2 tnz = __ffma2_rn(make_float2(byte_q(nz0, j), byte_q(nz1, j)), Az, NBz);
+        const float2 tfz = __ffma2_rn(make_float2(byte_q(fz0, j), byte_q(fz1, j)), Az, FBz);
+        const float2 tmx = __fmul2_rn(make_float2(fminf(min3f(tfx.x, tfy.x, tfz.x), tmax),
+                                                  fminf(min3f(tfx.y, tfy.y, tfz.y), tmax)), farS);
+        if (fmaxf(max3f(tnx.x, tny.x, tnz.x), 0.0f) <= tmx.x) hit_bits |= 1u << j;
+        if (fmaxf(max3f(tnx.y, tny.y, tnz.y), 0.0f) <= tmx.y) hit_bits |= 1u << (j + 4);
+    }
+#else
 #pragma unroll
     for (int s = 0; s < 8; ++s) {
         const int j = s & 3;
@@ -238,6 +267,7 @@ __host__ __device__ __forceinline__ void wide_node_test(const Bvh8Node *node, co
         }
 #endif
     }
+#endif
 #if DR_NODE_META_BITS
 #if DR_NODE_META_BITS == 2
     // leaf slots hit: their triangle bits from the metadata; empty slots have
