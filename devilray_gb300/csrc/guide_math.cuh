@@ -72,17 +72,11 @@ __host__ __device__ inline float guide_pdf(const GuideLobes &L, float wx, float 
     return p;
 }
 
-// Samples a direction: lobe by u0, then the lobe's vMF from (u1, u2).
-__host__ __device__ inline void guide_sample(const GuideLobes &L, float u0, float u1, float u2, float &wx, float &wy,
-                                             float &wz)
+// Samples the vMF lobe of concentration k and unit mean (mx, my, mz) from
+// (u1, u2).
+__host__ __device__ inline void vmf_sample(float k, float mx, float my, float mz, float u1, float u2, float &wx,
+                                           float &wy, float &wz)
 {
-    int j = 0;
-    float acc = L.pi[0];
-    while (j < kGuideLobes - 1 && u0 >= acc) {
-        ++j;
-        acc += L.pi[j];
-    }
-    const float k = L.kappa[j];
     // cosine to the mean: w = 1 + log(u1 + (1 - u1) e^{-2k}) / k
     float w = 1.0f + logf(u1 + (1.0f - u1) * guide_exp(-2.0f * k)) / k;
     w = fminf(fmaxf(w, -1.0f), 1.0f);
@@ -96,7 +90,6 @@ __host__ __device__ inline void guide_sample(const GuideLobes &L, float u0, floa
     cp = cosf(phi);
 #endif
     // orthonormal basis around mu (Duff et al., "Building an Orthonormal Basis, Revisited", 2017)
-    const float mx = L.mu[j][0], my = L.mu[j][1], mz = L.mu[j][2];
     const float sign = copysignf(1.0f, mz);
     const float a = -1.0f / (sign + mz);
     const float b = mx * my * a;
@@ -105,6 +98,19 @@ __host__ __device__ inline void guide_sample(const GuideLobes &L, float u0, floa
     wx = w * mx + sr * (cp * t1x + sp * t2x);
     wy = w * my + sr * (cp * t1y + sp * t2y);
     wz = w * mz + sr * (cp * t1z + sp * t2z);
+}
+
+// Samples a direction: lobe by u0, then the lobe's vMF from (u1, u2).
+__host__ __device__ inline void guide_sample(const GuideLobes &L, float u0, float u1, float u2, float &wx, float &wy,
+                                             float &wz)
+{
+    int j = 0;
+    float acc = L.pi[0];
+    while (j < kGuideLobes - 1 && u0 >= acc) {
+        ++j;
+        acc += L.pi[j];
+    }
+    vmf_sample(L.kappa[j], L.mu[j][0], L.mu[j][1], L.mu[j][2], u1, u2, wx, wy, wz);
 }
 
 // Loss term -c log q(w) of one sample and its gradient with respect to y

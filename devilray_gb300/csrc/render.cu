@@ -198,6 +198,110 @@ __device__ __forceinline__ uint32_t find_segment(const WaveSegment *segs, uint32
     return lo;
 }
 
+// Guided directions drawn below the surface are mirrored into the upper
+// hemisphere (w - 2 (w.n) n) instead of ending the path. With it the density
+// of the guided part at an upper-hemisphere direction w is q(w) + q(R w), R
+// the mirror; below the surface it is 0. Every use of the guided density (the
+// sampled bounce, the next-event MIS weight, the emission MIS weight through
+// prev_pdf) takes this one, so the estimator stays unbiased for any network.
+// Measured on the occluded-light scene (480x270, 1024 spp, 3 seeds): equal-spp
+// RMSE ratio against the plain tracer 1.32 without the mirror, 1.40 with it.
+#ifndef DR_GUIDE_REFLECT
+#define DR_GUIDE_REFLECT 1
+#endif
+// Training target of a guided vertex: the radiance that arrives along its
+// sampled direction, with an emitter hit there counted in full (1), or with
+// its MIS weight against next-event estimation, as the image counts it (0).
+#ifndef DR_GUIDE_FULL_EMISSION
+#define DR_GUIDE_FULL_EMISSION 1
+#endif
+
+// The mixture as the shading kernel uses it: the network output decoded once
+// per vertex, each lobe's vMF normalisation folded into its weight, so that a
+// density evaluation costs one exponential per lobe. Every loop over the lobes
+// is unrolled with constant indices, which keeps the mixture in registers (a
+// lobe picked by a run-time index would put the whole mixture in local memory).
+struct GuideMix {
+    float c[kGuideLobes];      // pi_j kappa_j / (2 pi (1 - e^{-2 kappa_j}))
+    float pi[kGuideLobes];     // mixture weights (lobe choice when sampling)
+    float kappa[kGuideLobes];
+    float mx[kGuideLobes], my[kGuideLobes], mz[kGuideLobes];  // unit mean directions
+};
+
+__device__ __forceinline__ GuideMix guide_mix(const float *y)
+{
+    float v[kGuideOut];
+#pragma unroll
+    for (int i = 0; i < kGuideOut / 4; ++i) {
+        const float4 q = reinterpret_cast<const float4 *>(y)[i];
+        v[4 * i] = q.x, v[4 * i + 1] = q.y, v[4 * i + 2] = q.z, v[4 * i + 3] = q.w;
+    }
+    GuideMix M;
+    float mx = v[0];
+#pragma unroll
+    for (int j = 1; j < kGuideLobes; ++j) mx = fmaxf(mx, v[5 * j]);
+    float s = 0.0f;
+#pragma unroll
+    for (int j = 0; j < kGuideLobes; ++j) {
+        M.pi[j] = __expf(v[5 * j] - mx);
+        s += M.pi[j];
+    }
+    const float inv = 1.0f / s;
+#pragma unroll
+    for (int j = 0; j < kGuideLobes; ++j) {
+        M.pi[j] *= inv;
+        const float k = __expf(fminf(fmaxf(v[5 * j + 1], kGuideLogKMin), kGuideLogKMax));
+        M.kappa[j] = k;
+        // kappa >= e^-4, so 1 - e^{-2 kappa} >= 0.036 and needs no series
+        M.c[j] = M.pi[j] * k / (6.28318530718f * (1.0f - __expf(-2.0f * k)));
+        const float a = v[5 * j + 2], b = v[5 * j + 3], c = v[5 * j + 4];
+        const float n2 = a * a + b * b + c * c;
+        const bool deg = n2 < 1e-24f;
+        const float r = deg ? 0.0f : rsqrtf(n2);
+        M.mx[j] = a * r, M.my[j] = b * r, M.mz[j] = deg ? 1.0f : c * r;
+    }
+    return M;
+}
+
+__device__ __forceinline__ float guide_mix_pdf(const GuideMix &M, F3 w)
+{
+    float p = 0.0f;
+#pragma unroll
+    for (int j = 0; j < kGuideLobes; ++j) {
+        const float c = M.mx[j] * w.x + M.my[j] * w.y + M.mz[j] * w.z;
+        p += M.c[j] * __expf(M.kappa[j] * (c - 1.0f));
+    }
+    return p;
+}
+
+// Lobe by u0 (cumulative weights, as guide_sample), then its vMF by (u1, u2).
+__device__ __forceinline__ F3 guide_mix_sample(const GuideMix &M, float u0, float u1, float u2)
+{
+    float k = M.kappa[0], ax = M.mx[0], ay = M.my[0], az = M.mz[0];
+    float acc = M.pi[0];
+#pragma unroll
+    for (int j = 1; j < kGuideLobes; ++j) {
+        if (u0 >= acc) k = M.kappa[j], ax = M.mx[j], ay = M.my[j], az = M.mz[j];
+        acc += M.pi[j];
+    }
+    float wx, wy, wz;
+    vmf_sample(k, ax, ay, az, u1, u2, wx, wy, wz);
+    return f3(wx, wy, wz);
+}
+
+// Density of the guided part at w, for a surface of normal n.
+__device__ __forceinline__ float guide_pdf_above(const GuideMix &M, F3 w, F3 n)
+{
+#if DR_GUIDE_REFLECT
+    const float c = dot(w, n);
+    if (!(c > 0.0f)) return 0.0f;
+    const F3 r = sub(w, mul(n, 2.0f * c));
+    return guide_mix_pdf(M, w) + guide_mix_pdf(M, r);
+#else
+    return guide_mix_pdf(M, w);
+#endif
+}
+
 __global__ void __launch_bounds__(kRenderBlock) k_camera(RenderParams p)
 {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -418,12 +522,14 @@ __global__ void __launch_bounds__(kRenderBlock, GUIDED ? 4 : kShadeMinBlocks) k_
             slot = list[i];
             p.casts[slot] += 1;
             const RenderJob &J = p.jobs[p.slot_job[slot]];
+            float *closed = nullptr;  // guided: the record this vertex closes
             if (GUIDED) {
                 // the radiance gathered before this vertex closes the last record
                 const uint32_t rn = p.rec_n[slot];
                 if (rn & kRecOpen) {
                     const uint32_t r = (rn & ~kRecOpen) - 1;
-                    p.rec[((size_t)slot * kGuideRecords + r) * kRecFloats + 11] = luminance(p.color[slot]);
+                    closed = p.rec + ((size_t)slot * kGuideRecords + r) * kRecFloats;
+                    closed[11] = luminance(p.color[slot]);
                     p.rec_n[slot] = rn & ~kRecOpen;
                 }
             }
@@ -468,12 +574,19 @@ __global__ void __launch_bounds__(kRenderBlock, GUIDED ? 4 : kShadeMinBlocks) k_
                         const float L = luminance(mul4s(E, kPi));
                         const float pdf_area = L / J.total_power;
                         const float pdf_nee = pdf_area * area_to_solid_angle(pp, hp, n);
-                        if (pdf_bsdf + pdf_nee > 0)
-                            col = add4(col, mul4s(mul4(E, thr), power_heuristic(pdf_bsdf, pdf_nee)));
+                        if (pdf_bsdf + pdf_nee > 0) {
+                            const float wm = power_heuristic(pdf_bsdf, pdf_nee);
+                            col = add4(col, mul4s(mul4(E, thr), wm));
+#if DR_GUIDE_FULL_EMISSION
+                            // training only: the emission's share left to next-event
+                            // estimation (1 - wm) counts in the closed record's target
+                            if (GUIDED && closed) closed[11] -= luminance(mul4(E, thr)) * (1.0f - wm);
+#endif
+                        }
                     }
-                    GuideLobes lobes;
+                    GuideMix lobes;
                     const float alpha = GUIDED && b < p.guide_bounces ? p.guide_alpha : 0.0f;
-                    if (GUIDED && alpha > 0.0f) lobes = guide_decode(p.guide_y + (size_t)slot * kGuideOut);
+                    if (GUIDED && alpha > 0.0f) lobes = guide_mix(p.guide_y + (size_t)slot * kGuideOut);
                     // next-event estimation: samplePointOnLights (:234-272) and
                     // evaluateDirectLighting (:336-361); visibility is the shadow ray
                     if (J.lights) {
@@ -507,7 +620,7 @@ __global__ void __launch_bounds__(kRenderBlock, GUIDED ? 4 : kShadeMinBlocks) k_
                         float nee_pdf_bsdf = cosine_pdf(hp, lp, n);
                         if (GUIDED && alpha > 0.0f) {
                             const F3 wl0 = normalized(sub(lp, hp));
-                            nee_pdf_bsdf = alpha * guide_pdf(lobes, wl0.x, wl0.y, wl0.z) + (1.0f - alpha) * nee_pdf_bsdf;
+                            nee_pdf_bsdf = alpha * guide_pdf_above(lobes, wl0, n) + (1.0f - alpha) * nee_pdf_bsdf;
                         }
                         const float nee_pdf_nee = lpdf * area_to_solid_angle(hp, lp, ln);
                         const float dist = length(sub(lp, hp));
@@ -534,9 +647,13 @@ __global__ void __launch_bounds__(kRenderBlock, GUIDED ? 4 : kShadeMinBlocks) k_
                     bool cosine = true;
                     if (GUIDED && u[9] < alpha) {
                         cosine = false;
-                        float wx, wy, wz;
-                        guide_sample(lobes, u[10], u[0], u[1], wx, wy, wz);
-                        new_v = f3(wx, wy, wz);
+                        new_v = guide_mix_sample(lobes, u[10], u[0], u[1]);
+#if DR_GUIDE_REFLECT
+                        // a direction below the surface is mirrored into the upper
+                        // hemisphere (guide_pdf_above is the density of the result)
+                        const float cb = dot(new_v, n);
+                        if (cb < 0.0f) new_v = sub(new_v, mul(n, 2.0f * cb));
+#endif
                     }
                     if (cosine) {
                         // cosineWeightedHemisphereSample (DistributionSamplers.hpp:33-42)
@@ -551,7 +668,7 @@ __global__ void __launch_bounds__(kRenderBlock, GUIDED ? 4 : kShadeMinBlocks) k_
                     if (GUIDED) {
                         // one-sample MIS over the mixture and the cosine lobe: f cos / pdf_mix
                         const float c = dot(new_v, n);
-                        const float pdf_mix = (alpha > 0.0f ? alpha * guide_pdf(lobes, new_v.x, new_v.y, new_v.z) : 0.0f) +
+                        const float pdf_mix = (alpha > 0.0f ? alpha * guide_pdf_above(lobes, new_v, n) : 0.0f) +
                                               (1.0f - alpha) * fmaxf(c, 0.0f) / kPi;
                         const float f = c > 0.0f && pdf_mix > 0.0f ? c / (kPi * pdf_mix) : 0.0f;
                         thr = mul4s(mul4(thr, alb), f);
