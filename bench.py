@@ -36,14 +36,14 @@ NUM_TRIS = 1 << 20
 NUM_RAYS = 1 << 24
 # DRAM bytes of one full 16.8 M-ray launch of the dominant kernel, from one
 # `ncu --set full` capture of this workload (the profiles named beside them).
-NCU_TRAFFIC = {8: 931_329_536 + 130_428_416, 2: 1_652_000_000 + 152_000_000}
+NCU_TRAFFIC = {8: 929_616_896 + 130_685_952, 2: 1_652_000_000 + 152_000_000}
 NCU_PROFILE = {8: "trace_closest_p8_incoherent_1M_tris_16M_rays.md",
                2: "trace_closest_bvh2_incoherent_1M_tris_16M_rays.md"}
 # Warp instructions per ray of the dominant kernel (smsp__inst_executed.sum of
 # the same capture / 16,777,216 rays): with the launch time and the sampled SM
 # clock it gives the issue-slot fraction (4 schedulers per SM, one instruction
 # per scheduler and cycle).
-NCU_WARP_INST_PER_RAY = {8: 3_446_000_000 / NUM_RAYS}
+NCU_WARP_INST_PER_RAY = {8: 3_217_281_377 / NUM_RAYS}
 METRIC = "Mrays/s closest-hit"
 WORKLOAD = "incoherent closest-hit: 2^20-triangle icosphere soup, 16,777,216 rays"
 L2_BYTES = 129 * 1024 * 1024
@@ -333,7 +333,9 @@ def run_ours(args):
     if not args.no_guided:
         torch.cuda.empty_cache()
         line["guided"] = guided_section(ctx, native, local, stream, ref_spp=args.guided_ref_spp,
-                                        scene=args.guided_scene)
+                                        scene=args.guided_scene, width=args.guided_size[0],
+                                        height=args.guided_size[1], spp=args.guided_spp,
+                                        hd=args.guided_size[0] < 1920)
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -512,7 +514,8 @@ def batch_section(ctx, native, device: int, stream, scenes_n: int = 64, spp: int
 
 
 def guided_section(ctx, native, device: int, stream, width: int = 480, height: int = 270, spp: int = 1024,
-                   depth: int = 16, ref_spp: int = 65536, hd_spp: int = 16, seeds: int = 3, scene: str = "gap"):
+                   depth: int = 16, ref_spp: int = 65536, hd_spp: int = 16, seeds: int = 3, scene: str = "gap",
+                   hd: bool = True):
     """Learned path guiding on the occluded-light scene (the many-light
     geometry, emitters only above an occluding slab): RMSE of the guided and of
     the plain MIS tracer against a converged render (the plain tracer,
@@ -531,16 +534,23 @@ def guided_section(ctx, native, device: int, stream, width: int = 480, height: i
     dev = f"cuda:{device}"
     acc = torch.zeros((npix, 4), dtype=torch.float32, device=dev)
 
-    # converged reference: chunks of 1024 samples, summed in FP64
+    # converged reference: two halves of ref_spp samples, each summed in FP64
+    # from chunks of 1024; the squared difference of the halves estimates the
+    # reference's own variance, which every MSE below has subtracted
     t0 = time.perf_counter()
-    ref = torch.zeros((npix, 4), dtype=torch.float64, device=dev)
-    for off in range(0, ref_spp, 1024):
-        acc.zero_()
-        sc.render(cam, acc, spp=min(1024, ref_spp - off), max_depth=depth, sample_offset=off, seed=12345,
-                  stream=stream)
-        stream.synchronize()
-        ref += acc.double()
-    ref_img = ref[:, :3] / ref[:, 3:4]
+    halves = []
+    for h in range(2):
+        ref = torch.zeros((npix, 4), dtype=torch.float64, device=dev)
+        for off in range(0, ref_spp // 2, 1024):
+            acc.zero_()
+            sc.render(cam, acc, spp=min(1024, ref_spp // 2 - off), max_depth=depth,
+                      sample_offset=h * (ref_spp // 2) + off, seed=12345, stream=stream)
+            stream.synchronize()
+            ref += acc.double()
+        halves.append(ref[:, :3] / ref[:, 3:4])
+    ref_img = 0.5 * (halves[0] + halves[1])
+    var_ref = float(torch.mean((halves[0] - halves[1]) ** 2).item()) / 4.0
+    del halves
     ref_s = time.perf_counter() - t0
     # the share of indirect light: 1 - (image mean at depth 1) / (converged mean)
     acc.zero_()
@@ -550,7 +560,7 @@ def guided_section(ctx, native, device: int, stream, width: int = 480, height: i
 
     def mse():
         img = acc[:, :3].double() / acc[:, 3:4].double()
-        return float(torch.mean((img - ref_img) ** 2).item())
+        return float(torch.mean((img - ref_img) ** 2).item()) - var_ref
 
     def timed(fn):
         acc.zero_()
@@ -597,30 +607,38 @@ def guided_section(ctx, native, device: int, stream, width: int = 480, height: i
     t_trained, m_trained, _ = runs(lambda sd: sc.render_guided(guides[sd], cam, acc, spp=spp, max_depth=depth,
                                                                 seed=400 + sd, alpha=alpha, train=False,
                                                                 bounces=bounces, wave_paths=wave, stream=stream))
-    # 1080p throughput of the guided tracer (training on)
-    hd = scenes.lower_camera(1920, 1080)
-    hd_acc = torch.zeros((1920 * 1080, 4), dtype=torch.float32, device=dev)
-    g = native.Guide(ctx, seed=9, center=center, half_extent=half)
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    sc.render_guided(g, hd, hd_acc, spp=hd_spp, max_depth=depth, seed=5, alpha=alpha, train=True,
-                     train_batch=batch, train_steps=steps, bounces=bounces, stream=stream)
-    e1.record(stream)
-    stream.synchronize()
-    t_hd = e0.elapsed_time(e1) / 1e3
-    e0.record(stream)
-    sc.render(hd, hd_acc, spp=hd_spp, max_depth=depth, seed=6, stream=stream)
-    e1.record(stream)
-    stream.synchronize()
-    t_hd_plain = e0.elapsed_time(e1) / 1e3
-    g.close()
+    # 1080p throughput of the guided tracer (training on), unless the section itself runs at 1080p
+    hd_out = None
+    if hd:
+        hd_cam = scenes.lower_camera(1920, 1080)
+        hd_acc = torch.zeros((1920 * 1080, 4), dtype=torch.float32, device=dev)
+        g = native.Guide(ctx, seed=9, center=center, half_extent=half)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sc.render_guided(g, hd_cam, hd_acc, spp=hd_spp, max_depth=depth, seed=5, alpha=alpha, train=True,
+                         train_batch=batch, train_steps=steps, bounces=bounces, stream=stream)
+        e1.record(stream)
+        stream.synchronize()
+        t_hd = e0.elapsed_time(e1) / 1e3
+        e0.record(stream)
+        sc.render(hd_cam, hd_acc, spp=hd_spp, max_depth=depth, seed=6, stream=stream)
+        e1.record(stream)
+        stream.synchronize()
+        t_hd_plain = e0.elapsed_time(e1) / 1e3
+        g.close()
+        del hd_acc
+        hd_out = {"spp": hd_spp, "guided_samples_per_s": 1920 * 1080 * hd_spp / t_hd,
+                  "plain_samples_per_s": 1920 * 1080 * hd_spp / t_hd_plain}
     desc = {"gap": "slab over the whole room but a gap of 0.15 half-widths along one wall",
             "centered": "centred slab over 0.7 of the width"}[scene]
     out = {"scene": f"occluded_light (2^20 triangles, 65,536 emitters above the slab, {desc}; floor and walls of "
                     f"albedo 0.4; half the spheres glass)",
            "indirect_fraction": indirect, "width": width, "height": height, "max_depth": depth,
            "reference_spp": ref_spp, "reference_accumulation": "fp64", "reference_seconds": round(ref_s, 2),
+           "reference_variance": var_ref,
+           "mse": "mean over pixels and channels of the squared error against the reference, minus the "
+                  "reference's variance (a quarter of the mean squared difference of its two halves)",
            "spp": spp, "seeds": seeds, "alpha": alpha,
            "plain": {"rmse": m_plain ** 0.5, "seconds": t_plain, "mse_per_seed": m_plain_s},
            "guided": {"rmse": m_guided ** 0.5, "seconds": t_guided, "mse_per_seed": m_guided_s, "final_loss": loss,
@@ -630,11 +648,10 @@ def guided_section(ctx, native, device: int, stream, width: int = 480, height: i
            "guided_trained_equal_spp": {"rmse": m_trained ** 0.5, "seconds": t_trained},
            "rmse_ratio_equal_spp": (m_plain / m_guided) ** 0.5, "rmse_ratio_equal_time": (m_eq / m_guided) ** 0.5,
            "rmse_ratio_trained_equal_spp": (m_plain / m_trained) ** 0.5,
-           "hd_1080p": {"spp": hd_spp, "guided_samples_per_s": 1920 * 1080 * hd_spp / t_hd,
-                        "plain_samples_per_s": 1920 * 1080 * hd_spp / t_hd_plain}}
+           "hd_1080p": hd_out}
     for g in guides:
         g.close()
-    del sc, acc, ref, hd_acc
+    del sc, acc, ref_img
     torch.cuda.empty_cache()
     return out
 
@@ -850,6 +867,8 @@ def main():
     ap.add_argument("--no-guided", action="store_true")
     ap.add_argument("--guided-ref-spp", type=int, default=65536)
     ap.add_argument("--guided-scene", choices=["gap", "centered"], default="gap")
+    ap.add_argument("--guided-size", type=int, nargs=2, default=[480, 270], metavar=("W", "H"))
+    ap.add_argument("--guided-spp", type=int, default=1024)
     ap.add_argument("--batch-scenes", type=int, default=64)
     ap.add_argument("--layout", type=int, default=0, help="BVH layout of the trace workload: 0 default, 2, 8")
     ap.add_argument("--render-layout", type=int, default=0, help="BVH layout of the render workloads")

@@ -6,9 +6,12 @@
 namespace dr {
 
 // Network outputs y[slot][40] for the rows list[0 .. *count) (positions and
-// directions read at the same slots). At most max_rows rows.
+// directions read at the same slots). At most max_rows rows. With `decoded`,
+// each row's mixture is stored decoded for the shading kernel instead
+// (guide_store_decoded).
 cudaError_t launch_guide_infer(const dr_guide *g, const float *pos, const float *dir, const uint32_t *list,
-                               const uint32_t *count, uint32_t max_rows, float *y, cudaStream_t st);
+                               const uint32_t *count, uint32_t max_rows, float *y, cudaStream_t st,
+                               bool decoded = false);
 
 // Adam steps the network has taken (enqueued).
 uint32_t guide_steps(const dr_guide *g);

@@ -154,4 +154,72 @@ __host__ __device__ inline float guide_loss_grad(const float *y, float wx, float
     return logq;
 }
 
+#if defined(__CUDACC__)
+// The mixture as the shading kernel uses it: the network output decoded once
+// per vertex, each lobe's vMF normalisation folded into its weight, so that a
+// density evaluation costs one exponential per lobe. Every loop over the lobes
+// is unrolled with constant indices, which keeps the mixture in registers (a
+// lobe picked by a run-time index would put the whole mixture in local memory).
+struct GuideMix {
+    float c[kGuideLobes];      // pi_j kappa_j / (2 pi (1 - e^{-2 kappa_j}))
+    float pi[kGuideLobes];     // mixture weights (lobe choice when sampling)
+    float kappa[kGuideLobes];
+    float mx[kGuideLobes], my[kGuideLobes], mz[kGuideLobes];  // unit mean directions
+};
+
+// From the 40 network outputs v (in registers).
+__device__ __forceinline__ GuideMix guide_mix_values(const float (&v)[kGuideOut])
+{
+    GuideMix M;
+    float mx = v[0];
+#pragma unroll
+    for (int j = 1; j < kGuideLobes; ++j) mx = fmaxf(mx, v[5 * j]);
+    float s = 0.0f;
+#pragma unroll
+    for (int j = 0; j < kGuideLobes; ++j) {
+        M.pi[j] = __expf(v[5 * j] - mx);
+        s += M.pi[j];
+    }
+    const float inv = 1.0f / s;
+#pragma unroll
+    for (int j = 0; j < kGuideLobes; ++j) {
+        M.pi[j] *= inv;
+        const float k = __expf(fminf(fmaxf(v[5 * j + 1], kGuideLogKMin), kGuideLogKMax));
+        M.kappa[j] = k;
+        // kappa >= e^-4, so 1 - e^{-2 kappa} >= 0.036 and needs no series
+        M.c[j] = M.pi[j] * k / (6.28318530718f * (1.0f - __expf(-2.0f * k)));
+        const float a = v[5 * j + 2], b = v[5 * j + 3], c = v[5 * j + 4];
+        const float n2 = a * a + b * b + c * c;
+        const bool deg = n2 < 1e-24f;
+        const float r = deg ? 0.0f : rsqrtf(n2);
+        M.mx[j] = a * r, M.my[j] = b * r, M.mz[j] = deg ? 1.0f : c * r;
+    }
+    return M;
+}
+
+__device__ __forceinline__ GuideMix guide_mix(const float *y)
+{
+    float v[kGuideOut];
+#pragma unroll
+    for (int i = 0; i < kGuideOut / 4; ++i) {
+        const float4 q = reinterpret_cast<const float4 *>(y)[i];
+        v[4 * i] = q.x, v[4 * i + 1] = q.y, v[4 * i + 2] = q.z, v[4 * i + 3] = q.w;
+    }
+    return guide_mix_values(v);
+}
+
+// Decoded layout for the shading kernel: five arrays of 8 floats (c_j,
+// kappa_j, mu_j x, y, z), 16-byte aligned.
+__device__ __forceinline__ void guide_store_decoded(float *y, const GuideMix &M)
+{
+    float4 *d = reinterpret_cast<float4 *>(y);
+    d[0] = make_float4(M.c[0], M.c[1], M.c[2], M.c[3]), d[1] = make_float4(M.c[4], M.c[5], M.c[6], M.c[7]);
+    d[2] = make_float4(M.kappa[0], M.kappa[1], M.kappa[2], M.kappa[3]);
+    d[3] = make_float4(M.kappa[4], M.kappa[5], M.kappa[6], M.kappa[7]);
+    d[4] = make_float4(M.mx[0], M.mx[1], M.mx[2], M.mx[3]), d[5] = make_float4(M.mx[4], M.mx[5], M.mx[6], M.mx[7]);
+    d[6] = make_float4(M.my[0], M.my[1], M.my[2], M.my[3]), d[7] = make_float4(M.my[4], M.my[5], M.my[6], M.my[7]);
+    d[8] = make_float4(M.mz[0], M.mz[1], M.mz[2], M.mz[3]), d[9] = make_float4(M.mz[4], M.mz[5], M.mz[6], M.mz[7]);
+}
+#endif
+
 }  // namespace dr

@@ -357,7 +357,7 @@ __device__ __forceinline__ void fetch_weight_image(uint32_t dst, const unsigned 
 __global__ void __launch_bounds__(128) k_guide_infer_tc(const unsigned char *img, const float *params, GuideParams gp,
                                                         const float *pos, const float *dir, const uint32_t *list,
                                                         const uint32_t *count, uint32_t n_fixed, float *y,
-                                                        uint32_t *error)
+                                                        uint32_t *error, bool decoded)
 {
     extern __shared__ __align__(1024) unsigned char smem[];
     const int tid = threadIdx.x, warp = tid >> 5;
@@ -457,6 +457,11 @@ __global__ void __launch_bounds__(128) k_guide_infer_tc(const unsigned char *img
                     *reinterpret_cast<uint4 *>(smem + kTcA + canon_off(tid, 8 * j, kTcRows)) =
                         make_uint4(q[0], q[1], q[2], q[3]);
                 }
+            } else if (slot != 0xffffffffu && decoded) {
+                float o[kGuideOut];
+#pragma unroll
+                for (int i = 0; i < kGuideOut; ++i) o[i] = v[i] + b[i];
+                guide_store_decoded(y + (size_t)slot * kGuideOut, guide_mix_values(o));
             } else if (slot != 0xffffffffu) {
                 float4 *dst = reinterpret_cast<float4 *>(y + (size_t)slot * kGuideOut);
 #pragma unroll
@@ -1204,20 +1209,35 @@ dr_status run_gradients(dr_guide *g, const float *pos, const float *dir, const f
 
 namespace dr {
 
+// Rewrites rows list[0 .. *count) of y (or rows 0 .. n_fixed) in the decoded
+// layout, after the mma.sync inference (whose rows are spread over 4 lanes).
+__global__ void __launch_bounds__(128) k_guide_decode_rows(const uint32_t *list, const uint32_t *count, uint32_t n_fixed,
+                                                           float *y)
+{
+    const uint32_t n = count ? *count : n_fixed;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float *row = y + (size_t)(list ? list[i] : i) * kGuideOut;
+        guide_store_decoded(row, guide_mix(row));
+    }
+}
+
 cudaError_t launch_guide_infer(const dr_guide *g, const float *pos, const float *dir, const uint32_t *list,
-                               const uint32_t *count, uint32_t max_rows, float *y, cudaStream_t st)
+                               const uint32_t *count, uint32_t max_rows, float *y, cudaStream_t st, bool decoded)
 {
     if (max_rows == 0) return cudaSuccess;
     if (g->cfg.infer_kernel == DR_GUIDE_INFER_TCGEN05) {
         const unsigned tiles = (max_rows + kTcRows - 1) / kTcRows;
         const unsigned blocks = std::min<unsigned>(tiles, (unsigned)g->ctx->num_sms * 3);
         k_guide_infer_tc<<<blocks, 128, kTcSmem, st>>>(g->img, g->params, guide_params(g), pos, dir, list, count,
-                                                       max_rows, y, g->ctx->d_error);
+                                                       max_rows, y, g->ctx->d_error, decoded);
     } else {
         const unsigned tiles = (max_rows + 15) / 16;
         const unsigned blocks = std::min<unsigned>((tiles + 3) / 4, (unsigned)g->ctx->num_sms * 4);
         k_guide_infer<<<blocks, 128, kInferSmem, st>>>(g->wb, g->params, guide_params(g), pos, dir, list, count,
                                                        max_rows, y);
+        if (decoded)
+            k_guide_decode_rows<<<std::min<unsigned>((max_rows + 127) / 128, (unsigned)g->ctx->num_sms * 8), 128, 0,
+                                  st>>>(list, count, max_rows, y);
     }
     return cudaGetLastError();
 }

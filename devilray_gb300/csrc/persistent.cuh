@@ -152,6 +152,7 @@ __device__ __forceinline__ void persistent_wide(const Wide8Args &a, const Source
                                                 unsigned long long &nhits, uint32_t fixed_chunk = 0)
 {
     constexpr unsigned FULL = 0xffffffffu;
+    constexpr bool HALF = !ANY && DR_HALF_CVT;  // node tests with FP16 grid planes (closest hit)
     const int lane = threadIdx.x & 31;
     const unsigned lower = (1u << lane) - 1u;
     WideState s;
@@ -221,14 +222,14 @@ __device__ __forceinline__ void persistent_wide(const Wide8Args &a, const Source
         bool fin = false;  // no node left (found during the extra node tests)
         if constexpr (BATCH) {
             // 1. node test(s)
-            if (active && !waiting && s.have_node) wide_visit<MODE>(a, s, cn, cb);
+            if (active && !waiting && s.have_node) wide_visit<MODE, HALF>(a, s, cn, cb);
 #pragma unroll 1
             for (int k = 1; k < DR_INNER_STEPS_BATCH; ++k) {
                 const bool go = active && !waiting && !fin && s.tmask == 0;
                 if (__popc(__ballot_sync(FULL, go)) < DR_INNER_MIN_LANES_BATCH) break;
                 if (go) {
                     fin = wide_advance<ANY>(a, s, stack);
-                    if (!fin && s.have_node) wide_visit<MODE>(a, s, cn, cb);
+                    if (!fin && s.have_node) wide_visit<MODE, HALF>(a, s, cn, cb);
                 }
             }
             // 2. leaf triangles join the warp batch (whole groups, in lane
@@ -279,14 +280,14 @@ __device__ __forceinline__ void persistent_wide(const Wide8Args &a, const Source
             }
         } else {
             // 1. node test(s)
-            if (active && s.have_node) wide_visit<MODE>(a, s, cn, cb);
+            if (active && s.have_node) wide_visit<MODE, HALF>(a, s, cn, cb);
 #pragma unroll 1
             for (int k = 1; k < DR_INNER_STEPS_LANE; ++k) {
                 const bool go = active && !fin && s.tmask == 0;
                 if (__popc(__ballot_sync(FULL, go)) < DR_INNER_MIN_LANES_LANE) break;
                 if (go) {
                     fin = wide_advance<ANY>(a, s, stack);
-                    if (!fin && s.have_node) wide_visit<MODE>(a, s, cn, cb);
+                    if (!fin && s.have_node) wide_visit<MODE, HALF>(a, s, cn, cb);
                 }
             }
             // 2. leaf triangles: tested now when enough lanes of the warp have

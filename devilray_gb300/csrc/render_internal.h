@@ -89,6 +89,7 @@ struct GuideRun {
     uint32_t streams = 1; // concurrent waves; training of the waves runs one after another
     uint32_t target = 0;  // training target: 0 radiance, 1 log(1 + radiance)
     uint32_t bounces = 64;  // bounces b < bounces are guided
+    uint32_t alpha_ramp = 0;  // alpha rises linearly over the network's first alpha_ramp steps, 0 = none
 };
 
 // Packs the samples of `jobs` (their npix and spp) into waves.

@@ -434,11 +434,11 @@ class Scene:
                       max_depth: int = 10, sample_offset: int = 0, pixel_sampling: int = 1, seed: int = 0,
                       alpha: float = 0.5, train: bool = True, train_batch: int = 0, train_steps: int = 0,
                       train_budget: int = 0, target: int = 0, bounces: int = 0, wave_paths: int = 0, streams: int = 0,
-                      stream=None):
+                      alpha_ramp: int = 0, stream=None):
         c = make_camera(cam)
         cfg = RenderConfig(max_depth, spp, sample_offset, pixel_sampling, seed, DR_TRI_REFERENCE, wave_paths, 0, 0,
                            streams, 0, 0)
-        g = GuidedConfig(alpha, 1 if train else 0, train_batch, train_steps, train_budget, target, bounces)
+        g = GuidedConfig(alpha, 1 if train else 0, train_batch, train_steps, train_budget, target, bounces, alpha_ramp)
         check(load().dr_render_guided(self.handle, C.byref(c), C.byref(cfg), guide.handle, C.byref(g), _ptr(accum_dev),
                                       _ptr(casts_dev), _stream_ptr(stream)))
 
@@ -562,7 +562,8 @@ def render_batch(ctx: "Context", jobs: list, wave_paths: int = 0, streams: int =
 
 class GuidedConfig(C.Structure):
     _fields_ = [("alpha", C.c_float), ("train", C.c_uint32), ("train_batch", C.c_uint32), ("train_steps", C.c_uint32),
-                ("train_budget", C.c_uint32), ("target", C.c_uint32), ("bounces", C.c_uint32)]
+                ("train_budget", C.c_uint32), ("target", C.c_uint32), ("bounces", C.c_uint32),
+                ("alpha_ramp", C.c_uint32)]
 
 
 class GuideConfig(C.Structure):

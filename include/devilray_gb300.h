@@ -463,6 +463,9 @@ typedef struct dr_guided_config {
                                  sampled direction), 1 = log(1 + L) cos (less dominated by rare bright paths) */
     uint32_t bounces;         /* guide the vertices of bounces 0 .. bounces-1 only (later ones sample the
                                  cosine lobe, no network evaluation), 0 = all */
+    uint32_t alpha_ramp;      /* a wave uses alpha x min(1, s / alpha_ramp), s the Adam steps the network
+                                 has taken when the wave is issued: an untrained network proposes
+                                 little; 0 = alpha throughout */
 } dr_guided_config;
 
 /* dr_render with path guiding: at each diffuse vertex the network's mixture
