@@ -697,6 +697,7 @@ def _read_probes(ctx, device: int):
 #   python bench.py --case render_many_light [spp]
 #   python bench.py --case batch_small            # 8 uneven scenes, graph, 2 renders
 #   python bench.py --case guided [spp]           # occluded-light scene, plain vs guided
+#   python bench.py --case guided_phases          # training, plain and frozen guided renders (NVTX ranges)
 # Each case prints one line with its timing; run it once plainly before running
 # it under a profiler.
 
@@ -849,8 +850,57 @@ def case_guided(spp: int = 32) -> None:
 
 
 
+def case_guided_phases(width: int = 480, height: int = 270, later_spp: int = 448) -> None:
+    """The guided render's phases for a launch list, at width x height
+    (480x270 by default), depth 16, waves of 16 spp: a fresh network trains
+    over 64 spp inside the NVTX range "train" (alpha 0.75, 3 guided bounces,
+    16 Adam steps of 65,536 samples after every wave) and over `later_spp`
+    more outside any range (448: 512 steps in all); then, inside the range
+    "measure", the plain tracer renders 64 spp and the guided one 64 spp with
+    the network frozen. Torch fills mark the phases."""
+    import torch
+    from devilray_gb300 import scenes
+    native, ctx = _case_ctx()
+    spec = scenes.occluded_light(slab_gap=0.15)
+    sc = native.Scene.from_spec(ctx, spec)
+    cam = scenes.lower_camera(width, height)
+    n = width * height
+    acc = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+    pos = spec.positions.reshape(-1, 3)
+    lo, hi = pos.min(0), pos.max(0)
+    g = native.Guide(ctx, seed=1, center=tuple(float(x) for x in (lo + hi) / 2),
+                     half_extent=float((hi - lo).max() / 2))
+    kw = dict(max_depth=16, alpha=0.75, train_batch=65536, train_steps=16, train_budget=512, bounces=3,
+              wave_paths=16 * n)
+    marker = torch.zeros(7777, device="cuda")
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_push("train")
+    marker.fill_(0.5)
+    sc.render_guided(g, cam, acc, spp=64, seed=11, train=True, **kw)
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
+    if later_spp:
+        sc.render_guided(g, cam, acc, spp=later_spp, seed=1, train=True, **kw)
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_push("measure")
+    marker.fill_(1.0)
+    sc.render(cam, acc, spp=64, max_depth=16, seed=2, wave_paths=16 * n)
+    torch.cuda.synchronize()
+    marker.fill_(2.0)
+    sc.render_guided(g, cam, acc, spp=64, seed=3, train=False, **{k: kw[k] for k in ("max_depth", "alpha", "bounces",
+                                                                                       "wave_paths")})
+    torch.cuda.synchronize()
+    marker.fill_(3.0)
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
+    print(f"guided_phases: loss {g.last_loss():.4f}")
+    g.close()
+    ctx.check()
+
+
 CASES = {"guide_infer": case_guide_infer, "guide_train": case_guide_train, "render_box_room": case_render_box_room,
-         "render_many_light": case_render_many_light, "batch_small": case_batch_small, "guided": case_guided}
+         "render_many_light": case_render_many_light, "batch_small": case_batch_small, "guided": case_guided,
+         "guided_phases": case_guided_phases}
 
 
 def main():

@@ -34,6 +34,12 @@ namespace dr {
 namespace {
 
 constexpr int kIn = 80, kHid = 64, kOut = 48, kLayers = 5;
+
+// CTAs per SM of the tcgen05 inference launch (at most 3 fit: 62.7 KB of
+// shared memory each).
+#ifndef DR_INFER_CTAS_PER_SM
+#define DR_INFER_CTAS_PER_SM 3
+#endif
 __host__ __device__ constexpr int fan_in(int l) { return l == 0 ? kIn : kHid; }
 __host__ __device__ constexpr int fan_out(int l) { return l == kLayers - 1 ? kOut : kHid; }
 
@@ -1227,7 +1233,7 @@ cudaError_t launch_guide_infer(const dr_guide *g, const float *pos, const float 
     if (max_rows == 0) return cudaSuccess;
     if (g->cfg.infer_kernel == DR_GUIDE_INFER_TCGEN05) {
         const unsigned tiles = (max_rows + kTcRows - 1) / kTcRows;
-        const unsigned blocks = std::min<unsigned>(tiles, (unsigned)g->ctx->num_sms * 3);
+        const unsigned blocks = std::min<unsigned>(tiles, (unsigned)g->ctx->num_sms * DR_INFER_CTAS_PER_SM);
         k_guide_infer_tc<<<blocks, 128, kTcSmem, st>>>(g->img, g->params, guide_params(g), pos, dir, list, count,
                                                        max_rows, y, g->ctx->d_error, decoded);
     } else {

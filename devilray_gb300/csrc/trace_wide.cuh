@@ -69,6 +69,26 @@ constexpr int kWideStack = 64;
 #ifndef DR_HALF_CVT
 #define DR_HALF_CVT 1
 #endif
+// FP16 path only: near/far plane words chosen by integer multiply-adds on the
+// FMA pipe instead of selects (DR_SEL_IMAD; it spills: 3.269 -> 3.417 ms),
+// and the hit bits accumulated by FP32 FMAs of set.le.f32 results instead of
+// predicated ORs (DR_HIT_FSET: 3.269 -> 3.192 ms on the incoherent workload).
+#ifndef DR_SEL_IMAD
+#define DR_SEL_IMAD 0
+#endif
+#ifndef DR_HIT_FSET
+#define DR_HIT_FSET 1
+#endif
+// The same accumulation in the packed and scalar node tests (any hit,
+// renderer): measured without effect (any hit 2.842 / 2.844 ms), so off.
+#ifndef DR_HIT_FSET_ALL
+#define DR_HIT_FSET_ALL 0
+#endif
+// Children in slot order instead of the ray's octant order (off: an
+// experiment; results are the same, only the visiting order changes).
+#ifndef DR_NO_OCT_ORDER
+#define DR_NO_OCT_ORDER 0
+#endif
 // Prefetch into L1 of the next sibling node when a node is chosen (off).
 #ifndef DR_PREFETCH_NEXT
 #define DR_PREFETCH_NEXT 0
@@ -195,6 +215,21 @@ __host__ __device__ __forceinline__ SlabAxis slab_axis_h(float a, float b)
 }
 
 #if defined(__CUDA_ARCH__)
+// 1.0f when a <= b, else 0.0f (false for NaN operands, as the comparison)
+__device__ __forceinline__ float set_le(float a, float b)
+{
+    float r;
+    asm("set.le.f32.f32 %0, %1, %2;" : "=f"(r) : "f"(a), "f"(b));
+    return r;
+}
+
+__device__ __forceinline__ uint32_t mad_u32(uint32_t a, uint32_t b, uint32_t c)
+{
+    uint32_t d;
+    asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+    return d;
+}
+
 // Bytes j and j + 2 of w as the FP32 values 1024 + q (j = 0 or 1).
 __device__ __forceinline__ float2 byte_pair_h(uint32_t w, uint32_t j)
 {
@@ -239,6 +274,27 @@ __host__ __device__ __forceinline__ void wide_node_test(const Bvh8Node *node, co
     uint32_t boxes = 0, hit_bits = 0;
 #if DR_FAST_SLAB && DR_NODE_META_BITS == 2 && defined(__CUDA_ARCH__)
     if (HALF) {
+#if DR_SEL_IMAD
+    // s = 1 for a negative direction: near = lo + s (hi - lo), far = hi - s (hi - lo)
+    const uint32_t sgx = __float_as_uint(r.inv.x) >> 31, sgy = __float_as_uint(r.inv.y) >> 31,
+                   sgz = __float_as_uint(r.inv.z) >> 31;
+    const uint32_t ngx = 0u - sgx, ngy = 0u - sgy, ngz = 0u - sgz, m1 = 0xffffffffu;
+    const uint32_t dx0 = mad_u32(wx.x, m1, wx.z), dx1 = mad_u32(wx.y, m1, wx.w);
+    const uint32_t dy0 = mad_u32(wy.x, m1, wy.z), dy1 = mad_u32(wy.y, m1, wy.w);
+    const uint32_t dz0 = mad_u32(wz.x, m1, wz.z), dz1 = mad_u32(wz.y, m1, wz.w);
+    const uint32_t hnx0 = mad_u32(sgx, dx0, wx.x), hnx1 = mad_u32(sgx, dx1, wx.y);
+    const uint32_t hfx0 = mad_u32(ngx, dx0, wx.z), hfx1 = mad_u32(ngx, dx1, wx.w);
+    const uint32_t hny0 = mad_u32(sgy, dy0, wy.x), hny1 = mad_u32(sgy, dy1, wy.y);
+    const uint32_t hfy0 = mad_u32(ngy, dy0, wy.z), hfy1 = mad_u32(ngy, dy1, wy.w);
+    const uint32_t hnz0 = mad_u32(sgz, dz0, wz.x), hnz1 = mad_u32(sgz, dz1, wz.y);
+    const uint32_t hfz0 = mad_u32(ngz, dz0, wz.z), hfz1 = mad_u32(ngz, dz1, wz.w);
+#else
+    const uint32_t hnx0 = nx0, hnx1 = nx1, hfx0 = fx0, hfx1 = fx1, hny0 = ny0, hny1 = ny1, hfy0 = fy0, hfy1 = fy1;
+    const uint32_t hnz0 = nz0, hnz1 = nz1, hfz0 = fz0, hfz1 = fz1;
+#endif
+#if DR_HIT_FSET
+    float hit_f = 0.0f;
+#endif
     // slots 4h + j and 4h + j + 2 (bytes j and j + 2 of word h) as pairs
     const SlabAxis hx = slab_axis_h(ax, bx), hy = slab_axis_h(ay, by), hz = slab_axis_h(az, bz);
     const float2 Ax = make_float2(hx.a, hx.a), NBx = make_float2(hx.near_b, hx.near_b),
@@ -252,19 +308,29 @@ __host__ __device__ __forceinline__ void wide_node_test(const Bvh8Node *node, co
     for (int h = 0; h < 2; ++h) {
 #pragma unroll
         for (uint32_t j = 0; j < 2; ++j) {
-            const float2 tnx = __ffma2_rn(byte_pair_h(h ? nx1 : nx0, j), Ax, NBx);
-            const float2 tfx = __ffma2_rn(byte_pair_h(h ? fx1 : fx0, j), Ax, FBx);
-            const float2 tny = __ffma2_rn(byte_pair_h(h ? ny1 : ny0, j), Ay, NBy);
-            const float2 tfy = __ffma2_rn(byte_pair_h(h ? fy1 : fy0, j), Ay, FBy);
-            const float2 tnz = __ffma2_rn(byte_pair_h(h ? nz1 : nz0, j), Az, NBz);
-            const float2 tfz = __ffma2_rn(byte_pair_h(h ? fz1 : fz0, j), Az, FBz);
+            const float2 tnx = __ffma2_rn(byte_pair_h(h ? hnx1 : hnx0, j), Ax, NBx);
+            const float2 tfx = __ffma2_rn(byte_pair_h(h ? hfx1 : hfx0, j), Ax, FBx);
+            const float2 tny = __ffma2_rn(byte_pair_h(h ? hny1 : hny0, j), Ay, NBy);
+            const float2 tfy = __ffma2_rn(byte_pair_h(h ? hfy1 : hfy0, j), Ay, FBy);
+            const float2 tnz = __ffma2_rn(byte_pair_h(h ? hnz1 : hnz0, j), Az, NBz);
+            const float2 tfz = __ffma2_rn(byte_pair_h(h ? hfz1 : hfz0, j), Az, FBz);
             const float2 tmx = __fmul2_rn(make_float2(fminf(min3f(tfx.x, tfy.x, tfz.x), tmax),
                                                       fminf(min3f(tfx.y, tfy.y, tfz.y), tmax)), farS);
             const uint32_t s0 = 4u * h + j;
+#if DR_HIT_FSET
+            hit_f = fmaf(set_le(fmaxf(max3f(tnx.x, tny.x, tnz.x), 0.0f), tmx.x), (float)(1u << s0),
+                         fmaf(set_le(fmaxf(max3f(tnx.y, tny.y, tnz.y), 0.0f), tmx.y), (float)(1u << (s0 + 2)), hit_f));
+#else
             if (fmaxf(max3f(tnx.x, tny.x, tnz.x), 0.0f) <= tmx.x) hit_bits |= 1u << s0;
             if (fmaxf(max3f(tnx.y, tny.y, tnz.y), 0.0f) <= tmx.y) hit_bits |= 1u << (s0 + 2);
+#endif
         }
     }
+#if DR_HIT_FSET
+    // a sum of distinct powers of two below 256 is exact: 2^23 + sum has it in
+    // its low mantissa bits
+    hit_bits = __float_as_uint(hit_f + 8388608.0f) & 0xffu;
+#endif
     } else
 #endif
     {
@@ -279,6 +345,9 @@ __host__ __device__ __forceinline__ void wide_node_test(const Bvh8Node *node, co
     const float2 Az = make_float2(cz.a, cz.a), NBz = make_float2(cz.near_b, cz.near_b),
                  FBz = make_float2(cz.far_b, cz.far_b);
     const float2 farS = make_float2(kBoxFarScale, kBoxFarScale);
+#if DR_HIT_FSET_ALL
+    float hit_f = 0.0f;
+#endif
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
         const float2 tnx = __ffma2_rn(make_float2(byte_q(nx0, j), byte_q(nx1, j)), Ax, NBx);
@@ -289,10 +358,21 @@ __host__ __device__ __forceinline__ void wide_node_test(const Bvh8Node *node, co
         const float2 tfz = __ffma2_rn(make_float2(byte_q(fz0, j), byte_q(fz1, j)), Az, FBz);
         const float2 tmx = __fmul2_rn(make_float2(fminf(min3f(tfx.x, tfy.x, tfz.x), tmax),
                                                   fminf(min3f(tfx.y, tfy.y, tfz.y), tmax)), farS);
+#if DR_HIT_FSET_ALL
+        hit_f = fmaf(set_le(fmaxf(max3f(tnx.x, tny.x, tnz.x), 0.0f), tmx.x), (float)(1u << j),
+                     fmaf(set_le(fmaxf(max3f(tnx.y, tny.y, tnz.y), 0.0f), tmx.y), (float)(1u << (j + 4)), hit_f));
+#else
         if (fmaxf(max3f(tnx.x, tny.x, tnz.x), 0.0f) <= tmx.x) hit_bits |= 1u << j;
         if (fmaxf(max3f(tnx.y, tny.y, tnz.y), 0.0f) <= tmx.y) hit_bits |= 1u << (j + 4);
+#endif
     }
+#if DR_HIT_FSET_ALL
+    hit_bits = __float_as_uint(hit_f + 8388608.0f) & 0xffu;
+#endif
 #else
+#if DR_HIT_FSET_ALL && defined(__CUDA_ARCH__)
+    float hit_fs = 0.0f;
+#endif
 #pragma unroll
     for (int s = 0; s < 8; ++s) {
         const int j = s & 3;
@@ -312,7 +392,11 @@ __host__ __device__ __forceinline__ void wide_node_test(const Bvh8Node *node, co
         const float tmx = fminf(min3f(tfx, tfy, tfz), tmax) * kBoxFarScale;
 #if DR_NODE_META_BITS == 2
         // one bit per slot; the metadata is read after the loop
+#if DR_HIT_FSET_ALL && defined(__CUDA_ARCH__)
+        hit_fs = fmaf(set_le(tmin, tmx), (float)(1u << s), hit_fs);
+#else
         if (tmin <= tmx) hit_bits |= 1u << s;
+#endif
 #else
         const uint32_t meta = ((s < 4 ? w1.z : w1.w) >> (8 * j)) & 0xffu;
         if (meta != 0) ++boxes;
@@ -335,6 +419,9 @@ __host__ __device__ __forceinline__ void wide_node_test(const Bvh8Node *node, co
         }
 #endif
     }
+#if DR_HIT_FSET_ALL && defined(__CUDA_ARCH__) && DR_NODE_META_BITS == 2
+    hit_bits = __float_as_uint(hit_fs + 8388608.0f) & 0xffu;
+#endif
 #endif
     }
 #if DR_NODE_META_BITS
@@ -353,9 +440,11 @@ __host__ __device__ __forceinline__ void wide_node_test(const Bvh8Node *node, co
     uint32_t m = hit_bits >> 24;
 #endif
     // internal hits from slot order to traversal order: bit s -> bit s ^ oct
+#if !DR_NO_OCT_ORDER
     if (oct & 1u) m = ((m & 0x55u) << 1) | ((m >> 1) & 0x55u);
     if (oct & 2u) m = ((m & 0x33u) << 2) | ((m >> 2) & 0x33u);
     if (oct & 4u) m = ((m & 0x0fu) << 4) | ((m >> 4) & 0x0fu);
+#endif
     hit_internal = m;
 #endif
     nboxes = boxes;
@@ -384,7 +473,7 @@ __host__ __device__ __forceinline__ void wide_init(WideState &s, const DevRay &r
 {
     s.r = r;
     if (MODE == 1) s.w = wt_setup(r.v);
-    s.oct = ray_octant(r);
+    s.oct = DR_NO_OCT_ORDER ? 0u : ray_octant(r);
     s.best_t = r.tmax;
     s.best_prim = INT_MAX;
     s.node = root;
@@ -523,7 +612,7 @@ __host__ __device__ __forceinline__ bool wide_traverse(const Wide8Args &a, const
     if (root == kNoRoot) return false;
     WtSetup w;
     if (MODE == 1) w = wt_setup(r.v);
-    const uint32_t oct = ray_octant(r);
+    const uint32_t oct = DR_NO_OCT_ORDER ? 0u : ray_octant(r);
     uint2 stack[kWideStack];
     int sp = 0;
     // the root is visited directly
