@@ -36,14 +36,14 @@ NUM_TRIS = 1 << 20
 NUM_RAYS = 1 << 24
 # DRAM bytes of one full 16.8 M-ray launch of the dominant kernel, from one
 # `ncu --set full` capture of this workload (the profiles named beside them).
-NCU_TRAFFIC = {8: 929_616_896 + 130_685_952, 2: 1_652_000_000 + 152_000_000}
+NCU_TRAFFIC = {8: 930_092_288 + 130_737_664, 2: 1_652_000_000 + 152_000_000}
 NCU_PROFILE = {8: "trace_closest_p8_incoherent_1M_tris_16M_rays.md",
                2: "trace_closest_bvh2_incoherent_1M_tris_16M_rays.md"}
 # Warp instructions per ray of the dominant kernel (smsp__inst_executed.sum of
 # the same capture / 16,777,216 rays): with the launch time and the sampled SM
 # clock it gives the issue-slot fraction (4 schedulers per SM, one instruction
 # per scheduler and cycle).
-NCU_WARP_INST_PER_RAY = {8: 3_217_281_377 / NUM_RAYS}
+NCU_WARP_INST_PER_RAY = {8: 3_200_962_454 / NUM_RAYS}
 METRIC = "Mrays/s closest-hit"
 WORKLOAD = "incoherent closest-hit: 2^20-triangle icosphere soup, 16,777,216 rays"
 L2_BYTES = 129 * 1024 * 1024
