@@ -504,10 +504,8 @@ struct WideBuilder {
             return (uint32_t)b[0] | ((uint32_t)b[1] << 8) | ((uint32_t)b[2] << 16) | ((uint32_t)b[3] << 24);
         };
         nd.w[1] = make_uint4(child_base, tri_base, pack(meta), pack(meta + 4));
-        uint4 planes[3];
         for (int a = 0; a < 3; ++a)
-            planes[a] = make_uint4(pack(qlo[a]), pack(qlo[a] + 4), pack(qhi[a]), pack(qhi[a] + 4));
-        store_planes(nd, planes);
+            nd.w[2 + a] = make_uint4(pack(qlo[a]), pack(qlo[a] + 4), pack(qhi[a]), pack(qhi[a] + 4));
         for (auto &[t, i] : todo) emit(t, i, depth + 1);
     }
 };

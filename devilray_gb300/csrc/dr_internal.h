@@ -100,43 +100,10 @@ struct Bvh2 {
 // Child slots are ordered by octant: slot s sits towards the corner
 // (s&1 ? +x : -x, s&2 ? +y : -y, s&4 ? +z : -z), so a ray whose direction
 // signs are o (bit set = negative) visits slots in the order k ^ o.
-// DR_NODE16 (an alternative layout, 128 bytes): the grid planes as FP16 values
-// 1024 + q instead of bytes, one 16-byte word per plane of an axis:
-//   w[2 + 2a] = lower planes of axis a, w[3 + 2a] = upper planes;
-//   32-bit word k of a plane = (1024 + q[k]) | (1024 + q[k + 4]) << 16 as FP16.
-// The traversal then loads a ray's near and far planes by address (no
-// selects) and converts them with cvt.f32.f16 (no byte permutes).
-#ifndef DR_NODE16
-#define DR_NODE16 0
-#endif
-constexpr int kBvh8Words = DR_NODE16 ? 8 : 5;
 struct alignas(16) Bvh8Node {
-    uint4 w[kBvh8Words];
+    uint4 w[5];
 };
-static_assert(sizeof(Bvh8Node) == 16 * kBvh8Words, "Bvh8Node size");
-
-// Stores the byte planes b[a] = (lo[0..3], lo[4..7], hi[0..3], hi[4..7]) of
-// axis a in the node's layout.
-#if defined(__CUDACC__)
-__host__ __device__
-#endif
-inline void store_planes(Bvh8Node &nd, const uint4 (&b)[3])
-{
-#if DR_NODE16
-    auto half_pair = [](uint32_t w03, uint32_t w47, int k) {
-        const uint32_t q0 = (w03 >> (8 * k)) & 0xffu, q1 = (w47 >> (8 * k)) & 0xffu;
-        return (0x6400u | q0) | ((0x6400u | q1) << 16);
-    };
-    for (int a = 0; a < 3; ++a) {
-        nd.w[2 + 2 * a] = make_uint4(half_pair(b[a].x, b[a].y, 0), half_pair(b[a].x, b[a].y, 1),
-                                     half_pair(b[a].x, b[a].y, 2), half_pair(b[a].x, b[a].y, 3));
-        nd.w[3 + 2 * a] = make_uint4(half_pair(b[a].z, b[a].w, 0), half_pair(b[a].z, b[a].w, 1),
-                                     half_pair(b[a].z, b[a].w, 2), half_pair(b[a].z, b[a].w, 3));
-    }
-#else
-    for (int a = 0; a < 3; ++a) nd.w[2 + a] = b[a];
-#endif
-}
+static_assert(sizeof(Bvh8Node) == 80, "Bvh8Node must be 80 bytes");
 
 struct Bvh8 {
     std::vector<Bvh8Node> nodes;

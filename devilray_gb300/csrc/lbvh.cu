@@ -674,9 +674,7 @@ __global__ void k_wide_emit(const float *pos, const uint32_t *order, const int *
     nd.w[0] = make_uint4(__float_as_uint(u.lo[0]), __float_as_uint(u.lo[1]), __float_as_uint(u.lo[2]),
                          ebias[0] | (ebias[1] << 8) | (ebias[2] << 16) | (imask << 24));
     nd.w[1] = make_uint4(child_base, tri_base, meta[0], meta[1]);
-    uint4 planes[3];
-    for (int a = 0; a < 3; ++a) planes[a] = make_uint4(qlo[a][0], qlo[a][1], qhi[a][0], qhi[a][1]);
-    store_planes(nd, planes);
+    for (int a = 0; a < 3; ++a) nd.w[2 + a] = make_uint4(qlo[a][0], qlo[a][1], qhi[a][0], qhi[a][1]);
     nodes[task_node[t]] = nd;
 }
 
@@ -705,9 +703,7 @@ __global__ void k_wide_single(const float *pos, float slack, Bvh8Node *nodes, ui
     nd.w[0] = make_uint4(__float_as_uint(cb.lo[0]), __float_as_uint(cb.lo[1]), __float_as_uint(cb.lo[2]),
                          ebias[0] | (ebias[1] << 8) | (ebias[2] << 16));
     nd.w[1] = make_uint4(1u, 0u, 0x20u, 0u);  // slot 0: one triangle at offset 0
-    uint4 planes[3];
-    for (int a = 0; a < 3; ++a) planes[a] = make_uint4(0xffffff00u | ql[a], 0xffffffffu, qh[a], 0u);
-    store_planes(nd, planes);
+    for (int a = 0; a < 3; ++a) nd.w[2 + a] = make_uint4(0xffffff00u | ql[a], 0xffffffffu, qh[a], 0u);
     nodes[0] = nd;
     order8[0] = 0;
 }

@@ -89,6 +89,10 @@ constexpr int kWideStack = 64;
 #ifndef DR_NO_OCT_ORDER
 #define DR_NO_OCT_ORDER 0
 #endif
+// (Measured and dropped, same workload: the children in slot order instead of
+// the ray's octant order, 3.19 -> 3.71 ms; 128-byte nodes that store the
+// grid planes as FP16 words, so that no byte permute or near/far select is
+// left, 3.96 ms: the node loads cost more than the instructions saved.)
 // Prefetch into L1 of the next sibling node when a node is chosen (off).
 #ifndef DR_PREFETCH_NEXT
 #define DR_PREFETCH_NEXT 0
@@ -205,12 +209,6 @@ __host__ __device__ __forceinline__ SlabAxis slab_axis(float a, float b)
     return SlabAxis{a * 0.00390625f, x - off, x + off};
 }
 
-// Word k (0-3, a constant after unrolling) of a 16-byte vector.
-__host__ __device__ __forceinline__ uint32_t u4_word(const uint4 &v, int k)
-{
-    return k == 0 ? v.x : k == 1 ? v.y : k == 2 ? v.z : v.w;
-}
-
 // The same constants for grid values 1024 + q (DR_HALF_CVT): A = a,
 // B = fl(b - 1024 a) -+ off, with the bound of slab_axis.
 __host__ __device__ __forceinline__ SlabAxis slab_axis_h(float a, float b)
@@ -236,14 +234,6 @@ __device__ __forceinline__ uint32_t mad_u32(uint32_t a, uint32_t b, uint32_t c)
     return d;
 }
 
-// The two FP16 halves of w as FP32 (low, high).
-__device__ __forceinline__ float2 half_pair_f(uint32_t w)
-{
-    float lo, hi;
-    asm("{\n .reg .b16 l, h;\n mov.b32 {l, h}, %2;\n cvt.f32.f16 %0, l;\n cvt.f32.f16 %1, h;\n}" : "=f"(lo), "=f"(hi) : "r"(w));
-    return make_float2(lo, hi);
-}
-
 // Bytes j and j + 2 of w as the FP32 values 1024 + q (j = 0 or 1).
 __device__ __forceinline__ float2 byte_pair_h(uint32_t w, uint32_t j)
 {
@@ -264,11 +254,9 @@ __host__ __device__ __forceinline__ void wide_node_test(const Bvh8Node *node, co
 {
     const uint4 w0 = DR_LD(&node->w[0]);
     const uint4 w1 = DR_LD(&node->w[1]);
-#if !DR_NODE16
     const uint4 wx = DR_LD(&node->w[2]);
     const uint4 wy = DR_LD(&node->w[3]);
     const uint4 wz = DR_LD(&node->w[4]);
-#endif
     const float px = bits_f(w0.x), py = bits_f(w0.y), pz = bits_f(w0.z);
     const float sx = exp2_bits(w0.w & 0xffu), sy = exp2_bits((w0.w >> 8) & 0xffu), sz = exp2_bits((w0.w >> 16) & 0xffu);
     imask = w0.w >> 24;
@@ -277,54 +265,6 @@ __host__ __device__ __forceinline__ void wide_node_test(const Bvh8Node *node, co
     // slab time of grid coordinate q on each axis: t = q * a + b
     const float ax = sx * r.inv.x, ay = sy * r.inv.y, az = sz * r.inv.z;
     const float bx = (px - r.o.x) * r.inv.x, by = (py - r.o.y) * r.inv.y, bz = (pz - r.o.z) * r.inv.z;
-#if DR_NODE16
-    hit_internal = 0;
-    tri_mask = 0;
-    uint32_t boxes = 0, hit_bits = 0;
-    // the ray's near and far planes by address: the upper planes of an axis
-    // come first for a negative direction
-    const uint32_t gx = r.inv.x < 0.0f ? 1u : 0u, gy = r.inv.y < 0.0f ? 1u : 0u, gz = r.inv.z < 0.0f ? 1u : 0u;
-    const uint4 *pl = node->w + 2;
-    const uint4 pnx = DR_LD(pl + gx), pfx = DR_LD(pl + (gx ^ 1u));
-    const uint4 pny = DR_LD(pl + 2 + gy), pfy = DR_LD(pl + 3 - gy);
-    const uint4 pnz = DR_LD(pl + 4 + gz), pfz = DR_LD(pl + 5 - gz);
-    const SlabAxis hx = slab_axis_h(ax, bx), hy = slab_axis_h(ay, by), hz = slab_axis_h(az, bz);
-#if defined(__CUDA_ARCH__)
-    const float2 Ax = make_float2(hx.a, hx.a), NBx = make_float2(hx.near_b, hx.near_b),
-                 FBx = make_float2(hx.far_b, hx.far_b);
-    const float2 Ay = make_float2(hy.a, hy.a), NBy = make_float2(hy.near_b, hy.near_b),
-                 FBy = make_float2(hy.far_b, hy.far_b);
-    const float2 Az = make_float2(hz.a, hz.a), NBz = make_float2(hz.near_b, hz.near_b),
-                 FBz = make_float2(hz.far_b, hz.far_b);
-    const float2 farS = make_float2(kBoxFarScale, kBoxFarScale);
-    float hit_f = 0.0f;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        // word k of a plane holds slots k and k + 4
-        const float2 tnx = __ffma2_rn(half_pair_f(u4_word(pnx, k)), Ax, NBx);
-        const float2 tfx = __ffma2_rn(half_pair_f(u4_word(pfx, k)), Ax, FBx);
-        const float2 tny = __ffma2_rn(half_pair_f(u4_word(pny, k)), Ay, NBy);
-        const float2 tfy = __ffma2_rn(half_pair_f(u4_word(pfy, k)), Ay, FBy);
-        const float2 tnz = __ffma2_rn(half_pair_f(u4_word(pnz, k)), Az, NBz);
-        const float2 tfz = __ffma2_rn(half_pair_f(u4_word(pfz, k)), Az, FBz);
-        const float2 tmx = __fmul2_rn(make_float2(fminf(min3f(tfx.x, tfy.x, tfz.x), tmax),
-                                                  fminf(min3f(tfx.y, tfy.y, tfz.y), tmax)), farS);
-        hit_f = fmaf(set_le(fmaxf(max3f(tnx.x, tny.x, tnz.x), 0.0f), tmx.x), (float)(1u << k),
-                     fmaf(set_le(fmaxf(max3f(tnx.y, tny.y, tnz.y), 0.0f), tmx.y), (float)(1u << (k + 4)), hit_f));
-    }
-    hit_bits = __float_as_uint(hit_f + 8388608.0f) & 0xffu;
-#else
-    for (int sl = 0; sl < 8; ++sl) {
-        const int k = sl & 3, sh = 16 * (sl >> 2);
-        auto q = [&](const uint4 &v) { return (float)(1024u + ((u4_word(v, k) >> sh) & 0xffu)); };
-        const float tmin = fmaxf(max3f(fmaf(q(pnx), hx.a, hx.near_b), fmaf(q(pny), hy.a, hy.near_b),
-                                       fmaf(q(pnz), hz.a, hz.near_b)), 0.0f);
-        const float tmx = fminf(min3f(fmaf(q(pfx), hx.a, hx.far_b), fmaf(q(pfy), hy.a, hy.far_b),
-                                      fmaf(q(pfz), hz.a, hz.far_b)), tmax) * kBoxFarScale;
-        if (tmin <= tmx) hit_bits |= 1u << sl;
-    }
-#endif
-#else
 #if DR_FAST_SLAB
     const SlabAxis cx = slab_axis(ax, bx), cy = slab_axis(ay, by), cz = slab_axis(az, bz);
 #endif
@@ -488,7 +428,6 @@ __host__ __device__ __forceinline__ void wide_node_test(const Bvh8Node *node, co
 #endif
 #endif
     }
-#endif  // DR_NODE16
 #if DR_NODE_META_BITS
 #if DR_NODE_META_BITS == 2
     // leaf slots hit: their triangle bits from the metadata; empty slots have
