@@ -82,3 +82,25 @@ def test_online_training_changes_the_network_and_keeps_the_image(native, ctx):
     b, _ = _render(native, scene, cam, 256, 12, 10)
     ref, noise = 0.5 * (a.mean() + b.mean()), abs(a.mean() - b.mean())
     assert abs(guided.mean() - ref) < max(6.0 * noise, 0.05 * ref), (guided.mean(), a.mean(), b.mean())
+
+
+def test_alpha_ramp_and_step_budget(native, ctx):
+    """With alpha rising over the network's first steps the image still
+    converges to the plain tracer's; once the step budget is spent, further
+    training renders leave the network unchanged (no records, no steps)."""
+    spec = scenes.occluded_light(24 * 1280, 3000, seed=2, half=12.0)
+    scene = native.Scene.from_spec(ctx, spec)
+    cam = scenes.lower_camera(64, 48, distance=36.0, half=12.0)
+    g = _guide_for(native, ctx, spec, seed=6)
+    wave = 64 * 48 * 4
+    guided, _ = _render(native, scene, cam, 256, 12, 4, guide=g, alpha=0.5, train=True, train_batch=4096,
+                        train_steps=4, train_budget=32, alpha_ramp=24, wave_paths=wave)
+    assert np.all(np.isfinite(guided))
+    p_spent = g.params()
+    _render(native, scene, cam, 64, 12, 5, guide=g, alpha=0.5, train=True, train_batch=4096, train_steps=4,
+            train_budget=32, wave_paths=wave)
+    assert np.array_equal(p_spent, g.params())
+    a, _ = _render(native, scene, cam, 256, 12, 9)
+    b, _ = _render(native, scene, cam, 256, 12, 10)
+    ref, noise = 0.5 * (a.mean() + b.mean()), abs(a.mean() - b.mean())
+    assert abs(guided.mean() - ref) < max(6.0 * noise, 0.05 * ref), (guided.mean(), a.mean(), b.mean())
