@@ -45,6 +45,9 @@ NCU_PROFILE = {8: "trace_closest_p8_incoherent_1M_tris_16M_rays.md",
 # per scheduler and cycle).
 NCU_WARP_INST_PER_RAY = {8: 3_200_962_454 / NUM_RAYS}
 METRIC = "Mrays/s closest-hit"
+# Seconds the reference arm's timed steps may take in all (it sizes its
+# per-step sample of the workload to fit).
+REF_TIMED_BUDGET_S = 150
 WORKLOAD = "incoherent closest-hit: 2^20-triangle icosphere soup, 16,777,216 rays"
 L2_BYTES = 129 * 1024 * 1024
 
@@ -148,10 +151,21 @@ def run_reference(args):
     po.build(ref=False)
     bbh = po.BBH(soup)
     from devilray_gb300.scenes import rays6
-    sample = args.ref_sample
-    r6 = rays6(rays[:sample])
+    # Rays per timed step: the whole workload when the timed steps fit about
+    # REF_TIMED_BUDGET_S at the rate the warm-up measures, else the largest
+    # multiple of 2^16 rays that does (--ref-sample fixes it instead).
+    warm = rays6(rays[: 1 << 18])
+    rate = 0.0
     for _ in range(args.warmup):
-        bbh.trace_reference(r6[: max(1, sample // 8)], threads=threads)
+        t0 = time.perf_counter()
+        bbh.trace_reference(warm, threads=threads)
+        rate = max(rate, len(warm) / (time.perf_counter() - t0))
+    if args.ref_sample:
+        sample = min(NUM_RAYS, args.ref_sample)
+    else:
+        fit = int(rate * REF_TIMED_BUDGET_S / max(1, args.steps))
+        sample = NUM_RAYS if fit >= NUM_RAYS else max(1 << 16, fit >> 16 << 16)
+    r6 = rays6(rays[:sample])
     times = []
     for _ in range(args.steps):
         t0 = time.perf_counter()
@@ -166,9 +180,11 @@ def run_reference(args):
         "config": {"workload": WORKLOAD, "num_triangles": NUM_TRIS, "num_rays": NUM_RAYS,
                    "step_sample_rays": sample, "tri_mode": "reference"},
         "cpu_baseline": {"value": value, "unit": "Mrays/s", "cores": threads, "kind": "port",
-                         "sample": f"{sample} rays per step of the {NUM_RAYS}-ray workload; the reference's "
-                                   "median-split BBH and getIntersectionImpl restated in C++ (oracle), "
-                                   "std::thread over ray chunks on all host cores"},
+                         "sample": (f"all {NUM_RAYS} rays of the workload every step" if sample == NUM_RAYS else
+                                    f"{sample} rays per step of the {NUM_RAYS}-ray workload (the timed steps "
+                                    f"kept to about {REF_TIMED_BUDGET_S} s)") +
+                                   "; the reference's median-split BBH and getIntersectionImpl restated in C++ "
+                                   "(oracle), std::thread over ray chunks on all host cores"},
         "e2e": {"value": value, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -910,7 +926,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-sample", type=int, default=1 << 20)
-    ap.add_argument("--ref-sample", type=int, default=1 << 19)
+    ap.add_argument("--ref-sample", type=int, default=0,
+                    help="rays per timed step of --impl reference (0: the whole workload if the steps fit)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-render", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
