@@ -1337,6 +1337,62 @@ dr_status dr_guide_set_params(dr_guide *g, const float *host, uint32_t n)
     return DR_OK;
 }
 
+// State blob: a header (magic, version, parameter count, Adam step), the
+// configuration, then params, m and v (FP32, kNumParams each).
+namespace {
+constexpr uint32_t kStateMagic = 0x53475244u;  // "DRGS"
+constexpr uint32_t kStateVersion = 1;
+struct StateHeader {
+    uint32_t magic, version, num_params, step;
+    dr_guide_config cfg;
+};
+constexpr uint64_t kStateBytes = sizeof(StateHeader) + 3ull * kNumParams * sizeof(float);
+}  // namespace
+
+uint64_t dr_guide_state_bytes(void) { return kStateBytes; }
+
+dr_status dr_guide_get_state(dr_guide *g, void *host, uint64_t bytes)
+{
+    DR_CHECK_ARG(g && host, "dr_guide_get_state: NULL argument");
+    if (bytes != kStateBytes)
+        return fail(DR_ERR_INVALID_ARGUMENT, "dr_guide_get_state: the state takes %llu bytes, got %llu",
+                    (unsigned long long)kStateBytes, (unsigned long long)bytes);
+    DR_CUDA(cudaSetDevice(g->ctx->device));
+    DR_CUDA(cudaDeviceSynchronize());
+    StateHeader h{kStateMagic, kStateVersion, (uint32_t)kNumParams, (uint32_t)g->step, g->cfg};
+    auto *out = static_cast<unsigned char *>(host);
+    memcpy(out, &h, sizeof h);
+    float *f = reinterpret_cast<float *>(out + sizeof h);
+    DR_CUDA(cudaMemcpy(f, g->params, kNumParams * 4, cudaMemcpyDeviceToHost));
+    DR_CUDA(cudaMemcpy(f + kNumParams, g->m, kNumParams * 4, cudaMemcpyDeviceToHost));
+    DR_CUDA(cudaMemcpy(f + 2 * kNumParams, g->v, kNumParams * 4, cudaMemcpyDeviceToHost));
+    return DR_OK;
+}
+
+dr_status dr_guide_set_state(dr_guide *g, const void *host, uint64_t bytes)
+{
+    DR_CHECK_ARG(g && host, "dr_guide_set_state: NULL argument");
+    if (bytes != kStateBytes)
+        return fail(DR_ERR_INVALID_ARGUMENT, "dr_guide_set_state: the state takes %llu bytes, got %llu",
+                    (unsigned long long)kStateBytes, (unsigned long long)bytes);
+    StateHeader h;
+    memcpy(&h, host, sizeof h);
+    DR_CHECK_ARG(h.magic == kStateMagic && h.version == kStateVersion && h.num_params == (uint32_t)kNumParams,
+                 "dr_guide_set_state: not a guiding-network state of this version");
+    const float *f = reinterpret_cast<const float *>(static_cast<const unsigned char *>(host) + sizeof h);
+    DR_CUDA(cudaSetDevice(g->ctx->device));
+    DR_CUDA(cudaDeviceSynchronize());
+    DR_CUDA(cudaMemcpy(g->params, f, kNumParams * 4, cudaMemcpyHostToDevice));
+    DR_CUDA(cudaMemcpy(g->m, f + kNumParams, kNumParams * 4, cudaMemcpyHostToDevice));
+    DR_CUDA(cudaMemcpy(g->v, f + 2 * kNumParams, kNumParams * 4, cudaMemcpyHostToDevice));
+    g->cfg = h.cfg;
+    g->step = (int)h.step;
+    k_guide_export<<<(kNumParams + 255) / 256, 256>>>(g->params, g->wb, g->img);
+    DR_CUDA(cudaGetLastError());
+    DR_CUDA(cudaDeviceSynchronize());
+    return DR_OK;
+}
+
 dr_status dr_guide_get_params(dr_guide *g, float *host, uint32_t n)
 {
     DR_CHECK_ARG(g && host && n == (uint32_t)kNumParams, "dr_guide_get_params: bad argument");

@@ -191,6 +191,9 @@ SIGNATURES = {
     "dr_guide_destroy": (C.c_int, [C.c_void_p]),
     "dr_guide_set_params": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
     "dr_guide_get_params": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32]),
+    "dr_guide_state_bytes": (C.c_uint64, []),
+    "dr_guide_get_state": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
+    "dr_guide_set_state": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64]),
     "dr_guide_encode": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]),
     "dr_guide_infer": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
     "dr_guide_gradients": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32,
@@ -588,6 +591,18 @@ class Guide:
         out = np.zeros(self.num_params, np.float32)
         check(load().dr_guide_get_params(self.handle, _ptr(out), self.num_params))
         return out
+
+    def get_state(self) -> np.ndarray:
+        """The network's whole training state (configuration, Adam step,
+        parameters, Adam moments) as bytes, for a checkpoint."""
+        out = np.zeros(int(load().dr_guide_state_bytes()), np.uint8)
+        check(load().dr_guide_get_state(self.handle, _ptr(out), out.size))
+        return out
+
+    def set_state(self, state: np.ndarray) -> None:
+        """Restores a state from get_state (of any network of this library)."""
+        state = np.ascontiguousarray(state, np.uint8)
+        check(load().dr_guide_set_state(self.handle, _ptr(state), state.size))
 
     def set_params(self, p: np.ndarray) -> None:
         p = np.ascontiguousarray(p, np.float32)

@@ -431,6 +431,17 @@ dr_status dr_guide_destroy(dr_guide *guide);
  * 64, 64, 64, 64; fan-outs 64, 64, 64, 64, 48). Setting resets Adam. Synchronous. */
 dr_status dr_guide_set_params(dr_guide *guide, const float *params_host, uint32_t n);
 dr_status dr_guide_get_params(dr_guide *guide, float *params_host, uint32_t n);
+/* Checkpoint and resume of a network that trains: its whole state (the
+ * configuration, the Adam step count, the FP32 parameters and both Adam
+ * moments) as one host blob of dr_guide_state_bytes() bytes. dr_guide_set_state
+ * restores it into any network of this library (its configuration included),
+ * after which training continues as the saved network would have. No
+ * counterpart in the reference (the guiding network is a north-star
+ * addition); with the image accumulation (the caller's buffer) and the
+ * render's sample offset it resumes a guided render. Synchronous. */
+uint64_t dr_guide_state_bytes(void);
+dr_status dr_guide_get_state(dr_guide *guide, void *state_host, uint64_t bytes);
+dr_status dr_guide_set_state(dr_guide *guide, const void *state_host, uint64_t bytes);
 /* Network input of each row (pos, dir: 3 floats per row; out: 80 floats per row). */
 dr_status dr_guide_encode(dr_guide *guide, const float *pos_dev, const float *dir_dev, uint32_t n, float *out_dev);
 /* Network output y (40 floats per row). Asynchronous on `stream`. */

@@ -172,3 +172,40 @@ def test_training_fits_a_direction_field(native, ctx):
         if step % 50 == 0 or step == 299:
             losses.append(g.last_loss())
     assert losses[-1] < losses[0] - 1.5, losses
+
+
+def test_state_checkpoint_resumes_training(native, ctx):
+    """A network restored from a checkpoint (dr_guide_get_state / _set_state,
+    into a network created with another seed and centre) trains on exactly as
+    the saved one: same parameters after the same further Adam steps, up to
+    the order of the gradient sums' atomics. Restarting from the parameters
+    alone (dr_guide_set_params resets Adam) lands elsewhere."""
+    batches = [tuple(_dev(a) for a in _batch(4096, 50 + k)) for k in range(8)]
+    g1 = _guide(native, ctx, seed=3)
+    for b in batches[:4]:
+        g1.train_step(*b, 4096)
+    state = g1.get_state()
+    params_at_save = g1.params()
+    for b in batches[4:]:
+        g1.train_step(*b, 4096)
+    want = g1.params()
+    g2 = native.Guide(ctx, seed=99, center=(0.0, 0.0, 0.0), half_extent=1.0)
+    g2.set_state(state)
+    assert np.array_equal(g2.get_state(), state)
+    for b in batches[4:]:
+        g2.train_step(*b, 4096)
+    got = g2.params()
+    g3 = _guide(native, ctx, seed=5)
+    g3.set_params(params_at_save)
+    for b in batches[4:]:
+        g3.train_step(*b, 4096)
+    moved = np.abs(want - params_at_save).max()
+    assert moved > 1e-5
+    assert np.abs(got - want).max() < 1e-3 * moved, (np.abs(got - want).max(), moved)
+    assert np.abs(g3.params() - want).max() > 0.1 * moved
+    bad = state.copy()
+    bad[0] ^= 0xff
+    with pytest.raises(Exception):
+        g2.set_state(bad)
+    for g in (g1, g2, g3):
+        g.close()
