@@ -530,7 +530,7 @@ def batch_section(ctx, native, device: int, stream, scenes_n: int = 64, spp: int
 
 
 def guided_section(ctx, native, device: int, stream, width: int = 480, height: int = 270, spp: int = 1024,
-                   depth: int = 16, ref_spp: int = 65536, hd_spp: int = 16, seeds: int = 3, scene: str = "gap",
+                   depth: int = 16, ref_spp: int = 65536, hd_spp: int = 16, seeds: int = 5, scene: str = "gap",
                    hd: bool = True):
     """Learned path guiding on the occluded-light scene (the many-light
     geometry, emitters only above an occluding slab): RMSE of the guided and of
