@@ -6,7 +6,10 @@
 #include "alias_kernels.cuh"
 
 #include <cmath>
+#include <cstdio>
+#include <cstring>
 #include <new>
+#include <vector>
 
 struct dr_framebuffer {
     dr_context *ctx = nullptr;
@@ -48,6 +51,17 @@ __global__ void k_tonemap(const float4 *__restrict__ accum, int32_t w, int32_t h
     const uint32_t v = (to_u32(to_srgb(r, gamma) * 255)) | (to_u32(to_srgb(g, gamma) * 255) << 8) |
                        (to_u32(to_srgb(b, gamma) * 255) << 16) | (to_u32(1.0f * 255) << 24);
     out[x + (size_t)(h - y - 1) * w] = v;
+}
+
+__global__ void k_resolve(const float4 *__restrict__ accum, uint64_t n, float *__restrict__ rgb)
+{
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 p = accum[i];
+    const bool any = p.w != 0.f;
+    rgb[3 * i] = any ? p.x / p.w : 0.0f;
+    rgb[3 * i + 1] = any ? p.y / p.w : 0.0f;
+    rgb[3 * i + 2] = any ? p.z / p.w : 0.0f;
 }
 
 }  // namespace
@@ -147,6 +161,54 @@ dr_status dr_tonemap(const float *accum_dev, int32_t width, int32_t height, int3
     k_tonemap<<<grid, 128, 0, static_cast<cudaStream_t>(stream)>>>(reinterpret_cast<const float4 *>(accum_dev), width,
                                                                  height, gamma_corrected ? 1 : 0, rgba_dev);
     DR_CUDA(cudaGetLastError());
+    return DR_OK;
+}
+
+dr_status dr_resolve(const float *accum_dev, int32_t width, int32_t height, float *rgb_dev, void *stream)
+{
+    DR_CHECK_ARG(accum_dev && rgb_dev && width > 0 && height > 0, "dr_resolve: bad argument");
+    DR_CHECK_ARG(((uintptr_t)accum_dev & 15) == 0, "dr_resolve: accum_dev must be 16-byte aligned");
+    const uint64_t n = (uint64_t)width * (uint64_t)height;
+    k_resolve<<<(unsigned)((n + 255) / 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        reinterpret_cast<const float4 *>(accum_dev), n, rgb_dev);
+    DR_CUDA(cudaGetLastError());
+    return DR_OK;
+}
+
+dr_status dr_framebuffer_write_pfm(dr_framebuffer *fb, const char *path)
+{
+    DR_CHECK_ARG(fb && path, "dr_framebuffer_write_pfm: NULL");
+    DR_CUDA(cudaSetDevice(fb->ctx->device));
+    const size_t n = (size_t)fb->width * fb->height;
+    float *rgb = nullptr;
+    DR_CUDA(dev_malloc(&rgb, n * 3 * sizeof(float)));
+    std::vector<float> host(n * 3);
+    dr_status st = dr_resolve(reinterpret_cast<const float *>(fb->accum), fb->width, fb->height, rgb, nullptr);
+    cudaError_t e = st == DR_OK ? cudaMemcpy(host.data(), rgb, n * 3 * sizeof(float), cudaMemcpyDeviceToHost)
+                                : cudaSuccess;
+    cudaFree(rgb);
+    if (st != DR_OK) return st;
+    if (e != cudaSuccess) return cuda_fail(e, "dr_framebuffer_write_pfm");
+    FILE *f = fopen(path, "wb");
+    if (!f) return fail(DR_ERR_INVALID_ARGUMENT, "dr_framebuffer_write_pfm: cannot open %s", path);
+    // PFM header: colour, width height, negative scale = little-endian samples
+    const int hdr = fprintf(f, "PF\n%d %d\n-1.0\n", fb->width, fb->height);
+    uint32_t probe = 1;
+    const bool little = *reinterpret_cast<unsigned char *>(&probe) == 1;
+    bool ok = hdr > 0;
+    if (ok && little) {
+        ok = fwrite(host.data(), sizeof(float), host.size(), f) == host.size();
+    } else if (ok) {
+        for (size_t i = 0; ok && i < host.size(); ++i) {
+            uint32_t b;
+            memcpy(&b, &host[i], 4);
+            const unsigned char le[4] = {(unsigned char)b, (unsigned char)(b >> 8), (unsigned char)(b >> 16),
+                                         (unsigned char)(b >> 24)};
+            ok = fwrite(le, 1, 4, f) == 4;
+        }
+    }
+    ok = (fclose(f) == 0) && ok;
+    if (!ok) return fail(DR_ERR_INVALID_ARGUMENT, "dr_framebuffer_write_pfm: writing %s failed", path);
     return DR_OK;
 }
 

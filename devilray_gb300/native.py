@@ -179,6 +179,8 @@ SIGNATURES = {
     "dr_framebuffer_read": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_uint64)]),
     "dr_framebuffer_tonemap": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
     "dr_tonemap": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
+    "dr_resolve": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]),
+    "dr_framebuffer_write_pfm": (C.c_int, [C.c_void_p, C.c_char_p]),
     "dr_batch_create": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.POINTER(C.c_void_p)]),
     "dr_batch_render": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "dr_batch_get_info": (C.c_int, [C.c_void_p, C.c_void_p]),
@@ -499,6 +501,15 @@ class Framebuffer:
         out = np.zeros(self.width * self.height, np.uint32)
         check(load().dr_framebuffer_tonemap(self.handle, 1 if gamma else 0, _ptr(out)))
         return out
+
+    def write_pfm(self, path) -> None:
+        """The linear image as a PFM file (rows from the bottom)."""
+        check(load().dr_framebuffer_write_pfm(self.handle, str(path).encode()))
+
+
+def resolve(accum_dev, width: int, height: int, rgb_dev, stream=None) -> None:
+    """dr_resolve: the linear image (sum / samples) of a device accumulation buffer."""
+    check(load().dr_resolve(_ptr(accum_dev), width, height, _ptr(rgb_dev), _stream_ptr(stream)))
 
 
 def make_job(scene: "Scene", cam: dict, accum_dev, casts_dev=None, spp: int = 1, max_depth: int = 10,

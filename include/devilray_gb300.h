@@ -315,6 +315,16 @@ dr_status dr_framebuffer_tonemap(dr_framebuffer *fb, int32_t gamma_corrected, ui
  * height <= 65535. */
 dr_status dr_tonemap(const float *accum_dev, int32_t width, int32_t height, int32_t gamma_corrected,
                      uint32_t *rgba_dev, void *stream);
+/* The linear image of an accumulation buffer on the device, for headless
+ * output: rgb_dev[3 (x + y width) + c] = accum[c] / accum.w (0 for pixels
+ * without samples), rows in the accumulation's order (row 0 at the bottom).
+ * Replaces the host averaging of Renderer::createPixels
+ * (src/Renderer.cpp:51-90) where no display is attached. Asynchronous on
+ * `stream`. */
+dr_status dr_resolve(const float *accum_dev, int32_t width, int32_t height, float *rgb_dev, void *stream);
+/* Writes the framebuffer's linear image (dr_resolve) as a little-endian PFM
+ * file ("PF", rows from the bottom, as the format stores them). Synchronous. */
+dr_status dr_framebuffer_write_pfm(dr_framebuffer *fb, const char *path);
 
 /* ---- batched rendering ------------------------------------------------------------ */
 

@@ -85,3 +85,41 @@ def test_alias_build_host_equals_oracle(native, ctx, oracle, mode):
     native.check(native.load().dr_alias_build_host(ctx.handle, native._ptr(w), len(w), native._ptr(table), mode))
     want = oracle.alias_build_ref(w) if mode == 0 else oracle.alias_build_sweep(w)
     assert table.tobytes() == want.tobytes()
+
+
+def _read_pfm(path):
+    data = path.read_bytes()
+    parts = data.split(b"\n", 3)
+    assert parts[0] == b"PF"
+    w, h = (int(x) for x in parts[1].split())
+    assert float(parts[2]) < 0  # little-endian
+    return np.frombuffer(parts[3], dtype="<f4").reshape(h, w, 3), w, h
+
+
+def test_resolve_and_pfm_output(native, ctx, tmp_path):
+    """Headless output: dr_resolve gives sum / samples on the device (0 where
+    a pixel has no samples), bit for bit the FP32 quotient, and the
+    framebuffer's PFM file holds the same values, bottom row first."""
+    w, h = 37, 23
+    acc = _accum(w, h, 5)
+    dev = torch.from_numpy(acc).cuda()
+    rgb = torch.full((w * h, 3), -1.0, dtype=torch.float32, device="cuda")
+    native.resolve(dev, w, h, rgb)
+    torch.cuda.synchronize()
+    got = rgb.cpu().numpy()
+    want = np.where(acc[:, 3:4] != 0, acc[:, :3] / np.where(acc[:, 3:4] != 0, acc[:, 3:4], 1), 0).astype(np.float32)
+    assert np.array_equal(got, want)
+
+    spec = scenes.box_room(sphere_level=2)
+    scene = native.Scene.from_spec(ctx, spec)
+    fb = native.Framebuffer(ctx, 40, 30)
+    acc_dev, casts_dev = fb.device_buffers()
+    scene.render(scenes.camera(40, 30), acc_dev, casts_dev, spp=3, max_depth=6)
+    path = tmp_path / "image.pfm"
+    fb.write_pfm(path)
+    img, pw, ph = _read_pfm(path)
+    assert (pw, ph) == (40, 30)
+    a, _, _ = fb.read()
+    lin = (a[:, :3] / a[:, 3:4]).reshape(30, 40, 3)
+    assert np.array_equal(img, lin)
+    fb.close()
