@@ -446,9 +446,9 @@ dr_status dr_guide_get_params(dr_guide *guide, float *params_host, uint32_t n);
  * moments) as one host blob of dr_guide_state_bytes() bytes. dr_guide_set_state
  * restores it into any network of this library (its configuration included),
  * after which training continues as the saved network would have. No
- * counterpart in the reference (the guiding network is a north-star
- * addition); with the image accumulation (the caller's buffer) and the
- * render's sample offset it resumes a guided render. Synchronous. */
+ * counterpart in the reference, which has no guiding network; with the image
+ * accumulation (the caller's buffer) and the render's sample offset it
+ * resumes a guided render. Synchronous. */
 uint64_t dr_guide_state_bytes(void);
 dr_status dr_guide_get_state(dr_guide *guide, void *state_host, uint64_t bytes);
 dr_status dr_guide_set_state(dr_guide *guide, const void *state_host, uint64_t bytes);
