@@ -39,8 +39,9 @@ constexpr int kRenderBlock = 128;
 // Resident blocks per SM the plain shading kernel is compiled for (at most 64
 // registers). Measured on the box room, 256x256 x 16 spp: a minimum of 1 block
 // (138 registers) 2.99 ms, the compiler's choice without a minimum (80
-// registers, 6 blocks) about 2.69 ms, 8 blocks 2.60-2.64 ms. The guided one is
-// bound to 4 blocks (at most 128 registers).
+// registers, 6 blocks) about 2.69 ms, 8 blocks 2.60-2.64 ms; many-light 1080p
+// (16 spp): 8 blocks 40.6 ms, 10 blocks (48 registers, spills) 41.0 ms, 12
+// blocks 41.3 ms. The guided one has its own bound (DR_GUIDE_SHADE_BLOCKS).
 #ifndef DR_SHADE_MIN_BLOCKS
 #define DR_SHADE_MIN_BLOCKS 8
 #endif
