@@ -479,6 +479,11 @@ dr_status dr_trace_any(dr_scene *s, const dr_ray *rays, uint64_t n, uint8_t *occ
     return DR_OK;
 }
 
+// Chunk sizes of dr_trace_closest_host in relative units (see there).
+#ifndef DR_HOST_CHUNKS
+#define DR_HOST_CHUNKS 1, 1, 2, 2, 4, 4, 4, 4, 4, 4, 2
+#endif
+
 dr_status dr_trace_closest_host(dr_scene *s, const dr_ray *rays_host, uint64_t n, dr_hit *hits_host,
                                 int32_t tri_mode, void *stream)
 {
@@ -508,14 +513,17 @@ dr_status dr_trace_closest_host(dr_scene *s, const dr_ray *rays_host, uint64_t n
     // traversal starts sooner) 4.01 ms; short chunks at the end as well
     // 4.07 ms. Reading the rays and writing the hits in place in mapped
     // page-locked memory, in one launch: 4.82 ms; copying the chunks in on
-    // two alternating streams: 4.43 ms.
+    // two alternating streams: 4.43 ms. With the 3.19 ms traversal (chunks
+    // in 32nds): 1,2,4,4,4,5,4,4,4 3.87 ms; 1,1,2,2,4,4,4,4,4,4,2 3.77-3.79;
+    // 1,1,2,3,4,4,4,4,4,3,2 3.77; 1,2,5,6,6,6,6 3.91; 1,1,2,2,3 x 8,1,1 3.86.
     auto *d_rays = static_cast<dr_ray *>(s->d_stage_rays);
     auto *d_hits = static_cast<dr_hit *>(s->d_stage_hits);
     // chunk boundaries, in 32nds of the rays: short first chunks so the
-    // traversal starts sooner (chunks under 2^18 rays join the next)
+    // traversal starts sooner, a short last one so less of it waits for the
+    // final copy-out (chunks under 2^18 rays join the next)
     std::vector<uint64_t> bounds{0};
     {
-        static const int parts[] = {1, 2, 4, 4, 4, 5, 4, 4, 4, 0};
+        static const int parts[] = {DR_HOST_CHUNKS, 0};
         int total = 0;
         for (int i = 0; parts[i]; ++i) total += parts[i];
         uint64_t acc = 0;
