@@ -218,5 +218,5 @@ struct dr_scene {
     void *d_stage_rays = nullptr;
     void *d_stage_hits = nullptr;
     uint64_t stage_capacity = 0;
-    cudaStream_t stage_streams[3] = {};  // host-buffer tracing: copy in, copy out, second compute stream
+    cudaStream_t stage_streams[4] = {};  // host-buffer tracing: copy in, copy out, more compute streams
 };
