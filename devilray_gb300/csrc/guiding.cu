@@ -1434,7 +1434,10 @@ dr_status dr_guide_train_step(dr_guide *g, const float *pos_dev, const float *di
     dr_status r = run_gradients(g, pos_dev, dir_dev, sdir_dev, weight_dev, n, st);
     if (r != DR_OK) return r;
     ++g->step;
-    k_guide_adam<<<(kNumParams + 255) / 256, 256, 0, st>>>(g->params, g->m, g->v, g->grad, g->step, g->cfg.learning_rate,
+    const float lr = g->cfg.warmup_steps && (uint32_t)g->step < g->cfg.warmup_steps
+                         ? g->cfg.learning_rate * (float)g->step / (float)g->cfg.warmup_steps
+                         : g->cfg.learning_rate;
+    k_guide_adam<<<(kNumParams + 255) / 256, 256, 0, st>>>(g->params, g->m, g->v, g->grad, g->step, lr,
                                                            g->cfg.beta1, g->cfg.beta2, g->cfg.epsilon, g->wb, g->img);
     DR_CUDA(cudaGetLastError());
     return DR_OK;

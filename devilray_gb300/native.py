@@ -583,16 +583,17 @@ class GuidedConfig(C.Structure):
 class GuideConfig(C.Structure):
     _fields_ = [("seed", C.c_uint64), ("learning_rate", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float),
                 ("epsilon", C.c_float), ("center", C.c_float * 3), ("half_extent", C.c_float),
-                ("infer_kernel", C.c_uint32)]
+                ("infer_kernel", C.c_uint32), ("warmup_steps", C.c_uint32)]
 
 
 class Guide:
     """The path-guiding network (dr_guide)."""
 
     def __init__(self, ctx: "Context", seed: int = 0, learning_rate: float = 1e-3, center=(0.0, 0.0, 0.0),
-                 half_extent: float = 1.0, infer_kernel: int = 0):
+                 half_extent: float = 1.0, infer_kernel: int = 0, warmup_steps: int = 0):
         self.ctx = ctx
-        cfg = GuideConfig(seed, learning_rate, 0.9, 0.999, 1e-8, (C.c_float * 3)(*center), half_extent, infer_kernel)
+        cfg = GuideConfig(seed, learning_rate, 0.9, 0.999, 1e-8, (C.c_float * 3)(*center), half_extent, infer_kernel,
+                          warmup_steps)
         h = C.c_void_p()
         check(load().dr_guide_create(ctx.handle, C.byref(cfg), C.byref(h)))
         self.handle = h.value

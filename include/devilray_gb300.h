@@ -427,6 +427,8 @@ typedef struct dr_guide_config {
     float half_extent;        /* 0 = 1 */
     uint32_t infer_kernel;    /* dr_guide_infer_kernel: the tensor-core path of inference and of the
                                  forward/backward pass of training */
+    uint32_t warmup_steps;    /* the learning rate rises linearly over the first warmup_steps Adam steps
+                                 (step s uses learning_rate x min(1, s / warmup_steps)); 0 = none */
 } dr_guide_config;
 
 typedef enum dr_guide_infer_kernel {
