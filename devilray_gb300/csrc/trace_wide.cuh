@@ -79,6 +79,12 @@ constexpr int kWideStack = 64;
 #ifndef DR_HIT_FSET
 #define DR_HIT_FSET 1
 #endif
+// The FP16 path's slab FMAs as scalar FMAs instead of packed pairs (fewer
+// registers). Measured: 3.283 ms at 7 blocks per SM, 3.371 ms at 8 (64
+// registers, spills); packed pairs 3.192 ms at 7 blocks, 3.308 ms at 8.
+#ifndef DR_HALF_SCALAR
+#define DR_HALF_SCALAR 0
+#endif
 // The same accumulation in the packed and scalar node tests (any hit,
 // renderer): measured without effect (any hit 2.842 / 2.844 ms), so off.
 #ifndef DR_HIT_FSET_ALL
@@ -312,6 +318,17 @@ __host__ __device__ __forceinline__ void wide_node_test(const Bvh8Node *node, co
     for (int h = 0; h < 2; ++h) {
 #pragma unroll
         for (uint32_t j = 0; j < 2; ++j) {
+#if DR_HALF_SCALAR
+            auto ffma_s = [](float2 q, float2 a, float2 b) { return make_float2(fmaf(q.x, a.x, b.x), fmaf(q.y, a.y, b.y)); };
+            const float2 tnx = ffma_s(byte_pair_h(h ? hnx1 : hnx0, j), Ax, NBx);
+            const float2 tfx = ffma_s(byte_pair_h(h ? hfx1 : hfx0, j), Ax, FBx);
+            const float2 tny = ffma_s(byte_pair_h(h ? hny1 : hny0, j), Ay, NBy);
+            const float2 tfy = ffma_s(byte_pair_h(h ? hfy1 : hfy0, j), Ay, FBy);
+            const float2 tnz = ffma_s(byte_pair_h(h ? hnz1 : hnz0, j), Az, NBz);
+            const float2 tfz = ffma_s(byte_pair_h(h ? hfz1 : hfz0, j), Az, FBz);
+            const float2 tmx = make_float2(fminf(min3f(tfx.x, tfy.x, tfz.x), tmax) * kBoxFarScale,
+                                           fminf(min3f(tfx.y, tfy.y, tfz.y), tmax) * kBoxFarScale);
+#else
             const float2 tnx = __ffma2_rn(byte_pair_h(h ? hnx1 : hnx0, j), Ax, NBx);
             const float2 tfx = __ffma2_rn(byte_pair_h(h ? hfx1 : hfx0, j), Ax, FBx);
             const float2 tny = __ffma2_rn(byte_pair_h(h ? hny1 : hny0, j), Ay, NBy);
@@ -320,6 +337,7 @@ __host__ __device__ __forceinline__ void wide_node_test(const Bvh8Node *node, co
             const float2 tfz = __ffma2_rn(byte_pair_h(h ? hfz1 : hfz0, j), Az, FBz);
             const float2 tmx = __fmul2_rn(make_float2(fminf(min3f(tfx.x, tfy.x, tfz.x), tmax),
                                                       fminf(min3f(tfx.y, tfy.y, tfz.y), tmax)), farS);
+#endif
             const uint32_t s0 = 4u * h + j;
 #if DR_HIT_FSET
             hit_f = fmaf(set_le(fmaxf(max3f(tnx.x, tny.x, tnz.x), 0.0f), tmx.x), (float)(1u << s0),
