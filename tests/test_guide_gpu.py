@@ -179,7 +179,14 @@ def test_state_checkpoint_resumes_training(native, ctx):
     into a network created with another seed and centre) trains on exactly as
     the saved one: same parameters after the same further Adam steps, up to
     the order of the gradient sums' atomics. Restarting from the parameters
-    alone (dr_guide_set_params resets Adam) lands elsewhere."""
+    alone (dr_guide_set_params resets Adam) lands elsewhere.
+
+    The atomics' order changes a gradient sum in its last bits. Adam divides
+    by the root of the second moment, so a parameter whose gradient is near
+    zero can take a visibly different step from that alone (up to the
+    learning rate per step); the comparison therefore bounds the RMS of the
+    difference and lets a few parameters move by a few percent of the
+    largest step."""
     batches = [tuple(_dev(a) for a in _batch(4096, 50 + k)) for k in range(8)]
     g1 = _guide(native, ctx, seed=3)
     for b in batches[:4]:
@@ -200,9 +207,11 @@ def test_state_checkpoint_resumes_training(native, ctx):
     for b in batches[4:]:
         g3.train_step(*b, 4096)
     moved = np.abs(want - params_at_save).max()
+    rms = lambda a: float(np.sqrt(np.mean(np.square(a, dtype=np.float64))))
     assert moved > 1e-5
-    assert np.abs(got - want).max() < 1e-3 * moved, (np.abs(got - want).max(), moved)
-    assert np.abs(g3.params() - want).max() > 0.1 * moved
+    assert rms(got - want) < 1e-3 * rms(want - params_at_save), (rms(got - want), rms(want - params_at_save))
+    assert np.abs(got - want).max() < 0.05 * moved, (np.abs(got - want).max(), moved)
+    assert rms(g3.params() - want) > 0.1 * rms(want - params_at_save)
     bad = state.copy()
     bad[0] ^= 0xff
     with pytest.raises(Exception):
