@@ -6,6 +6,7 @@
 #include "alias_kernels.cuh"
 
 #include <algorithm>
+#include <cfloat>
 #include <chrono>
 #include <cmath>
 #include <cstdarg>
@@ -206,12 +207,24 @@ dr_status dr_scene_create(dr_context *ctx, const dr_scene_desc *desc, const dr_b
     if (n >= kMaxTriangles) return fail(DR_ERR_TOO_LARGE, "dr_scene_create: %u triangles (max %u)", n, kMaxTriangles - 1);
     DR_CHECK_ARG(desc->light_tables == DR_LIGHT_TABLES_SWEEP || desc->light_tables == DR_LIGHT_TABLES_REFERENCE,
                  "dr_scene_create: unknown light_tables value");
+    // largest coordinate magnitude, and whether any coordinate is not finite
+    std::vector<float> part_mag(std::max(1u, std::thread::hardware_concurrency()) + 1, 0.0f);
+    std::atomic<bool> non_finite{false};
+    std::atomic<uint32_t> next_part{0};
+    host_parallel_chunks((size_t)n * 9, size_t(1) << 20, [&](size_t b, size_t e) {
+        float m = 0.0f;
+        bool bad = false;
+        for (size_t i = b; i < e; ++i) {
+            const float a = std::fabs(desc->positions_host[i]);
+            bad |= !(a <= FLT_MAX);  // NaN or infinity
+            m = std::max(m, a);
+        }
+        part_mag[next_part.fetch_add(1)] = m;
+        if (bad) non_finite = true;
+    });
+    if (non_finite) return fail(DR_ERR_INVALID_ARGUMENT, "dr_scene_create: non-finite vertex coordinate");
     float mag = 0.0f;
-    for (size_t i = 0; i < (size_t)n * 9; ++i) {
-        const float v = desc->positions_host[i];
-        if (!std::isfinite(v)) return fail(DR_ERR_INVALID_ARGUMENT, "dr_scene_create: non-finite vertex coordinate");
-        mag = std::max(mag, std::fabs(v));
-    }
+    for (float m : part_mag) mag = std::max(mag, m);
     if (desc->objects_host) {
         for (uint32_t o = 0; o < desc->num_objects; ++o) {
             const dr_object &ob = desc->objects_host[o];

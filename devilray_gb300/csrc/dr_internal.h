@@ -1,6 +1,7 @@
 // dr_internal.h -- internal types of the GB300 path-tracing core.
 #pragma once
 
+#include <algorithm>
 #include <atomic>
 
 #include "devilray_gb300.h"
@@ -9,6 +10,7 @@
 
 #include <cstdint>
 #include <string>
+#include <thread>
 #include <vector>
 
 namespace dr {
@@ -45,6 +47,26 @@ template <typename T>
 inline cudaError_t dev_malloc(T **p, size_t bytes)
 {
     return dev_malloc_raw(reinterpret_cast<void **>(p), bytes);
+}
+
+// Runs f(begin, end) over [0, n) in contiguous chunks of at least `grain`
+// items on up to hardware_concurrency host threads (the caller's thread takes
+// the first chunk). Each chunk writes only its own outputs, so the result does
+// not depend on the split.
+template <typename F>
+inline void host_parallel_chunks(size_t n, size_t grain, F &&f)
+{
+    const size_t hw = std::max(1u, std::thread::hardware_concurrency());
+    const size_t parts = std::max<size_t>(1, std::min(hw, n / std::max<size_t>(1, grain)));
+    if (parts == 1) {
+        f(size_t(0), n);
+        return;
+    }
+    std::vector<std::thread> pool;
+    pool.reserve(parts - 1);
+    for (size_t k = 1; k < parts; ++k) pool.emplace_back([&, k] { f(n * k / parts, n * (k + 1) / parts); });
+    f(size_t(0), n / parts);
+    for (auto &t : pool) t.join();
 }
 
 // Device error word bits (dr_context::d_error), set by kernels instead of

@@ -83,15 +83,17 @@ dr_status build_render_data(dr_scene *s, const dr_scene_desc *d)
             tri_mat[i] = m;
         }
     std::vector<float4> shade((size_t)n * 3);
-    for (uint32_t i = 0; i < n; ++i) {
-        const float *q = d->positions_host + (size_t)i * 9;
-        shade[(size_t)i * 3 + 0] = make_float4(q[0], q[1], q[2], q[3]);
-        shade[(size_t)i * 3 + 1] = make_float4(q[4], q[5], q[6], q[7]);
-        float fo, fm;  // object and material ids travel as int32 bit patterns
-        std::memcpy(&fo, &tri_obj[i], 4);
-        std::memcpy(&fm, &tri_mat[i], 4);
-        shade[(size_t)i * 3 + 2] = make_float4(q[8], fo, fm, 0.0f);
-    }
+    host_parallel_chunks(n, size_t(1) << 16, [&](size_t b, size_t e) {
+        for (size_t i = b; i < e; ++i) {
+            const float *q = d->positions_host + i * 9;
+            shade[i * 3 + 0] = make_float4(q[0], q[1], q[2], q[3]);
+            shade[i * 3 + 1] = make_float4(q[4], q[5], q[6], q[7]);
+            float fo, fm;  // object and material ids travel as int32 bit patterns
+            std::memcpy(&fo, &tri_obj[i], 4);
+            std::memcpy(&fm, &tri_mat[i], 4);
+            shade[i * 3 + 2] = make_float4(q[8], fo, fm, 0.0f);
+        }
+    });
 
     // level 1: objects by emitted power
     const size_t N = objects.size();

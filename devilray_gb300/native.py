@@ -315,15 +315,15 @@ def scene_desc(positions: np.ndarray, objects=None, materials=None, tri_material
     desc.num_triangles = positions.shape[0]
     keep = [positions]
     if objects is not None:
-        objs = (Object * len(objects))(*objects)
+        objs = _records(objects, Object)
         keep.append(objs)
-        desc.objects_host = C.addressof(objs)
-        desc.num_objects = len(objects)
+        desc.objects_host = objs.ctypes.data
+        desc.num_objects = len(objs)
     if materials is not None:
-        mats = (Material * len(materials))(*materials)
+        mats = _records(materials, Material)
         keep.append(mats)
-        desc.materials_host = C.addressof(mats)
-        desc.num_materials = len(materials)
+        desc.materials_host = mats.ctypes.data
+        desc.num_materials = len(mats)
     if tri_material is not None:
         tm = np.ascontiguousarray(tri_material, np.int32)
         keep.append(tm)
@@ -335,17 +335,26 @@ def scene_desc(positions: np.ndarray, objects=None, materials=None, tri_material
     return desc, keep
 
 
+def _records(items, struct) -> np.ndarray:
+    """Contiguous bytes of `struct` records: a sequence of ctypes `struct`
+    instances, or a numpy array whose rows have the struct's size (the
+    structured arrays of SceneSpec.objects_array / materials_array)."""
+    size = C.sizeof(struct)
+    if isinstance(items, np.ndarray):
+        a = np.ascontiguousarray(items)
+        if a.dtype.itemsize * (a.shape[1] if a.ndim == 2 else 1) != size:
+            raise ValueError(f"{struct.__name__} records are {size} bytes")
+        return a.view(np.uint8).reshape(-1, size)
+    out = np.empty((len(items), size), np.uint8)
+    for i, it in enumerate(items):
+        out[i] = np.frombuffer(bytes(it), np.uint8)
+    return out
+
+
 def spec_parts(spec):
-    """(objects, materials) ctypes records of a devilray_gb300.scenes.SceneSpec."""
-    objs = [Object(int(b), int(c), int(m), float(a)) for (b, c, m, a) in spec.objects]
-    mats = []
-    for m in spec.materials:
-        mm = Material()
-        mm.kind, mm.ior = m["kind"], m["ior"]
-        for i in range(4):
-            mm.emission[i], mm.albedo[i], mm.debug_color[i] = m["emission"][i], m["albedo"][i], m["debug"][i]
-        mats.append(mm)
-    return objs, mats
+    """(objects, materials) records of a devilray_gb300.scenes.SceneSpec, as
+    numpy arrays laid out like dr_object and dr_material."""
+    return spec.objects_array(), spec.materials_array()
 
 
 def autotune(ctx: "Context", spec, cam: dict, spp: int = 1, max_depth: int = 10, pixel_sampling: int = 1,

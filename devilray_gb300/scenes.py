@@ -165,6 +165,7 @@ class SceneSpec:
         self.objects: list[tuple[int, int, int, float]] = []
         self.materials: list[dict] = []
         self.count = 0
+        self._soup: np.ndarray | None = None  # the joined parts, read-only, until the next add_object
 
     def add_material(self, m: dict) -> int:
         self.materials.append(m)
@@ -173,24 +174,32 @@ class SceneSpec:
     def add_object(self, soup: np.ndarray, mat: int, area: float | None = None) -> int:
         soup = _f32(soup).reshape(-1, 9)
         self.parts.append(soup)
+        self._soup = None
         self.objects.append((self.count, soup.shape[0], mat, surface_area(soup) if area is None else area))
         self.count += soup.shape[0]
         return len(self.objects) - 1
 
     @property
     def positions(self) -> np.ndarray:
-        return np.concatenate(self.parts).astype(np.float32) if self.parts else np.zeros((0, 9), np.float32)
+        """The soup [N, 9] float32, joined once and shared by later reads (read-only)."""
+        if self._soup is None:
+            soup = np.concatenate(self.parts) if self.parts else np.zeros((0, 9), np.float32)
+            soup = soup.astype(np.float32, copy=False)
+            soup.flags.writeable = False
+            self._soup = soup
+        return self._soup
 
     def materials_array(self) -> np.ndarray:
         """dr_material layout: [kind, ior, 0, 0, emission4, albedo4, debug4] as float32
         (kind stored as its int32 bit pattern)."""
-        out = np.zeros((len(self.materials), 16), np.float32)
-        for i, m in enumerate(self.materials):
-            out[i, 0] = np.array([m["kind"]], np.int32).view(np.float32)[0]
-            out[i, 1] = m["ior"]
-            out[i, 4:8] = m["emission"]
-            out[i, 8:12] = m["albedo"]
-            out[i, 12:16] = m["debug"]
+        ms = self.materials
+        out = np.zeros((len(ms), 16), np.float32)
+        if ms:
+            out[:, 0] = np.array([m["kind"] for m in ms], np.int32).view(np.float32)
+            out[:, 1] = [m["ior"] for m in ms]
+            out[:, 4:8] = [m["emission"] for m in ms]
+            out[:, 8:12] = [m["albedo"] for m in ms]
+            out[:, 12:16] = [m["debug"] for m in ms]
         return out
 
     def objects_array(self) -> np.ndarray:
