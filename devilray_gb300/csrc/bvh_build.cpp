@@ -67,6 +67,8 @@ struct TreeNode {
     int8_t slot_split[9] = {};  // left child's share of j slots; 0: one slot
     bool wide_leaf = false;     // its one slot is a leaf slot
     uint8_t tris = 0;           // triangles, counted up to 4
+    uint32_t ntris = 0;         // triangles of the subtree
+    uint32_t wide_size = 0;     // wide nodes of the subtree when it becomes a wide node
 };
 
 struct Builder {
@@ -81,8 +83,146 @@ struct Builder {
 
     static constexpr float kTraversalCost = 1.0f;
     static constexpr float kTriangleCost = 1.5f;
+    static constexpr uint32_t kParallelBinning = 1u << 18;  // ranges binned on several threads
+    static constexpr uint32_t kKnownSides = 1u << 12;        // ranges that pass their sides' bounds down
 
-    std::unique_ptr<TreeNode> build(uint32_t begin, uint32_t end, int depth)
+    // Bins of one axis: the primitives' boxes, their centroids' box and count.
+    // A bin's boxes are written by its first primitive (count 0 -> 1), so
+    // only the counts are cleared per range and empty bins are never read.
+    struct AxisBins {
+        Box box[64], cbox[64];
+        uint32_t count[64];
+    };
+
+    // The best SAH split of a range, with the bounds of its two sides.
+    struct Split {
+        float cost = std::numeric_limits<float>::infinity();
+        int axis = -1;
+        uint32_t bin = 0;
+        bool sides = false;  // the bounds of the two sides are known
+        Box left, left_c, right, right_c;
+    };
+
+    // Bins [begin, end) on every axis with a centroid extent in one pass over
+    // the primitives (large ranges on several threads; boxes and counts merge
+    // exactly), then evaluates the SAH at the bin boundaries. Only boundaries
+    // after an occupied bin are evaluated: past an empty bin both sides, and
+    // so the cost, equal those of the boundary before it, which the strict
+    // comparison already preferred. (Not inlined: its 10 KB of bins stay out
+    // of the recursion's frames.)
+    __attribute__((noinline)) Split best_split(uint32_t begin, uint32_t end, const Box &cbounds, uint32_t B) const
+    {
+        bool active[3];
+        float cmin[3], scale[3];
+        for (int a = 0; a < 3; ++a) {
+            cmin[a] = cbounds.lo[a];
+            active[a] = cbounds.hi[a] > cbounds.lo[a];
+            scale[a] = active[a] ? (float)B / (cbounds.hi[a] - cbounds.lo[a]) : 0.0f;
+        }
+        // centroid boxes per bin only for ranges whose children would
+        // otherwise make another pass over many primitives
+        const uint32_t n = end - begin;
+        const bool sides = n >= kKnownSides;
+        auto bin_into = [&](AxisBins *bins, size_t b0, size_t b1) {
+            for (int a = 0; a < 3; ++a) std::memset(bins[a].count, 0, B * sizeof(uint32_t));
+            for (size_t i = b0; i < b1; ++i) {
+                const Prim &p = prims[idx[i]];
+                for (int a = 0; a < 3; ++a) {
+                    if (!active[a]) continue;
+                    uint32_t b = (uint32_t)((p.c[a] - cmin[a]) * scale[a]);
+                    if (b >= B) b = B - 1;
+                    AxisBins &ab = bins[a];
+                    if (ab.count[b]++ == 0) {
+                        ab.box[b] = p.box;
+                        if (sides) {
+                            for (int k = 0; k < 3; ++k) ab.cbox[b].lo[k] = ab.cbox[b].hi[k] = p.c[k];
+                        }
+                    } else {
+                        ab.box[b].grow(p.box);
+                        if (sides) ab.cbox[b].grow(p.c);
+                    }
+                }
+            }
+        };
+        AxisBins bins[3];
+        if (n >= kParallelBinning) {
+            const size_t hw = std::max(1u, std::thread::hardware_concurrency());
+            std::vector<AxisBins> parts(3 * (hw + 1));
+            std::atomic<uint32_t> next{0};
+            host_parallel_chunks(n, kParallelBinning / 4, [&](size_t b0, size_t b1) {
+                bin_into(parts.data() + 3 * next.fetch_add(1), begin + b0, begin + b1);
+            });
+            for (int a = 0; a < 3; ++a) std::memset(bins[a].count, 0, B * sizeof(uint32_t));
+            for (uint32_t k = 0; k < next.load(); ++k)
+                for (int a = 0; a < 3; ++a)
+                    for (uint32_t b = 0; b < B; ++b) {
+                        const AxisBins &pb = parts[3 * k + a];
+                        if (pb.count[b] == 0) continue;
+                        if (bins[a].count[b] == 0) {
+                            bins[a].box[b] = pb.box[b];
+                            bins[a].cbox[b] = pb.cbox[b];
+                        } else {
+                            bins[a].box[b].grow(pb.box[b]);
+                            bins[a].cbox[b].grow(pb.cbox[b]);
+                        }
+                        bins[a].count[b] += pb.count[b];
+                    }
+        } else {
+            bin_into(bins, begin, end);
+        }
+        Split best;
+        for (int axis = 0; axis < 3; ++axis) {
+            if (!active[axis]) continue;
+            const AxisBins &ab = bins[axis];
+            uint32_t occ[64], k = 0;  // occupied bins, ascending
+            for (uint32_t b = 0; b < B; ++b)
+                if (ab.count[b]) occ[k++] = b;
+            // right side of the boundary after occupied bin occ[i]: bins occ[i + 1 ..]
+            float right_area[64];
+            uint32_t right_count[64];
+            Box acc;
+            acc.reset();
+            uint32_t cnt = 0;
+            for (uint32_t i = k; i-- > 1;) {
+                acc.grow(ab.box[occ[i]]);
+                cnt += ab.count[occ[i]];
+                right_area[i - 1] = acc.area();
+                right_count[i - 1] = cnt;
+            }
+            acc.reset();
+            cnt = 0;
+            for (uint32_t i = 0; i + 1 < k; ++i) {
+                const uint32_t b = occ[i];
+                acc.grow(ab.box[b]);
+                cnt += ab.count[b];
+                if (b + 1 >= B) break;
+                const float cost = acc.area() * cnt + right_area[i] * right_count[i];
+                if (cost < best.cost) {
+                    best.cost = cost;
+                    best.axis = axis;
+                    best.bin = b + 1;
+                }
+            }
+        }
+        best.sides = sides && best.axis >= 0;
+        if (best.sides) {
+            const AxisBins &ab = bins[best.axis];
+            best.left.reset();
+            best.left_c.reset();
+            best.right.reset();
+            best.right_c.reset();
+            for (uint32_t b = 0; b < B; ++b) {
+                if (ab.count[b] == 0) continue;
+                (b < best.bin ? best.left : best.right).grow(ab.box[b]);
+                (b < best.bin ? best.left_c : best.right_c).grow(ab.cbox[b]);
+            }
+        }
+        return best;
+    }
+
+    // Builds the subtree of [begin, end); `known` (if given) holds the
+    // range's box and centroid box, as the parent's bins found them.
+    std::unique_ptr<TreeNode> build(uint32_t begin, uint32_t end, int depth, const Box *known = nullptr)
     {
         auto node = std::make_unique<TreeNode>();
         node->depth = depth;
@@ -90,12 +230,17 @@ struct Builder {
         while (depth > prev && !max_depth.compare_exchange_weak(prev, depth)) {}
 
         Box bounds, cbounds;
-        bounds.reset();
-        cbounds.reset();
-        for (uint32_t i = begin; i < end; ++i) {
-            const Prim &p = prims[idx[i]];
-            bounds.grow(p.box);
-            cbounds.grow(p.c);
+        if (known) {
+            bounds = known[0];
+            cbounds = known[1];
+        } else {
+            bounds.reset();
+            cbounds.reset();
+            for (uint32_t i = begin; i < end; ++i) {
+                const Prim &p = prims[idx[i]];
+                bounds.grow(p.box);
+                cbounds.grow(p.c);
+            }
         }
         node->box = bounds;
         const uint32_t n = end - begin;
@@ -107,58 +252,14 @@ struct Builder {
 
         // Binned SAH over the three axes.
         const uint32_t B = std::max<uint32_t>(4, std::min<uint32_t>(params.bins, 64));
-        float best_cost = std::numeric_limits<float>::infinity();
-        int best_axis = -1;
-        uint32_t best_split = 0;
         const bool force_median = depth >= 32;  // bounds the depth: <= 32 + log2(n) levels
-        if (!force_median) {
-            for (int axis = 0; axis < 3; ++axis) {
-                const float cmin = cbounds.lo[axis], cmax = cbounds.hi[axis];
-                if (!(cmax > cmin)) continue;
-                const float scale = (float)B / (cmax - cmin);
-                Box bin_box[64];
-                uint32_t bin_count[64];
-                for (uint32_t b = 0; b < B; ++b) {
-                    bin_box[b].reset();
-                    bin_count[b] = 0;
-                }
-                for (uint32_t i = begin; i < end; ++i) {
-                    const Prim &p = prims[idx[i]];
-                    uint32_t b = (uint32_t)((p.c[axis] - cmin) * scale);
-                    if (b >= B) b = B - 1;
-                    bin_box[b].grow(p.box);
-                    ++bin_count[b];
-                }
-                float right_area[64];
-                uint32_t right_count[64];
-                Box acc;
-                acc.reset();
-                uint32_t cnt = 0;
-                for (uint32_t b = B - 1; b > 0; --b) {
-                    acc.grow(bin_box[b]);
-                    cnt += bin_count[b];
-                    right_area[b] = acc.area();
-                    right_count[b] = cnt;
-                }
-                acc.reset();
-                cnt = 0;
-                for (uint32_t b = 0; b + 1 < B; ++b) {
-                    acc.grow(bin_box[b]);
-                    cnt += bin_count[b];
-                    if (cnt == 0 || right_count[b + 1] == 0) continue;
-                    const float cost = acc.area() * cnt + right_area[b + 1] * right_count[b + 1];
-                    if (cost < best_cost) {
-                        best_cost = cost;
-                        best_axis = axis;
-                        best_split = b + 1;
-                    }
-                }
-            }
-        }
+        Split best;
+        if (!force_median) best = best_split(begin, end, cbounds, B);
+        const int best_axis = best.axis;
         const float parent_area = bounds.area();
         const float leaf_cost = kTriangleCost * n;
         const float split_cost = best_axis >= 0 && parent_area > 0.0f
-                                     ? kTraversalCost + kTriangleCost * best_cost / parent_area
+                                     ? kTraversalCost + kTriangleCost * best.cost / parent_area
                                      : std::numeric_limits<float>::infinity();
         if (n <= params.max_leaf && (leaf_cost <= split_cost || best_axis < 0)) {
             node->first = begin;
@@ -167,15 +268,17 @@ struct Builder {
         }
 
         uint32_t mid;
+        bool sides_known = false;
         if (best_axis >= 0) {
             const float cmin = cbounds.lo[best_axis], cmax = cbounds.hi[best_axis];
             const float scale = (float)B / (cmax - cmin);
             auto it = std::partition(idx.begin() + begin, idx.begin() + end, [&](uint32_t i) {
                 uint32_t b = (uint32_t)((prims[i].c[best_axis] - cmin) * scale);
                 if (b >= B) b = B - 1;
-                return b < best_split;
+                return b < best.bin;
             });
             mid = (uint32_t)(it - idx.begin());
+            sides_known = best.sides && mid != begin && mid != end;
             if (mid == begin || mid == end) mid = begin + n / 2;
         } else {
             // No useful SAH split (coincident centroids, or the depth cap):
@@ -194,18 +297,20 @@ struct Builder {
                                  return a < b;
                              });
         }
+        const Box lk[2] = {best.left, best.left_c}, rk[2] = {best.right, best.right_c};
+        const Box *lknown = sides_known ? lk : nullptr, *rknown = sides_known ? rk : nullptr;
 
         if (n > 65536 && spare_threads.fetch_sub(1) > 0) {
             std::unique_ptr<TreeNode> left;
-            std::thread th([&] { left = build(begin, mid, depth + 1); });
-            node->child[1] = build(mid, end, depth + 1);
+            std::thread th([&] { left = build(begin, mid, depth + 1, lknown); });
+            node->child[1] = build(mid, end, depth + 1, rknown);
             th.join();
             spare_threads.fetch_add(1);
             node->child[0] = std::move(left);
         } else {
             if (n > 65536) spare_threads.fetch_add(1);
-            node->child[0] = build(begin, mid, depth + 1);
-            node->child[1] = build(mid, end, depth + 1);
+            node->child[0] = build(begin, mid, depth + 1, lknown);
+            node->child[1] = build(mid, end, depth + 1, rknown);
         }
         return node;
     }
@@ -272,16 +377,37 @@ float scene_slack(float mag)
 namespace {
 
 // The binned-SAH binary tree over the soup; idx receives the leaf order.
+// Boxes and centroids of the triangles (on all cores).
+std::vector<Prim> make_prims(const float *pos, uint32_t num_tris)
+{
+    std::vector<Prim> prims(num_tris);
+    host_parallel_chunks(num_tris, size_t(1) << 16, [&](size_t b, size_t e) {
+        for (size_t i = b; i < e; ++i) {
+            Prim &p = prims[i];
+            p.box.reset();
+            for (int k = 0; k < 3; ++k) p.box.grow(pos + i * 9 + k * 3);
+            for (int a = 0; a < 3; ++a) p.c[a] = 0.5f * (p.box.lo[a] + p.box.hi[a]);
+        }
+    });
+    return prims;
+}
+
+// Releases a binary tree, the subtrees of the top `spawn_levels` levels on
+// their own threads.
+void free_tree(std::unique_ptr<TreeNode> n, int spawn_levels)
+{
+    if (!n || n->leaf()) return;
+    if (spawn_levels > 0) {
+        std::thread th([&] { free_tree(std::move(n->child[0]), spawn_levels - 1); });
+        free_tree(std::move(n->child[1]), spawn_levels - 1);
+        th.join();
+    }
+}
+
 std::unique_ptr<TreeNode> build_tree(const float *pos, uint32_t num_tris, const BuildParams &params,
                                      std::vector<uint32_t> &idx, int &depth)
 {
-    std::vector<Prim> prims(num_tris);
-    for (uint32_t i = 0; i < num_tris; ++i) {
-        Prim &p = prims[i];
-        p.box.reset();
-        for (int k = 0; k < 3; ++k) p.box.grow(pos + (size_t)i * 9 + k * 3);
-        for (int a = 0; a < 3; ++a) p.c[a] = 0.5f * (p.box.lo[a] + p.box.hi[a]);
-    }
+    const std::vector<Prim> prims = make_prims(pos, num_tris);
     idx.resize(num_tris);
     for (uint32_t i = 0; i < num_tris; ++i) idx[i] = i;
     int threads = (int)params.threads;
@@ -296,8 +422,8 @@ struct WideBuilder {
     Bvh8 &out;
     const std::vector<uint32_t> &idx;  // binary-tree leaf order
     float slack;
-    std::vector<uint32_t> order;       // wide leaf order
-    int max_depth = 0;
+    std::vector<uint32_t> &order;      // wide leaf order (sized to the triangle count)
+    std::atomic<int> spare_threads;
 
     // Collapse of the binary tree into 8-wide nodes by dynamic programming
     // (Ylitie, Karras and Laine, "Efficient Incoherent Ray Traversal on GPUs
@@ -314,11 +440,23 @@ struct WideBuilder {
     static constexpr float kLeafTriCost = 1.0f;
     static constexpr uint32_t kMaxLeafTris = 3;
 
-    static void solve(TreeNode *n)
+    // The subtrees that fill at most 8 child slots (a fixed array: emit runs
+    // once per wide node, and per-node heap allocations dominated its time).
+    struct Slots {
+        const TreeNode *t[8];
+        int n = 0;
+    };
+
+    // Solves the subtree of n; the subtrees of the top `spawn_levels` levels
+    // run on their own threads (every node's result depends only on its
+    // children's, so the split changes nothing).
+    static void solve(TreeNode *n, int spawn_levels)
     {
         const float A = std::max(n->box.area(), 0.0f);
         if (n->leaf()) {
             n->tris = (uint8_t)std::min<uint32_t>(n->count, 4);
+            n->ntris = n->count;
+            n->wide_size = 1;
             n->wide_leaf = true;
             for (int j = 1; j <= 8; ++j) {
                 n->slot_cost[j] = kLeafTriCost * (float)n->count * A;
@@ -327,8 +465,15 @@ struct WideBuilder {
             return;
         }
         TreeNode *l = n->child[0].get(), *r = n->child[1].get();
-        solve(l);
-        solve(r);
+        if (spawn_levels > 0) {
+            std::thread th([&] { solve(l, spawn_levels - 1); });
+            solve(r, spawn_levels - 1);
+            th.join();
+        } else {
+            solve(l, 0);
+            solve(r, 0);
+        }
+        n->ntris = l->ntris + r->ntris;
         n->tris = (uint8_t)std::min<uint32_t>(l->tris + r->tris, 4);
         float open[9];
         int8_t open_split[9];
@@ -356,12 +501,19 @@ struct WideBuilder {
             n->slot_cost[j] = opened ? open[j] : one;
             n->slot_split[j] = opened ? open_split[j] : (int8_t)0;
         }
+        // the wide nodes n would take as a wide node: itself and the subtrees
+        // of its internal slots (their children are solved already)
+        Slots ch;
+        collect(n, ch);
+        n->wide_size = 1;
+        for (int i = 0; i < ch.n; ++i)
+            if (!ch.t[i]->wide_leaf) n->wide_size += ch.t[i]->wide_size;
     }
 
-    static void expand(const TreeNode *n, int j, std::vector<const TreeNode *> &ch)
+    static void expand(const TreeNode *n, int j, Slots &ch)
     {
         if (n->leaf() || n->slot_split[j] == 0) {
-            ch.push_back(n);
+            ch.t[ch.n++] = n;
             return;
         }
         expand(n->child[0].get(), n->slot_split[j], ch);
@@ -369,9 +521,9 @@ struct WideBuilder {
     }
 
     // The child slots of the wide node of internal subtree n.
-    static void collect(const TreeNode *n, std::vector<const TreeNode *> &ch)
+    static void collect(const TreeNode *n, Slots &ch)
     {
-        ch.clear();
+        ch.n = 0;
         const TreeNode *l = n->child[0].get(), *r = n->child[1].get();
         float best = INFINITY;
         int k_best = 1;
@@ -386,29 +538,38 @@ struct WideBuilder {
         expand(r, 8 - k_best, ch);
     }
 
-    // Triangles of subtree n in leaf order.
-    void gather(const TreeNode *n, std::vector<uint32_t> &out) const
+    // Triangles of subtree n in leaf order, written from order[at].
+    void gather(const TreeNode *n, uint32_t &at)
     {
         if (n->leaf()) {
-            for (uint32_t k = 0; k < n->count; ++k) out.push_back(idx[n->first + k]);
+            for (uint32_t k = 0; k < n->count; ++k) order[at++] = idx[n->first + k];
             return;
         }
-        gather(n->child[0].get(), out);
-        gather(n->child[1].get(), out);
+        gather(n->child[0].get(), at);
+        gather(n->child[1].get(), at);
     }
 
-    // Writes the node for binary subtree `n` at out.nodes[index].
-    void emit(const TreeNode *n, uint32_t index, int depth)
+    // Writes the node for binary subtree `n` at out.nodes[index]; the wide
+    // nodes below it take out.nodes[node_at ...] and its triangles
+    // order[tri_at ...], in the depth-first order of a serial emission: each
+    // wide node's internal children are contiguous, in slot order, and a
+    // child's subtree follows the subtrees of the children before it. The
+    // subtree sizes come from solve, so large child subtrees are written by
+    // other threads at the same places. Returns the depth of the deepest wide
+    // node written.
+    int emit(const TreeNode *n, uint32_t index, int depth, uint32_t node_at, uint32_t tri_at)
     {
-        max_depth = std::max(max_depth, depth);
-        std::vector<const TreeNode *> ch;
-        if (n->leaf()) ch.push_back(n);  // only the root can be a leaf
-        else collect(n, ch);
+        int max_depth = depth;
+        Slots slots;
+        if (n->leaf()) slots.t[slots.n++] = n;  // only the root can be a leaf
+        else collect(n, slots);
+        const TreeNode *const *ch = slots.t;
+        const int nch = slots.n;
         // widened child boxes and their union
         Box cb[8];
         Box u;
         u.reset();
-        for (size_t i = 0; i < ch.size(); ++i) {
+        for (int i = 0; i < nch; ++i) {
             for (int a = 0; a < 3; ++a) {
                 cb[i].lo[a] = std::nextafter(ch[i]->box.lo[a] - slack, -INFINITY);
                 cb[i].hi[a] = std::nextafter(ch[i]->box.hi[a] + slack, INFINITY);
@@ -416,7 +577,8 @@ struct WideBuilder {
             u.grow(cb[i]);
         }
         // octant slots: greedy assignment of the child whose centroid lies
-        // furthest towards the slot's corner
+        // furthest towards the slot's corner (candidates by descending reach,
+        // equal reaches in (child, slot) order)
         int slot_of[8], child_in[8];
         for (int s = 0; s < 8; ++s) child_in[s] = -1;
         {
@@ -426,22 +588,25 @@ struct WideBuilder {
                 float v;
                 int c, s;
             };
-            std::vector<Cand> cand;
-            for (int c = 0; c < (int)ch.size(); ++c)
+            Cand cand[64];
+            int nc = 0;
+            for (int c = 0; c < nch; ++c)
                 for (int s = 0; s < 8; ++s) {
                     float v = 0.0f;
                     for (int a = 0; a < 3; ++a) {
                         const float d = ((s >> a) & 1) ? 1.0f : -1.0f;
                         v += d * (0.5f * (cb[c].lo[a] + cb[c].hi[a]) - pc[a]);
                     }
-                    cand.push_back(Cand{v, c, s});
+                    cand[nc++] = Cand{v, c, s};
                 }
-            std::stable_sort(cand.begin(), cand.end(), [](const Cand &x, const Cand &y) { return x.v > y.v; });
+            std::sort(cand, cand + nc, [](const Cand &x, const Cand &y) {
+                return x.v > y.v || (x.v == y.v && 8 * x.c + x.s < 8 * y.c + y.s);
+            });
             for (int c = 0; c < 8; ++c) slot_of[c] = -1;
-            for (const Cand &k : cand)
-                if (slot_of[k.c] < 0 && child_in[k.s] < 0) {
-                    slot_of[k.c] = k.s;
-                    child_in[k.s] = k.c;
+            for (int k = 0; k < nc; ++k)
+                if (slot_of[cand[k].c] < 0 && child_in[cand[k].s] < 0) {
+                    slot_of[cand[k].c] = cand[k].s;
+                    child_in[cand[k].s] = cand[k].c;
                 }
         }
         // quantisation grid
@@ -466,15 +631,15 @@ struct WideBuilder {
             }
         }
         // internal children first (contiguous, slot order), then triangles
-        const uint32_t child_base = (uint32_t)out.nodes.size();
-        std::vector<std::pair<const TreeNode *, uint32_t>> todo;
+        const uint32_t child_base = node_at;
+        std::pair<const TreeNode *, uint32_t> todo[8];
+        int ntodo = 0;
         uint32_t n_internal = 0;
         for (int s = 0; s < 8; ++s) {
             const int c = child_in[s];
             if (c >= 0 && !ch[c]->wide_leaf) ++n_internal;
         }
-        out.nodes.resize(out.nodes.size() + n_internal);
-        const uint32_t tri_base = (uint32_t)order.size();
+        const uint32_t tri_base = tri_at;
         uint32_t next_child = child_base, tri_off = 0;
         for (int s = 0; s < 8; ++s) {
             const int c = child_in[s];
@@ -489,10 +654,10 @@ struct WideBuilder {
             if (!t->wide_leaf) {
                 imask |= 1u << s;
                 meta[s] = (uint8_t)(0x20 | (24 + s));  // hit-mask bit 24 + s
-                todo.push_back({t, next_child++});
+                todo[ntodo++] = {t, next_child++};
             } else if (t->tris > 0) {
                 meta[s] = (uint8_t)((((1u << t->tris) - 1u) << 5) | tri_off);
-                gather(t, order);
+                gather(t, tri_at);
                 tri_off += t->tris;
             }
         }
@@ -506,8 +671,34 @@ struct WideBuilder {
         nd.w[1] = make_uint4(child_base, tri_base, pack(meta), pack(meta + 4));
         for (int a = 0; a < 3; ++a)
             nd.w[2 + a] = make_uint4(pack(qlo[a]), pack(qlo[a] + 4), pack(qhi[a]), pack(qhi[a] + 4));
-        for (auto &[t, i] : todo) emit(t, i, depth + 1);
+        // the children's subtrees: node and triangle ranges in serial order
+        uint32_t sub_node = child_base + n_internal, sub_tri = tri_at;
+        std::thread helpers[8];
+        int sub_depth[8] = {};
+        for (int k = 0; k < ntodo; ++k) {
+            const TreeNode *t = todo[k].first;
+            const uint32_t at_node = sub_node, at_tri = sub_tri;
+            sub_node += t->wide_size - 1;
+            sub_tri += t->ntris;
+            if (t->wide_size >= kSpawnWideNodes && k + 1 < ntodo && spare_threads.fetch_sub(1) > 0) {
+                helpers[k] = std::thread([this, t, k, depth, at_node, at_tri, &todo, &sub_depth] {
+                    sub_depth[k] = emit(t, todo[k].second, depth + 1, at_node, at_tri);
+                });
+            } else {
+                if (t->wide_size >= kSpawnWideNodes && k + 1 < ntodo) spare_threads.fetch_add(1);
+                sub_depth[k] = emit(t, todo[k].second, depth + 1, at_node, at_tri);
+            }
+        }
+        for (int k = 0; k < ntodo; ++k) {
+            if (helpers[k].joinable()) {
+                helpers[k].join();
+                spare_threads.fetch_add(1);
+            }
+            max_depth = std::max(max_depth, sub_depth[k]);
+        }
+        return max_depth;
     }
+    static constexpr uint32_t kSpawnWideNodes = 2048;  // smallest subtree given its own thread
 };
 
 }  // namespace
@@ -522,13 +713,16 @@ Bvh8 build_bvh8(const float *pos, uint32_t num_tris, const BuildParams &params, 
     std::vector<uint32_t> idx;
     int depth2 = 0;
     std::unique_ptr<TreeNode> root = build_tree(pos, num_tris, bp, idx, depth2);
-    WideBuilder::solve(root.get());
-    WideBuilder wb{bvh, idx, slack, {}, 0};
-    wb.order.reserve(num_tris);
-    bvh.nodes.resize(1);
-    wb.emit(root.get(), 0, 1);
-    bvh.order = std::move(wb.order);
-    bvh.depth = wb.max_depth;
+    int threads = (int)params.threads;
+    if (threads <= 0) threads = (int)std::max(1u, std::thread::hardware_concurrency());
+    int spawn_levels = 0;
+    while ((1 << spawn_levels) < threads && spawn_levels < 6) ++spawn_levels;
+    WideBuilder::solve(root.get(), spawn_levels);
+    bvh.order.resize(num_tris);
+    bvh.nodes.resize(root->wide_size);
+    WideBuilder wb{bvh, idx, slack, bvh.order, {threads - 1}};
+    bvh.depth = wb.emit(root.get(), 0, 1, 1, 0);
+    free_tree(std::move(root), spawn_levels);
     return bvh;
 }
 
@@ -537,13 +731,7 @@ Bvh2 build_bvh2(const float *pos, uint32_t num_tris, const BuildParams &params, 
     Bvh2 bvh;
     bvh.slack = slack;
     if (num_tris == 0) return bvh;
-    std::vector<Prim> prims(num_tris);
-    for (uint32_t i = 0; i < num_tris; ++i) {
-        Prim &p = prims[i];
-        p.box.reset();
-        for (int k = 0; k < 3; ++k) p.box.grow(pos + (size_t)i * 9 + k * 3);
-        for (int a = 0; a < 3; ++a) p.c[a] = 0.5f * (p.box.lo[a] + p.box.hi[a]);
-    }
+    const std::vector<Prim> prims = make_prims(pos, num_tris);
     std::vector<uint32_t> idx(num_tris);
     for (uint32_t i = 0; i < num_tris; ++i) idx[i] = i;
     int threads = (int)params.threads;
@@ -568,6 +756,9 @@ Bvh2 build_bvh2(const float *pos, uint32_t num_tris, const BuildParams &params, 
         fl.emit(root.get());
         bvh.depth = builder.max_depth.load() + 1;
     }
+    int levels = 0;
+    while ((1 << levels) < threads && levels < 6) ++levels;
+    free_tree(std::move(root), levels);
     bvh.order = std::move(idx);
     return bvh;
 }
@@ -578,36 +769,38 @@ void make_tri_records(const float *pos, const std::vector<uint32_t> &order,
     const size_t n = order.size();
     ref.resize(n * 3);
     wt.resize(n * 3);
-    for (size_t k = 0; k < n; ++k) {
-        const float *q = pos + (size_t)order[k] * 9;
-        const float Ax = q[0], Ay = q[1], Az = q[2];
-        const float Bx = q[3], By = q[4], Bz = q[5];
-        const float Cx = q[6], Cy = q[7], Cz = q[8];
-        // n_f = (A - B) x (A - C), sgn_area2 = n_f . n_f, n = n_f / |n_f|
-        // (IntersectionTestsImpl.hpp:261-266; Utils.hpp:88-109), compiled with
-        // -ffp-contract=off so it rounds like the reference.
-        const float ux = Ax - Bx, uy = Ay - By, uz = Az - Bz;
-        const float vx = Ax - Cx, vy = Ay - Cy, vz = Az - Cz;
-        const float nfx = uy * vz - uz * vy;
-        const float nfy = uz * vx - ux * vz;
-        const float nfz = ux * vy - uy * vx;
-        const float s = nfx * nfx + nfy * nfy + nfz * nfz;
-        float nx = 0.0f, ny = 0.0f, nz = 0.0f;
-        if (!(s < 1e-14f)) {
-            const float l = std::sqrt(nfx * nfx + nfy * nfy + nfz * nfz);
-            nx = nfx / l;
-            ny = nfy / l;
-            nz = nfz / l;
+    host_parallel_chunks(n, size_t(1) << 16, [&](size_t k0, size_t k1) {
+        for (size_t k = k0; k < k1; ++k) {
+            const float *q = pos + (size_t)order[k] * 9;
+            const float Ax = q[0], Ay = q[1], Az = q[2];
+            const float Bx = q[3], By = q[4], Bz = q[5];
+            const float Cx = q[6], Cy = q[7], Cz = q[8];
+            // n_f = (A - B) x (A - C), sgn_area2 = n_f . n_f, n = n_f / |n_f|
+            // (IntersectionTestsImpl.hpp:261-266; Utils.hpp:88-109), compiled with
+            // -ffp-contract=off so it rounds like the reference.
+            const float ux = Ax - Bx, uy = Ay - By, uz = Az - Bz;
+            const float vx = Ax - Cx, vy = Ay - Cy, vz = Az - Cz;
+            const float nfx = uy * vz - uz * vy;
+            const float nfy = uz * vx - ux * vz;
+            const float nfz = ux * vy - uy * vx;
+            const float s = nfx * nfx + nfy * nfy + nfz * nfz;
+            float nx = 0.0f, ny = 0.0f, nz = 0.0f;
+            if (!(s < 1e-14f)) {
+                const float l = std::sqrt(nfx * nfx + nfy * nfy + nfz * nfz);
+                nx = nfx / l;
+                ny = nfy / l;
+                nz = nfz / l;
+            }
+            const float BAx = Bx - Ax, BAy = By - Ay, BAz = Bz - Az;
+            const float CAx = Cx - Ax, CAy = Cy - Ay, CAz = Cz - Az;
+            ref[k * 3 + 0] = make_float4(Ax, Ay, Az, nx);
+            ref[k * 3 + 1] = make_float4(ny, nz, BAx, BAy);
+            ref[k * 3 + 2] = make_float4(BAz, CAx, CAy, CAz);
+            wt[k * 3 + 0] = make_float4(Ax, Ay, Az, Bx);
+            wt[k * 3 + 1] = make_float4(By, Bz, Cx, Cy);
+            wt[k * 3 + 2] = make_float4(Cz, 0.0f, 0.0f, 0.0f);
         }
-        const float BAx = Bx - Ax, BAy = By - Ay, BAz = Bz - Az;
-        const float CAx = Cx - Ax, CAy = Cy - Ay, CAz = Cz - Az;
-        ref[k * 3 + 0] = make_float4(Ax, Ay, Az, nx);
-        ref[k * 3 + 1] = make_float4(ny, nz, BAx, BAy);
-        ref[k * 3 + 2] = make_float4(BAz, CAx, CAy, CAz);
-        wt[k * 3 + 0] = make_float4(Ax, Ay, Az, Bx);
-        wt[k * 3 + 1] = make_float4(By, Bz, Cx, Cy);
-        wt[k * 3 + 2] = make_float4(Cz, 0.0f, 0.0f, 0.0f);
-    }
+    });
 }
 
 }  // namespace dr
