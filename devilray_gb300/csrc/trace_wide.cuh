@@ -79,6 +79,12 @@ constexpr int kWideStack = 64;
 #ifndef DR_HIT_FSET
 #define DR_HIT_FSET 1
 #endif
+// Independent accumulators of the FMA hit bits (1, 2 or 4), summed at the end
+// (exact: distinct powers of two below 256). Measured on the incoherent
+// workload: 1 chain 3.194-3.195 ms, 2 chains 3.215-3.216 ms; 4 spill.
+#ifndef DR_HIT_CHAINS
+#define DR_HIT_CHAINS 1
+#endif
 // The FP16 path's slab FMAs as scalar FMAs instead of packed pairs (fewer
 // registers). Measured: 3.283 ms at 7 blocks per SM, 3.371 ms at 8 (64
 // registers, spills); packed pairs 3.192 ms at 7 blocks, 3.308 ms at 8.
@@ -303,7 +309,7 @@ __host__ __device__ __forceinline__ void wide_node_test(const Bvh8Node *node, co
     const uint32_t hnz0 = nz0, hnz1 = nz1, hfz0 = fz0, hfz1 = fz1;
 #endif
 #if DR_HIT_FSET
-    float hit_f = 0.0f;
+    float hit_acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
 #endif
     // slots 4h + j and 4h + j + 2 (bytes j and j + 2 of word h) as pairs
     const SlabAxis hx = slab_axis_h(ax, bx), hy = slab_axis_h(ay, by), hz = slab_axis_h(az, bz);
@@ -340,6 +346,7 @@ __host__ __device__ __forceinline__ void wide_node_test(const Bvh8Node *node, co
 #endif
             const uint32_t s0 = 4u * h + j;
 #if DR_HIT_FSET
+            float &hit_f = hit_acc[DR_HIT_CHAINS == 4 ? 2 * h + (int)j : DR_HIT_CHAINS == 2 ? h : 0];
             hit_f = fmaf(set_le(fmaxf(max3f(tnx.x, tny.x, tnz.x), 0.0f), tmx.x), (float)(1u << s0),
                          fmaf(set_le(fmaxf(max3f(tnx.y, tny.y, tnz.y), 0.0f), tmx.y), (float)(1u << (s0 + 2)), hit_f));
 #else
@@ -351,6 +358,9 @@ __host__ __device__ __forceinline__ void wide_node_test(const Bvh8Node *node, co
 #if DR_HIT_FSET
     // a sum of distinct powers of two below 256 is exact: 2^23 + sum has it in
     // its low mantissa bits
+    const float hit_f = DR_HIT_CHAINS == 4   ? (hit_acc[0] + hit_acc[1]) + (hit_acc[2] + hit_acc[3])
+                        : DR_HIT_CHAINS == 2 ? hit_acc[0] + hit_acc[1]
+                                             : hit_acc[0];
     hit_bits = __float_as_uint(hit_f + 8388608.0f) & 0xffu;
 #endif
     } else
