@@ -153,6 +153,21 @@ __device__ __forceinline__ void persistent_wide(const Wide8Args &a, const Source
 {
     constexpr unsigned FULL = 0xffffffffu;
     constexpr bool HALF = !ANY && DR_HALF_CVT;  // node tests with FP16 grid planes (closest hit)
+    constexpr bool LUT = !DR_NO_OCT_ORDER && (DR_OCT_LUT == 1 || (DR_OCT_LUT == 2 && ANY));
+    const uint8_t *oct_lut = nullptr;
+    if constexpr (LUT) {
+        // entry (oct << 8) | m: mask m with bit s moved to bit s ^ oct (every
+        // thread of the block calls this function first)
+        __shared__ uint8_t s_oct[8 * 256];
+        for (uint32_t i = threadIdx.x; i < 8 * 256; i += blockDim.x) {
+            const uint32_t o = i >> 8, m = i & 255u;
+            uint32_t t = 0;
+            for (uint32_t b = 0; b < 8; ++b) t |= ((m >> b) & 1u) << (b ^ o);
+            s_oct[i] = (uint8_t)t;
+        }
+        __syncthreads();
+        oct_lut = s_oct;
+    }
     const int lane = threadIdx.x & 31;
     const unsigned lower = (1u << lane) - 1u;
     WideState s;
@@ -222,14 +237,14 @@ __device__ __forceinline__ void persistent_wide(const Wide8Args &a, const Source
         bool fin = false;  // no node left (found during the extra node tests)
         if constexpr (BATCH) {
             // 1. node test(s)
-            if (active && !waiting && s.have_node) wide_visit<MODE, HALF>(a, s, cn, cb);
+            if (active && !waiting && s.have_node) wide_visit<MODE, HALF, LUT>(a, s, cn, cb, oct_lut);
 #pragma unroll 1
             for (int k = 1; k < DR_INNER_STEPS_BATCH; ++k) {
                 const bool go = active && !waiting && !fin && s.tmask == 0;
                 if (__popc(__ballot_sync(FULL, go)) < DR_INNER_MIN_LANES_BATCH) break;
                 if (go) {
                     fin = wide_advance<ANY>(a, s, stack);
-                    if (!fin && s.have_node) wide_visit<MODE, HALF>(a, s, cn, cb);
+                    if (!fin && s.have_node) wide_visit<MODE, HALF, LUT>(a, s, cn, cb, oct_lut);
                 }
             }
             // 2. leaf triangles join the warp batch (whole groups, in lane
@@ -280,14 +295,14 @@ __device__ __forceinline__ void persistent_wide(const Wide8Args &a, const Source
             }
         } else {
             // 1. node test(s)
-            if (active && s.have_node) wide_visit<MODE, HALF>(a, s, cn, cb);
+            if (active && s.have_node) wide_visit<MODE, HALF, LUT>(a, s, cn, cb, oct_lut);
 #pragma unroll 1
             for (int k = 1; k < DR_INNER_STEPS_LANE; ++k) {
                 const bool go = active && !fin && s.tmask == 0;
                 if (__popc(__ballot_sync(FULL, go)) < DR_INNER_MIN_LANES_LANE) break;
                 if (go) {
                     fin = wide_advance<ANY>(a, s, stack);
-                    if (!fin && s.have_node) wide_visit<MODE, HALF>(a, s, cn, cb);
+                    if (!fin && s.have_node) wide_visit<MODE, HALF, LUT>(a, s, cn, cb, oct_lut);
                 }
             }
             // 2. leaf triangles: tested now when enough lanes of the warp have
