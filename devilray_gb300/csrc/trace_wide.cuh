@@ -583,7 +583,9 @@ __device__ __forceinline__ bool wide_triangles(const Wide8Args &a, WideState &s,
 // in shared memory (a per-warp array, one column per lane: 256 B per entry
 // and warp), the rest in local memory. Measured on the incoherent workload:
 // local only 3.74, 8 entries 3.83, 16 entries 3.82 Grays/s (before the later
-// node-test changes); 4 and 8 entries 4.37 Grays/s after them. The public
+// node-test changes); 4 and 8 entries 4.37 Grays/s after them; with the
+// FP16 planes and FMA hit bits, closest hit 0 / 4 / 8 entries 3.233 / 3.200 /
+// 3.192 ms (4 entries leave the SM more L1 and gain nothing). The public
 // kernels use DR_SMEM_STACK entries; the renderer's depth is a schedule knob
 // (dr_render_config.stack), chosen by the autotuner.
 #ifndef DR_SMEM_STACK
