@@ -94,7 +94,12 @@ constexpr int kP8MinBlocks = DR_P8_MIN_BLOCKS;
 //   4 batch steps with at least 12 / 16 / 20 / 24 lanes: 4.84 / 4.86 / 4.89 /
 //   4.86 Grays/s; 4 per-lane steps with 24 lanes: render 50.8 ms. Letting
 //   lanes with leaf triangles push them as a postponed group and go on in
-//   the extra node tests: 4.96 -> 4.63 Grays/s.
+//   the extra node tests: 4.96 -> 4.63 Grays/s. Re-measured with the FP16
+//   planes and FMA hit bits (closest / any hit, ms): 4 steps with 20 lanes
+//   3.192 / 2.793; 5 or 6 steps 3.208 / 2.803 and 3.213 / 2.809; 16 lanes
+//   3.196 / 2.796; 24 lanes 3.233 / 2.820; batch flush at 10 or 16 pairs
+//   3.198 / 2.784 and 3.198 / 2.823; refills at 2 or 6 idle lanes 3.191 /
+//   2.790 and 3.193 / 2.794.
 // Results do not depend on it.
 #ifndef DR_INNER_STEPS_BATCH
 #define DR_INNER_STEPS_BATCH 4
