@@ -105,10 +105,11 @@ constexpr int kWideStack = 64;
 // s ^ oct) by one lookup in a 2 KB shared-memory table per block
 // instead of three conditional swaps, in the persistent kernels: 1 all of
 // them, 2 the any-hit ones. Measured on the incoherent workload: any hit
-// 2.842 -> 2.791 ms with the table; closest hit 3.192 -> 3.307 ms (the
-// extra shared memory of 7 blocks per SM takes L1 from the node fetches), so
-// only the any-hit kernels use it (many-light 1080p render, 16 spp: 40.46-40.55
-// -> 40.40-40.43 ms).
+// 2.842 -> 2.791 ms with the table; closest hit 3.192 -> 3.307 ms, and
+// 3.275 / 3.285 ms with 6 / 4 shared stack entries, which give back the L1
+// the table takes (with the table the closest-hit kernel spills 26 bytes at
+// its 72 registers). So only the any-hit kernels use it (many-light 1080p
+// render, 16 spp: 40.46-40.55 -> 40.40-40.43 ms).
 #ifndef DR_OCT_LUT
 #define DR_OCT_LUT 2
 #endif
