@@ -78,8 +78,10 @@ struct Builder {
     std::atomic<int> spare_threads;
     std::atomic<int> max_depth{0};
 
+    const int threads;  // host threads the build may use
+
     Builder(const std::vector<Prim> &p, std::vector<uint32_t> &i, const BuildParams &bp, int threads)
-        : prims(p), idx(i), params(bp), spare_threads(threads - 1) {}
+        : prims(p), idx(i), params(bp), spare_threads(threads - 1), threads(threads) {}
 
     static constexpr float kTraversalCost = 1.0f;
     static constexpr float kTriangleCost = 1.5f;
@@ -145,13 +147,13 @@ struct Builder {
             }
         };
         AxisBins bins[3];
-        if (n >= kParallelBinning) {
-            const size_t hw = std::max(1u, std::thread::hardware_concurrency());
-            std::vector<AxisBins> parts(3 * (hw + 1));
+        if (n >= kParallelBinning && threads > 1) {
+            std::vector<AxisBins> parts(3 * (size_t)threads);
             std::atomic<uint32_t> next{0};
-            host_parallel_chunks(n, kParallelBinning / 4, [&](size_t b0, size_t b1) {
-                bin_into(parts.data() + 3 * next.fetch_add(1), begin + b0, begin + b1);
-            });
+            host_parallel_chunks(
+                n, kParallelBinning / 4,
+                [&](size_t b0, size_t b1) { bin_into(parts.data() + 3 * next.fetch_add(1), begin + b0, begin + b1); },
+                (size_t)threads);
             for (int a = 0; a < 3; ++a) std::memset(bins[a].count, 0, B * sizeof(uint32_t));
             for (uint32_t k = 0; k < next.load(); ++k)
                 for (int a = 0; a < 3; ++a)
@@ -376,19 +378,27 @@ float scene_slack(float mag)
 
 namespace {
 
-// The binned-SAH binary tree over the soup; idx receives the leaf order.
-// Boxes and centroids of the triangles (on all cores).
-std::vector<Prim> make_prims(const float *pos, uint32_t num_tris)
+// Host threads a build may use: BuildParams::threads, 0 for all cores.
+int build_threads(const BuildParams &params)
+{
+    return params.threads > 0 ? (int)params.threads : (int)std::max(1u, std::thread::hardware_concurrency());
+}
+
+// Boxes and centroids of the triangles.
+std::vector<Prim> make_prims(const float *pos, uint32_t num_tris, int threads)
 {
     std::vector<Prim> prims(num_tris);
-    host_parallel_chunks(num_tris, size_t(1) << 16, [&](size_t b, size_t e) {
-        for (size_t i = b; i < e; ++i) {
-            Prim &p = prims[i];
-            p.box.reset();
-            for (int k = 0; k < 3; ++k) p.box.grow(pos + i * 9 + k * 3);
-            for (int a = 0; a < 3; ++a) p.c[a] = 0.5f * (p.box.lo[a] + p.box.hi[a]);
-        }
-    });
+    host_parallel_chunks(
+        num_tris, size_t(1) << 16,
+        [&](size_t b, size_t e) {
+            for (size_t i = b; i < e; ++i) {
+                Prim &p = prims[i];
+                p.box.reset();
+                for (int k = 0; k < 3; ++k) p.box.grow(pos + i * 9 + k * 3);
+                for (int a = 0; a < 3; ++a) p.c[a] = 0.5f * (p.box.lo[a] + p.box.hi[a]);
+            }
+        },
+        (size_t)threads);
     return prims;
 }
 
@@ -404,14 +414,14 @@ void free_tree(std::unique_ptr<TreeNode> n, int spawn_levels)
     }
 }
 
+// The binned-SAH binary tree over the soup; idx receives the leaf order.
 std::unique_ptr<TreeNode> build_tree(const float *pos, uint32_t num_tris, const BuildParams &params,
                                      std::vector<uint32_t> &idx, int &depth)
 {
-    const std::vector<Prim> prims = make_prims(pos, num_tris);
+    const int threads = build_threads(params);
+    const std::vector<Prim> prims = make_prims(pos, num_tris, threads);
     idx.resize(num_tris);
     for (uint32_t i = 0; i < num_tris; ++i) idx[i] = i;
-    int threads = (int)params.threads;
-    if (threads <= 0) threads = (int)std::max(1u, std::thread::hardware_concurrency());
     Builder builder(prims, idx, params, threads);
     std::unique_ptr<TreeNode> root = builder.build(0, num_tris, 0);
     depth = builder.max_depth.load() + 1;
@@ -713,8 +723,7 @@ Bvh8 build_bvh8(const float *pos, uint32_t num_tris, const BuildParams &params, 
     std::vector<uint32_t> idx;
     int depth2 = 0;
     std::unique_ptr<TreeNode> root = build_tree(pos, num_tris, bp, idx, depth2);
-    int threads = (int)params.threads;
-    if (threads <= 0) threads = (int)std::max(1u, std::thread::hardware_concurrency());
+    const int threads = build_threads(params);
     int spawn_levels = 0;
     while ((1 << spawn_levels) < threads && spawn_levels < 6) ++spawn_levels;
     WideBuilder::solve(root.get(), spawn_levels);
@@ -731,11 +740,10 @@ Bvh2 build_bvh2(const float *pos, uint32_t num_tris, const BuildParams &params, 
     Bvh2 bvh;
     bvh.slack = slack;
     if (num_tris == 0) return bvh;
-    const std::vector<Prim> prims = make_prims(pos, num_tris);
+    const int threads = build_threads(params);
+    const std::vector<Prim> prims = make_prims(pos, num_tris, threads);
     std::vector<uint32_t> idx(num_tris);
     for (uint32_t i = 0; i < num_tris; ++i) idx[i] = i;
-    int threads = (int)params.threads;
-    if (threads <= 0) threads = (int)std::max(1u, std::thread::hardware_concurrency());
     BuildParams bp = params;
     bp.max_leaf = std::max<uint32_t>(1, std::min(bp.max_leaf, kMaxLeafSize));
     Builder builder(prims, idx, bp, threads);

@@ -50,13 +50,13 @@ inline cudaError_t dev_malloc(T **p, size_t bytes)
 }
 
 // Runs f(begin, end) over [0, n) in contiguous chunks of at least `grain`
-// items on up to hardware_concurrency host threads (the caller's thread takes
-// the first chunk). Each chunk writes only its own outputs, so the result does
-// not depend on the split.
+// items on up to `max_threads` host threads (0: hardware_concurrency; the
+// caller's thread takes the first chunk). Each chunk writes only its own
+// outputs, so the result does not depend on the split.
 template <typename F>
-inline void host_parallel_chunks(size_t n, size_t grain, F &&f)
+inline void host_parallel_chunks(size_t n, size_t grain, F &&f, size_t max_threads = 0)
 {
-    const size_t hw = std::max(1u, std::thread::hardware_concurrency());
+    const size_t hw = max_threads ? max_threads : std::max(1u, std::thread::hardware_concurrency());
     const size_t parts = std::max<size_t>(1, std::min(hw, n / std::max<size_t>(1, grain)));
     if (parts == 1) {
         f(size_t(0), n);
