@@ -89,11 +89,13 @@ struct Builder {
     static constexpr uint32_t kKnownSides = 1u << 12;        // ranges that pass their sides' bounds down
 
     // Bins of one axis: the primitives' boxes, their centroids' box and count.
-    // A bin's boxes are written by its first primitive (count 0 -> 1), so
-    // only the counts are cleared per range and empty bins are never read.
+    // A bin's entries are written by its first primitive, which also sets its
+    // bit of `occupied`; empty bins are never read, so nothing is cleared per
+    // range but the mask.
     struct AxisBins {
         Box box[64], cbox[64];
         uint32_t count[64];
+        uint64_t occupied;
     };
 
     // The best SAH split of a range, with the bounds of its two sides.
@@ -126,7 +128,7 @@ struct Builder {
         const uint32_t n = end - begin;
         const bool sides = n >= kKnownSides;
         auto bin_into = [&](AxisBins *bins, size_t b0, size_t b1) {
-            for (int a = 0; a < 3; ++a) std::memset(bins[a].count, 0, B * sizeof(uint32_t));
+            for (int a = 0; a < 3; ++a) bins[a].occupied = 0;
             for (size_t i = b0; i < b1; ++i) {
                 const Prim &p = prims[idx[i]];
                 for (int a = 0; a < 3; ++a) {
@@ -134,12 +136,15 @@ struct Builder {
                     uint32_t b = (uint32_t)((p.c[a] - cmin[a]) * scale[a]);
                     if (b >= B) b = B - 1;
                     AxisBins &ab = bins[a];
-                    if (ab.count[b]++ == 0) {
+                    if (!((ab.occupied >> b) & 1u)) {
+                        ab.occupied |= 1ull << b;
+                        ab.count[b] = 1;
                         ab.box[b] = p.box;
                         if (sides) {
                             for (int k = 0; k < 3; ++k) ab.cbox[b].lo[k] = ab.cbox[b].hi[k] = p.c[k];
                         }
                     } else {
+                        ++ab.count[b];
                         ab.box[b].grow(p.box);
                         if (sides) ab.cbox[b].grow(p.c);
                     }
@@ -154,21 +159,24 @@ struct Builder {
                 n, kParallelBinning / 4,
                 [&](size_t b0, size_t b1) { bin_into(parts.data() + 3 * next.fetch_add(1), begin + b0, begin + b1); },
                 (size_t)threads);
-            for (int a = 0; a < 3; ++a) std::memset(bins[a].count, 0, B * sizeof(uint32_t));
+            for (int a = 0; a < 3; ++a) bins[a].occupied = 0;
             for (uint32_t k = 0; k < next.load(); ++k)
-                for (int a = 0; a < 3; ++a)
-                    for (uint32_t b = 0; b < B; ++b) {
-                        const AxisBins &pb = parts[3 * k + a];
-                        if (pb.count[b] == 0) continue;
-                        if (bins[a].count[b] == 0) {
+                for (int a = 0; a < 3; ++a) {
+                    const AxisBins &pb = parts[3 * k + a];
+                    for (uint64_t m = pb.occupied; m != 0; m &= m - 1) {
+                        const int b = __builtin_ctzll(m);
+                        if (!((bins[a].occupied >> b) & 1u)) {
+                            bins[a].occupied |= 1ull << b;
+                            bins[a].count[b] = pb.count[b];
                             bins[a].box[b] = pb.box[b];
                             bins[a].cbox[b] = pb.cbox[b];
                         } else {
+                            bins[a].count[b] += pb.count[b];
                             bins[a].box[b].grow(pb.box[b]);
                             bins[a].cbox[b].grow(pb.cbox[b]);
                         }
-                        bins[a].count[b] += pb.count[b];
                     }
+                }
         } else {
             bin_into(bins, begin, end);
         }
@@ -177,8 +185,7 @@ struct Builder {
             if (!active[axis]) continue;
             const AxisBins &ab = bins[axis];
             uint32_t occ[64], k = 0;  // occupied bins, ascending
-            for (uint32_t b = 0; b < B; ++b)
-                if (ab.count[b]) occ[k++] = b;
+            for (uint64_t m = ab.occupied; m != 0; m &= m - 1) occ[k++] = (uint32_t)__builtin_ctzll(m);
             // right side of the boundary after occupied bin occ[i]: bins occ[i + 1 ..]
             float right_area[64];
             uint32_t right_count[64];
@@ -213,8 +220,8 @@ struct Builder {
             best.left_c.reset();
             best.right.reset();
             best.right_c.reset();
-            for (uint32_t b = 0; b < B; ++b) {
-                if (ab.count[b] == 0) continue;
+            for (uint64_t m = ab.occupied; m != 0; m &= m - 1) {
+                const uint32_t b = (uint32_t)__builtin_ctzll(m);
                 (b < best.bin ? best.left : best.right).grow(ab.box[b]);
                 (b < best.bin ? best.left_c : best.right_c).grow(ab.cbox[b]);
             }
