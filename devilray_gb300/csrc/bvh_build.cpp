@@ -50,9 +50,13 @@ struct Box {
     }
 };
 
+// A triangle's box and centroid, and its index in the soup. The builder
+// partitions these records themselves (not indices to them), so every pass
+// over a range reads contiguous memory.
 struct Prim {
     Box box;
     float c[3];
+    uint32_t id;
 };
 
 struct TreeNode {
@@ -72,16 +76,15 @@ struct TreeNode {
 };
 
 struct Builder {
-    const std::vector<Prim> &prims;
-    std::vector<uint32_t> &idx;
+    std::vector<Prim> &prims;  // partitioned in place; ids give the leaf order
     BuildParams params;
     std::atomic<int> spare_threads;
     std::atomic<int> max_depth{0};
 
     const int threads;  // host threads the build may use
 
-    Builder(const std::vector<Prim> &p, std::vector<uint32_t> &i, const BuildParams &bp, int threads)
-        : prims(p), idx(i), params(bp), spare_threads(threads - 1), threads(threads) {}
+    Builder(std::vector<Prim> &p, const BuildParams &bp, int threads)
+        : prims(p), params(bp), spare_threads(threads - 1), threads(threads) {}
 
     static constexpr float kTraversalCost = 1.0f;
     static constexpr float kTriangleCost = 1.5f;
@@ -130,7 +133,7 @@ struct Builder {
         auto bin_into = [&](AxisBins *bins, size_t b0, size_t b1) {
             for (int a = 0; a < 3; ++a) bins[a].occupied = 0;
             for (size_t i = b0; i < b1; ++i) {
-                const Prim &p = prims[idx[i]];
+                const Prim &p = prims[i];
                 for (int a = 0; a < 3; ++a) {
                     if (!active[a]) continue;
                     uint32_t b = (uint32_t)((p.c[a] - cmin[a]) * scale[a]);
@@ -246,7 +249,7 @@ struct Builder {
             bounds.reset();
             cbounds.reset();
             for (uint32_t i = begin; i < end; ++i) {
-                const Prim &p = prims[idx[i]];
+                const Prim &p = prims[i];
                 bounds.grow(p.box);
                 cbounds.grow(p.c);
             }
@@ -281,12 +284,12 @@ struct Builder {
         if (best_axis >= 0) {
             const float cmin = cbounds.lo[best_axis], cmax = cbounds.hi[best_axis];
             const float scale = (float)B / (cmax - cmin);
-            auto it = std::partition(idx.begin() + begin, idx.begin() + end, [&](uint32_t i) {
-                uint32_t b = (uint32_t)((prims[i].c[best_axis] - cmin) * scale);
+            auto it = std::partition(prims.begin() + begin, prims.begin() + end, [&](const Prim &p) {
+                uint32_t b = (uint32_t)((p.c[best_axis] - cmin) * scale);
                 if (b >= B) b = B - 1;
                 return b < best.bin;
             });
-            mid = (uint32_t)(it - idx.begin());
+            mid = (uint32_t)(it - prims.begin());
             sides_known = best.sides && mid != begin && mid != end;
             if (mid == begin || mid == end) mid = begin + n / 2;
         } else {
@@ -300,10 +303,10 @@ struct Builder {
                     axis = a;
                 }
             mid = begin + n / 2;
-            std::nth_element(idx.begin() + begin, idx.begin() + mid, idx.begin() + end,
-                             [&](uint32_t a, uint32_t b) {
-                                 if (prims[a].c[axis] != prims[b].c[axis]) return prims[a].c[axis] < prims[b].c[axis];
-                                 return a < b;
+            std::nth_element(prims.begin() + begin, prims.begin() + mid, prims.begin() + end,
+                             [&](const Prim &a, const Prim &b) {
+                                 if (a.c[axis] != b.c[axis]) return a.c[axis] < b.c[axis];
+                                 return a.id < b.id;
                              });
         }
         const Box lk[2] = {best.left, best.left_c}, rk[2] = {best.right, best.right_c};
@@ -403,10 +406,24 @@ std::vector<Prim> make_prims(const float *pos, uint32_t num_tris, int threads)
                 p.box.reset();
                 for (int k = 0; k < 3; ++k) p.box.grow(pos + i * 9 + k * 3);
                 for (int a = 0; a < 3; ++a) p.c[a] = 0.5f * (p.box.lo[a] + p.box.hi[a]);
+                p.id = (uint32_t)i;
             }
         },
         (size_t)threads);
     return prims;
+}
+
+// The soup indices of the partitioned records: leaf position -> triangle.
+std::vector<uint32_t> leaf_order(const std::vector<Prim> &prims, int threads)
+{
+    std::vector<uint32_t> idx(prims.size());
+    host_parallel_chunks(
+        prims.size(), size_t(1) << 16,
+        [&](size_t b, size_t e) {
+            for (size_t i = b; i < e; ++i) idx[i] = prims[i].id;
+        },
+        (size_t)threads);
+    return idx;
 }
 
 // Releases a binary tree, the subtrees of the top `spawn_levels` levels on
@@ -426,12 +443,11 @@ std::unique_ptr<TreeNode> build_tree(const float *pos, uint32_t num_tris, const 
                                      std::vector<uint32_t> &idx, int &depth)
 {
     const int threads = build_threads(params);
-    const std::vector<Prim> prims = make_prims(pos, num_tris, threads);
-    idx.resize(num_tris);
-    for (uint32_t i = 0; i < num_tris; ++i) idx[i] = i;
-    Builder builder(prims, idx, params, threads);
+    std::vector<Prim> prims = make_prims(pos, num_tris, threads);
+    Builder builder(prims, params, threads);
     std::unique_ptr<TreeNode> root = builder.build(0, num_tris, 0);
     depth = builder.max_depth.load() + 1;
+    idx = leaf_order(prims, threads);
     return root;
 }
 
@@ -748,13 +764,12 @@ Bvh2 build_bvh2(const float *pos, uint32_t num_tris, const BuildParams &params, 
     bvh.slack = slack;
     if (num_tris == 0) return bvh;
     const int threads = build_threads(params);
-    const std::vector<Prim> prims = make_prims(pos, num_tris, threads);
-    std::vector<uint32_t> idx(num_tris);
-    for (uint32_t i = 0; i < num_tris; ++i) idx[i] = i;
+    std::vector<Prim> prims = make_prims(pos, num_tris, threads);
     BuildParams bp = params;
     bp.max_leaf = std::max<uint32_t>(1, std::min(bp.max_leaf, kMaxLeafSize));
-    Builder builder(prims, idx, bp, threads);
+    Builder builder(prims, bp, threads);
     std::unique_ptr<TreeNode> root = builder.build(0, num_tris, 0);
+    std::vector<uint32_t> idx = leaf_order(prims, threads);
 
     Flattener fl{bvh.nodes, slack};
     bvh.nodes.reserve(2 * (size_t)num_tris / std::max<uint32_t>(1, bp.max_leaf) + 4);
